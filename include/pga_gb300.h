@@ -1,0 +1,237 @@
+/*
+ * pga_gb300.h -- C ABI of the GB300 derivation engine for PGA shape grammars.
+ *
+ * Plain C: pointers, sizes and POD structs only; streams are passed as
+ * `void*` holding a cudaStream_t (0 = the legacy default stream).
+ *
+ * The data formats follow the reference's dispatch-table path so that a grammar
+ * written for it runs unchanged:
+ *   - PgaParameter / PgaSuccessor / PgaEntry  ~ PGA::DispatchTableEntry
+ *     (include/pga/core/DispatchTableEntry.h:8-36), minus the instrumentation
+ *     fields numEdgeIndices/edgeIndices/subGraphIndex, which the engine has no use for.
+ *   - PgaProc ~ one Proc<ShapeT, OperatorT, NumThreadsT> of a procedure list
+ *     (include/pga/core/Proc.cuh:19-27); an entry's operatorCode indexes the
+ *     procedure list exactly as in the reference (CPUEvaluator.h:230-239,
+ *     GPUEvaluator.cuh:194-211).
+ *   - PgaTerminal ~ the instanced-mesh record written by
+ *     GenerationFunction<GenFuncFilter, 1>::perShape
+ *     (include/pga/rendering/GenerationFunctions.cuh:158-188): the model matrix
+ *     model4 * scale(size) (row-major 3x4 here; the 4th row is always 0 0 0 1)
+ *     plus the custom attribute, extended with the emitting rule and a
+ *     derivation-path hash.
+ */
+#ifndef PGA_GB300_H
+#define PGA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Limits of one dispatch-table entry (include/pga/core/GlobalConstants.h:9-14). */
+#define PGA_MAX_NUM_PARAMETERS 17
+#define PGA_MAX_NUM_PARAMETER_VALUES 16
+#define PGA_MAX_NUM_SUCCESSORS 20
+#define PGA_MAX_EXP_LEVELS 4
+
+/* Parameter types: 0..5 are PGA::ParameterType (include/pga/core/ParameterType.h).
+ * PGA_PT_BLOCK is an addition: value[0] is a slot in the axiom's parameter block
+ * (per-axiom continuous parameters, the ones pga_adjoint differentiates). */
+typedef enum PgaParameterType {
+  PGA_PT_SCALAR = 0,
+  PGA_PT_RAND = 1,
+  PGA_PT_SHAPE_ATTR = 2,
+  PGA_PT_EXP = 3,
+  PGA_PT_VEC2 = 4,
+  PGA_PT_VEC4 = 5,
+  PGA_PT_BLOCK = 16
+} PgaParameterType;
+
+typedef struct PgaParameter {
+  int32_t type;                                  /* PgaParameterType */
+  float value[PGA_MAX_NUM_PARAMETER_VALUES];
+} PgaParameter;                                  /* 68 B */
+
+typedef struct PgaSuccessor {
+  int32_t entryIndex;
+  int32_t phaseIndex;                            /* single-phase engine: ignored */
+} PgaSuccessor;
+
+typedef struct PgaEntry {
+  int32_t operatorCode;                          /* index into the procedure list */
+  uint32_t numParameters;
+  uint32_t numSuccessors;
+  uint32_t reserved;
+  PgaParameter parameters[PGA_MAX_NUM_PARAMETERS];
+  PgaSuccessor successors[PGA_MAX_NUM_SUCCESSORS];
+} PgaEntry;                                      /* 1332 B */
+
+/* Operator kinds of the hot path (include/pga/core/{Subdivide,Repeat,
+ * ComponentSplit,Extrude,If,Generate,Discard}.cuh). */
+typedef enum PgaOperator {
+  PGA_OP_SUBDIVIDE = 0,        /* Subdivide<DynParams>: axis = p0, factors = p1.., successor j for factor j+1 */
+  PGA_OP_SUBDIVIDE_STATIC = 1, /* Subdivide<DynParam<0>, Pair<DynParam<k+1>, DCall<k>>...>: numChildren pairs, zero factors skipped */
+  PGA_OP_REPEAT = 2,           /* Repeat<false, DynParam<0> axis, DynParam<1> extent, DynParam<2> mode, DCall<0>> */
+  PGA_OP_COMPONENT_SPLIT = 3,  /* ComponentSplit<false, DCall<0> top, DCall<1> bottom, DCall<2> sides> (Box only) */
+  PGA_OP_EXTRUDE = 4,          /* Extrude<DynParam<0> axis (unused), DynParam<1> extent, DCall<0>> (Quad -> Box) */
+  PGA_OP_IF_SIZE_LESS = 5,     /* IfSizeLess<DynParam<0> axis, DynParam<1> size, DCall<0> true, DCall<1> false> */
+  PGA_OP_GENERATE = 6,         /* Generate<false, 1, DynParam<0> terminal index>: instanced terminal */
+  PGA_OP_DISCARD = 7           /* Discard */
+} PgaOperator;
+
+typedef enum PgaShape { PGA_SHAPE_BOX = 0, PGA_SHAPE_QUAD = 1 } PgaShape;
+
+/* One procedure of the procedure list: Proc<ShapeT, OperatorT, NumThreadsT>. */
+typedef struct PgaProc {
+  uint32_t op;           /* PgaOperator */
+  uint32_t shape;        /* PgaShape the procedure expects */
+  uint32_t numChildren;  /* PGA_OP_SUBDIVIDE_STATIC: number of Pair<> arguments; otherwise 0 */
+  uint32_t numThreads;   /* NumThreadsT; accepted and ignored (one thread per shape) */
+} PgaProc;
+
+typedef struct PgaRuleTable {
+  const PgaProc* procs;
+  uint32_t numProcs;
+  const PgaEntry* entries;
+  uint32_t numEntries;
+} PgaRuleTable;
+
+/* One axiom. Rotation is the identity, as for the reference's axiom generators
+ * (Grid.cuh:140-144, 199-204 set position, size, seed and custom attribute). */
+typedef struct PgaAxiom {
+  float position[3];
+  float seed;
+  float size[3];
+  float custom;
+  uint32_t entry;        /* root dispatch-table entry */
+  uint32_t shape;        /* PgaShape; must match the root procedure's shape */
+  uint32_t block;        /* parameter block used by PGA_PT_BLOCK parameters */
+  uint32_t flags;        /* reserved, 0 */
+} PgaAxiom;              /* 48 B */
+
+/* One instanced terminal, 64 B, written with four 16-byte stores. */
+typedef struct PgaTerminal {
+  float m[12];           /* row-major 3x4 of model4 * scale(size) */
+  uint32_t rule;         /* bits 0..23 entry of the Generate rule, bits 24..30 terminal (mesh) index, bit 31 = 1 for a Quad */
+  float custom;          /* custom attribute (attr1 of the instanced generation function) */
+  uint64_t path;         /* derivation-path hash */
+} PgaTerminal;
+
+typedef struct PgaEngineConfig {
+  uint64_t nodeCapacity;     /* non-terminal shapes held per derivation (queue storage) */
+  uint64_t maxTerminals;     /* sizes the LBVH / adjoint scratch */
+  uint32_t blockStride;      /* floats per parameter block (PGA_PT_BLOCK) */
+  uint32_t threadsPerBlock;  /* 0 = default */
+  uint32_t blocksPerSM;      /* 0 = occupancy maximum */
+  uint32_t recordTape;       /* 1 = keep the derivation tape so pga_adjoint can run */
+  uint32_t spinLimit;        /* iterations before a bounded wait gives up (0 = default) */
+  uint32_t maxLevels;        /* derivation depth limit (0 = default 4096) */
+  uint32_t flags;            /* reserved, 0 */
+  uint32_t reserved;
+} PgaEngineConfig;
+
+typedef enum PgaStatus {
+  PGA_OK = 0,
+  PGA_ERR_QUEUE_OVERFLOW = 1,   /* nodeCapacity too small */
+  PGA_ERR_OUTPUT_OVERFLOW = 2,  /* terminal capacity too small (the count keeps counting) */
+  PGA_ERR_TIMEOUT = 3,          /* a bounded wait ran out */
+  PGA_ERR_BAD_OPCODE = 4,       /* operatorCode / entry index out of range, or shape mismatch */
+  PGA_ERR_BAD_PARAM = 5,        /* an operator argument the reference rejects (e.g. Repeat extent <= 0) */
+  PGA_ERR_CUDA = 6,             /* a CUDA runtime call failed */
+  PGA_ERR_INVALID_ARGUMENT = 7, /* bad host-side argument */
+  PGA_ERR_NO_TAPE = 8,          /* pga_adjoint without a recorded tape */
+  PGA_ERR_DEPTH = 9             /* maxLevels exceeded (likely a recursive grammar) */
+} PgaStatus;
+
+/* Result of the last derivation, read back by pga_engine_sync_report. */
+typedef struct PgaDeriveReport {
+  int32_t status;            /* PgaStatus raised on the device (first error wins) */
+  int32_t detail;            /* entry index or level where it was raised */
+  uint64_t terminals;        /* terminals emitted (may exceed capacity on overflow) */
+  uint64_t nodes;            /* non-terminal shapes queued */
+  uint32_t levels;           /* derivation levels run */
+  uint32_t reserved;
+  uint64_t maxLevelNodes;    /* largest level */
+} PgaDeriveReport;
+
+typedef struct PgaBounds { float min[3]; float max[3]; } PgaBounds;
+
+/* LBVH over n terminals; every pointer is caller-owned device memory. */
+typedef struct PgaLbvh {
+  int32_t* nodes;            /* (n-1) x {parent, left, right}; child >= 0: leaf, < 0: -internal index (RadixTree.h:7-13) */
+  uint32_t* leafParents;     /* n */
+  float* aabbs;              /* (n-1) x {min xyz, max xyz} of internal nodes */
+  uint32_t* leafTerminal;    /* n: terminal index of leaf i (sorted order) */
+  uint64_t* keys;            /* n: sorted keys, morton30 << 34 | path >> 30 */
+} PgaLbvh;
+
+typedef struct PgaEngine PgaEngine;
+
+/* Library version string. */
+const char* pga_version(void);
+
+/* Message of the last host-side failure in this thread. */
+const char* pga_last_error(void);
+
+/* The generic procedure list used by the reference's interpreter-style grammars
+ * (src/interpreter/PGAFacade.cu, src/test_runner/MengerSponge.cuh:28-33),
+ * every argument a DynParam and every successor a DCall. Operator codes:
+ *   0 Box  Subdivide<DynParams>          1 Quad Subdivide<DynParams>
+ *   2 Box  Subdivide, 3 static pairs     3 Quad Subdivide, 3 static pairs
+ *   4 Box  Repeat                        5 Quad Repeat
+ *   6 Box  ComponentSplit                7 Quad Extrude
+ *   8 Box  IfSizeLess                    9 Quad IfSizeLess
+ *  10 Box  Generate (instanced)         11 Quad Generate (instanced)
+ *  12 Box  Discard                      13 Quad Discard */
+const PgaProc* pga_default_procs(uint32_t* numProcs);
+
+/* Replaces SinglePhaseEvaluator::initialize(DispatchTableEntry*, n)
+ * (include/pga/core/GPUEvaluator.cuh:475-506, CPUEvaluator.h:444-451):
+ * validates and lowers the table to the device rule table and allocates all
+ * work storage. No later call allocates device memory. */
+PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* config, PgaEngine** engine);
+
+/* Replaces SinglePhaseEvaluator::release() (GPUEvaluator.cuh:528-536). */
+PgaStatus pga_engine_destroy(PgaEngine* engine);
+
+/* Replaces SinglePhaseEvaluator::execute(numAxioms) (GPUEvaluator.cuh:508-521)
+ * for the batched persistent engine: derives every axiom in one persistent
+ * launch. dAxioms, dParamBlocks (may be NULL), dOut and dCount are device
+ * pointers; *dCount receives the number of terminals. Asynchronous on
+ * `stream`; capturable in a CUDA graph. */
+PgaStatus pga_derive(PgaEngine* engine, const PgaAxiom* dAxioms, uint32_t numAxioms,
+                     const float* dParamBlocks, PgaTerminal* dOut, uint64_t capacity,
+                     uint64_t* dCount, void* stream);
+
+/* The plain GPU form: one axiom (grammar) per launch sequence, one kernel
+ * launch per derivation level, the host reading the level size back each time.
+ * Same outputs as pga_derive; synchronous. */
+PgaStatus pga_derive_plain(PgaEngine* engine, const PgaAxiom* dAxioms, uint32_t numAxioms,
+                           const float* dParamBlocks, PgaTerminal* dOut, uint64_t capacity,
+                           uint64_t* dCount, void* stream);
+
+/* Synchronises `stream` and reports the device status of the last derivation. */
+PgaStatus pga_engine_sync_report(PgaEngine* engine, void* stream, PgaDeriveReport* report);
+
+/* Replaces ContextSensitivity::GPU::BVHConstructor::construct(min, max)
+ * (include/pga/core/GPUBVHConstructor.cuh:265-331), applied to terminal boxes:
+ * 30-bit Morton codes of the terminal centres in `bounds`, radix sort,
+ * Karras topology and bottom-up AABB refit. `bounds` is a host pointer. */
+PgaStatus pga_lbvh_build(PgaEngine* engine, const PgaTerminal* dTerminals, uint64_t n,
+                         const PgaBounds* bounds, const PgaLbvh* out, void* stream);
+
+/* Adjoint of the last pga_derive (recordTape = 1): dGradTerminals holds
+ * dL/dm (12 floats per terminal, same order as that derivation's output).
+ * Accumulates dL/dDynParam into dGradParams (numBlocks x blockStride; may be NULL)
+ * and dL/d(axiom size) into dGradAxiomSizes (3 per axiom; may be NULL).
+ * Both outputs are overwritten, not added to. No reference counterpart. */
+PgaStatus pga_adjoint(PgaEngine* engine, const float* dGradTerminals, float* dGradParams,
+                      uint32_t numBlocks, float* dGradAxiomSizes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PGA_GB300_H */

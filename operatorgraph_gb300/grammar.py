@@ -1,0 +1,212 @@
+"""Grammar-as-data: the reference's dispatch-table format, in numpy.
+
+Mirrors PGA::DispatchTable / DispatchTable::Entry / Parameter / Successor
+(include/pga/core/DispatchTable.h:16-106) and the POD DispatchTableEntry
+(include/pga/core/DispatchTableEntry.h:8-36).  Values are given as Python
+floats (doubles) and narrowed to float32 exactly like
+DispatchTable::Parameter::fill (DispatchTable.h:27-35, static_cast<float>).
+
+The numpy record layouts are byte-identical to the C structs of
+include/pga_gb300.h (PgaEntry, PgaProc, PgaAxiom, PgaTerminal).
+"""
+import struct
+
+import numpy as np
+
+MAX_PARAMS = 17
+MAX_VALUES = 16
+MAX_SUCC = 20
+
+# PGA::ParameterType (include/pga/core/ParameterType.h) plus the per-axiom block type.
+PT_SCALAR, PT_RAND, PT_SHAPE_ATTR, PT_EXP, PT_VEC2, PT_VEC4 = 0, 1, 2, 3, 4, 5
+PT_BLOCK = 16
+
+# PgaOperator
+OP_SUBDIVIDE, OP_SUBDIVIDE_STATIC, OP_REPEAT, OP_COMPONENT_SPLIT = 0, 1, 2, 3
+OP_EXTRUDE, OP_IF_SIZE_LESS, OP_GENERATE, OP_DISCARD = 4, 5, 6, 7
+OP_NAMES = ["Subdivide", "SubdivideStatic", "Repeat", "ComponentSplit", "Extrude", "IfSizeLess", "Generate", "Discard"]
+
+SHAPE_BOX, SHAPE_QUAD = 0, 1
+
+# PGA::RepeatMode (include/pga/core/RepeatMode.h)
+ANCHOR_TO_START, ANCHOR_TO_END, ADJUST_TO_FILL = 0, 1, 2
+
+# Operator codes of the generic procedure list (pga_default_procs()).
+BOX_SUBDIVIDE, QUAD_SUBDIVIDE = 0, 1
+BOX_SUBDIVIDE3, QUAD_SUBDIVIDE3 = 2, 3
+BOX_REPEAT, QUAD_REPEAT = 4, 5
+BOX_COMPONENT_SPLIT, QUAD_EXTRUDE = 6, 7
+BOX_IF_SIZE_LESS, QUAD_IF_SIZE_LESS = 8, 9
+BOX_GENERATE, QUAD_GENERATE = 10, 11
+BOX_DISCARD, QUAD_DISCARD = 12, 13
+
+PARAM_DT = np.dtype([("type", "<i4"), ("value", "<f4", (MAX_VALUES,))])
+SUCC_DT = np.dtype([("entryIndex", "<i4"), ("phaseIndex", "<i4")])
+ENTRY_DT = np.dtype([
+    ("operatorCode", "<i4"), ("numParameters", "<u4"), ("numSuccessors", "<u4"), ("reserved", "<u4"),
+    ("parameters", PARAM_DT, (MAX_PARAMS,)), ("successors", SUCC_DT, (MAX_SUCC,)),
+])
+PROC_DT = np.dtype([("op", "<u4"), ("shape", "<u4"), ("numChildren", "<u4"), ("numThreads", "<u4")])
+AXIOM_DT = np.dtype([
+    ("position", "<f4", (3,)), ("seed", "<f4"), ("size", "<f4", (3,)), ("custom", "<f4"),
+    ("entry", "<u4"), ("shape", "<u4"), ("block", "<u4"), ("flags", "<u4"),
+])
+TERMINAL_DT = np.dtype([("m", "<f4", (12,)), ("rule", "<u4"), ("custom", "<f4"), ("path", "<u8")])
+assert ENTRY_DT.itemsize == 1332 and AXIOM_DT.itemsize == 48 and TERMINAL_DT.itemsize == 64
+
+# The generic procedure list: (operator, shape, numChildren) per operator code.
+DEFAULT_PROCS = np.array([
+    (OP_SUBDIVIDE, SHAPE_BOX, 0, 1), (OP_SUBDIVIDE, SHAPE_QUAD, 0, 1),
+    (OP_SUBDIVIDE_STATIC, SHAPE_BOX, 3, 1), (OP_SUBDIVIDE_STATIC, SHAPE_QUAD, 3, 1),
+    (OP_REPEAT, SHAPE_BOX, 0, 1), (OP_REPEAT, SHAPE_QUAD, 0, 1),
+    (OP_COMPONENT_SPLIT, SHAPE_BOX, 0, 1), (OP_EXTRUDE, SHAPE_QUAD, 0, 1),
+    (OP_IF_SIZE_LESS, SHAPE_BOX, 0, 1), (OP_IF_SIZE_LESS, SHAPE_QUAD, 0, 1),
+    (OP_GENERATE, SHAPE_BOX, 0, 1), (OP_GENERATE, SHAPE_QUAD, 0, 1),
+    (OP_DISCARD, SHAPE_BOX, 0, 1), (OP_DISCARD, SHAPE_QUAD, 0, 1),
+], dtype=PROC_DT)
+
+
+class Parameter:
+    """DispatchTable::Parameter: a type and up to 16 values (doubles)."""
+
+    def __init__(self, type=PT_SCALAR, values=(0.0,)):
+        self.type = int(type)
+        self.values = [float(v) for v in values]
+        if len(self.values) > MAX_VALUES:
+            raise ValueError("values.size() > MaxNumParameterValues")
+
+
+class Successor:
+    def __init__(self, entryIndex=-1, phaseIndex=0):
+        self.entryIndex = int(entryIndex)
+        self.phaseIndex = int(phaseIndex)
+
+
+class Entry:
+    """DispatchTable::Entry: operator code, parameters and successors."""
+
+    def __init__(self, operatorCode, parameters=(), successors=()):
+        self.operatorCode = int(operatorCode)
+        self.parameters = [p if isinstance(p, Parameter) else Parameter(*p) for p in parameters]
+        self.successors = [s if isinstance(s, Successor) else Successor(*s) for s in successors]
+        if len(self.parameters) > MAX_PARAMS:
+            raise ValueError("parameters.size() > MaxNumParameters")
+        if len(self.successors) > MAX_SUCC:
+            raise ValueError("successors.size() > MaxNumSuccessors")
+
+
+class DispatchTable:
+    def __init__(self, entries=()):
+        self.entries = list(entries)
+
+    def __len__(self):
+        return len(self.entries)
+
+    def to_array(self):
+        """Like DispatchTable::toDispatchTableEntriesPtr (DispatchTable.h:98-104)."""
+        arr = np.zeros(len(self.entries), dtype=ENTRY_DT)
+        arr["successors"]["entryIndex"] = -1
+        arr["successors"]["phaseIndex"] = -1
+        for i, e in enumerate(self.entries):
+            arr[i]["operatorCode"] = e.operatorCode
+            arr[i]["numParameters"] = len(e.parameters)
+            arr[i]["numSuccessors"] = len(e.successors)
+            for k, p in enumerate(e.parameters):
+                arr[i]["parameters"][k]["type"] = p.type
+                vals = np.zeros(MAX_VALUES, dtype=np.float32)
+                vals[: len(p.values)] = np.array(p.values, dtype=np.float64).astype(np.float32)
+                arr[i]["parameters"][k]["value"] = vals
+            for k, s in enumerate(e.successors):
+                arr[i]["successors"][k]["entryIndex"] = s.entryIndex
+                arr[i]["successors"][k]["phaseIndex"] = s.phaseIndex
+        return arr
+
+
+def scalar(v):
+    return Parameter(PT_SCALAR, (v,))
+
+
+def shape_attr(i):
+    return Parameter(PT_SHAPE_ATTR, (i,))
+
+
+def rand(lo, hi):
+    return Parameter(PT_RAND, (lo, hi))
+
+
+def block(slot):
+    return Parameter(PT_BLOCK, (slot,))
+
+
+def make_axioms(n):
+    a = np.zeros(n, dtype=AXIOM_DT)
+    a["size"] = 1.0
+    a["block"] = np.arange(n, dtype=np.uint32)
+    return a
+
+
+def concat_tables(tables):
+    """Concatenate entry arrays, rebasing successor indices; returns (array, offsets)."""
+    offsets, parts, base = [], [], 0
+    for t in tables:
+        t = t.copy()
+        succ = t["successors"]["entryIndex"]
+        succ[succ >= 0] += base
+        t["successors"]["entryIndex"] = succ
+        offsets.append(base)
+        parts.append(t)
+        base += len(t)
+    return np.concatenate(parts), offsets
+
+
+def write_batch_file(path, entries, axioms):
+    """Grammar-batch file read by oracle/_ref/ref_harness and the oracle CLI."""
+    entries = np.ascontiguousarray(entries, dtype=ENTRY_DT)
+    axioms = np.ascontiguousarray(axioms, dtype=AXIOM_DT)
+    with open(path, "wb") as f:
+        f.write(b"PGAB" + struct.pack("<III", 1, len(entries), len(axioms)))
+        f.write(entries.tobytes())
+        f.write(axioms.tobytes())
+
+
+def read_terminal_file(path):
+    with open(path, "rb") as f:
+        head = f.read(16)
+        assert head[:4] == b"PGAT", head
+        (n,) = struct.unpack("<Q", head[8:16])
+        return np.frombuffer(f.read(n * TERMINAL_DT.itemsize), dtype=TERMINAL_DT).copy()
+
+
+def expand_blocks(entries, axioms, blocks, block_stride):
+    """Realise per-axiom parameter blocks as per-axiom copies of the table.
+
+    PGA_PT_BLOCK has no counterpart in the reference; for the reference's own
+    evaluator a batch with blocks becomes one table copy per axiom, with the
+    block values written in as PT_SCALAR and the axiom rooted in its copy.
+    """
+    n_e = len(entries)
+    out, ax = [], axioms.copy()
+    for i, a in enumerate(axioms):
+        t = entries.copy()
+        p = t["parameters"]
+        is_blk = p["type"] == PT_BLOCK
+        slots = p["value"][..., 0].astype(np.int64)
+        vals = blocks[int(a["block"]) * block_stride + slots]
+        p["value"][..., 0] = np.where(is_blk, vals, p["value"][..., 0])
+        p["type"] = np.where(is_blk, PT_SCALAR, p["type"])
+        t["parameters"] = p
+        succ = t["successors"]["entryIndex"]
+        succ[succ >= 0] += i * n_e
+        t["successors"]["entryIndex"] = succ
+        out.append(t)
+        ax[i]["entry"] = a["entry"] + i * n_e
+    return np.concatenate(out), ax
+
+
+def sort_terminals(t, by_path=False):
+    """Canonical order for multiset comparison (queue order is free)."""
+    if by_path:
+        return t[np.argsort(t["path"], kind="stable")]
+    m = t["m"].view(np.uint32)
+    keys = [t["custom"].view(np.uint32), t["rule"]] + [m[:, i] for i in range(11, -1, -1)]
+    return t[np.lexsort(keys)]

@@ -1,0 +1,241 @@
+"""Synthetic grammar batches (seeded) for the benchmark and parity workloads.
+
+All use the generic procedure list (grammar.DEFAULT_PROCS).  Each function
+returns a dict with ``entries`` (ENTRY_DT array), ``axioms`` (AXIOM_DT array),
+``blocks`` (float32 array or None) and ``block_stride``.
+
+* menger(threshold): the reference's Menger sponge scene
+  (src/test_runner/MengerSponge.cuh:28-45) on one unit box at the origin.
+  Threshold 0.05 -> depth 3 (8,000 terminals), 0.005 -> depth 5 (3.2M).
+* city(n): Quad footprints on a 64-wide grid (pitch 50 m), widths and depths
+  U[10, 40] m, heights LogN(ln 30, 0.5) clamped to [6, 300] m, drawn from
+  numpy default_rng(seed) in the order w, d, h.  Extrude to the height
+  (custom attribute, PT_SHAPE_ATTR 16), ComponentSplit, facades Repeat along Y
+  (3.0 m) and X (2.5 m), IfSizeLess(X, 1.2){Discard | Window}, windows
+  Subdivide X {0.2 | -1 | 0.2}.  Walls, windows and roofs are instanced
+  terminals.  Footprints lie in the XY plane; buildings rise along +Z.
+* facades(n): unit boxes with 16 per-axiom continuous parameters (8 split
+  ratios U[0.1, 0.9], 8 extents U[0.5, 2.0], default_rng(seed)) used as
+  relative Subdivide factors along Y and X; 8 x 8 cells, each ComponentSplit
+  into 4 sides (IfSizeLess guard) and a top halved along X: 384 terminals.
+* random_grammars(): 64-rule random grammars (branching U{2..6}, IfSizeLess
+  thresholds U[0.01, 0.2], Discard probability 0.15, depth cap 12).
+* mixed(n): 40 % Menger (depth 1-3), 40 % city buildings, 20 % random grammars.
+"""
+import math
+
+import numpy as np
+
+from . import grammar as G
+from .grammar import DispatchTable, Entry, block, scalar, shape_attr
+
+
+def _batch(entries, axioms, blocks=None, block_stride=0, name=""):
+    return {"entries": entries, "axioms": axioms, "blocks": blocks, "block_stride": block_stride, "name": name}
+
+
+def menger_table(threshold):
+    """The Menger sponge dispatch table (MengerSponge.cuh:35-45) on generic codes."""
+    S3, DIS, IFL, GEN = G.BOX_SUBDIVIDE3, G.BOX_DISCARD, G.BOX_IF_SIZE_LESS, G.BOX_GENERATE
+    rel = [scalar(-1), scalar(-1), scalar(-1)]
+    return DispatchTable([
+        Entry(IFL, [scalar(0), scalar(threshold)], [(1, 0), (2, 0)]),   # 0 A
+        Entry(GEN, [scalar(0)], []),                                     # 1 B (terminal)
+        Entry(S3, [scalar(0)] + rel, [(3, 0), (7, 0), (3, 0)]),          # 2 SubX
+        Entry(S3, [scalar(1)] + rel, [(4, 0), (5, 0), (4, 0)]),          # 3 SubY
+        Entry(S3, [scalar(2)] + rel, [(0, 0), (0, 0), (0, 0)]),          # 4 SubZ
+        Entry(S3, [scalar(2)] + rel, [(0, 0), (6, 0), (0, 0)]),          # 5 ZDiscard
+        Entry(DIS, [], []),                                              # 6
+        Entry(S3, [scalar(1)] + rel, [(5, 0), (8, 0), (5, 0)]),          # 7 YDiscard
+        Entry(DIS, [], []),                                              # 8
+    ]).to_array()
+
+
+def menger(threshold=0.05, n=1, seed=0.5):
+    ax = G.make_axioms(n)
+    ax["seed"] = seed
+    ax["custom"] = seed
+    ax["shape"] = G.SHAPE_BOX
+    ax["entry"] = 0
+    if n > 1:
+        cols = int(math.ceil(math.sqrt(n)))
+        i = np.arange(n)
+        ax["position"][:, 0] = 1.5 * (i % cols)
+        ax["position"][:, 2] = 1.5 * (i // cols)
+    return _batch(menger_table(threshold), ax, name=f"menger(threshold={threshold})")
+
+
+def building_table(mode=G.ANCHOR_TO_START):
+    """One city building: Extrude -> ComponentSplit -> Repeat Y -> Repeat X -> IfSizeLess -> Subdivide."""
+    return DispatchTable([
+        Entry(G.QUAD_EXTRUDE, [scalar(1), shape_attr(16)], [(1, 0)]),                      # 0 extrude to height
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(9, 0), (7, 0), (2, 0)]),                       # 1 top, bottom, sides
+        Entry(G.QUAD_REPEAT, [scalar(1), scalar(3.0), scalar(mode)], [(3, 0)]),           # 2 floors
+        Entry(G.QUAD_REPEAT, [scalar(0), scalar(2.5), scalar(mode)], [(4, 0)]),           # 3 tiles
+        Entry(G.QUAD_IF_SIZE_LESS, [scalar(0), scalar(1.2)], [(7, 0), (5, 0)]),           # 4 narrow tile?
+        Entry(G.QUAD_SUBDIVIDE, [scalar(0), scalar(0.2), scalar(-1), scalar(0.2)],
+              [(8, 0), (6, 0), (8, 0)]),                                                  # 5 window
+        Entry(G.QUAD_GENERATE, [scalar(1)], []),                                          # 6 window terminal
+        Entry(G.QUAD_DISCARD, [], []),                                                    # 7
+        Entry(G.QUAD_GENERATE, [scalar(0)], []),                                          # 8 wall terminal
+        Entry(G.QUAD_GENERATE, [scalar(2)], []),                                          # 9 roof terminal
+    ]).to_array()
+
+
+def building(w=25.0, d=20.0, h=31.0, mode=G.ANCHOR_TO_START):
+    ax = G.make_axioms(1)
+    ax["size"] = (w, d, 1.0)
+    ax["seed"] = 0.5
+    ax["custom"] = h
+    ax["shape"] = G.SHAPE_QUAD
+    return _batch(building_table(mode), ax, name="building")
+
+
+def city_axioms(n=4096, seed=1234, cols=64, pitch=50.0):
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(10.0, 40.0, n)
+    d = rng.uniform(10.0, 40.0, n)
+    h = np.clip(rng.lognormal(math.log(30.0), 0.5, n), 6.0, 300.0)
+    ax = G.make_axioms(n)
+    i = np.arange(n)
+    ax["position"][:, 0] = pitch * (i % cols)
+    ax["position"][:, 1] = pitch * (i // cols)
+    ax["size"][:, 0] = w
+    ax["size"][:, 1] = d
+    ax["size"][:, 2] = 1.0
+    ax["custom"] = h
+    ax["seed"] = 0.5
+    ax["shape"] = G.SHAPE_QUAD
+    ax["entry"] = 0
+    return ax
+
+
+def city(n=4096, seed=1234, mode=G.ANCHOR_TO_START):
+    return _batch(building_table(mode), city_axioms(n, seed), name=f"city({n})")
+
+
+FACADE_STRIDE = 16
+
+
+def facade_table():
+    BLK = [block(k) for k in range(16)]
+    return DispatchTable([
+        Entry(G.BOX_SUBDIVIDE, [scalar(1)] + BLK[0:8], [(1, 0)] * 8),        # 0 eight bands along Y
+        Entry(G.BOX_SUBDIVIDE, [scalar(0)] + BLK[8:16], [(2, 0)] * 8),       # 1 eight cells along X
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(3, 0), (4, 0), (5, 0)]),          # 2 top, bottom, sides
+        Entry(G.QUAD_SUBDIVIDE, [scalar(0), scalar(-1), scalar(-1)], [(6, 0), (6, 0)]),  # 3 top halves
+        Entry(G.QUAD_DISCARD, [], []),                                       # 4
+        Entry(G.QUAD_IF_SIZE_LESS, [scalar(0), scalar(0.01)], [(4, 0), (6, 0)]),          # 5 side guard
+        Entry(G.QUAD_GENERATE, [scalar(0)], []),                             # 6 terminal
+    ]).to_array()
+
+
+def facade_params(n=1024, seed=7):
+    rng = np.random.default_rng(seed)
+    ratios = rng.uniform(0.1, 0.9, (n, 8))
+    extents = rng.uniform(0.5, 2.0, (n, 8))
+    # Negative factors are relative shares (Subdivide.cuh:196-205).
+    return np.concatenate([-ratios, -extents], axis=1).astype(np.float32)
+
+
+def facades(n=1024, seed=7):
+    ax = G.make_axioms(n)
+    cols = int(math.ceil(math.sqrt(n)))
+    i = np.arange(n)
+    ax["position"][:, 0] = 2.0 * (i % cols)
+    ax["position"][:, 2] = 2.0 * (i // cols)
+    ax["seed"] = 0.5
+    ax["shape"] = G.SHAPE_BOX
+    ax["entry"] = 0
+    blocks = facade_params(n, seed).reshape(-1)
+    return _batch(facade_table(), ax, blocks, FACADE_STRIDE, name=f"facades({n})")
+
+
+def facade_target_params(params, seed=8, sigma=0.02):
+    """Target parameters: each parameter perturbed by N(0, sigma), clamped so the
+    relative factors keep their sign (no branch or count can change)."""
+    rng = np.random.default_rng(seed)
+    p = params.reshape(-1, FACADE_STRIDE).astype(np.float64)
+    q = p + rng.normal(0.0, sigma, p.shape)
+    q = np.minimum(q, -0.05)
+    return q.astype(np.float32).reshape(-1)
+
+
+def random_grammar_table(rng, num_rules=64, depth_cap=12):
+    """A random grammar of `num_rules` rules arranged in `depth_cap` levels.
+
+    Rule r (two entries): IfSizeLess(axis, t ~ U[0.01, 0.2]) { terminal |
+    Subdivide<DynParams>(axis', k ~ U{2..6} relative factors) }, each child slot a
+    Discard with probability 0.15, else a rule of the next level (a terminal at
+    the last level).
+    """
+    levels = np.sort(rng.integers(0, depth_cap, num_rules))
+    levels[0] = 0
+    levels = np.sort(levels)
+    by_level = [np.nonzero(levels == L)[0] for L in range(depth_cap)]
+    GEN, DIS = 2 * num_rules, 2 * num_rules + 1
+    entries = [None] * (2 * num_rules + 2)
+    for r in range(num_rules):
+        L = levels[r]
+        axis_t = int(rng.integers(0, 3))
+        thr = float(rng.uniform(0.01, 0.2))
+        entries[2 * r] = Entry(G.BOX_IF_SIZE_LESS, [scalar(axis_t), scalar(thr)], [(GEN, 0), (2 * r + 1, 0)])
+        k = int(rng.integers(2, 7))
+        axis_s = int(rng.integers(0, 3))
+        factors = [scalar(-float(rng.uniform(0.5, 1.5))) for _ in range(k)]
+        succ = []
+        nxt = [i for i in range(L + 1, depth_cap) if len(by_level[i])]
+        for _ in range(k):
+            if rng.random() < 0.15:
+                succ.append((DIS, 0))
+            elif not nxt:
+                succ.append((GEN, 0))
+            else:
+                cand = by_level[nxt[0]]
+                succ.append((2 * int(cand[rng.integers(0, len(cand))]), 0))
+        entries[2 * r + 1] = Entry(G.BOX_SUBDIVIDE, [scalar(axis_s)] + factors, succ)
+    entries[GEN] = Entry(G.BOX_GENERATE, [scalar(3)], [])
+    entries[DIS] = Entry(G.BOX_DISCARD, [], [])
+    return DispatchTable(entries).to_array()
+
+
+def random_grammars(num_grammars=16, seed=99):
+    rng = np.random.default_rng(seed)
+    tables = [random_grammar_table(rng) for _ in range(num_grammars)]
+    return tables
+
+
+def mixed(n=65536, seed=99, menger_depths=(1, 2, 3), num_random_grammars=16):
+    """Heterogeneous batch: 40 % Menger, 40 % buildings, 20 % random grammars."""
+    rng = np.random.default_rng(seed)
+    thresholds = {1: 0.5, 2: 0.15, 3: 0.05, 4: 0.015, 5: 0.005}
+    menger_tables = [menger_table(thresholds[d]) for d in menger_depths]
+    rand_tables = random_grammars(num_random_grammars, seed)
+    tables = menger_tables + [building_table()] + rand_tables
+    entries, offs = G.concat_tables(tables)
+    kind = rng.choice(3, size=n, p=[0.4, 0.4, 0.2])
+    ax = G.make_axioms(n)
+    cols = int(math.ceil(math.sqrt(n)))
+    i = np.arange(n)
+    ax["position"][:, 0] = 50.0 * (i % cols)
+    ax["position"][:, 1] = 50.0 * (i // cols)
+    ax["seed"] = 0.5
+    city_ax = city_axioms(n, seed + 1, cols=cols)
+    depth_pick = rng.integers(0, len(menger_depths), n)
+    rand_pick = rng.integers(0, num_random_grammars, n)
+    b_off = offs[len(menger_tables)]
+    for j in range(n):
+        if kind[j] == 0:
+            ax[j]["shape"] = G.SHAPE_BOX
+            ax[j]["entry"] = offs[depth_pick[j]]
+            ax[j]["size"] = (1.0, 1.0, 1.0)
+        elif kind[j] == 1:
+            ax[j]["shape"] = G.SHAPE_QUAD
+            ax[j]["entry"] = b_off
+            ax[j]["size"] = city_ax[j]["size"]
+            ax[j]["custom"] = city_ax[j]["custom"]
+        else:
+            ax[j]["shape"] = G.SHAPE_BOX
+            ax[j]["entry"] = offs[len(menger_tables) + 1 + rand_pick[j]]
+            ax[j]["size"] = (1.0, 1.0, 1.0)
+    return _batch(entries, ax, name=f"mixed({n})")

@@ -1,0 +1,218 @@
+// Test infrastructure (a checker), never part of the product.
+//
+// Harness around the reference's OWN host-side derivation path:
+// PGA::CPU::SinglePhaseEvaluator (include/pga/core/CPUEvaluator.h:393-459)
+// running the reference's __host__ __device__ operator templates on the CPU.
+// It is compiled by oracle/make_ref.py against a patched shadow copy of the
+// reference headers (oracle/_ref/shadow, git-ignored).
+//
+// Input  (argv[1]): a grammar batch, format written by
+//                   operatorgraph_gb300/grammar.py::write_batch_file
+// Output (argv[2]): terminal records, 64 B each (same layout as PgaTerminal in
+//                   include/pga_gb300.h, path hash left 0 because the reference
+//                   has no derivation-path hash)
+// argv[3] (optional): number of timed repetitions of execute().
+//
+// The procedure list is the generic "interpreter style" list: one procedure per
+// (operator, shape) with every argument a DynParam and every successor a DCall,
+// as in src/interpreter/PGAFacade.cu and src/test_runner/MengerSponge.cuh:28-33.
+// Its indices are the operator codes that the grammar batch uses and that
+// pga_default_procs() in the product exposes.
+#define PGA_CORE_EXPORT 0
+#include <cuda_runtime_api.h>
+#include <pga/core/CPUEvaluator.h>
+#include <pga/core/ComponentSplit.cuh>
+#include <pga/core/Discard.cuh>
+#include <pga/core/DispatchTable.h>
+#include <pga/core/Extrude.cuh>
+#include <pga/core/Generate.cuh>
+#include <pga/core/If.cuh>
+#include <pga/core/Proc.cuh>
+#include <pga/core/Repeat.cuh>
+#include <pga/core/ShapeGenerator.cuh>
+#include <pga/core/Subdivide.cuh>
+#include <pga/core/TStdLib.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+using namespace PGA;
+using namespace PGA::Operators;
+using namespace PGA::Shapes;
+using namespace PGA::Parameters;
+
+struct HarnessFilter;
+
+struct HarnessTerminal {
+  float m[12];
+  uint32_t rule;
+  float custom;
+  uint64_t path;
+};
+static_assert(sizeof(HarnessTerminal) == 64, "terminal record must be 64 B");
+
+static std::vector<HarnessTerminal> g_terminals;
+
+template <typename ShapeT> struct IsQuadShape { static const uint32_t value = 0; };
+template <> struct IsQuadShape<Quad> { static const uint32_t value = 1; };
+
+namespace PGA {
+// Instanced terminal emission, mirroring GenerationFunction<GenFuncFilter, 1>::perShape
+// (include/pga/rendering/GenerationFunctions.cuh:158-188): model4 * scale(size)
+// (kept row-major here, not transposed) plus the custom attribute (attr1).
+template <> struct GenerationFunction<HarnessFilter, 1> {
+  template <typename ShapeT, typename... ArgsT>
+  static void perShape(ShapeT& shape, unsigned int terminalIndex, float attr1, ArgsT...) {
+    math::float4x4 M = shape.getModel4() * math::float4x4::scale(shape.getSize());
+    HarnessTerminal t;
+    t.m[0] = M._11; t.m[1] = M._12; t.m[2] = M._13; t.m[3] = M._14;
+    t.m[4] = M._21; t.m[5] = M._22; t.m[6] = M._23; t.m[7] = M._24;
+    t.m[8] = M._31; t.m[9] = M._32; t.m[10] = M._33; t.m[11] = M._34;
+    // The shape handed to perShape is the base sub-object of the Symbol that
+    // Generate dispatched (CPUEvaluator.h:268-276), so its entry index is
+    // reachable through the derived type.
+    int entry = static_cast<Symbol<ShapeT>&>(shape).entryIndex;
+    t.rule = (uint32_t(entry) & 0xFFFFFFu) | ((terminalIndex & 0x7Fu) << 24) | (IsQuadShape<ShapeT>::value << 31);
+    t.custom = attr1;
+    t.path = 0;
+    g_terminals.push_back(t);
+  }
+  template <typename ShapeT, typename... ArgsT> static unsigned int allocateVertices(ShapeT&, unsigned int, ArgsT...) { return 0; }
+  template <typename... ArgsT> static void perVertex(unsigned int, const math::float4&, const math::float3&, const math::float2&, unsigned int, ArgsT...) {}
+  template <typename ShapeT, typename... ArgsT> static unsigned int allocateIndices(ShapeT&, unsigned int, ArgsT...) { return 0; }
+  template <typename... ArgsT> static void perTriangle(unsigned int, unsigned int, unsigned int, unsigned int, unsigned int, ArgsT...) {}
+};
+}  // namespace PGA
+
+// Operator codes 0..13 (see pga_default_procs() in include/pga_gb300.h).
+struct HarnessProcs : T::List<
+  /* 0 */ Proc<Box, Subdivide<DynParams>, 1>,
+  /* 1 */ Proc<Quad, Subdivide<DynParams>, 1>,
+  /* 2 */ Proc<Box, Subdivide<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>, T::Pair<DynParam<3>, DCall<2>>>, 1>,
+  /* 3 */ Proc<Quad, Subdivide<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>, T::Pair<DynParam<3>, DCall<2>>>, 1>,
+  /* 4 */ Proc<Box, Repeat<false, DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 5 */ Proc<Quad, Repeat<false, DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 6 */ Proc<Box, ComponentSplit<false, DCall<0>, DCall<1>, DCall<2>>, 1>,
+  /* 7 */ Proc<Quad, Extrude<DynParam<0>, DynParam<1>, DCall<0>>, 1>,
+  /* 8 */ Proc<Box, IfSizeLess<DynParam<0>, DynParam<1>, DCall<0>, DCall<1>>, 1>,
+  /* 9 */ Proc<Quad, IfSizeLess<DynParam<0>, DynParam<1>, DCall<0>, DCall<1>>, 1>,
+  /* 10 */ Proc<Box, Generate<false, 1, DynParam<0>>, 1>,
+  /* 11 */ Proc<Quad, Generate<false, 1, DynParam<0>>, 1>,
+  /* 12 */ Proc<Box, Discard, 1>,
+  /* 13 */ Proc<Quad, Discard, 1>
+> {};
+
+#pragma pack(push, 1)
+struct FileHeader { char magic[4]; uint32_t version, nEntries, nAxioms; };
+struct FileParam { int32_t type; float value[16]; };
+struct FileSucc { int32_t entry, phase; };
+struct FileEntry { int32_t opcode; uint32_t nParams, nSucc, pad; FileParam params[17]; FileSucc succ[20]; };
+struct FileAxiom { float position[3]; float seed; float size[3]; float custom; uint32_t entry, shape, block, flags; };
+#pragma pack(pop)
+static_assert(sizeof(FileEntry) == 1332, "entry size");
+static_assert(sizeof(FileAxiom) == 48, "axiom size");
+
+static std::vector<FileAxiom> g_axioms;
+
+struct HarnessAxioms {
+  static unsigned int getNumAxioms() { return (unsigned int)g_axioms.size(); }
+  template <typename SymbolManagerT, typename QueueT>
+  static void generateAxiom(int id, QueueT* queue) {
+    const FileAxiom& a = g_axioms[id];
+    if (a.shape == 1) {
+      Quad q;
+      q.setSize(math::float3(a.size[0], a.size[1], a.size[2]));
+      q.setPosition(math::float3(a.position[0], a.position[1], a.position[2]));
+      q.setSeed(a.seed);
+      q.setCustomAttribute(a.custom);
+      SymbolManagerT::dispatchAxiom(q, (int)a.entry, queue);
+    } else {
+      Box b;
+      b.setSize(math::float3(a.size[0], a.size[1], a.size[2]));
+      b.setPosition(math::float3(a.position[0], a.position[1], a.position[2]));
+      b.setSeed(a.seed);
+      b.setCustomAttribute(a.custom);
+      SymbolManagerT::dispatchAxiom(b, (int)a.entry, queue);
+    }
+  }
+};
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    fprintf(stderr, "usage: ref_harness <batch.bin> <terminals.bin> [repeats]\n");
+    return 2;
+  }
+  int repeats = argc > 3 ? atoi(argv[3]) : 1;
+  FILE* f = fopen(argv[1], "rb");
+  if (!f) { perror("open input"); return 2; }
+  FileHeader h;
+  if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, "PGAB", 4) != 0) { fprintf(stderr, "bad header\n"); return 2; }
+  std::vector<FileEntry> entries(h.nEntries);
+  g_axioms.resize(h.nAxioms);
+  if (fread(entries.data(), sizeof(FileEntry), h.nEntries, f) != h.nEntries ||
+      fread(g_axioms.data(), sizeof(FileAxiom), h.nAxioms, f) != h.nAxioms) {
+    fprintf(stderr, "truncated input\n");
+    return 2;
+  }
+  fclose(f);
+
+  // Build the reference's own DispatchTableEntry array (DispatchTableEntry.h:8-36).
+  std::vector<DispatchTableEntry> table(h.nEntries);
+  for (uint32_t i = 0; i < h.nEntries; i++) {
+    DispatchTableEntry& e = table[i];
+    memset(&e, 0, sizeof e);
+    e.operatorCode = entries[i].opcode;
+    e.numParameters = entries[i].nParams;
+    for (uint32_t p = 0; p < 17; p++) {
+      e.parameters[p].type = (ParameterType)entries[i].params[p].type;
+      for (int v = 0; v < 16; v++) e.parameters[p].value[v] = entries[i].params[p].value[v];
+    }
+    e.numSuccessors = entries[i].nSucc;
+    for (uint32_t s = 0; s < 20; s++) {
+      e.successors[s].entryIndex = s < entries[i].nSucc ? entries[i].succ[s].entry : -1;
+      e.successors[s].phaseIndex = s < entries[i].nSucc ? entries[i].succ[s].phase : -1;
+    }
+    e.numEdgeIndices = 0;
+    for (int s = 0; s < 20; s++) e.edgeIndices[s] = -1;
+    e.subGraphIndex = -1;
+  }
+
+  std::vector<double> times;
+  int rc = 0;
+  for (int r = 0; r < repeats; r++) {
+    g_terminals.clear();
+    g_terminals.reserve(1 << 20);
+    CPU::SinglePhaseEvaluator<HarnessProcs, HarnessAxioms, HarnessFilter> ev;
+    ev.initialize(table.data(), table.size());
+    try {
+      auto t0 = std::chrono::steady_clock::now();
+      ev.execute();
+      auto t1 = std::chrono::steady_clock::now();
+      times.push_back(std::chrono::duration<double>(t1 - t0).count());
+    } catch (const std::exception& ex) {
+      fprintf(stderr, "reference threw: %s\n", ex.what());
+      rc = 3;
+    }
+    ev.release();
+    if (rc) break;
+  }
+  FILE* o = fopen(argv[2], "wb");
+  if (!o) { perror("open output"); return 2; }
+  uint64_t n = g_terminals.size();
+  fwrite("PGAT", 1, 4, o);
+  uint32_t zero = 0;
+  fwrite(&zero, 4, 1, o);
+  fwrite(&n, 8, 1, o);
+  fwrite(g_terminals.data(), sizeof(HarnessTerminal), n, o);
+  fclose(o);
+  std::sort(times.begin(), times.end());
+  double med = times.empty() ? 0.0 : times[times.size() / 2];
+  printf("{\"terminals\": %llu, \"seconds\": %.9g, \"repeats\": %d, \"status\": %d}\n",
+         (unsigned long long)n, med, (int)times.size(), rc);
+  return rc;
+}
