@@ -1,0 +1,425 @@
+#!/usr/bin/env python3
+"""Benchmark: terminals/s of the batched persistent derivation engine.
+
+Workload (one step): the 4096-building procedural city (Quad footprints on a
+64 x 64 grid, seed 1234; Extrude, ComponentSplit, Repeat floors/tiles,
+IfSizeLess, window Subdivide) derived in one pga_derive call -> 5,856,274
+instanced terminals (375 MB of 64-byte records, larger than the 129 MB L2;
+L2 is also flushed with a 256 MB write before every timed step).
+
+value  : terminals/s with axioms and grammar resident in HBM (CUDA events on
+         the launching stream around pga_derive).
+e2e    : the same through the C ABI with host buffers: pinned-host -> device
+         copy of the axioms, derivation, device -> pinned-host copy of the
+         count and of every terminal record, all inside the timed region.
+roofline: algorithmic bytes of the derivation kernel (64 B per terminal
+         written + 48 B per axiom read) / kernel time, against the measured
+         HBM copy bandwidth.
+extra  : the plain one-grammar-per-launch GPU form on the same city, the
+         Menger sponge at depth 5 and the LBVH over the city's terminals.
+
+`--impl reference` times the reference's own CPU derivation (oracle/_ref,
+built from the reference sources) on the same workload, sharded by axiom
+ranges over all host cores.
+
+Synthetic data: every input is generated from fixed seeds.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from operatorgraph_gb300 import grammar as G  # noqa: E402
+from operatorgraph_gb300 import scenes  # noqa: E402
+
+METRIC = "terminals/s (batched persistent derivation, 4096-building city)"
+UNIT = "terminals/s"
+WORKLOAD = {"workload": "city-4096 (64x64 grid, seed 1234, Repeat anchor-to-start)", "axioms": 4096,
+            "terminals": 5856274, "l2": "256 MB flush before each timed step; outputs 375 MB > L2"}
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def read_profile_traffic(name):
+    """Per-launch DRAM bytes recorded from an ncu capture under profiles/."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def host_info():
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except AttributeError:
+        cores = os.cpu_count()
+    model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    import platform
+
+    return cores, f"{platform.machine()} {model}".strip()
+
+
+# ------------------------------------------------------------- CPU reference
+
+
+def ref_harness_available():
+    import oracle
+
+    if os.path.exists(oracle.REF_HARNESS):
+        return oracle.REF_HARNESS
+    return oracle.build_ref()
+
+
+def run_reference_sharded(batch, shards, repeats=1):
+    """Runs the reference's CPU evaluator on `shards` axiom ranges in parallel
+    processes; returns (terminals, wall seconds of the slowest shard's median)."""
+    import oracle
+
+    harness = ref_harness_available()
+    tmp = tempfile.mkdtemp()
+    ax = batch["axioms"]
+    parts = np.array_split(np.arange(len(ax)), shards)
+    procs = []
+    t0 = time.perf_counter()
+    for k, idx in enumerate(parts):
+        bf = os.path.join(tmp, f"b{k}.bin")
+        G.write_batch_file(bf, batch["entries"], ax[idx])
+        procs.append(subprocess.Popen([harness, bf, os.path.join(tmp, f"t{k}.bin"), str(repeats)],
+                                      stdout=subprocess.PIPE, text=True))
+    total, secs = 0, []
+    for p in procs:
+        out, _ = p.communicate()
+        d = json.loads(out.strip().splitlines()[-1])
+        total += d["terminals"]
+        secs.append(d["seconds"])
+    wall = time.perf_counter() - t0
+    return total, max(secs), wall
+
+
+def cpu_baseline_single(batch):
+    """The reference's own CPU evaluator, 1 thread, on a bounded sample."""
+    cores, model = host_info()
+    try:
+        ref_harness_available()
+        n, secs, _ = run_reference_sharded(batch, 1, repeats=3)
+        return {"value": n / secs, "unit": UNIT, "cores": 1, "kind": "reference",
+                "sample": f"full city-4096 ({n} terminals), median of 3 execute() calls, 1 thread, {model}"}
+    except Exception:
+        import oracle
+
+        t0 = time.perf_counter()
+        t = oracle.derive(G.DEFAULT_PROCS, batch["entries"], batch["axioms"])
+        secs = time.perf_counter() - t0
+        return {"value": len(t) / secs, "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": f"full city-4096 ({len(t)} terminals), oracle restatement, 1 thread, {model}"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    batch = scenes.city(4096)
+    cores, model = host_info()
+    kind = "reference"
+    try:
+        ref_harness_available()
+    except Exception:
+        kind = "port"
+    if kind == "port":
+        print(json.dumps({"impl": "reference", "unavailable": "reference CPU evaluator could not be built here"}))
+        return
+    for _ in range(args.warmup):
+        run_reference_sharded(batch, cores)
+    times, total = [], 0
+    for _ in range(args.steps):
+        n, _, wall = run_reference_sharded(batch, cores)
+        times.append(wall)
+        total = n
+    mean = sum(times) / len(times)
+    value = total / mean
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": WORKLOAD, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"full city-4096 per step, {cores} axiom shards in parallel processes "
+                                       f"(wall time incl. process start), {model}"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU arm
+
+
+def our_arm(args):
+    import torch
+
+    from operatorgraph_gb300 import build as B
+    from operatorgraph_gb300.engine import Engine, load_library
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    if not B.up_to_date():
+        B.build()
+    load_library()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+
+    batch = scenes.city(4096)
+    n_ax = len(batch["axioms"])
+    cap = 6_000_000
+    eng = Engine(batch["entries"], node_capacity=1 << 22, max_terminals=cap)
+    d_ax = torch.from_numpy(batch["axioms"].view(np.uint8).copy()).to(dev)
+    out = torch.empty((cap, 64), dtype=torch.uint8, device=dev)
+    count = torch.zeros(1, dtype=torch.int64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        eng.derive_raw(d_ax.data_ptr(), n_ax, None, out.data_ptr(), cap, count.data_ptr())
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    rep = eng.report()
+    assert rep["status"] == 0, rep
+    n_term = int(count.item())
+    assert n_term == WORKLOAD["terminals"], n_term
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timing (value, roofline)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        barrier()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            evs[k][0].record(stream)
+            step()
+            evs[k][1].record(stream)
+        barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n_term / (ms * 1e-3)
+
+    # ---- end-to-end through the C ABI with host buffers
+    h_ax = torch.from_numpy(batch["axioms"].view(np.uint8).copy()).pin_memory()
+    h_out = torch.empty((n_term, 64), dtype=torch.uint8).pin_memory()
+    h_cnt = torch.empty(1, dtype=torch.int64).pin_memory()
+    d_ax2 = torch.empty_like(d_ax)
+
+    def e2e_step():
+        d_ax2.copy_(h_ax, non_blocking=True)
+        eng.derive_raw(d_ax2.data_ptr(), n_ax, None, out.data_ptr(), cap, count.data_ptr())
+        h_cnt.copy_(count, non_blocking=True)
+        h_out.copy_(out[:n_term], non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    e2e_steps = max(1, min(args.steps, 10))
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    assert int(h_cnt.item()) == n_term
+    e2e_value = world * n_term / (e2e_ms * 1e-3)
+
+    line = None
+    if rank == 0:
+        peak, peak_kind = read_peaks()
+        alg_bytes = 64.0 * n_term + 48.0 * n_ax
+        achieved = alg_bytes / (ms * 1e-3) / 1e9
+        traffic = read_profile_traffic("k_derive_persistent_city4096.md")
+        extra = extras(eng, batch, out, n_term, dev, stream, flush)
+        cores, model = host_info()
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": WORKLOAD,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h_ax.numel()),
+                    "d2h_bytes_per_step": int(h_out.numel() + h_cnt.numel() * 8), "ms_per_step": e2e_ms},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_derive_persistent", "algorithmic_bytes": alg_bytes},
+            "gpu_launches": args.steps,
+            "clocks": clocks.summary(),
+            "extra": extra,
+            "cpu_baseline": cpu_baseline_single(batch),
+            "host": {"cores": cores, "cpu": model},
+        }
+    eng.release()
+    if line is not None:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def extras(eng, batch, out, n_term, dev, stream, flush):
+    """Plain GPU form, Menger depth 5 and LBVH timings (reported beside the headline)."""
+    import torch
+
+    from operatorgraph_gb300.engine import Engine
+
+    res = {}
+    n_ax = len(batch["axioms"])
+    d_ax = torch.from_numpy(batch["axioms"].view(np.uint8).copy()).to(dev)
+    count = torch.zeros(1, dtype=torch.int64, device=dev)
+    # Plain form: one grammar (axiom) per launch sequence, host-driven levels.
+    eng.derive_raw(d_ax.data_ptr(), n_ax, None, out.data_ptr(), out.shape[0], count.data_ptr(), plain=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.derive_raw(d_ax.data_ptr(), n_ax, None, out.data_ptr(), out.shape[0], count.data_ptr(), plain=True)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    assert int(count.item()) == n_term
+    res["plain_city_terminals_per_s"] = n_term / plain_s
+    # Restore the batched output for the LBVH below.
+    eng.derive_raw(d_ax.data_ptr(), n_ax, None, out.data_ptr(), out.shape[0], count.data_ptr())
+    torch.cuda.synchronize()
+    # LBVH over the city's terminals.
+    bounds = (-50.0, -50.0, -1.0, 3250.0, 3250.0, 400.0)
+    for _ in range(2):
+        eng.lbvh(out, n_term, bounds)
+    ts = []
+    for _ in range(5):
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.lbvh(out, n_term, bounds)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    lb = statistics.median(ts)
+    res["lbvh_city_ms"] = lb
+    res["lbvh_city_leaves_per_s"] = n_term / (lb * 1e-3)
+    # Menger sponge, depth 5 (3.2M terminals), one axiom in one launch.
+    m = scenes.menger(0.005)
+    em = Engine(m["entries"], node_capacity=1 << 22, max_terminals=4_000_000)
+    d_m = torch.from_numpy(m["axioms"].view(np.uint8).copy()).to(dev)
+    for _ in range(3):
+        em.derive_raw(d_m.data_ptr(), 1, None, out.data_ptr(), out.shape[0], count.data_ptr())
+    ts = []
+    for _ in range(5):
+        flush.fill_(2)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        em.derive_raw(d_m.data_ptr(), 1, None, out.data_ptr(), out.shape[0], count.data_ptr())
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    assert int(count.item()) == 3_200_000
+    res["menger_d5_ms"] = statistics.median(ts)
+    res["menger_d5_terminals_per_s"] = 3.2e6 / (res["menger_d5_ms"] * 1e-3)
+    em.release()
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        our_arm(args)
+
+
+if __name__ == "__main__":
+    main()

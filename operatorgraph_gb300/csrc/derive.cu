@@ -1,0 +1,915 @@
+// Derivation kernels and the engine's C ABI (creation, derive, report).
+//
+// Work model: level-synchronous expansion.  A level is the set of queued
+// shapes whose rule branches (Subdivide, Repeat, ComponentSplit); one thread
+// executes one shape's operator and produces its children in order.  Each child
+// is then resolved in the same thread through its chain of 1 -> 1 rules
+// (IfSizeLess, Extrude), and ends as a terminal (Generate: written out
+// directly), a discard, or a queued shape of the next level.  Terminals and
+// queued shapes are appended with one atomic per warp (ballot + popc), so each
+// warp writes contiguous 64-byte terminal records and 80-byte shape records.
+//
+// pga_derive runs every level of every axiom in ONE persistent cooperative
+// launch (a bounded grid barrier between levels, warps pulling 32 shapes at a
+// time from a level cursor); pga_derive_plain is the plain GPU form: one axiom
+// at a time, one launch per level, the host reading each level's size back.
+//
+// The reference executes the same operators from per-procedure queues in a
+// Whippletree megakernel (deps/whippletree/include/techniqueMegakernel.cuh:374-473)
+// or from std::deque queues on the host (include/pga/core/CPUEvaluator.h:38-76);
+// the order in which shapes are processed is free in both, so outputs are
+// compared as multisets.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine_host.h"
+
+namespace pga {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+enum Kind { kNone = 0, kTerm = 1, kNode = 2 };
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ------------------------------------------------------------- parameters
+
+__device__ __forceinline__ float eval_param(const DeriveArgs& a, const DevParam& p, const Shape& x) {
+  switch (p.type) {
+    case PGA_PT_SCALAR:
+      return p.v0;
+    case PGA_PT_RAND:
+      return rand_range(x.seed, p.v0, p.v1);
+    case PGA_PT_SHAPE_ATTR: {
+      uint32_t i = f2u(p.v0);
+      float custom = (i == 16) ? __ldg(&a.axioms[x.axiom].custom) : 0.0f;
+      return shape_attr(x, i, custom);
+    }
+    case PGA_PT_EXP:
+      return eval_exp(a.tab.expPool + p.aux, x, __ldg(&a.axioms[x.axiom].custom), a.st);
+    case PGA_PT_BLOCK: {
+      uint32_t slot = f2u(p.v0);
+      if (a.blocks == nullptr || slot >= a.blockStride) {
+        raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+        return 0.0f;
+      }
+      uint32_t b = __ldg(&a.axioms[x.axiom].block);
+      return __ldg(&a.blocks[(size_t)b * a.blockStride + slot]);
+    }
+    default:
+      return 0.0f;  // unknown types evaluate to 0 (Parameters.cuh:697-709 without invariant checks)
+  }
+}
+
+__device__ __forceinline__ float param(const DeriveArgs& a, const DevRule& r, uint32_t k, const Shape& x) {
+  DevParam p = a.tab.params[r.paramBase + k];
+  return eval_param(a, p, x);
+}
+
+__device__ __forceinline__ bool axis_param(const DeriveArgs& a, const DevRule& r, const Shape& x, uint32_t& axis) {
+  axis = f2u(param(a, r, 0, x));
+  if (axis > 2) {
+    raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+    return false;
+  }
+  return true;
+}
+
+// Translation by o along model axis `ax`: t' = fl(fl(R[:,ax] * o) + t).
+__device__ __forceinline__ void translate_axis(Shape& y, const Shape& x, uint32_t ax, float o) {
+#pragma unroll
+  for (int i = 0; i < 3; i++) y.t[i] = __fadd_rn(__fmul_rn(pick3(x.r[i], ax), o), x.t[i]);
+}
+
+// ------------------------------------------------- 1 -> 1 chain resolution
+
+// Resolves a freshly created shape through IfSizeLess / Extrude rules
+// (If.cuh:65-89, Extrude.cuh:29-56) until it reaches a Generate (terminal),
+// a Discard, or a branching rule (queued).
+__device__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
+  for (int step = 0; step < kMaxChain; step++) {
+    if (x.entry < 0 || (uint32_t)x.entry >= a.tab.numEntries) {
+      raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry);
+      return kNone;
+    }
+    const DevRule r = a.tab.rules[x.entry];
+    if (r.op == 0xFF || r.shape != x.kind) {
+      raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry);
+      return kNone;
+    }
+    switch (r.op) {
+      case PGA_OP_IF_SIZE_LESS: {
+        if (r.nParams < 2) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        uint32_t axis;
+        if (!axis_param(a, r, x, axis)) return kNone;
+        float size = param(a, r, 1, x);
+        uint32_t branch = (pick3(x.s, axis) < size) ? 0u : 1u;
+        if (branch >= r.nSucc) { raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry); return kNone; }
+        int32_t nxt = a.tab.succ[r.succBase + branch];
+        x.path = child_path(x.path, branch, nxt);
+        x.entry = nxt;
+        continue;
+      }
+      case PGA_OP_EXTRUDE: {
+        if (r.nParams < 2 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        float extent = param(a, r, 1, x);
+        int32_t nxt = a.tab.succ[r.succBase];
+        // model * [x, -z, y] column permutation; size (sx, extent, sy).
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          float c1 = x.r[i][1];
+          x.r[i][1] = x.r[i][2];
+          x.r[i][2] = -c1;
+        }
+        x.s[2] = x.s[1];
+        x.s[1] = extent;
+        x.seed = next_seed(x.seed, 0u);
+        x.kind = PGA_SHAPE_BOX;
+        x.path = child_path(x.path, 0u, nxt);
+        x.entry = nxt;
+        continue;
+      }
+      case PGA_OP_GENERATE: {
+        if (r.nParams < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        tidx = f2u(param(a, r, 0, x));
+        if (tidx > 127u) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        return kTerm;
+      }
+      case PGA_OP_DISCARD:
+        return kNone;
+      default:
+        return kNode;
+    }
+  }
+  raise_error(a.st, PGA_ERR_DEPTH, x.entry);
+  return kNone;
+}
+
+// ---------------------------------------------------- branching operators
+
+// Per-lane state of one branching operator while its children are produced.
+struct Expander {
+  Shape base;      // the executing shape
+  Shape cur;       // Subdivide<DynParams>: the symbol as updated in place
+  DevRule r;
+  uint32_t nChild;
+  uint32_t axis;
+  float offset;    // running offset along the axis
+  float scale;
+  uint32_t reps;
+  float e1, e2, e3, startExt, endExt, halfMid;
+  bool start;
+};
+
+// Operator set-up; returns the number of child slots (0 on error).
+__device__ uint32_t expander_init(const DeriveArgs& a, Expander& E) {
+  const Shape& x = E.base;
+  const DevRule& r = E.r;
+  E.nChild = 0;
+  switch (r.op) {
+    case PGA_OP_SUBDIVIDE: {
+      // Subdivide<DynParams>::execute (Subdivide.cuh:177-216).
+      if (r.nParams < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+      if (!axis_param(a, r, x, E.axis)) return 0;
+      float total = pick3(x.s, E.axis);
+      E.offset = __fmul_rn(total, -0.5f);
+      float absSum = 0.0f, relSum = 0.0f;
+      for (uint32_t i = 1; i < r.nParams; i++) {
+        float f = param(a, r, i, x);
+        absSum = __fadd_rn(absSum, __fmul_rn((float)(f > 0.0f), f));
+        relSum = __fadd_rn(relSum, __fmul_rn((float)(f < 0.0f), __fmul_rn(f, -1.0f)));
+      }
+      E.scale = (relSum == 0.0f) ? 0.0f : __fdiv_rn(__fsub_rn(total, absSum), relSum);
+      if (E.scale < 0.0f) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+      E.cur = x;
+      E.nChild = r.nParams - 1;
+      return E.nChild;
+    }
+    case PGA_OP_SUBDIVIDE_STATIC: {
+      // Subdivide<Axis, Pair<DynParam<k+1>, DCall<k>>...>::execute (Subdivide.cuh:139-156).
+      uint32_t K = r.nChildren;
+      if (r.nParams < K + 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+      if (!axis_param(a, r, x, E.axis)) return 0;
+      float total = pick3(x.s, E.axis);
+      E.offset = __fmul_rn(total, -0.5f);
+      float absSum = 0.0f, relSum = 0.0f;
+      for (uint32_t k = 0; k < K; k++) {
+        float f = param(a, r, k + 1, x);
+        absSum = __fadd_rn(absSum, __fmul_rn((float)(f > 0.0f), f));
+        relSum = __fadd_rn(relSum, __fmul_rn((float)(f < 0.0f), __fmul_rn(f, -1.0f)));
+      }
+      E.scale = (relSum == 0.0f) ? 0.0f : __fdiv_rn(__fsub_rn(total, absSum), relSum);
+      E.nChild = K;
+      return K;
+    }
+    case PGA_OP_REPEAT: {
+      // Repeat<false, ...>::execute (Repeat.cuh:70-146).
+      if (r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+      if (!axis_param(a, r, x, E.axis)) return 0;
+      uint32_t mode = f2u(param(a, r, 2, x));
+      float ext = param(a, r, 1, x);
+      float total = pick3(x.s, E.axis);
+      float extent = __fadd_rn(__fmul_rn(__fmul_rn((float)(ext < 0.0f), total), fabsf(ext)),
+                               __fmul_rn((float)(ext > 0.0f), ext));
+      if (extent <= 0.0f || total < 0.0f) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+      float division = __fdiv_rn(total, extent);
+      if (mode == 0u || mode == 1u) {
+        float rest = fmodf(total, extent);
+        bool exact = (rest == 0.0f);
+        E.reps = f2u(ceilf(division));
+        E.e1 = __fadd_rn(__fmul_rn((float)exact, extent), __fmul_rn((float)(!exact), rest));
+        E.e2 = E.e3 = extent;
+      } else if (mode == 2u) {
+        E.reps = f2u(floorf(division));
+        E.e1 = E.e2 = E.e3 = (E.reps > 0) ? __fdiv_rn(total, __uint2float_rn(E.reps)) : 0.0f;
+      } else {
+        raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+        return 0;
+      }
+      E.start = (mode == 0u);
+      E.startExt = __fadd_rn(__fmul_rn((float)E.start, E.e1), __fmul_rn((float)(!E.start), E.e3));
+      E.endExt = __fadd_rn(__fmul_rn((float)E.start, E.e3), __fmul_rn((float)(!E.start), E.e1));
+      E.halfMid = __fmul_rn(E.e2, 0.5f);
+      E.nChild = E.reps > 1 ? E.reps : 1;
+      return E.nChild;
+    }
+    case PGA_OP_COMPONENT_SPLIT:
+      // ComponentSplit<false, Top, Bottom, Sides>::execute (ComponentSplit.cuh:238-255).
+      if (r.nSucc < 3) { raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry); return 0; }
+      E.nChild = 6;
+      return 6;
+    default:
+      raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry);
+      return 0;
+  }
+}
+
+// Produces child slot c (called for c = 0, 1, ... in order).  Returns false
+// when the slot yields no child (a zero factor of a static Subdivide).
+__device__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Shape& y, uint32_t& ordinal) {
+  const Shape& x = E.base;
+  const DevRule& r = E.r;
+  switch (r.op) {
+    case PGA_OP_SUBDIVIDE: {
+      // Subdivide.cuh:220-235: the factor is read from the symbol as left by
+      // the previous child; children are built from the saved base state.
+      float f = param(a, r, c + 1, E.cur);
+      float newSize = __fadd_rn(__fmul_rn(__fmul_rn(__fmul_rn((float)(f < 0.0f), E.scale), f), -1.0f),
+                                __fmul_rn((float)(f > 0.0f), f));
+      float o = __fadd_rn(E.offset, __fmul_rn(newSize, 0.5f));
+      if (c >= r.nSucc) { raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry); return false; }
+      int32_t nxt = a.tab.succ[r.succBase + c];
+      y = x;
+      put3(y.s, E.axis, newSize);
+      translate_axis(y, x, E.axis, o);
+      y.seed = next_seed(x.seed, c);
+      y.entry = nxt;
+      y.path = child_path(x.path, c, nxt);
+      E.offset = __fadd_rn(E.offset, newSize);
+      E.cur = y;
+      ordinal = c;
+      return true;
+    }
+    case PGA_OP_SUBDIVIDE_STATIC: {
+      float f = param(a, r, c + 1, x);
+      if (f == 0.0f) return false;
+      float newSize = __fadd_rn(__fmul_rn(__fmul_rn(__fmul_rn((float)(f < 0.0f), E.scale), f), -1.0f),
+                                __fmul_rn((float)(f > 0.0f), f));
+      float o = __fadd_rn(E.offset, __fmul_rn(newSize, 0.5f));
+      if (c >= r.nSucc) { raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry); return false; }
+      int32_t nxt = a.tab.succ[r.succBase + c];
+      y = x;
+      put3(y.s, E.axis, newSize);
+      translate_axis(y, x, E.axis, o);
+      y.seed = next_seed(x.seed, c);
+      y.entry = nxt;
+      y.path = child_path(x.path, c, nxt);
+      E.offset = __fadd_rn(E.offset, newSize);
+      ordinal = c;
+      return true;
+    }
+    case PGA_OP_REPEAT: {
+      // Repeat.cuh:145-190: first piece, middle pieces, last piece.
+      int32_t nxt = a.tab.succ[r.succBase];
+      float size, o;
+      uint32_t mod;
+      if (c == 0) {
+        float half = __fmul_rn(E.startExt, 0.5f);
+        o = __fadd_rn(__fmul_rn(pick3(x.s, E.axis), -0.5f), half);
+        E.offset = __fadd_rn(o, half);
+        size = E.startExt;
+        mod = 1u;
+      } else if (c + 1 < E.reps) {
+        o = __fadd_rn(E.offset, E.halfMid);
+        E.offset = __fadd_rn(o, E.halfMid);
+        size = E.e2;
+        mod = c + 1;
+      } else {
+        o = __fadd_rn(E.offset, __fmul_rn(E.endExt, 0.5f));
+        size = E.endExt;
+        mod = E.reps;
+      }
+      y = x;
+      put3(y.s, E.axis, size);
+      translate_axis(y, x, E.axis, o);
+      y.seed = next_seed(x.seed, mod);
+      y.entry = nxt;
+      y.path = child_path(x.path, mod, nxt);
+      ordinal = mod;
+      return true;
+    }
+    case PGA_OP_COMPONENT_SPLIT: {
+      // FaceSplitter<Box> (ComponentSplit.cuh:85-172): sides 0..3 (back, front,
+      // left, right; seed modifier face + 2), then bottom (1), then top (0).
+      y = x;
+      y.kind = PGA_SHAPE_QUAD;
+      float hx = __fmul_rn(x.s[0], 0.5f), hy = __fmul_rn(x.s[1], 0.5f), hz = __fmul_rn(x.s[2], 0.5f);
+      uint32_t succ, mod;
+      switch (c) {
+        case 0:  // back: translate(0, 0, -hz) * diag(-1, 1, -1)
+          translate_axis(y, x, 2, -hz);
+          for (int i = 0; i < 3; i++) { y.r[i][0] = -x.r[i][0]; y.r[i][2] = -x.r[i][2]; }
+          y.s[0] = x.s[0]; y.s[1] = x.s[1];
+          succ = 2; mod = 2;
+          break;
+        case 1:  // front: translate(0, 0, hz)
+          translate_axis(y, x, 2, hz);
+          y.s[0] = x.s[0]; y.s[1] = x.s[1];
+          succ = 2; mod = 3;
+          break;
+        case 2:  // left: translate(-hx, 0, 0) * [z, y, -x]
+          translate_axis(y, x, 0, -hx);
+          for (int i = 0; i < 3; i++) { y.r[i][0] = x.r[i][2]; y.r[i][2] = -x.r[i][0]; }
+          y.s[0] = x.s[2]; y.s[1] = x.s[1];
+          succ = 2; mod = 4;
+          break;
+        case 3:  // right: translate(hx, 0, 0) * [-z, y, x]
+          translate_axis(y, x, 0, hx);
+          for (int i = 0; i < 3; i++) { y.r[i][0] = -x.r[i][2]; y.r[i][2] = x.r[i][0]; }
+          y.s[0] = x.s[2]; y.s[1] = x.s[1];
+          succ = 2; mod = 5;
+          break;
+        case 4:  // bottom: translate(0, -hy, 0) * [x, z, -y]
+          translate_axis(y, x, 1, -hy);
+          for (int i = 0; i < 3; i++) { y.r[i][1] = x.r[i][2]; y.r[i][2] = -x.r[i][1]; }
+          y.s[0] = x.s[0]; y.s[1] = x.s[2];
+          succ = 1; mod = 1;
+          break;
+        default:  // top: translate(0, hy, 0) * [x, -z, y]
+          translate_axis(y, x, 1, hy);
+          for (int i = 0; i < 3; i++) { y.r[i][1] = -x.r[i][2]; y.r[i][2] = x.r[i][1]; }
+          y.s[0] = x.s[0]; y.s[1] = x.s[2];
+          succ = 0; mod = 0;
+          break;
+      }
+      y.s[2] = 1.0f;
+      int32_t nxt = a.tab.succ[r.succBase + succ];
+      y.seed = next_seed(x.seed, mod);
+      y.entry = nxt;
+      y.path = child_path(x.path, mod, nxt);
+      ordinal = c;
+      return true;
+    }
+    default:
+      return false;
+  }
+}
+
+// ------------------------------------------------------ records in memory
+
+__device__ __forceinline__ void load_node(const Node* nodes, unsigned long long i, Shape& x) {
+  const float4* p = reinterpret_cast<const float4*>(nodes + i);
+  float4 a = __ldcg(p + 0), b = __ldcg(p + 1), c = __ldcg(p + 2), d = __ldcg(p + 3);
+  uint4 m = __ldcg(reinterpret_cast<const uint4*>(p + 4));
+  x.r[0][0] = a.x; x.r[0][1] = a.y; x.r[0][2] = a.z; x.t[0] = a.w;
+  x.r[1][0] = b.x; x.r[1][1] = b.y; x.r[1][2] = b.z; x.t[1] = b.w;
+  x.r[2][0] = c.x; x.r[2][1] = c.y; x.r[2][2] = c.z; x.t[2] = c.w;
+  x.s[0] = d.x; x.s[1] = d.y; x.s[2] = d.z; x.seed = d.w;
+  x.entry = (int32_t)m.x;
+  x.axiom = m.y;
+  x.path = ((uint64_t)m.w << 32) | m.z;
+}
+
+__device__ __forceinline__ void store_node(Node* nodes, unsigned long long i, const Shape& x) {
+  float4* p = reinterpret_cast<float4*>(nodes + i);
+  __stcg(p + 0, make_float4(x.r[0][0], x.r[0][1], x.r[0][2], x.t[0]));
+  __stcg(p + 1, make_float4(x.r[1][0], x.r[1][1], x.r[1][2], x.t[1]));
+  __stcg(p + 2, make_float4(x.r[2][0], x.r[2][1], x.r[2][2], x.t[2]));
+  __stcg(p + 3, make_float4(x.s[0], x.s[1], x.s[2], x.seed));
+  __stcg(reinterpret_cast<uint4*>(p + 4),
+         make_uint4((uint32_t)x.entry, x.axiom, (uint32_t)x.path, (uint32_t)(x.path >> 32)));
+}
+
+// GenerationFunction<.., 1>::perShape (GenerationFunctions.cuh:158-188):
+// model4 * scale(size) and the custom attribute, as four 16-byte stores.
+__device__ __forceinline__ void store_terminal(const DeriveArgs& a, unsigned long long slot, const Shape& x,
+                                               uint32_t tidx) {
+  float4* p = reinterpret_cast<float4*>(a.out + slot);
+  float custom = __ldg(&a.axioms[x.axiom].custom);
+  uint32_t rule = ((uint32_t)x.entry & 0xFFFFFFu) | (tidx << 24) | (x.kind == PGA_SHAPE_QUAD ? 0x80000000u : 0u);
+  __stcs(p + 0, make_float4(__fmul_rn(x.r[0][0], x.s[0]), __fmul_rn(x.r[0][1], x.s[1]), __fmul_rn(x.r[0][2], x.s[2]), x.t[0]));
+  __stcs(p + 1, make_float4(__fmul_rn(x.r[1][0], x.s[0]), __fmul_rn(x.r[1][1], x.s[1]), __fmul_rn(x.r[1][2], x.s[2]), x.t[1]));
+  __stcs(p + 2, make_float4(__fmul_rn(x.r[2][0], x.s[0]), __fmul_rn(x.r[2][1], x.s[1]), __fmul_rn(x.r[2][2], x.s[2]), x.t[2]));
+  __stcs(reinterpret_cast<uint4*>(p + 3),
+         make_uint4(rule, __float_as_uint(custom), (uint32_t)x.path, (uint32_t)(x.path >> 32)));
+}
+
+// Warp-collective emission of one shape per lane (kind kNone/kTerm/kNode):
+// one atomic per warp and kind, contiguous slots in lane order.
+__device__ __forceinline__ void emit(const DeriveArgs& a, int kind, const Shape& y, uint32_t tidx, uint32_t link,
+                                     uint32_t ordinal) {
+  const unsigned lane = threadIdx.x & 31u;
+  unsigned tm = __ballot_sync(kFull, kind == kTerm);
+  if (tm) {
+    unsigned leader = __ffs(tm) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&a.st->termCount, (unsigned long long)__popc(tm));
+    base = __shfl_sync(kFull, base, leader);
+    if (kind == kTerm) {
+      unsigned long long slot = base + __popc(tm & lanemask_lt());
+      if (slot < a.cap) {
+        store_terminal(a, slot, y, tidx);
+        if (a.termLinks != nullptr && slot < a.termLinkCap) a.termLinks[slot] = make_uint2(link, ordinal);
+      }
+    }
+  }
+  unsigned nm = __ballot_sync(kFull, kind == kNode);
+  if (nm) {
+    unsigned leader = __ffs(nm) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&a.st->nodeNext, (unsigned long long)__popc(nm));
+    base = __shfl_sync(kFull, base, leader);
+    if (kind == kNode) {
+      unsigned long long slot = base + __popc(nm & lanemask_lt());
+      if (slot < a.nodeCap) {
+        store_node(a.nodes, slot, y);
+        if (a.nodeLinks != nullptr) a.nodeLinks[slot] = make_uint2(link, ordinal);
+      } else {
+        raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, (int)(slot > 0x7FFFFFFFull ? 0x7FFFFFFF : slot));
+      }
+    }
+  }
+}
+
+// Root shape of axiom i, as Grid::...::generateAxiom builds it (Grid.cuh:199-204).
+__device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Shape& x) {
+  const PgaAxiom* ax = a.axioms + i;
+  x.r[0][0] = 1.0f; x.r[0][1] = 0.0f; x.r[0][2] = 0.0f;
+  x.r[1][0] = 0.0f; x.r[1][1] = 1.0f; x.r[1][2] = 0.0f;
+  x.r[2][0] = 0.0f; x.r[2][1] = 0.0f; x.r[2][2] = 1.0f;
+  x.t[0] = __ldg(&ax->position[0]); x.t[1] = __ldg(&ax->position[1]); x.t[2] = __ldg(&ax->position[2]);
+  x.s[0] = __ldg(&ax->size[0]); x.s[1] = __ldg(&ax->size[1]); x.s[2] = __ldg(&ax->size[2]);
+  x.seed = __ldg(&ax->seed);
+  x.entry = (int32_t)__ldg(&ax->entry);
+  x.kind = __ldg(&ax->shape);
+  x.axiom = i;
+  x.path = mix64((uint64_t)i + 0x9E3779B97F4A7C15ULL);
+}
+
+// Seeds axioms [first, first + count) with a warp-uniform grid-stride loop.
+__device__ void seed_axioms(const DeriveArgs& a, uint32_t first, uint32_t count) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned long long warpId = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const unsigned long long numWarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+  for (unsigned long long b = warpId * 32; b < count; b += numWarps * 32) {
+    unsigned long long i = b + lane;
+    int kind = kNone;
+    Shape y;
+    uint32_t tidx = 0;
+    if (i < count) {
+      axiom_shape(a, first + (uint32_t)i, y);
+      kind = resolve(a, y, tidx);
+    }
+    emit(a, kind, y, tidx, kAxiomLink | (first + (uint32_t)i), 0u);
+  }
+}
+
+// Expands the queued shapes of one warp-wide chunk [base, base + 32) ∩ [.., hi).
+__device__ __forceinline__ void expand_chunk(const DeriveArgs& a, unsigned long long base, unsigned long long hi) {
+  const unsigned lane = threadIdx.x & 31u;
+  unsigned long long i = base + lane;
+  Expander E;
+  uint32_t n = 0;
+  if (i < hi) {
+    load_node(a.nodes, i, E.base);
+    int32_t e = E.base.entry;
+    if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
+      raise_error(a.st, PGA_ERR_BAD_OPCODE, e);
+    } else {
+      E.r = a.tab.rules[e];
+      E.base.kind = E.r.shape;
+      n = expander_init(a, E);
+    }
+  }
+  for (uint32_t c = 0; __any_sync(kFull, c < n); c++) {
+    int kind = kNone;
+    Shape y;
+    uint32_t tidx = 0, ordinal = 0;
+    if (c < n && expander_child(a, E, c, y, ordinal)) kind = resolve(a, y, tidx);
+    emit(a, kind, y, tidx, (uint32_t)i, ordinal);
+  }
+}
+
+// ---------------------------------------------------- bounded grid barrier
+
+// Thread 0 of every block arrives; the last arriver runs `leader()` and
+// releases the others.  Waits are bounded by spinLimit; a timeout raises
+// PGA_ERR_TIMEOUT and makes the caller leave the kernel.
+template <typename Leader>
+__device__ bool grid_barrier(const DeriveArgs& a, Leader leader) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    DevState* st = a.st;
+    volatile uint32_t* gen = &st->barrierGen;
+    uint32_t g = *gen;
+    __threadfence();
+    uint32_t prev = atomicAdd(&st->barrierArrive, 1u);
+    if (prev == gridDim.x - 1) {
+      atomicExch(&st->barrierArrive, 0u);
+      leader();
+      __threadfence();
+      atomicAdd(&st->barrierGen, 1u);
+    } else {
+      uint32_t spins = 0;
+      while (*gen == g) {
+        if (++spins > a.spinLimit) {
+          raise_error(st, PGA_ERR_TIMEOUT, -1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+__device__ __forceinline__ void level_snapshot(const DeriveArgs& a, uint32_t level) {
+  DevState* st = a.st;
+  volatile DevState* vs = st;
+  unsigned long long lo = vs->levelHi;
+  unsigned long long hi = atomicAdd(&st->nodeNext, 0ull);
+  if (hi > a.nodeCap) hi = a.nodeCap;
+  vs->levelLo = lo;
+  vs->levelHi = hi;
+  vs->cursor = lo;
+  if (level + 1 <= a.maxLevels) a.levelStart[level + 1] = hi;
+  unsigned long long sz = hi - lo;
+  if (sz > vs->maxLevelNodes) vs->maxLevelNodes = sz;
+  bool more = hi > lo;
+  if (more && level >= a.maxLevels) {
+    raise_error(st, PGA_ERR_DEPTH, (int)level);
+    more = false;
+  }
+  vs->levels = level;
+  vs->stop = (!more || vs->status != 0) ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(256) k_derive_persistent(DeriveArgs a) {
+  seed_axioms(a, 0, a.numAxioms);
+  if (!grid_barrier(a, [&] {
+        volatile DevState* vs = a.st;
+        vs->levelHi = 0;
+        a.levelStart[0] = 0;
+        level_snapshot(a, 0);
+      }))
+    return;
+  for (uint32_t level = 0;; level++) {
+    volatile DevState* vs = a.st;
+    if (vs->stop) break;
+    const unsigned long long hi = vs->levelHi;
+    const unsigned lane = threadIdx.x & 31u;
+    for (;;) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&a.st->cursor, 32ull);
+      base = __shfl_sync(kFull, base, 0);
+      if (base >= hi) break;
+      expand_chunk(a, base, hi);
+    }
+    if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && a.outCount != nullptr) *a.outCount = a.st->termCount;
+}
+
+__global__ void __launch_bounds__(256) k_seed(DeriveArgs a, uint32_t first, uint32_t count) {
+  seed_axioms(a, first, count);
+}
+
+__global__ void __launch_bounds__(256) k_expand_level(DeriveArgs a, unsigned long long lo, unsigned long long hi) {
+  unsigned long long warpId = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  unsigned long long base = lo + warpId * 32;
+  if (base < hi) expand_chunk(a, base, hi);
+}
+
+__global__ void k_write_count(const DevState* st, unsigned long long* out) { *out = st->termCount; }
+
+// ------------------------------------------------------------- host side
+
+static thread_local std::string g_error;
+
+void set_error(const std::string& msg) { g_error = msg; }
+
+PgaStatus cuda_status(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return PGA_ERR_CUDA;
+}
+
+DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, const float* blocks, PgaTerminal* out,
+                     unsigned long long cap, unsigned long long* count) {
+  DeriveArgs a;
+  a.tab.rules = e->dRules;
+  a.tab.params = e->dParams;
+  a.tab.succ = e->dSucc;
+  a.tab.expPool = e->dExpPool;
+  a.tab.numEntries = e->numEntries;
+  a.axioms = axioms;
+  a.numAxioms = numAxioms;
+  a.axiomBase = 0;
+  a.blocks = blocks;
+  a.blockStride = e->cfg.blockStride;
+  a.out = out;
+  a.cap = cap;
+  a.outCount = count;
+  a.nodes = e->dNodes;
+  a.nodeCap = e->cfg.nodeCapacity;
+  a.nodeLinks = e->dNodeLinks;
+  a.termLinks = e->dTermLinks;
+  a.termLinkCap = e->dTermLinks ? e->cfg.maxTerminals : 0;
+  a.levelStart = e->dLevelStart;
+  a.maxLevels = e->cfg.maxLevels;
+  a.spinLimit = e->cfg.spinLimit;
+  a.st = e->dState;
+  return a;
+}
+
+}  // namespace pga
+
+using namespace pga;
+
+static const PgaProc kDefaultProcs[14] = {
+    {PGA_OP_SUBDIVIDE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SUBDIVIDE, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_BOX, 3, 1}, {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_QUAD, 3, 1},
+    {PGA_OP_REPEAT, PGA_SHAPE_BOX, 0, 1},           {PGA_OP_REPEAT, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_COMPONENT_SPLIT, PGA_SHAPE_BOX, 0, 1},  {PGA_OP_EXTRUDE, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_IF_SIZE_LESS, PGA_SHAPE_BOX, 0, 1},     {PGA_OP_IF_SIZE_LESS, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_GENERATE, PGA_SHAPE_BOX, 0, 1},         {PGA_OP_GENERATE, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_DISCARD, PGA_SHAPE_BOX, 0, 1},          {PGA_OP_DISCARD, PGA_SHAPE_QUAD, 0, 1},
+};
+
+extern "C" {
+
+const char* pga_version(void) { return "pga_gb300 0.1.0 (sm_103a)"; }
+
+const char* pga_last_error(void) { return g_error.c_str(); }
+
+const PgaProc* pga_default_procs(uint32_t* numProcs) {
+  if (numProcs) *numProcs = 14;
+  return kDefaultProcs;
+}
+
+static void free_engine(PgaEngine* e) {
+  void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dNodeLinks,
+                  e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA, e->dKeysB,
+                  e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dNodeGrad, e->dAxiomGrad};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete e;
+}
+
+size_t pga_lbvh_temp_bytes(uint64_t n);  // lbvh.cu
+
+PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* config, PgaEngine** out) {
+  if (!table || !out || !table->entries || !table->procs || table->numEntries == 0) {
+    set_error("pga_engine_create: null table, procedure list or output pointer");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  *out = nullptr;
+  PgaEngine* e = new PgaEngine();
+  if (config) e->cfg = *config;
+  PgaEngineConfig& c = e->cfg;
+  if (c.nodeCapacity == 0) c.nodeCapacity = 1ull << 22;
+  if (c.maxTerminals == 0) c.maxTerminals = 1ull << 22;
+  if (c.threadsPerBlock == 0) c.threadsPerBlock = 256;
+  if (c.spinLimit == 0) c.spinLimit = 1u << 24;
+  if (c.maxLevels == 0) c.maxLevels = 4096;
+  if (c.threadsPerBlock != 256) {
+    set_error("pga_engine_create: threadsPerBlock must be 256");
+    delete e;
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  e->threads = (int)c.threadsPerBlock;
+
+  // Lower the dispatch table: one DevRule per entry, parameters and successors
+  // packed, expression parameters' 16 values in a pool.
+  e->numEntries = table->numEntries;
+  for (uint32_t i = 0; i < table->numEntries; i++) {
+    const PgaEntry& en = table->entries[i];
+    DevRule r;
+    memset(&r, 0, sizeof r);
+    r.op = 0xFF;
+    if (en.operatorCode >= 0 && (uint32_t)en.operatorCode < table->numProcs) {
+      const PgaProc& p = table->procs[en.operatorCode];
+      if (p.op <= PGA_OP_DISCARD && p.shape <= PGA_SHAPE_QUAD) {
+        r.op = (uint8_t)p.op;
+        r.shape = (uint8_t)p.shape;
+        r.nChildren = p.numChildren;
+      }
+    }
+    if (en.numParameters > PGA_MAX_NUM_PARAMETERS || en.numSuccessors > PGA_MAX_NUM_SUCCESSORS) {
+      set_error("pga_engine_create: entry " + std::to_string(i) + " exceeds MaxNumParameters/MaxNumSuccessors");
+      delete e;
+      return PGA_ERR_BAD_PARAM;
+    }
+    if (r.op == PGA_OP_SUBDIVIDE_STATIC && (r.nChildren > PGA_MAX_NUM_SUCCESSORS || r.nChildren == 0)) {
+      set_error("pga_engine_create: static Subdivide with an invalid number of pairs");
+      delete e;
+      return PGA_ERR_BAD_PARAM;
+    }
+    r.nParams = (uint8_t)en.numParameters;
+    r.nSucc = (uint8_t)en.numSuccessors;
+    r.paramBase = (uint32_t)e->hParams.size();
+    r.succBase = (uint32_t)e->hSucc.size();
+    for (uint32_t k = 0; k < en.numParameters; k++) {
+      const PgaParameter& p = en.parameters[k];
+      DevParam d;
+      d.type = p.type;
+      d.v0 = p.value[0];
+      d.v1 = p.value[1];
+      d.aux = 0;
+      if (p.type == PGA_PT_EXP) {
+        d.aux = (uint32_t)e->hExpPool.size();
+        e->hExpPool.insert(e->hExpPool.end(), p.value, p.value + PGA_MAX_NUM_PARAMETER_VALUES);
+      }
+      e->hParams.push_back(d);
+    }
+    for (uint32_t k = 0; k < en.numSuccessors; k++) e->hSucc.push_back(en.successors[k].entryIndex);
+    e->hRules.push_back(r);
+  }
+  if (e->hParams.empty()) e->hParams.push_back(DevParam{0, 0.f, 0.f, 0});
+  if (e->hSucc.empty()) e->hSucc.push_back(-1);
+  if (e->hExpPool.empty()) e->hExpPool.push_back(0.f);
+
+  auto fail = [&](PgaStatus s) {
+    free_engine(e);
+    return s;
+  };
+  cudaError_t err;
+#define ALLOC(ptr, bytes)                                                      \
+  do {                                                                         \
+    err = cudaMalloc((void**)&(ptr), (bytes));                                 \
+    if (err != cudaSuccess) return fail(cuda_status(err, "cudaMalloc " #ptr)); \
+  } while (0)
+  ALLOC(e->dRules, e->hRules.size() * sizeof(DevRule));
+  ALLOC(e->dParams, e->hParams.size() * sizeof(DevParam));
+  ALLOC(e->dSucc, e->hSucc.size() * sizeof(int32_t));
+  ALLOC(e->dExpPool, e->hExpPool.size() * sizeof(float));
+  ALLOC(e->dState, sizeof(DevState));
+  ALLOC(e->dNodes, c.nodeCapacity * sizeof(Node));
+  ALLOC(e->dLevelStart, (c.maxLevels + 2) * sizeof(unsigned long long));
+  ALLOC(e->dScratchCount, sizeof(unsigned long long));
+  if (c.recordTape) {
+    ALLOC(e->dNodeLinks, c.nodeCapacity * sizeof(uint2));
+    ALLOC(e->dTermLinks, c.maxTerminals * sizeof(uint2));
+    ALLOC(e->dNodeGrad, c.nodeCapacity * 6 * sizeof(float));
+  }
+  // LBVH scratch for up to maxTerminals leaves.
+  e->sortTempBytes = pga_lbvh_temp_bytes(c.maxTerminals);
+  ALLOC(e->dSortTemp, e->sortTempBytes);
+  ALLOC(e->dKeysA, c.maxTerminals * sizeof(unsigned long long));
+  ALLOC(e->dKeysB, c.maxTerminals * sizeof(unsigned long long));
+  ALLOC(e->dValsA, c.maxTerminals * sizeof(uint32_t));
+  ALLOC(e->dValsB, c.maxTerminals * sizeof(uint32_t));
+  ALLOC(e->dArrival, c.maxTerminals * sizeof(uint32_t));
+#undef ALLOC
+  err = cudaMemcpy(e->dRules, e->hRules.data(), e->hRules.size() * sizeof(DevRule), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(e->dParams, e->hParams.data(), e->hParams.size() * sizeof(DevParam), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(e->dSucc, e->hSucc.data(), e->hSucc.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(e->dExpPool, e->hExpPool.data(), e->hExpPool.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemset(e->dState, 0, sizeof(DevState));
+  if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create upload"));
+
+  err = cudaGetDevice(&e->device);
+  if (err == cudaSuccess) err = cudaDeviceGetAttribute(&e->numSMs, cudaDevAttrMultiProcessorCount, e->device);
+  int perSM = 0;
+  if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_derive_persistent, e->threads, 0);
+  if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create occupancy"));
+  if (c.blocksPerSM > 0 && (int)c.blocksPerSM < perSM) perSM = (int)c.blocksPerSM;
+  if (perSM < 1) perSM = 1;
+  e->persistentBlocks = perSM * e->numSMs;
+  *out = e;
+  return PGA_OK;
+}
+
+PgaStatus pga_engine_destroy(PgaEngine* e) {
+  if (!e) return PGA_ERR_INVALID_ARGUMENT;
+  cudaDeviceSynchronize();
+  free_engine(e);
+  return PGA_OK;
+}
+
+PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dParamBlocks,
+                     PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount, void* stream) {
+  if (!e || (!dAxioms && numAxioms) || (!dOut && capacity)) {
+    set_error("pga_derive: null engine or buffers");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  PGA_CUDA_TRY(cudaMemsetAsync(e->dState, 0, sizeof(DevState), s));
+  DeriveArgs a = make_args(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
+  void* args[] = {&a};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)e->persistentBlocks);
+  cfg.blockDim = dim3((unsigned)e->threads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, (const void*)k_derive_persistent, args));
+  e->lastAxioms = dAxioms;
+  e->lastNumAxioms = numAxioms;
+  e->lastBlocks = dParamBlocks;
+  e->lastWasBatched = true;
+  return PGA_OK;
+}
+
+PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dParamBlocks,
+                           PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount, void* stream) {
+  if (!e || (!dAxioms && numAxioms) || (!dOut && capacity)) {
+    set_error("pga_derive_plain: null engine or buffers");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  PGA_CUDA_TRY(cudaMemsetAsync(e->dState, 0, sizeof(DevState), s));
+  DeriveArgs a = make_args(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
+  a.nodeLinks = nullptr;  // the arena is reused per axiom: no tape
+  a.termLinks = nullptr;
+  const unsigned threads = (unsigned)e->threads;
+  for (uint32_t ax = 0; ax < numAxioms; ax++) {
+    // One grammar (axiom) at a time: reset the queue, seed, expand level by level.
+    PGA_CUDA_TRY(cudaMemsetAsync(&e->dState->nodeNext, 0, sizeof(unsigned long long), s));
+    k_seed<<<1, 32, 0, s>>>(a, ax, 1);
+    PGA_CUDA_TRY(cudaGetLastError());
+    unsigned long long lo = 0, hi = 0;
+    int32_t status = 0;
+    for (uint32_t level = 0;; level++) {
+      DevState snap;
+      PGA_CUDA_TRY(cudaMemcpyAsync(&snap, e->dState, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+      PGA_CUDA_TRY(cudaStreamSynchronize(s));
+      status = snap.status;
+      hi = std::min<unsigned long long>(snap.nodeNext, e->cfg.nodeCapacity);
+      if (status != 0 || hi == lo) break;
+      if (level >= e->cfg.maxLevels) {
+        set_error("pga_derive_plain: maxLevels exceeded");
+        return PGA_ERR_DEPTH;
+      }
+      unsigned long long n = hi - lo;
+      unsigned long long blocks = (n + threads - 1) / threads;
+      k_expand_level<<<(unsigned)blocks, threads, 0, s>>>(a, lo, hi);
+      PGA_CUDA_TRY(cudaGetLastError());
+      lo = hi;
+    }
+    if (status != 0) break;
+  }
+  if (dCount) {
+    k_write_count<<<1, 1, 0, s>>>(e->dState, (unsigned long long*)dCount);
+    PGA_CUDA_TRY(cudaGetLastError());
+  }
+  PGA_CUDA_TRY(cudaStreamSynchronize(s));
+  e->lastWasBatched = false;
+  return PGA_OK;
+}
+
+PgaStatus pga_engine_sync_report(PgaEngine* e, void* stream, PgaDeriveReport* report) {
+  if (!e || !report) return PGA_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  DevState snap;
+  PGA_CUDA_TRY(cudaMemcpyAsync(&snap, e->dState, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+  PGA_CUDA_TRY(cudaStreamSynchronize(s));
+  memset(report, 0, sizeof *report);
+  report->status = snap.status;
+  report->detail = snap.detail;
+  report->terminals = snap.termCount;
+  report->nodes = snap.nodeNext;
+  report->levels = snap.levels;
+  report->maxLevelNodes = snap.maxLevelNodes;
+  return (PgaStatus)snap.status;
+}
+
+}  // extern "C"

@@ -1,0 +1,69 @@
+// Host-side engine object shared by the translation units of libpga_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+
+struct PgaEngine {
+  // Lowered rule table (device).
+  pga::DevRule* dRules = nullptr;
+  pga::DevParam* dParams = nullptr;
+  int32_t* dSucc = nullptr;
+  float* dExpPool = nullptr;
+  uint32_t numEntries = 0;
+  std::vector<pga::DevRule> hRules;
+  std::vector<pga::DevParam> hParams;
+  std::vector<int32_t> hSucc;
+  std::vector<float> hExpPool;
+
+  PgaEngineConfig cfg{};
+  int device = 0;
+  int numSMs = 0;
+  int persistentBlocks = 0;
+  int threads = 256;
+
+  // Work storage (allocated once in pga_engine_create).
+  pga::DevState* dState = nullptr;
+  pga::Node* dNodes = nullptr;
+  uint2* dNodeLinks = nullptr;
+  uint2* dTermLinks = nullptr;
+  unsigned long long* dLevelStart = nullptr;
+  unsigned long long* dScratchCount = nullptr;
+
+  // LBVH scratch.
+  void* dSortTemp = nullptr;
+  size_t sortTempBytes = 0;
+  unsigned long long* dKeysA = nullptr;
+  unsigned long long* dKeysB = nullptr;
+  uint32_t* dValsA = nullptr;
+  uint32_t* dValsB = nullptr;
+  uint32_t* dArrival = nullptr;
+  float* dLeafAabb = nullptr;
+
+  // Adjoint scratch: per-node gradient of (translation, size).
+  float* dNodeGrad = nullptr;
+  float* dAxiomGrad = nullptr;
+
+  // Last pga_derive, for pga_adjoint.
+  const PgaAxiom* lastAxioms = nullptr;
+  uint32_t lastNumAxioms = 0;
+  const float* lastBlocks = nullptr;
+  bool lastWasBatched = false;
+};
+
+namespace pga {
+void set_error(const std::string& msg);
+PgaStatus cuda_status(cudaError_t e, const char* what);
+DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, const float* blocks,
+                     PgaTerminal* out, unsigned long long cap, unsigned long long* count);
+}  // namespace pga
+
+#define PGA_CUDA_TRY(call)                                     \
+  do {                                                         \
+    cudaError_t _e = (call);                                   \
+    if (_e != cudaSuccess) return pga::cuda_status(_e, #call); \
+  } while (0)

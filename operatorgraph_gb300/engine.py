@@ -1,0 +1,219 @@
+"""Python side of the C ABI (include/pga_gb300.h) over ctypes.
+
+`Engine` mirrors the reference's evaluator interface
+(PGA::GPU::SinglePhaseEvaluator, include/pga/core/GPUEvaluator.cuh:475-536):
+``initialize`` (here: the constructor, from a dispatch table), ``execute``
+(derive a batch of axioms) and ``release``.  Device memory and streams come
+from PyTorch; the work itself runs in libpga_gb300.so.  There is no CPU
+fallback: without the compiled library every call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import grammar as G
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpga_gb300.so")
+
+STATUS = {
+    0: "PGA_OK", 1: "PGA_ERR_QUEUE_OVERFLOW", 2: "PGA_ERR_OUTPUT_OVERFLOW", 3: "PGA_ERR_TIMEOUT",
+    4: "PGA_ERR_BAD_OPCODE", 5: "PGA_ERR_BAD_PARAM", 6: "PGA_ERR_CUDA", 7: "PGA_ERR_INVALID_ARGUMENT",
+    8: "PGA_ERR_NO_TAPE", 9: "PGA_ERR_DEPTH",
+}
+
+# Every symbol include/pga_gb300.h declares.
+EXPORTS = ["pga_version", "pga_last_error", "pga_default_procs", "pga_engine_create", "pga_engine_destroy",
+           "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_lbvh_build", "pga_adjoint"]
+
+
+class PgaError(RuntimeError):
+    def __init__(self, status, message=""):
+        self.status = int(status)
+        super().__init__(f"{STATUS.get(self.status, self.status)}: {message}")
+
+
+class PgaProc(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_uint32), ("shape", ctypes.c_uint32), ("numChildren", ctypes.c_uint32),
+                ("numThreads", ctypes.c_uint32)]
+
+
+class PgaRuleTable(ctypes.Structure):
+    _fields_ = [("procs", ctypes.c_void_p), ("numProcs", ctypes.c_uint32), ("entries", ctypes.c_void_p),
+                ("numEntries", ctypes.c_uint32)]
+
+
+class PgaEngineConfig(ctypes.Structure):
+    _fields_ = [("nodeCapacity", ctypes.c_uint64), ("maxTerminals", ctypes.c_uint64),
+                ("blockStride", ctypes.c_uint32), ("threadsPerBlock", ctypes.c_uint32),
+                ("blocksPerSM", ctypes.c_uint32), ("recordTape", ctypes.c_uint32), ("spinLimit", ctypes.c_uint32),
+                ("maxLevels", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class PgaDeriveReport(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("detail", ctypes.c_int32), ("terminals", ctypes.c_uint64),
+                ("nodes", ctypes.c_uint64), ("levels", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("maxLevelNodes", ctypes.c_uint64)]
+
+
+class PgaBounds(ctypes.Structure):
+    _fields_ = [("min", ctypes.c_float * 3), ("max", ctypes.c_float * 3)]
+
+
+class PgaLbvh(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_void_p), ("leafParents", ctypes.c_void_p), ("aabbs", ctypes.c_void_p),
+                ("leafTerminal", ctypes.c_void_p), ("keys", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Loads libpga_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise PgaError(6, f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(path)
+    vp, u32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64
+    L.pga_version.restype = ctypes.c_char_p
+    L.pga_last_error.restype = ctypes.c_char_p
+    L.pga_default_procs.argtypes = [ctypes.POINTER(u32)]
+    L.pga_default_procs.restype = ctypes.POINTER(PgaProc)
+    L.pga_engine_create.argtypes = [ctypes.POINTER(PgaRuleTable), ctypes.POINTER(PgaEngineConfig), ctypes.POINTER(vp)]
+    L.pga_engine_destroy.argtypes = [vp]
+    for name in ("pga_derive", "pga_derive_plain"):
+        getattr(L, name).argtypes = [vp, vp, u32, vp, vp, u64, vp, vp]
+    L.pga_engine_sync_report.argtypes = [vp, vp, ctypes.POINTER(PgaDeriveReport)]
+    L.pga_lbvh_build.argtypes = [vp, vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
+    L.pga_adjoint.argtypes = [vp, vp, vp, u32, vp, vp]
+    for name in EXPORTS[3:]:
+        getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def last_error():
+    return load_library().pga_last_error().decode()
+
+
+def _check(status, what=""):
+    if status != 0:
+        raise PgaError(status, f"{what}: {last_error()}")
+
+
+def _stream_handle(stream):
+    import torch
+
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _dev(arr_or_tensor):
+    """Device copy (torch uint8) of a numpy record array, or the tensor itself."""
+    import torch
+
+    if isinstance(arr_or_tensor, torch.Tensor):
+        return arr_or_tensor
+    a = np.ascontiguousarray(arr_or_tensor)
+    return torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).cuda()
+
+
+class Engine:
+    """A dispatch table lowered to the device, plus all of its work storage."""
+
+    def __init__(self, entries, procs=None, node_capacity=1 << 22, max_terminals=1 << 22, block_stride=0,
+                 record_tape=False, blocks_per_sm=0, spin_limit=0, max_levels=0):
+        L = load_library()
+        self.entries = np.ascontiguousarray(entries, dtype=G.ENTRY_DT)
+        self.procs = np.ascontiguousarray(G.DEFAULT_PROCS if procs is None else procs, dtype=G.PROC_DT)
+        table = PgaRuleTable(self.procs.ctypes.data, len(self.procs), self.entries.ctypes.data, len(self.entries))
+        self.config = PgaEngineConfig(node_capacity, max_terminals, block_stride, 256, blocks_per_sm,
+                                      1 if record_tape else 0, spin_limit, max_levels, 0, 0)
+        h = ctypes.c_void_p()
+        _check(L.pga_engine_create(ctypes.byref(table), ctypes.byref(self.config), ctypes.byref(h)),
+               "pga_engine_create")
+        self.handle = h
+        self.block_stride = block_stride
+
+    # -- raw C-ABI calls on device pointers ------------------------------------------------
+    def derive_raw(self, d_axioms, n_axioms, d_blocks, d_out, capacity, d_count, stream=None, plain=False):
+        L = load_library()
+        fn = L.pga_derive_plain if plain else L.pga_derive
+        _check(fn(self.handle, d_axioms, n_axioms, d_blocks, d_out, capacity, d_count, _stream_handle(stream)),
+               "pga_derive_plain" if plain else "pga_derive")
+
+    def report(self, stream=None):
+        rep = PgaDeriveReport()
+        st = load_library().pga_engine_sync_report(self.handle, _stream_handle(stream), ctypes.byref(rep))
+        return {"status": st, "detail": rep.detail, "terminals": rep.terminals, "nodes": rep.nodes,
+                "levels": rep.levels, "max_level_nodes": rep.maxLevelNodes}
+
+    # -- convenience on torch tensors --------------------------------------------------------
+    def execute(self, axioms, blocks=None, capacity=None, plain=False, out=None, stream=None, check=True):
+        """Derives `axioms` (AXIOM_DT array or device uint8 tensor); returns (terminals, count, report)."""
+        import torch
+
+        d_ax = _dev(axioms)
+        n_ax = d_ax.numel() // G.AXIOM_DT.itemsize
+        d_blk = None
+        if blocks is not None:
+            d_blk = blocks if isinstance(blocks, torch.Tensor) else torch.from_numpy(
+                np.ascontiguousarray(blocks, np.float32)).cuda()
+        if out is None:
+            out = torch.empty((capacity, G.TERMINAL_DT.itemsize), dtype=torch.uint8, device="cuda")
+        capacity = out.shape[0]
+        count = torch.zeros(1, dtype=torch.int64, device="cuda")
+        self.derive_raw(d_ax.data_ptr(), n_ax, None if d_blk is None else d_blk.data_ptr(), out.data_ptr(), capacity,
+                        count.data_ptr(), stream, plain)
+        rep = self.report(stream)
+        if check and rep["status"] != 0:
+            raise PgaError(rep["status"], f"device status (detail {rep['detail']})")
+        n = int(count.item())
+        if check and n > capacity:
+            raise PgaError(2, f"{n} terminals > capacity {capacity}")
+        return out, n, rep
+
+    def lbvh(self, terminals, n, bounds, stream=None):
+        """Builds the LBVH over terminals[:n]; returns a dict of device tensors."""
+        import torch
+
+        L = load_library()
+        dev = "cuda"
+        res = {
+            "nodes": torch.empty((n - 1, 3), dtype=torch.int32, device=dev),
+            "leafParents": torch.empty(n, dtype=torch.int32, device=dev),
+            "aabbs": torch.empty((n - 1, 6), dtype=torch.float32, device=dev),
+            "leafTerminal": torch.empty(n, dtype=torch.int32, device=dev),
+            "keys": torch.empty(n, dtype=torch.int64, device=dev),
+        }
+        b = np.asarray(bounds, np.float32).reshape(6)
+        pb = PgaBounds((ctypes.c_float * 3)(*b[:3]), (ctypes.c_float * 3)(*b[3:]))
+        out = PgaLbvh(res["nodes"].data_ptr(), res["leafParents"].data_ptr(), res["aabbs"].data_ptr(),
+                      res["leafTerminal"].data_ptr(), res["keys"].data_ptr())
+        _check(L.pga_lbvh_build(self.handle, terminals.data_ptr(), n, ctypes.byref(pb), ctypes.byref(out),
+                                _stream_handle(stream)), "pga_lbvh_build")
+        return res
+
+    def adjoint_raw(self, d_grad_terminals, d_grad_params, num_blocks, d_grad_sizes, stream=None):
+        L = load_library()
+        _check(L.pga_adjoint(self.handle, d_grad_terminals, d_grad_params, num_blocks, d_grad_sizes,
+                             _stream_handle(stream)), "pga_adjoint")
+
+    def release(self):
+        if getattr(self, "handle", None):
+            load_library().pga_engine_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def terminals_to_numpy(out, n):
+    return out[:n].cpu().numpy().reshape(-1).view(G.TERMINAL_DT).copy()

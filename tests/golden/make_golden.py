@@ -1,0 +1,57 @@
+#!/usr/bin/env python3
+"""Writes tests/golden/<case>.npz from the reference's own evaluator.
+
+Runs oracle/_ref/ref_harness (the reference's SinglePhaseEvaluator, built by
+oracle/make_ref.py from the reference sources) on every case of cases.py and
+stores: the grammar batch, the terminal count, a SHA-256 digest and checksum
+of the canonical (sorted, path-free) terminal records, and -- for cases of at
+most 2,000 terminals -- the canonical records themselves.
+
+Usage: python tests/golden/make_golden.py   (needs oracle/_ref built)
+"""
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+import oracle  # noqa: E402
+from operatorgraph_gb300 import grammar as G  # noqa: E402
+
+import cases as C  # noqa: E402
+
+FULL_LIMIT = 2000
+
+
+def main():
+    tmp = tempfile.mkdtemp()
+    for name, b in C.cases():
+        entries, axioms = b["entries"], b["axioms"]
+        n_base = None
+        if b["blocks"] is not None:
+            entries, axioms = G.expand_blocks(entries, axioms, b["blocks"], b["block_stride"])
+            n_base = len(b["entries"])
+        bf, tf = os.path.join(tmp, "b.bin"), os.path.join(tmp, "t.bin")
+        G.write_batch_file(bf, entries, axioms)
+        info = oracle.run_reference(bf, tf)
+        ref = G.read_terminal_file(tf)
+        canon = C.canonical(ref, n_base)
+        m = canon["m"].astype(np.float64)
+        checksum = float((m[:, 3] + 2 * m[:, 7] + 3 * m[:, 11] + m[:, 0]).sum())
+        payload = dict(entries=b["entries"].view(np.uint8), axioms=b["axioms"].view(np.uint8),
+                       count=np.int64(len(ref)), digest=np.array(C.digest(canon)), checksum=np.float64(checksum))
+        if b["blocks"] is not None:
+            payload["blocks"] = b["blocks"]
+            payload["block_stride"] = np.int64(b["block_stride"])
+        if len(ref) <= FULL_LIMIT:
+            payload["terminals"] = canon.view(np.uint8)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **payload)
+        print(f"{name}: {len(ref)} terminals, checksum {checksum:.6f}, reference {info['seconds']:.6f} s")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+"""The oracle (CPU restatement) pinned against the reference's own outputs.
+
+The golden fixtures were produced by the reference's SinglePhaseEvaluator
+(tests/golden/make_golden.py); the known answers below are the reference's
+probe values for the Menger sponge.  No GPU needed.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from operatorgraph_gb300 import grammar as G
+from operatorgraph_gb300 import scenes
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+
+
+def load_case(path):
+    z = np.load(path)
+    b = {"entries": z["entries"].view(G.ENTRY_DT), "axioms": z["axioms"].view(G.AXIOM_DT)}
+    b["blocks"] = z["blocks"] if "blocks" in z else None
+    b["block_stride"] = int(z["block_stride"]) if "block_stride" in z else 0
+    return b, z
+
+
+def canonical(t, num_entries=None):
+    import sys
+
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import cases
+
+    return cases.canonical(t, num_entries), cases.digest
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_oracle_matches_reference_golden(path):
+    b, z = load_case(path)
+    t = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"], b["blocks"], b["block_stride"])
+    n_base = len(b["entries"]) if b["blocks"] is not None else None
+    canon, digest = canonical(t, n_base)
+    assert len(t) == int(z["count"])
+    if "terminals" in z:
+        ref = z["terminals"].view(G.TERMINAL_DT)
+        assert np.array_equal(canon["m"].view(np.uint32), ref["m"].view(np.uint32))
+        assert np.array_equal(canon["rule"], ref["rule"])
+        assert np.array_equal(canon["custom"], ref["custom"])
+    assert digest(canon) == str(z["digest"])
+
+
+def test_golden_fixtures_present():
+    assert len(GOLDEN) >= 15
+
+
+def test_menger_depth5_known_answer():
+    """Reference probe: threshold 0.005 -> 3,200,000 terminals, checksum 13169.1925,
+    first terminal (FIFO order) at (-0.497942358)^3 with size 0.00411522621."""
+    b = scenes.menger(0.005)
+    t = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    assert len(t) == 3_200_000
+    # The probe summed the float expression M14 + 2 M24 + 3 M34 + M11 into a double.
+    m = t["m"]
+    per = ((m[:, 3] + np.float32(2) * m[:, 7]) + np.float32(3) * m[:, 11]) + m[:, 0]
+    checksum = per.astype(np.float64).sum()
+    assert abs(checksum - 13169.1925) < 1e-3
+    corner = np.isclose(t["m"][:, 3], -0.497942358) & np.isclose(t["m"][:, 7], -0.497942358) & \
+        np.isclose(t["m"][:, 11], -0.497942358)
+    assert corner.sum() == 1
+    assert np.isclose(t["m"][corner][0, 0], 0.00411522621)
+
+
+def test_city_4096_count():
+    """The 4096-building city (seed 1234) gives 5,856,274 terminals on the
+    reference's evaluator (measured with oracle/_ref)."""
+    b = scenes.city(4096)
+    t = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    assert len(t) == 5_856_274
+
+
+def test_path_hashes_unique():
+    b = scenes.city(64)
+    t = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    assert len(np.unique(t["path"])) == len(t)
+
+
+def test_errors_match_reference_behaviour():
+    """Subdivide<DynParams> with absolute factors larger than the shape throws in
+    the reference (Subdivide.cuh:208-216); Repeat with extent 0 throws
+    (Repeat.cuh:75-83); a shape of the wrong type is rejected (CPUEvaluator.h:64-68)."""
+    from operatorgraph_gb300.grammar import DispatchTable, Entry, scalar
+
+    bad_sub = DispatchTable([Entry(G.BOX_SUBDIVIDE, [scalar(0), scalar(5.0), scalar(-1)], [(1, 0), (1, 0)]),
+                             Entry(G.BOX_GENERATE, [scalar(0)], [])]).to_array()
+    with pytest.raises(oracle.OracleError) as e:
+        oracle.derive(G.DEFAULT_PROCS, bad_sub, G.make_axioms(1))
+    assert e.value.status == 5
+    bad_rep = DispatchTable([Entry(G.BOX_REPEAT, [scalar(0), scalar(0.0), scalar(0)], [(1, 0)]),
+                             Entry(G.BOX_GENERATE, [scalar(0)], [])]).to_array()
+    with pytest.raises(oracle.OracleError) as e:
+        oracle.derive(G.DEFAULT_PROCS, bad_rep, G.make_axioms(1))
+    assert e.value.status == 5
+    mismatch = DispatchTable([Entry(G.QUAD_GENERATE, [scalar(0)], [])]).to_array()
+    with pytest.raises(oracle.OracleError) as e:
+        oracle.derive(G.DEFAULT_PROCS, mismatch, G.make_axioms(1))  # Box axiom into a Quad procedure
+    assert e.value.status == 4
+
+
+def _check_lbvh_structure(nodes, lp, n):
+    """Each internal node has two children, every node but the root one parent,
+    every leaf is reached exactly once and node ranges are contiguous."""
+    seen_leaf = np.zeros(n, np.int64)
+    seen_int = np.zeros(n - 1, np.int64)
+    lo = np.zeros(n - 1, np.int64)
+    hi = np.zeros(n - 1, np.int64)
+    order = []
+    stack = [0]
+    while stack:
+        i = stack.pop()
+        order.append(i)
+        for c in nodes[i, 1:]:
+            if c >= 0:
+                seen_leaf[c] += 1
+                assert lp[c] == i
+            else:
+                seen_int[-c] += 1
+                assert nodes[-c, 0] == i
+                stack.append(-c)
+    assert (seen_leaf == 1).all() and (seen_int[1:] == 1).all() and seen_int[0] == 0
+    for i in reversed(order):
+        rng = []
+        for c in nodes[i, 1:]:
+            rng.append((c, c) if c >= 0 else (lo[-c], hi[-c]))
+        assert rng[0][1] + 1 == rng[1][0]
+        lo[i], hi[i] = rng[0][0], rng[1][1]
+    assert lo[0] == 0 and hi[0] == n - 1
+
+
+@pytest.mark.parametrize("scene", ["menger", "city"])
+def test_oracle_lbvh_invariants(scene):
+    b = scenes.menger(0.05) if scene == "menger" else scenes.city(16)
+    t = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    bounds = (-0.5, -0.5, -0.5, 0.5, 0.5, 0.5) if scene == "menger" else (-50, -50, -1, 800, 100, 400)
+    nodes, lp, aabb, lt, keys = oracle.lbvh(t, bounds)
+    n = len(t)
+    _check_lbvh_structure(nodes, lp, n)
+    assert np.all(keys[1:] >= keys[:-1])
+    assert sorted(lt.tolist()) == list(range(n))
+    # Every internal box contains its children's boxes; the root contains every terminal centre.
+    c = np.stack([t["m"][:, 3], t["m"][:, 7], t["m"][:, 11]], 1)
+    assert np.all(c >= aabb[0, :3] - 1e-6) and np.all(c <= aabb[0, 3:] + 1e-6)
+    for i in range(n - 1):
+        for ch in nodes[i, 1:]:
+            if ch < 0:
+                assert np.all(aabb[-ch, :3] >= aabb[i, :3]) and np.all(aabb[-ch, 3:] <= aabb[i, 3:])

@@ -1,0 +1,229 @@
+"""GPU parity: the CUDA engine against the reference's golden outputs and the
+oracle, through the C ABI.
+
+Bar: terminal count, rule ids, custom attributes, derivation-path hashes and
+transforms bit-exact (the derivation is written with round-to-nearest
+intrinsics and no FMA, so the FP32 transforms match to the bit, well inside
+the 1e-5 relative tolerance the target allows); Morton keys, LBVH topology and
+boxes bit-exact.  Multisets are compared after sorting (queue order is free).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from operatorgraph_gb300 import grammar as G
+from operatorgraph_gb300 import scenes
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+REL_TOL = 1e-5  # FP32 transform tolerance of the target; observed error is 0
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from operatorgraph_gb300 import build as B
+
+    B.build()
+    torch.cuda.set_device(0)
+
+
+def _engine(entries, **kw):
+    from operatorgraph_gb300.engine import Engine
+
+    kw.setdefault("node_capacity", 1 << 20)
+    kw.setdefault("max_terminals", 1 << 20)
+    return Engine(entries, **kw)
+
+
+def _run(b, plain=False, capacity=None, **kw):
+    from operatorgraph_gb300.engine import terminals_to_numpy
+
+    ref_n = None
+    if capacity is None:
+        ref_n = len(oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"], b["blocks"], b["block_stride"]))
+        capacity = max(ref_n, 1)
+    eng = _engine(b["entries"], block_stride=b["block_stride"], **kw)
+    out, n, rep = eng.execute(b["axioms"], blocks=b["blocks"], capacity=capacity, plain=plain)
+    torch.cuda.synchronize()
+    got = terminals_to_numpy(out, n)
+    return eng, out, got, rep
+
+
+def _assert_same(got, ref):
+    assert len(got) == len(ref)
+    a, c = G.sort_terminals(got, by_path=True), G.sort_terminals(ref, by_path=True)
+    assert np.array_equal(a["path"], c["path"]), "derivation-path hashes differ"
+    assert np.array_equal(a["rule"], c["rule"]), "rule ids differ"
+    assert np.array_equal(a["custom"].view(np.uint32), c["custom"].view(np.uint32))
+    am, cm = a["m"] + np.float32(0), c["m"] + np.float32(0)
+    denom = np.maximum(np.abs(cm), 1e-30)
+    assert np.max(np.abs(am - cm) / denom) <= REL_TOL
+    assert np.array_equal(am.view(np.uint32), cm.view(np.uint32)), "transforms not bit-exact"
+
+
+def _load(path):
+    z = np.load(path)
+    b = {"entries": z["entries"].view(G.ENTRY_DT), "axioms": z["axioms"].view(G.AXIOM_DT)}
+    b["blocks"] = z["blocks"] if "blocks" in z else None
+    b["block_stride"] = int(z["block_stride"]) if "block_stride" in z else 0
+    return b, z
+
+
+@pytest.mark.parametrize("plain", [False, True], ids=["persistent", "plain"])
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_case(path, plain):
+    import sys
+
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import cases
+
+    b, z = _load(path)
+    eng, out, got, rep = _run(b, plain=plain)
+    assert rep["status"] == 0
+    n_base = len(b["entries"]) if b["blocks"] is not None else None
+    canon = cases.canonical(got, n_base)
+    assert len(got) == int(z["count"])
+    assert cases.digest(canon) == str(z["digest"]), "differs from the reference's own output"
+    ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"], b["blocks"], b["block_stride"])
+    _assert_same(got, ref)
+    eng.release()
+
+
+@pytest.mark.parametrize("name", ["menger_d5", "city_4096", "facades_1024", "random_16"])
+def test_full_size_bit_exact(name):
+    if name == "menger_d5":
+        b = scenes.menger(0.005)
+    elif name == "city_4096":
+        b = scenes.city(4096)
+    elif name == "facades_1024":
+        b = scenes.facades(1024)
+    else:
+        tabs = scenes.random_grammars(16)
+        entries, offs = G.concat_tables(tabs)
+        ax = G.make_axioms(64)
+        ax["seed"] = 0.5
+        ax["entry"] = [offs[i % 16] for i in range(64)]
+        b = {"entries": entries, "axioms": ax, "blocks": None, "block_stride": 0}
+    ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"], b["blocks"], b["block_stride"])
+    eng, out, got, rep = _run(b, capacity=len(ref), node_capacity=1 << 23, max_terminals=1 << 23)
+    assert rep["status"] == 0
+    _assert_same(got, ref)
+    eng.release()
+
+
+@pytest.mark.parametrize("scene", ["menger_d3", "building", "city_16", "menger_d5"])
+def test_lbvh_bit_exact(scene):
+    if scene == "menger_d3":
+        b, bounds = scenes.menger(0.05), (-0.5, -0.5, -0.5, 0.5, 0.5, 0.5)
+    elif scene == "menger_d5":
+        b, bounds = scenes.menger(0.005), (-0.5, -0.5, -0.5, 0.5, 0.5, 0.5)
+    elif scene == "building":
+        b, bounds = scenes.building(), (-20, -20, -1, 20, 20, 40)
+    else:
+        b, bounds = scenes.city(16), (-50, -50, -1, 800, 100, 400)
+    eng, out, got, rep = _run(b, node_capacity=1 << 23, max_terminals=1 << 23)
+    n = len(got)
+    bv = eng.lbvh(out, n, bounds)
+    torch.cuda.synchronize()
+    nodes, lp, aabb, lt, keys = oracle.lbvh(got, bounds)
+    assert np.array_equal(bv["keys"].cpu().numpy().view(np.uint64), keys), "Morton keys differ"
+    assert np.array_equal(bv["leafTerminal"].cpu().numpy().view(np.uint32), lt), "leaf order differs"
+    assert np.array_equal(bv["nodes"].cpu().numpy(), nodes), "topology differs"
+    assert np.array_equal(bv["leafParents"].cpu().numpy().view(np.uint32), lp)
+    assert np.array_equal(bv["aabbs"].cpu().numpy().view(np.uint32), aabb.view(np.uint32)), "boxes differ"
+    eng.release()
+
+
+def test_repeat_runs_are_identical_as_multisets():
+    b = scenes.city(256)
+    eng, out, got1, _ = _run(b)
+    out2, n2, _ = eng.execute(b["axioms"], capacity=len(got1))
+    got2 = G.sort_terminals(
+        out2[:n2].cpu().numpy().reshape(-1).view(G.TERMINAL_DT), by_path=True)
+    assert np.array_equal(G.sort_terminals(got1, by_path=True).view(np.uint8), got2.view(np.uint8))
+    eng.release()
+
+
+def test_empty_batch():
+    b = scenes.menger(0.05)
+    eng = _engine(b["entries"])
+    ax = torch.empty(0, dtype=torch.uint8, device="cuda")
+    out, n, rep = eng.execute(ax, capacity=16)
+    assert n == 0 and rep["status"] == 0
+    eng.release()
+
+
+def test_all_discarded():
+    from operatorgraph_gb300.grammar import DispatchTable, Entry, scalar
+
+    tab = DispatchTable([Entry(G.BOX_SUBDIVIDE, [scalar(0), scalar(-1), scalar(-1)], [(1, 0), (1, 0)]),
+                         Entry(G.BOX_DISCARD, [], [])]).to_array()
+    b = {"entries": tab, "axioms": G.make_axioms(100), "blocks": None, "block_stride": 0}
+    eng, out, got, rep = _run(b, capacity=16)
+    assert len(got) == 0 and rep["status"] == 0
+
+
+def test_output_overflow_reports_status():
+    from operatorgraph_gb300.engine import PgaError
+
+    b = scenes.menger(0.05)
+    eng = _engine(b["entries"])
+    with pytest.raises(PgaError) as e:
+        eng.execute(b["axioms"], capacity=100)
+    assert e.value.status == 2
+    # The engine and the context stay usable.
+    out, n, rep = eng.execute(b["axioms"], capacity=8000)
+    assert n == 8000
+    eng.release()
+
+
+def test_queue_overflow_reports_status():
+    b = scenes.menger(0.05)
+    eng = _engine(b["entries"], node_capacity=8)
+    out, n, rep = eng.execute(b["axioms"], capacity=8000, check=False)
+    assert rep["status"] == 1
+    eng.release()
+
+
+@pytest.mark.parametrize("kind", ["bad_param", "bad_opcode", "depth"])
+def test_device_errors_are_statuses(kind):
+    from operatorgraph_gb300.grammar import DispatchTable, Entry, scalar
+
+    if kind == "bad_param":  # Repeat extent 0 (Repeat.cuh:75-83 traps on the GPU)
+        tab = DispatchTable([Entry(G.BOX_REPEAT, [scalar(0), scalar(0.0), scalar(0)], [(1, 0)]),
+                             Entry(G.BOX_GENERATE, [scalar(0)], [])]).to_array()
+        want = 5
+    elif kind == "bad_opcode":  # successor outside the table
+        tab = DispatchTable([Entry(G.BOX_SUBDIVIDE, [scalar(0), scalar(-1)], [(7, 0)])]).to_array()
+        want = 4
+    else:  # an IfSizeLess cycle never reaches a branching rule
+        tab = DispatchTable([Entry(G.BOX_IF_SIZE_LESS, [scalar(0), scalar(5.0)], [(0, 0), (0, 0)])]).to_array()
+        want = 9
+    eng = _engine(tab)
+    for plain in (False, True):
+        out, n, rep = eng.execute(G.make_axioms(4), capacity=64, plain=plain, check=False)
+        assert rep["status"] == want
+    eng.release()
+
+
+def test_bounded_barrier_timeout_is_a_status():
+    """With a spin limit of 1 the grid barrier gives up at once: the launch
+    ends with PGA_ERR_TIMEOUT (or completes when every block arrived before the
+    others polled), never a hang."""
+    b = scenes.menger(0.05)
+    eng = _engine(b["entries"], spin_limit=1)
+    out, n, rep = eng.execute(b["axioms"], capacity=8000, check=False)
+    assert rep["status"] in (0, 3)
+    eng.release()
+    eng = _engine(b["entries"])
+    out, n, rep = eng.execute(b["axioms"], capacity=8000)
+    assert n == 8000
+    eng.release()
