@@ -94,7 +94,10 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 7:
-                self.samples.append(parts)
+                self.samples.append([time.time()] + parts)
+
+    def mark(self, start, end):
+        self.window = (start, end)
 
     def __exit__(self, *exc):
         if self.proc:
@@ -105,14 +108,18 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        """Median SM clock and throttle reasons of the samples taken while the
+        timed steps ran (a sample arrives within one 200 ms period)."""
+        lo, hi = getattr(self, "window", (0.0, float("inf")))
+        inside = [s[1:] for s in self.samples if lo <= s[0] <= hi + 0.25]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(s[0]) for s in inside if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in inside if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        reasons = sorted({names[k] for s in inside for k in range(4) if s[3 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(inside)}
 
 
 def host_info():
@@ -273,13 +280,16 @@ def our_arm(args):
     # ---- device-resident timing (value, roofline)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with ClockSampler(local) as clocks:
+        time.sleep(1.0)  # let the sampler start
         barrier()
+        t_start = time.time()
         for k in range(args.steps):
             flush.fill_(k & 0xFF)
             evs[k][0].record(stream)
             step()
             evs[k][1].record(stream)
         barrier()
+        clocks.mark(t_start, time.time())
     step_ms = [a.elapsed_time(b) for a, b in evs]
     ms = sum(step_ms) / len(step_ms)
     if world > 1:
@@ -411,7 +421,7 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     args = ap.parse_args()

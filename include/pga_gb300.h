@@ -215,6 +215,14 @@ PgaStatus pga_derive_plain(PgaEngine* engine, const PgaAxiom* dAxioms, uint32_t 
 /* Synchronises `stream` and reports the device status of the last derivation. */
 PgaStatus pga_engine_sync_report(PgaEngine* engine, void* stream, PgaDeriveReport* report);
 
+/* Per-level profile of the last pga_derive: starts[l] = first node of level l
+ * (starts[l+1] its end), nanos[l] = device clock (ns) when level l's range was
+ * fixed, for up to `capacity` levels; *numLevels receives the level count.
+ * Synchronises `stream`.  Counterpart of the reference's per-subgraph clock
+ * instrumentation (include/pga/core/Instrumentation.cuh:44-74). */
+PgaStatus pga_engine_levels(PgaEngine* engine, void* stream, uint64_t* starts, uint64_t* nanos,
+                            uint32_t capacity, uint32_t* numLevels);
+
 /* Replaces ContextSensitivity::GPU::BVHConstructor::construct(min, max)
  * (include/pga/core/GPUBVHConstructor.cuh:265-331), applied to terminal boxes:
  * 30-bit Morton codes of the terminal centres in `bounds`, radix sort,

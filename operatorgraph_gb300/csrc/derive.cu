@@ -565,7 +565,12 @@ __device__ __forceinline__ void level_snapshot(const DeriveArgs& a, uint32_t lev
   vs->levelLo = lo;
   vs->levelHi = hi;
   vs->cursor = lo;
-  if (level + 1 <= a.maxLevels) a.levelStart[level + 1] = hi;
+  if (level + 1 <= a.maxLevels) {
+    a.levelStart[level + 1] = hi;
+    unsigned long long now;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+    a.levelClock[level] = now;
+  }
   unsigned long long sz = hi - lo;
   if (sz > vs->maxLevelNodes) vs->maxLevelNodes = sz;
   bool more = hi > lo;
@@ -648,6 +653,7 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.termLinks = e->dTermLinks;
   a.termLinkCap = e->dTermLinks ? e->cfg.maxTerminals : 0;
   a.levelStart = e->dLevelStart;
+  a.levelClock = e->dLevelClock;
   a.maxLevels = e->cfg.maxLevels;
   a.spinLimit = e->cfg.spinLimit;
   a.st = e->dState;
@@ -680,7 +686,7 @@ const PgaProc* pga_default_procs(uint32_t* numProcs) {
 }
 
 static void free_engine(PgaEngine* e) {
-  void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dNodeLinks,
+  void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dNodeLinks, e->dLevelClock,
                   e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA, e->dKeysB,
                   e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dNodeGrad, e->dAxiomGrad};
   for (void* p : ptrs)
@@ -778,6 +784,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   ALLOC(e->dState, sizeof(DevState));
   ALLOC(e->dNodes, c.nodeCapacity * sizeof(Node));
   ALLOC(e->dLevelStart, (c.maxLevels + 2) * sizeof(unsigned long long));
+  ALLOC(e->dLevelClock, (c.maxLevels + 2) * sizeof(unsigned long long));
   ALLOC(e->dScratchCount, sizeof(unsigned long long));
   if (c.recordTape) {
     ALLOC(e->dNodeLinks, c.nodeCapacity * sizeof(uint2));
@@ -910,6 +917,21 @@ PgaStatus pga_engine_sync_report(PgaEngine* e, void* stream, PgaDeriveReport* re
   report->levels = snap.levels;
   report->maxLevelNodes = snap.maxLevelNodes;
   return (PgaStatus)snap.status;
+}
+
+PgaStatus pga_engine_levels(PgaEngine* e, void* stream, uint64_t* starts, uint64_t* nanos, uint32_t capacity,
+                            uint32_t* numLevels) {
+  if (!e || !numLevels) return PGA_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = (cudaStream_t)stream;
+  DevState snap;
+  PGA_CUDA_TRY(cudaMemcpyAsync(&snap, e->dState, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+  PGA_CUDA_TRY(cudaStreamSynchronize(s));
+  uint32_t n = std::min<uint32_t>(snap.levels + 1, e->cfg.maxLevels + 1);
+  *numLevels = n;
+  uint32_t k = std::min(n, capacity);
+  if (k && starts) PGA_CUDA_TRY(cudaMemcpy(starts, e->dLevelStart, k * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  if (k && nanos) PGA_CUDA_TRY(cudaMemcpy(nanos, e->dLevelClock, k * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  return PGA_OK;
 }
 
 }  // extern "C"

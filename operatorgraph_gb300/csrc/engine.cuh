@@ -83,6 +83,7 @@ struct DeriveArgs {
   uint2* termLinks;
   unsigned long long termLinkCap;
   unsigned long long* levelStart;
+  unsigned long long* levelClock;  // %globaltimer when each level's range was fixed
   uint32_t maxLevels;
   uint32_t spinLimit;
   DevState* st;

@@ -32,6 +32,7 @@ struct PgaEngine {
   uint2* dNodeLinks = nullptr;
   uint2* dTermLinks = nullptr;
   unsigned long long* dLevelStart = nullptr;
+  unsigned long long* dLevelClock = nullptr;
   unsigned long long* dScratchCount = nullptr;
 
   // LBVH scratch.

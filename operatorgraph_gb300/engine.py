@@ -25,7 +25,8 @@ STATUS = {
 
 # Every symbol include/pga_gb300.h declares.
 EXPORTS = ["pga_version", "pga_last_error", "pga_default_procs", "pga_engine_create", "pga_engine_destroy",
-           "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_lbvh_build", "pga_adjoint"]
+           "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_engine_levels", "pga_lbvh_build",
+           "pga_adjoint"]
 
 
 class PgaError(RuntimeError):
@@ -89,6 +90,7 @@ def load_library(path=LIB_PATH):
     L.pga_engine_sync_report.argtypes = [vp, vp, ctypes.POINTER(PgaDeriveReport)]
     L.pga_lbvh_build.argtypes = [vp, vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
     L.pga_adjoint.argtypes = [vp, vp, vp, u32, vp, vp]
+    L.pga_engine_levels.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(u32)]
     for name in EXPORTS[3:]:
         getattr(L, name).restype = ctypes.c_int
     _lib = L
@@ -151,6 +153,17 @@ class Engine:
         st = load_library().pga_engine_sync_report(self.handle, _stream_handle(stream), ctypes.byref(rep))
         return {"status": st, "detail": rep.detail, "terminals": rep.terminals, "nodes": rep.nodes,
                 "levels": rep.levels, "max_level_nodes": rep.maxLevelNodes}
+
+    def levels(self, stream=None, capacity=4096):
+        """Per-level node ranges and device clock of the last pga_derive."""
+        L = load_library()
+        starts = np.zeros(capacity, np.uint64)
+        nanos = np.zeros(capacity, np.uint64)
+        n = ctypes.c_uint32()
+        _check(L.pga_engine_levels(self.handle, _stream_handle(stream), starts.ctypes.data, nanos.ctypes.data,
+                                   capacity, ctypes.byref(n)), "pga_engine_levels")
+        k = min(n.value, capacity)
+        return starts[: k + 1], nanos[:k]
 
     # -- convenience on torch tensors --------------------------------------------------------
     def execute(self, axioms, blocks=None, capacity=None, plain=False, out=None, stream=None, check=True):

@@ -1,0 +1,87 @@
+"""Command-line runner for the synthetic scenes (the role of the reference's
+test_runner app, src/test_runner/TestRunnerApp.cpp:303-345: derive a scene a
+number of times and log timings).
+
+    python -m operatorgraph_gb300.runner --scene city --runs 5 [--plain] [--lbvh]
+
+Prints one JSON line: terminals, per-run milliseconds (CUDA events) and the
+device report of the last run.
+"""
+import argparse
+import json
+import statistics
+
+import numpy as np
+
+from . import scenes
+
+
+def make_scene(name, n):
+    if name == "city":
+        return scenes.city(n or 4096), (-50.0, -50.0, -1.0, 3250.0, 3250.0, 400.0)
+    if name == "menger":
+        return scenes.menger({1: 0.5, 2: 0.15, 3: 0.05, 4: 0.015, 5: 0.005}[n or 5]), (-0.5, -0.5, -0.5, 0.5, 0.5, 0.5)
+    if name == "facades":
+        return scenes.facades(n or 1024), (-1.0, -1.0, -1.0, 70.0, 2.0, 70.0)
+    if name == "mixed":
+        return scenes.mixed(n or 65536), (-50.0, -50.0, -1.0, 13000.0, 13000.0, 400.0)
+    raise SystemExit(f"unknown scene {name}")
+
+
+def main(argv=None):
+    import torch
+
+    from .engine import Engine
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scene", default="city", choices=["city", "menger", "facades", "mixed"])
+    ap.add_argument("--n", type=int, default=0, help="axioms (city/facades/mixed) or depth (menger)")
+    ap.add_argument("--runs", type=int, default=3)
+    ap.add_argument("--plain", action="store_true", help="plain one-grammar-per-launch form")
+    ap.add_argument("--lbvh", action="store_true", help="also build the LBVH after each derivation")
+    ap.add_argument("--capacity", type=int, default=0)
+    ap.add_argument("--nodes", type=int, default=1 << 22)
+    args = ap.parse_args(argv)
+
+    b, bounds = make_scene(args.scene, args.n)
+    cap = args.capacity or 8_000_000
+    eng = Engine(b["entries"], node_capacity=args.nodes, max_terminals=cap, block_stride=b["block_stride"])
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).to(dev)
+    d_blk = None if b["blocks"] is None else torch.from_numpy(np.asarray(b["blocks"], np.float32)).to(dev)
+    out = torch.empty((cap, 64), dtype=torch.uint8, device=dev)
+    count = torch.zeros(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+    times, lb = [], []
+    for _ in range(args.runs):
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None if d_blk is None else d_blk.data_ptr(),
+                       out.data_ptr(), cap, count.data_ptr(), plain=args.plain)
+        z.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(z))
+        if args.lbvh:
+            n = int(count.item())
+            a.record(stream)
+            eng.lbvh(out, n, bounds)
+            z.record(stream)
+            torch.cuda.synchronize()
+            lb.append(a.elapsed_time(z))
+    rep = eng.report()
+    lv = {}
+    if not args.plain:
+        starts, nanos = eng.levels()
+        nanos = nanos.astype(np.int64)
+        lv = {"level_nodes": np.diff(starts.astype(np.int64)).tolist(),
+              "level_us": (np.diff(nanos) / 1e3).round(2).tolist()}
+    res = {"scene": args.scene, "n": args.n, "plain": args.plain, "terminals": int(count.item()),
+           "ms": times, "ms_median": statistics.median(times), "report": rep, **lv}
+    if lb:
+        res["lbvh_ms"] = lb
+    print(json.dumps(res))
+    eng.release()
+
+
+if __name__ == "__main__":
+    main()
