@@ -1,16 +1,23 @@
 // Derivation kernels and the engine's C ABI (creation, derive, report).
 //
-// Work model: level-synchronous expansion.  A level is the set of queued
-// shapes whose rule branches (Subdivide, Repeat, ComponentSplit); one thread
-// executes one shape's operator and produces its children in order.  Each child
-// is then resolved in the same thread through its chain of 1 -> 1 rules
-// (IfSizeLess, Extrude), and ends as a terminal (Generate: written out
-// directly), a discard, or a queued shape of the next level.  Terminals and
-// queued shapes are appended with one atomic per warp (ballot + popc), so each
-// warp writes contiguous 64-byte terminal records and 80-byte shape records.
+// Work model: level-synchronous expansion.  A level is the set of queued work
+// items; an item is a shape whose rule branches (Subdivide, Repeat,
+// ComponentSplit) together with a range of at most `subItem` of its children.
+// One thread executes one item's operator and produces those children in
+// order.  Each child is resolved in the same thread through its chain of
+// 1 -> 1 rules (IfSizeLess, Extrude) and ends as a terminal (Generate: written
+// out directly), a discard, or a branching shape that is queued as work items.
+//
+// A block works on 256 items at a time and emits in block-synchronous rounds:
+// one child per thread per round, block-wide prefix sums, one global atomic per
+// round for the terminals and one for the queued items, so each round writes a
+// contiguous run of 64-byte terminal records.  Small branching children are
+// staged in shared memory and expanded by the same block right after the
+// current chunk (their own branching children go to the next level), which
+// halves the queue traffic and the number of levels.
 //
 // pga_derive runs every level of every axiom in ONE persistent cooperative
-// launch (a bounded grid barrier between levels, warps pulling 32 shapes at a
+// launch (a bounded grid barrier between levels, blocks pulling 256 items at a
 // time from a level cursor); pga_derive_plain is the plain GPU form: one axiom
 // at a time, one launch per level, the host reading each level's size back.
 //
@@ -32,7 +39,38 @@
 namespace pga {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr uint32_t kStageCap = kThreads;
 enum Kind { kNone = 0, kTerm = 1, kNode = 2 };
+
+struct __align__(16) Smem {
+  Node stage[kStageCap];
+  unsigned long long termBase, nodeBase, chunkBase;
+  uint32_t warpW[kWarps], warpG[kWarps], warpT[kWarps];
+  uint32_t stageCount;
+  uint32_t pad;
+};
+
+extern __shared__ __align__(16) unsigned char smem_raw[];
+
+// Rule-table reads: from the block's shared-memory copy when the table fits
+// (tableInSmem), else from global memory.
+__device__ __forceinline__ DevRule rule_at(const DeriveArgs& a, uint32_t e) {
+  if (a.tableInSmem) return reinterpret_cast<const DevRule*>(smem_raw + sizeof(Smem))[e];
+  return a.tab.rules[e];
+}
+__device__ __forceinline__ DevParam param_at(const DeriveArgs& a, uint32_t k) {
+  if (a.tableInSmem)
+    return reinterpret_cast<const DevParam*>(smem_raw + sizeof(Smem) + (size_t)a.tab.numEntries * sizeof(DevRule))[k];
+  return a.tab.params[k];
+}
+__device__ __forceinline__ int32_t succ_at(const DeriveArgs& a, uint32_t k) {
+  if (a.tableInSmem)
+    return reinterpret_cast<const int32_t*>(smem_raw + sizeof(Smem) + (size_t)a.tab.numEntries * sizeof(DevRule) +
+                                            (size_t)a.numParams * sizeof(DevParam))[k];
+  return succ_at(a, k);
+}
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -40,9 +78,23 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t& total) {
+  const unsigned lane = threadIdx.x & 31u;
+  uint32_t x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t y = __shfl_up_sync(kFull, x, d);
+    if (lane >= (unsigned)d) x += y;
+  }
+  total = __shfl_sync(kFull, x, 31);
+  return x - v;
+}
+
 // ------------------------------------------------------------- parameters
 
-__device__ __forceinline__ float eval_param(const DeriveArgs& a, const DevParam& p, const Shape& x) {
+// Non-scalar parameters (random ranges, shape attributes, expressions, block
+// values) take this out-of-line path so the common scalar case stays small.
+__device__ __noinline__ float eval_param_slow(const DeriveArgs& a, DevParam p, Shape x) {
   switch (p.type) {
     case PGA_PT_SCALAR:
       return p.v0;
@@ -70,8 +122,9 @@ __device__ __forceinline__ float eval_param(const DeriveArgs& a, const DevParam&
 }
 
 __device__ __forceinline__ float param(const DeriveArgs& a, const DevRule& r, uint32_t k, const Shape& x) {
-  DevParam p = a.tab.params[r.paramBase + k];
-  return eval_param(a, p, x);
+  const DevParam p = param_at(a, r.paramBase + k);
+  if (p.type == PGA_PT_SCALAR) return p.v0;
+  return eval_param_slow(a, p, x);
 }
 
 __device__ __forceinline__ bool axis_param(const DeriveArgs& a, const DevRule& r, const Shape& x, uint32_t& axis) {
@@ -83,10 +136,17 @@ __device__ __forceinline__ bool axis_param(const DeriveArgs& a, const DevRule& r
   return true;
 }
 
-// Translation by o along model axis `ax`: t' = fl(fl(R[:,ax] * o) + t).
+__device__ __forceinline__ float seed_of(const DeriveArgs& a, float base, uint32_t modifier) {
+  return a.useSeeds ? next_seed(base, modifier) : 0.0f;
+}
+
+// Translation by o along model axis `ax`: t' = fl(fl(R[:,ax] * o) + t), which
+// for a signed-permutation R is one rounded add in row perm_ax.
 __device__ __forceinline__ void translate_axis(Shape& y, const Shape& x, uint32_t ax, float o) {
+  const uint32_t row = frame_row(x.frame, ax);
+  const float v = frame_neg(x.frame, ax) ? -o : o;
 #pragma unroll
-  for (int i = 0; i < 3; i++) y.t[i] = __fadd_rn(__fmul_rn(pick3(x.r[i], ax), o), x.t[i]);
+  for (uint32_t i = 0; i < 3; i++) y.t[i] = (i == row) ? __fadd_rn(v, x.t[i]) : x.t[i];
 }
 
 // ------------------------------------------------- 1 -> 1 chain resolution
@@ -100,7 +160,7 @@ __device__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
       raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry);
       return kNone;
     }
-    const DevRule r = a.tab.rules[x.entry];
+    const DevRule r = rule_at(a, (uint32_t)x.entry);
     if (r.op == 0xFF || r.shape != x.kind) {
       raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry);
       return kNone;
@@ -113,7 +173,7 @@ __device__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
         float size = param(a, r, 1, x);
         uint32_t branch = (pick3(x.s, axis) < size) ? 0u : 1u;
         if (branch >= r.nSucc) { raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry); return kNone; }
-        int32_t nxt = a.tab.succ[r.succBase + branch];
+        int32_t nxt = succ_at(a, r.succBase + branch);
         x.path = child_path(x.path, branch, nxt);
         x.entry = nxt;
         continue;
@@ -121,17 +181,15 @@ __device__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
       case PGA_OP_EXTRUDE: {
         if (r.nParams < 2 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
         float extent = param(a, r, 1, x);
-        int32_t nxt = a.tab.succ[r.succBase];
-        // model * [x, -z, y] column permutation; size (sx, extent, sy).
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-          float c1 = x.r[i][1];
-          x.r[i][1] = x.r[i][2];
-          x.r[i][2] = -c1;
+        int32_t nxt = succ_at(a, r.succBase);
+        // model * [x, z, -y] columns; size (sx, extent, sy).
+        {
+          const uint32_t f = x.frame;
+          x.frame = frame_set(frame_set(f, 1, f, 2, 0), 2, f, 1, 1);
         }
         x.s[2] = x.s[1];
         x.s[1] = extent;
-        x.seed = next_seed(x.seed, 0u);
+        x.seed = seed_of(a, x.seed, 0u);
         x.kind = PGA_SHAPE_BOX;
         x.path = child_path(x.path, 0u, nxt);
         x.entry = nxt;
@@ -155,96 +213,120 @@ __device__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
 
 // ---------------------------------------------------- branching operators
 
-// Per-lane state of one branching operator while its children are produced.
+// Per-thread state of one branching operator while its children are produced.
 struct Expander {
-  Shape base;      // the executing shape
-  Shape cur;       // Subdivide<DynParams>: the symbol as updated in place
+  Shape base;       // the executing shape
   DevRule r;
-  uint32_t nChild;
   uint32_t axis;
-  float offset;    // running offset along the axis
+  float offset;     // running offset along the axis
   float scale;
   uint32_t reps;
-  float e1, e2, e3, startExt, endExt, halfMid;
-  bool start;
+  float e2, startExt, endExt, halfMid;
+  float prevSize, prevOff;  // Subdivide<DynParams>: the previous child, i.e. the symbol as updated in place
 };
+
+// Repeat<false, ...> set-up (Repeat.cuh:70-146); false on an argument the reference rejects.
+__device__ __noinline__ bool repeat_setup(const DeriveArgs& a, const DevRule& r, const Shape& x, uint32_t& axis,
+                                             uint32_t& reps, float& e1, float& e2, float& e3, bool& start,
+                                             bool raise) {
+  if (r.nParams < 3 || r.nSucc < 1) {
+    if (raise) raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+    return false;
+  }
+  axis = f2u(param(a, r, 0, x));
+  if (axis > 2) {
+    if (raise) raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+    return false;
+  }
+  uint32_t mode = f2u(param(a, r, 2, x));
+  float ext = param(a, r, 1, x);
+  float total = pick3(x.s, axis);
+  float extent = __fadd_rn(__fmul_rn(__fmul_rn((float)(ext < 0.0f), total), fabsf(ext)),
+                           __fmul_rn((float)(ext > 0.0f), ext));
+  if (extent <= 0.0f || total < 0.0f) {
+    if (raise) raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+    return false;
+  }
+  float division = __fdiv_rn(total, extent);
+  if (mode == 0u || mode == 1u) {
+    float rest = fmodf(total, extent);
+    bool exact = (rest == 0.0f);
+    reps = f2u(ceilf(division));
+    e1 = __fadd_rn(__fmul_rn((float)exact, extent), __fmul_rn((float)(!exact), rest));
+    e2 = e3 = extent;
+  } else if (mode == 2u) {
+    reps = f2u(floorf(division));
+    e1 = e2 = e3 = (reps > 0) ? __fdiv_rn(total, __uint2float_rn(reps)) : 0.0f;
+  } else {
+    if (raise) raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+    return false;
+  }
+  start = (mode == 0u);
+  return true;
+}
+
+// Number of children a branching shape produces (decides how many work items
+// it is queued as).  Errors are raised when the item is executed.
+__device__ __forceinline__ uint32_t count_children(const DeriveArgs& a, const Shape& y) {
+  const DevRule r = rule_at(a, (uint32_t)y.entry);
+  switch (r.op) {
+    case PGA_OP_SUBDIVIDE:
+      return r.nParams >= 1 ? r.nParams - 1u : 1u;
+    case PGA_OP_SUBDIVIDE_STATIC:
+      return r.nChildren;
+    case PGA_OP_COMPONENT_SPLIT:
+      return 6u;
+    case PGA_OP_REPEAT: {
+      uint32_t axis, reps;
+      float e1, e2, e3;
+      bool start;
+      if (!repeat_setup(a, r, y, axis, reps, e1, e2, e3, start, false)) return 1u;
+      return reps > 1 ? reps : 1u;
+    }
+    default:
+      return 1u;  // raises BAD_OPCODE when executed
+  }
+}
 
 // Operator set-up; returns the number of child slots (0 on error).
 __device__ uint32_t expander_init(const DeriveArgs& a, Expander& E) {
   const Shape& x = E.base;
   const DevRule& r = E.r;
-  E.nChild = 0;
   switch (r.op) {
-    case PGA_OP_SUBDIVIDE: {
-      // Subdivide<DynParams>::execute (Subdivide.cuh:177-216).
-      if (r.nParams < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+    case PGA_OP_SUBDIVIDE:
+    case PGA_OP_SUBDIVIDE_STATIC: {
+      // Subdivide<DynParams>::execute (Subdivide.cuh:177-216) and the static
+      // form Subdivide<Axis, Pair<DynParam<k+1>, DCall<k>>...> (Subdivide.cuh:139-156).
+      const bool dyn = r.op == PGA_OP_SUBDIVIDE;
+      uint32_t n = dyn ? (r.nParams >= 1 ? r.nParams - 1u : 0u) : r.nChildren;
+      if (r.nParams < n + 1 || r.nParams < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
       if (!axis_param(a, r, x, E.axis)) return 0;
       float total = pick3(x.s, E.axis);
       E.offset = __fmul_rn(total, -0.5f);
       float absSum = 0.0f, relSum = 0.0f;
-      for (uint32_t i = 1; i < r.nParams; i++) {
+      for (uint32_t i = 1; i <= n; i++) {
         float f = param(a, r, i, x);
         absSum = __fadd_rn(absSum, __fmul_rn((float)(f > 0.0f), f));
         relSum = __fadd_rn(relSum, __fmul_rn((float)(f < 0.0f), __fmul_rn(f, -1.0f)));
       }
       E.scale = (relSum == 0.0f) ? 0.0f : __fdiv_rn(__fsub_rn(total, absSum), relSum);
-      if (E.scale < 0.0f) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
-      E.cur = x;
-      E.nChild = r.nParams - 1;
-      return E.nChild;
-    }
-    case PGA_OP_SUBDIVIDE_STATIC: {
-      // Subdivide<Axis, Pair<DynParam<k+1>, DCall<k>>...>::execute (Subdivide.cuh:139-156).
-      uint32_t K = r.nChildren;
-      if (r.nParams < K + 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
-      if (!axis_param(a, r, x, E.axis)) return 0;
-      float total = pick3(x.s, E.axis);
-      E.offset = __fmul_rn(total, -0.5f);
-      float absSum = 0.0f, relSum = 0.0f;
-      for (uint32_t k = 0; k < K; k++) {
-        float f = param(a, r, k + 1, x);
-        absSum = __fadd_rn(absSum, __fmul_rn((float)(f > 0.0f), f));
-        relSum = __fadd_rn(relSum, __fmul_rn((float)(f < 0.0f), __fmul_rn(f, -1.0f)));
-      }
-      E.scale = (relSum == 0.0f) ? 0.0f : __fdiv_rn(__fsub_rn(total, absSum), relSum);
-      E.nChild = K;
-      return K;
+      if (dyn && E.scale < 0.0f) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+      E.prevSize = 0.0f;
+      E.prevOff = 0.0f;
+      return n;
     }
     case PGA_OP_REPEAT: {
-      // Repeat<false, ...>::execute (Repeat.cuh:70-146).
-      if (r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
-      if (!axis_param(a, r, x, E.axis)) return 0;
-      uint32_t mode = f2u(param(a, r, 2, x));
-      float ext = param(a, r, 1, x);
-      float total = pick3(x.s, E.axis);
-      float extent = __fadd_rn(__fmul_rn(__fmul_rn((float)(ext < 0.0f), total), fabsf(ext)),
-                               __fmul_rn((float)(ext > 0.0f), ext));
-      if (extent <= 0.0f || total < 0.0f) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
-      float division = __fdiv_rn(total, extent);
-      if (mode == 0u || mode == 1u) {
-        float rest = fmodf(total, extent);
-        bool exact = (rest == 0.0f);
-        E.reps = f2u(ceilf(division));
-        E.e1 = __fadd_rn(__fmul_rn((float)exact, extent), __fmul_rn((float)(!exact), rest));
-        E.e2 = E.e3 = extent;
-      } else if (mode == 2u) {
-        E.reps = f2u(floorf(division));
-        E.e1 = E.e2 = E.e3 = (E.reps > 0) ? __fdiv_rn(total, __uint2float_rn(E.reps)) : 0.0f;
-      } else {
-        raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
-        return 0;
-      }
-      E.start = (mode == 0u);
-      E.startExt = __fadd_rn(__fmul_rn((float)E.start, E.e1), __fmul_rn((float)(!E.start), E.e3));
-      E.endExt = __fadd_rn(__fmul_rn((float)E.start, E.e3), __fmul_rn((float)(!E.start), E.e1));
+      float e1, e3;
+      bool start;
+      if (!repeat_setup(a, r, x, E.axis, E.reps, e1, E.e2, e3, start, true)) return 0;
+      E.startExt = __fadd_rn(__fmul_rn((float)start, e1), __fmul_rn((float)(!start), e3));
+      E.endExt = __fadd_rn(__fmul_rn((float)start, e3), __fmul_rn((float)(!start), e1));
       E.halfMid = __fmul_rn(E.e2, 0.5f);
-      E.nChild = E.reps > 1 ? E.reps : 1;
-      return E.nChild;
+      return E.reps > 1 ? E.reps : 1;
     }
     case PGA_OP_COMPONENT_SPLIT:
       // ComponentSplit<false, Top, Bottom, Sides>::execute (ComponentSplit.cuh:238-255).
       if (r.nSucc < 3) { raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry); return 0; }
-      E.nChild = 6;
       return 6;
     default:
       raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry);
@@ -252,53 +334,84 @@ __device__ uint32_t expander_init(const DeriveArgs& a, Expander& E) {
   }
 }
 
-// Produces child slot c (called for c = 0, 1, ... in order).  Returns false
-// when the slot yields no child (a zero factor of a static Subdivide).
+// Subdivide<DynParams> reads factor c+1 from the symbol as left by child c
+// (Subdivide.cuh:220-235 update the symbol in place).
+__device__ __forceinline__ float dyn_factor(const DeriveArgs& a, const Expander& E, uint32_t c) {
+  const DevRule& r = E.r;
+  if ((r.flags & kRulePure) || c == 0) return param(a, r, c + 1, E.base);
+  Shape cur = E.base;
+  put3(cur.s, E.axis, E.prevSize);
+  translate_axis(cur, E.base, E.axis, E.prevOff);
+  cur.seed = seed_of(a, E.base.seed, c - 1);
+  cur.entry = (c - 1 < r.nSucc) ? succ_at(a, r.succBase + c - 1) : -1;
+  return param(a, r, c + 1, cur);
+}
+
+__device__ __forceinline__ float subdivide_size(float f, float scale) {
+  return __fadd_rn(__fmul_rn(__fmul_rn(__fmul_rn((float)(f < 0.0f), scale), f), -1.0f),
+                   __fmul_rn((float)(f > 0.0f), f));
+}
+
+// Advances the running state past children [0, c0) without producing them.
+__device__ void expander_skip(const DeriveArgs& a, Expander& E, uint32_t c0) {
+  const DevRule& r = E.r;
+  if (c0 == 0) return;
+  switch (r.op) {
+    case PGA_OP_SUBDIVIDE:
+      for (uint32_t c = 0; c < c0; c++) {
+        float newSize = subdivide_size(dyn_factor(a, E, c), E.scale);
+        E.prevOff = __fadd_rn(E.offset, __fmul_rn(newSize, 0.5f));
+        E.prevSize = newSize;
+        E.offset = __fadd_rn(E.offset, newSize);
+      }
+      return;
+    case PGA_OP_SUBDIVIDE_STATIC:
+      for (uint32_t c = 0; c < c0; c++) {
+        float f = param(a, r, c + 1, E.base);
+        if (f != 0.0f) E.offset = __fadd_rn(E.offset, subdivide_size(f, E.scale));
+      }
+      return;
+    case PGA_OP_REPEAT: {
+      float half = __fmul_rn(E.startExt, 0.5f);
+      E.offset = __fadd_rn(__fadd_rn(__fmul_rn(pick3(E.base.s, E.axis), -0.5f), half), half);
+      for (uint32_t c = 1; c < c0; c++) E.offset = __fadd_rn(__fadd_rn(E.offset, E.halfMid), E.halfMid);
+      return;
+    }
+    default:
+      return;
+  }
+}
+
+// Produces child slot c (slots are produced in increasing order).  Returns
+// false when the slot yields no child (a zero factor of a static Subdivide).
 __device__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Shape& y, uint32_t& ordinal) {
   const Shape& x = E.base;
   const DevRule& r = E.r;
   switch (r.op) {
-    case PGA_OP_SUBDIVIDE: {
-      // Subdivide.cuh:220-235: the factor is read from the symbol as left by
-      // the previous child; children are built from the saved base state.
-      float f = param(a, r, c + 1, E.cur);
-      float newSize = __fadd_rn(__fmul_rn(__fmul_rn(__fmul_rn((float)(f < 0.0f), E.scale), f), -1.0f),
-                                __fmul_rn((float)(f > 0.0f), f));
-      float o = __fadd_rn(E.offset, __fmul_rn(newSize, 0.5f));
-      if (c >= r.nSucc) { raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry); return false; }
-      int32_t nxt = a.tab.succ[r.succBase + c];
-      y = x;
-      put3(y.s, E.axis, newSize);
-      translate_axis(y, x, E.axis, o);
-      y.seed = next_seed(x.seed, c);
-      y.entry = nxt;
-      y.path = child_path(x.path, c, nxt);
-      E.offset = __fadd_rn(E.offset, newSize);
-      E.cur = y;
-      ordinal = c;
-      return true;
-    }
+    case PGA_OP_SUBDIVIDE:
     case PGA_OP_SUBDIVIDE_STATIC: {
-      float f = param(a, r, c + 1, x);
-      if (f == 0.0f) return false;
-      float newSize = __fadd_rn(__fmul_rn(__fmul_rn(__fmul_rn((float)(f < 0.0f), E.scale), f), -1.0f),
-                                __fmul_rn((float)(f > 0.0f), f));
+      const bool dyn = r.op == PGA_OP_SUBDIVIDE;
+      float f = dyn ? dyn_factor(a, E, c) : param(a, r, c + 1, x);
+      if (!dyn && f == 0.0f) return false;
+      float newSize = subdivide_size(f, E.scale);
       float o = __fadd_rn(E.offset, __fmul_rn(newSize, 0.5f));
       if (c >= r.nSucc) { raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry); return false; }
-      int32_t nxt = a.tab.succ[r.succBase + c];
+      int32_t nxt = succ_at(a, r.succBase + c);
       y = x;
       put3(y.s, E.axis, newSize);
       translate_axis(y, x, E.axis, o);
-      y.seed = next_seed(x.seed, c);
+      y.seed = seed_of(a, x.seed, c);
       y.entry = nxt;
       y.path = child_path(x.path, c, nxt);
       E.offset = __fadd_rn(E.offset, newSize);
+      E.prevSize = newSize;
+      E.prevOff = o;
       ordinal = c;
       return true;
     }
     case PGA_OP_REPEAT: {
       // Repeat.cuh:145-190: first piece, middle pieces, last piece.
-      int32_t nxt = a.tab.succ[r.succBase];
+      int32_t nxt = succ_at(a, r.succBase);
       float size, o;
       uint32_t mod;
       if (c == 0) {
@@ -320,7 +433,7 @@ __device__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Sha
       y = x;
       put3(y.s, E.axis, size);
       translate_axis(y, x, E.axis, o);
-      y.seed = next_seed(x.seed, mod);
+      y.seed = seed_of(a, x.seed, mod);
       y.entry = nxt;
       y.path = child_path(x.path, mod, nxt);
       ordinal = mod;
@@ -333,10 +446,11 @@ __device__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Sha
       y.kind = PGA_SHAPE_QUAD;
       float hx = __fmul_rn(x.s[0], 0.5f), hy = __fmul_rn(x.s[1], 0.5f), hz = __fmul_rn(x.s[2], 0.5f);
       uint32_t succ, mod;
+      const uint32_t f = x.frame;
       switch (c) {
         case 0:  // back: translate(0, 0, -hz) * diag(-1, 1, -1)
           translate_axis(y, x, 2, -hz);
-          for (int i = 0; i < 3; i++) { y.r[i][0] = -x.r[i][0]; y.r[i][2] = -x.r[i][2]; }
+          y.frame = frame_set(frame_set(f, 0, f, 0, 1), 2, f, 2, 1);
           y.s[0] = x.s[0]; y.s[1] = x.s[1];
           succ = 2; mod = 2;
           break;
@@ -345,34 +459,34 @@ __device__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Sha
           y.s[0] = x.s[0]; y.s[1] = x.s[1];
           succ = 2; mod = 3;
           break;
-        case 2:  // left: translate(-hx, 0, 0) * [z, y, -x]
+        case 2:  // left: translate(-hx, 0, 0) * columns [z, y, -x]
           translate_axis(y, x, 0, -hx);
-          for (int i = 0; i < 3; i++) { y.r[i][0] = x.r[i][2]; y.r[i][2] = -x.r[i][0]; }
+          y.frame = frame_set(frame_set(f, 0, f, 2, 0), 2, f, 0, 1);
           y.s[0] = x.s[2]; y.s[1] = x.s[1];
           succ = 2; mod = 4;
           break;
-        case 3:  // right: translate(hx, 0, 0) * [-z, y, x]
+        case 3:  // right: translate(hx, 0, 0) * columns [-z, y, x]
           translate_axis(y, x, 0, hx);
-          for (int i = 0; i < 3; i++) { y.r[i][0] = -x.r[i][2]; y.r[i][2] = x.r[i][0]; }
+          y.frame = frame_set(frame_set(f, 0, f, 2, 1), 2, f, 0, 0);
           y.s[0] = x.s[2]; y.s[1] = x.s[1];
           succ = 2; mod = 5;
           break;
-        case 4:  // bottom: translate(0, -hy, 0) * [x, z, -y]
+        case 4:  // bottom: translate(0, -hy, 0) * columns [x, z, -y]
           translate_axis(y, x, 1, -hy);
-          for (int i = 0; i < 3; i++) { y.r[i][1] = x.r[i][2]; y.r[i][2] = -x.r[i][1]; }
+          y.frame = frame_set(frame_set(f, 1, f, 2, 0), 2, f, 1, 1);
           y.s[0] = x.s[0]; y.s[1] = x.s[2];
           succ = 1; mod = 1;
           break;
-        default:  // top: translate(0, hy, 0) * [x, -z, y]
+        default:  // top: translate(0, hy, 0) * columns [x, -z, y]
           translate_axis(y, x, 1, hy);
-          for (int i = 0; i < 3; i++) { y.r[i][1] = -x.r[i][2]; y.r[i][2] = x.r[i][1]; }
+          y.frame = frame_set(frame_set(f, 1, f, 2, 1), 2, f, 1, 0);
           y.s[0] = x.s[0]; y.s[1] = x.s[2];
           succ = 0; mod = 0;
           break;
       }
       y.s[2] = 1.0f;
-      int32_t nxt = a.tab.succ[r.succBase + succ];
-      y.seed = next_seed(x.seed, mod);
+      int32_t nxt = succ_at(a, r.succBase + succ);
+      y.seed = seed_of(a, x.seed, mod);
       y.entry = nxt;
       y.path = child_path(x.path, mod, nxt);
       ordinal = c;
@@ -385,27 +499,49 @@ __device__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Sha
 
 // ------------------------------------------------------ records in memory
 
-__device__ __forceinline__ void load_node(const Node* nodes, unsigned long long i, Shape& x) {
-  const float4* p = reinterpret_cast<const float4*>(nodes + i);
-  float4 a = __ldcg(p + 0), b = __ldcg(p + 1), c = __ldcg(p + 2), d = __ldcg(p + 3);
-  uint4 m = __ldcg(reinterpret_cast<const uint4*>(p + 4));
-  x.r[0][0] = a.x; x.r[0][1] = a.y; x.r[0][2] = a.z; x.t[0] = a.w;
-  x.r[1][0] = b.x; x.r[1][1] = b.y; x.r[1][2] = b.z; x.t[1] = b.w;
-  x.r[2][0] = c.x; x.r[2][1] = c.y; x.r[2][2] = c.z; x.t[2] = c.w;
-  x.s[0] = d.x; x.s[1] = d.y; x.s[2] = d.z; x.seed = d.w;
+__device__ __forceinline__ void unpack_node(float4 a, float4 b, uint4 m, Shape& x) {
+  x.t[0] = a.x; x.t[1] = a.y; x.t[2] = a.z; x.s[0] = a.w;
+  x.s[1] = b.x; x.s[2] = b.y; x.seed = b.z; x.frame = __float_as_uint(b.w);
   x.entry = (int32_t)m.x;
   x.axiom = m.y;
   x.path = ((uint64_t)m.w << 32) | m.z;
 }
 
-__device__ __forceinline__ void store_node(Node* nodes, unsigned long long i, const Shape& x) {
+__device__ __forceinline__ void load_node(const Node* nodes, unsigned long long i, Shape& x, uint4& ext) {
+  const float4* p = reinterpret_cast<const float4*>(nodes + i);
+  float4 a = __ldcg(p + 0), b = __ldcg(p + 1);
+  uint4 m = __ldcg(reinterpret_cast<const uint4*>(p + 2));
+  ext = __ldcg(reinterpret_cast<const uint4*>(p + 3));
+  unpack_node(a, b, m, x);
+}
+
+__device__ __forceinline__ void load_stage(const Node* stage, uint32_t i, Shape& x, uint4& ext) {
+  const Node& n = stage[i];
+  unpack_node(n.ts, n.sf, n.meta, x);
+  ext = n.ext;
+}
+
+__device__ __forceinline__ void pack_node(const Shape& x, float4& a, float4& b, uint4& m) {
+  a = make_float4(x.t[0], x.t[1], x.t[2], x.s[0]);
+  b = make_float4(x.s[1], x.s[2], x.seed, __uint_as_float(x.frame));
+  m = make_uint4((uint32_t)x.entry, x.axiom, (uint32_t)x.path, (uint32_t)(x.path >> 32));
+}
+
+__device__ __forceinline__ void store_node(Node* nodes, unsigned long long i, const Shape& x, uint4 ext) {
   float4* p = reinterpret_cast<float4*>(nodes + i);
-  __stcg(p + 0, make_float4(x.r[0][0], x.r[0][1], x.r[0][2], x.t[0]));
-  __stcg(p + 1, make_float4(x.r[1][0], x.r[1][1], x.r[1][2], x.t[1]));
-  __stcg(p + 2, make_float4(x.r[2][0], x.r[2][1], x.r[2][2], x.t[2]));
-  __stcg(p + 3, make_float4(x.s[0], x.s[1], x.s[2], x.seed));
-  __stcg(reinterpret_cast<uint4*>(p + 4),
-         make_uint4((uint32_t)x.entry, x.axiom, (uint32_t)x.path, (uint32_t)(x.path >> 32)));
+  float4 a, b;
+  uint4 m;
+  pack_node(x, a, b, m);
+  __stcg(p + 0, a);
+  __stcg(p + 1, b);
+  __stcg(reinterpret_cast<uint4*>(p + 2), m);
+  __stcg(reinterpret_cast<uint4*>(p + 3), ext);
+}
+
+__device__ __forceinline__ void store_stage(Node* stage, uint32_t i, const Shape& x, uint4 ext) {
+  Node& n = stage[i];
+  pack_node(x, n.ts, n.sf, n.meta);
+  n.ext = ext;
 }
 
 // GenerationFunction<.., 1>::perShape (GenerationFunctions.cuh:158-188):
@@ -415,56 +551,103 @@ __device__ __forceinline__ void store_terminal(const DeriveArgs& a, unsigned lon
   float4* p = reinterpret_cast<float4*>(a.out + slot);
   float custom = __ldg(&a.axioms[x.axiom].custom);
   uint32_t rule = ((uint32_t)x.entry & 0xFFFFFFu) | (tidx << 24) | (x.kind == PGA_SHAPE_QUAD ? 0x80000000u : 0u);
-  __stcs(p + 0, make_float4(__fmul_rn(x.r[0][0], x.s[0]), __fmul_rn(x.r[0][1], x.s[1]), __fmul_rn(x.r[0][2], x.s[2]), x.t[0]));
-  __stcs(p + 1, make_float4(__fmul_rn(x.r[1][0], x.s[0]), __fmul_rn(x.r[1][1], x.s[1]), __fmul_rn(x.r[1][2], x.s[2]), x.t[1]));
-  __stcs(p + 2, make_float4(__fmul_rn(x.r[2][0], x.s[0]), __fmul_rn(x.r[2][1], x.s[1]), __fmul_rn(x.r[2][2], x.s[2]), x.t[2]));
+  // R[i][j] * s_j is exactly +-s_j in row perm_j and zero elsewhere.
+  float m[3][3];
+#pragma unroll
+  for (uint32_t j = 0; j < 3; j++) {
+    const uint32_t row = frame_row(x.frame, j);
+    const float v = frame_neg(x.frame, j) ? -x.s[j] : x.s[j];
+#pragma unroll
+    for (uint32_t i = 0; i < 3; i++) m[i][j] = (i == row) ? v : 0.0f;
+  }
+  __stcs(p + 0, make_float4(m[0][0], m[0][1], m[0][2], x.t[0]));
+  __stcs(p + 1, make_float4(m[1][0], m[1][1], m[1][2], x.t[1]));
+  __stcs(p + 2, make_float4(m[2][0], m[2][1], m[2][2], x.t[2]));
   __stcs(reinterpret_cast<uint4*>(p + 3),
          make_uint4(rule, __float_as_uint(custom), (uint32_t)x.path, (uint32_t)(x.path >> 32)));
 }
 
-// Warp-collective emission of one shape per lane (kind kNone/kTerm/kNode):
-// one atomic per warp and kind, contiguous slots in lane order.
-__device__ __forceinline__ void emit(const DeriveArgs& a, int kind, const Shape& y, uint32_t tidx, uint32_t link,
-                                     uint32_t ordinal) {
-  const unsigned lane = threadIdx.x & 31u;
-  unsigned tm = __ballot_sync(kFull, kind == kTerm);
-  if (tm) {
-    unsigned leader = __ffs(tm) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&a.st->termCount, (unsigned long long)__popc(tm));
-    base = __shfl_sync(kFull, base, leader);
-    if (kind == kTerm) {
-      unsigned long long slot = base + __popc(tm & lanemask_lt());
-      if (slot < a.cap) {
-        store_terminal(a, slot, y, tidx);
-        if (a.termLinks != nullptr && slot < a.termLinkCap) a.termLinks[slot] = make_uint2(link, ordinal);
+// Block-collective emission of one shape per thread.  kind: kNone, kTerm or
+// kNode (a branching shape with `nChild` children, queued as ceil(nChild /
+// subItem) items).  Small nodes go to the shared-memory stage when allowed.
+// One global atomic per round for terminals and one for queued items.
+__device__ __forceinline__ void block_emit(const DeriveArgs& a, Smem& sm, int kind, const Shape& y, uint32_t tidx,
+                                           uint32_t nChild, uint32_t link, uint32_t ordinal, bool canStage) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t S = a.subItem;
+  uint32_t m = (kind == kNode) ? (nChild + S - 1) / S : 0u;
+  const bool want = canStage && m != 0 && m <= 2;
+  const uint32_t mW = want ? m : 0u, mG = want ? 0u : m, t = (kind == kTerm) ? 1u : 0u;
+  uint32_t totW, totG, totWG, totT;
+  const uint32_t eW = warp_excl_scan(mW, totW);
+  const uint32_t eG = warp_excl_scan(mG, totG);
+  const uint32_t eWG = warp_excl_scan(mW + mG, totWG);
+  const uint32_t eT = warp_excl_scan(t, totT);
+  if (lane == 0) {
+    sm.warpW[warp] = totW;
+    sm.warpG[warp] = totG;
+    sm.warpT[warp] = totT;
+  }
+  __syncthreads();
+  const uint32_t stage0 = sm.stageCount;
+  const uint32_t room = kStageCap - stage0;
+  uint32_t used = 0, glob = 0, term = 0, myStage = 0, myGlob = 0, myTerm = 0;
+  bool myFit = false;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) {
+    const uint32_t W = sm.warpW[w], Gw = sm.warpG[w], T = sm.warpT[w];
+    const bool fit = W != 0 && used + W <= room;
+    if (w == warp) {
+      myFit = fit;
+      myStage = used;
+      myGlob = glob;
+      myTerm = term;
+    }
+    if (fit) used += W;
+    glob += Gw + (fit ? 0u : W);
+    term += T;
+  }
+  if (tid == 0) {
+    if (term) sm.termBase = atomicAdd(&a.st->termCount, (unsigned long long)term);
+    if (glob) sm.nodeBase = atomicAdd(&a.st->nodeNext, (unsigned long long)glob);
+  }
+  __syncthreads();
+  if (tid == 0) sm.stageCount = stage0 + used;
+  if (kind == kTerm) {
+    unsigned long long slot = sm.termBase + myTerm + eT;
+    if (slot < a.cap) {
+      store_terminal(a, slot, y, tidx);
+      if (a.termLinks != nullptr && slot < a.termLinkCap) a.termLinks[slot] = make_uint2(link, ordinal);
+    }
+  } else if (kind == kNode) {
+    if (want && myFit) {
+      const uint32_t at = stage0 + myStage + eW;
+      for (uint32_t j = 0; j < m; j++)
+        store_stage(sm.stage, at + j, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
+    } else {
+      const unsigned long long at = sm.nodeBase + myGlob + (myFit ? eG : eWG);
+      for (uint32_t j = 0; j < m; j++) {
+        if (at + j < a.nodeCap) {
+          store_node(a.nodes, at + j, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
+        } else {
+          raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, -1);
+          break;
+        }
       }
     }
   }
-  unsigned nm = __ballot_sync(kFull, kind == kNode);
-  if (nm) {
-    unsigned leader = __ffs(nm) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&a.st->nodeNext, (unsigned long long)__popc(nm));
-    base = __shfl_sync(kFull, base, leader);
-    if (kind == kNode) {
-      unsigned long long slot = base + __popc(nm & lanemask_lt());
-      if (slot < a.nodeCap) {
-        store_node(a.nodes, slot, y);
-        if (a.nodeLinks != nullptr) a.nodeLinks[slot] = make_uint2(link, ordinal);
-      } else {
-        raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, (int)(slot > 0x7FFFFFFFull ? 0x7FFFFFFF : slot));
-      }
-    }
-  }
+}
+
+__device__ __forceinline__ void emit_resolved(const DeriveArgs& a, Smem& sm, int kind, const Shape& y,
+                                              uint32_t tidx, uint32_t link, uint32_t ordinal, bool canStage) {
+  uint32_t nChild = (kind == kNode) ? count_children(a, y) : 0u;
+  block_emit(a, sm, kind, y, tidx, nChild, link, ordinal, canStage);
 }
 
 // Root shape of axiom i, as Grid::...::generateAxiom builds it (Grid.cuh:199-204).
 __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Shape& x) {
   const PgaAxiom* ax = a.axioms + i;
-  x.r[0][0] = 1.0f; x.r[0][1] = 0.0f; x.r[0][2] = 0.0f;
-  x.r[1][0] = 0.0f; x.r[1][1] = 1.0f; x.r[1][2] = 0.0f;
-  x.r[2][0] = 0.0f; x.r[2][1] = 0.0f; x.r[2][2] = 1.0f;
+  x.frame = kIdentityFrame;
   x.t[0] = __ldg(&ax->position[0]); x.t[1] = __ldg(&ax->position[1]); x.t[2] = __ldg(&ax->position[2]);
   x.s[0] = __ldg(&ax->size[0]); x.s[1] = __ldg(&ax->size[1]); x.s[2] = __ldg(&ax->size[2]);
   x.seed = __ldg(&ax->seed);
@@ -474,13 +657,54 @@ __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Sha
   x.path = mix64((uint64_t)i + 0x9E3779B97F4A7C15ULL);
 }
 
-// Seeds axioms [first, first + count) with a warp-uniform grid-stride loop.
-__device__ void seed_axioms(const DeriveArgs& a, uint32_t first, uint32_t count) {
-  const unsigned lane = threadIdx.x & 31u;
-  const unsigned long long warpId = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const unsigned long long numWarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-  for (unsigned long long b = warpId * 32; b < count; b += numWarps * 32) {
-    unsigned long long i = b + lane;
+// Expands 256 work items: from the level queue [base, base + 256) ∩ [.., hi),
+// or (fromStage) the block's staged items.
+__device__ void process_chunk(const DeriveArgs& a, Smem& sm, unsigned long long base, unsigned long long hi,
+                              bool fromStage) {
+  const int tid = threadIdx.x;
+  Expander E;
+  uint4 ext = make_uint4(0, 0, 0, 0);
+  uint32_t c0 = 0, n = 0, link = 0;
+  bool valid = fromStage ? ((uint32_t)tid < sm.stageCount) : (base + tid < hi);
+  if (valid) {
+    if (fromStage) {
+      load_stage(sm.stage, tid, E.base, ext);
+    } else {
+      load_node(a.nodes, base + tid, E.base, ext);
+      link = (uint32_t)(base + tid);
+    }
+    const int32_t e = E.base.entry;
+    if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
+      raise_error(a.st, PGA_ERR_BAD_OPCODE, e);
+    } else {
+      E.r = rule_at(a, (uint32_t)e);
+      E.base.kind = E.r.shape;
+      uint32_t all = expander_init(a, E);
+      uint32_t c1 = min(ext.y, all);
+      c0 = ext.x;
+      if (c0 < c1) {
+        expander_skip(a, E, c0);
+        n = c1 - c0;
+      }
+    }
+  }
+  __syncthreads();  // the stage has been read
+  if (fromStage && tid == 0) sm.stageCount = 0;
+  const bool canStage = a.stage != 0 && !fromStage;
+  for (uint32_t r = 0; __syncthreads_or(r < n); r++) {
+    int kind = kNone;
+    Shape y;
+    uint32_t tidx = 0, ordinal = 0;
+    if (r < n && expander_child(a, E, c0 + r, y, ordinal)) kind = resolve(a, y, tidx);
+    emit_resolved(a, sm, kind, y, tidx, link, ordinal, canStage);
+  }
+}
+
+// Seeds the axioms [first, first + count): one axiom per thread, block-wide.
+__device__ void seed_axioms(const DeriveArgs& a, Smem& sm, uint32_t first, uint32_t count) {
+  for (unsigned long long b = (unsigned long long)blockIdx.x * kThreads; b < count;
+       b += (unsigned long long)gridDim.x * kThreads) {
+    const unsigned long long i = b + threadIdx.x;
     int kind = kNone;
     Shape y;
     uint32_t tidx = 0;
@@ -488,34 +712,24 @@ __device__ void seed_axioms(const DeriveArgs& a, uint32_t first, uint32_t count)
       axiom_shape(a, first + (uint32_t)i, y);
       kind = resolve(a, y, tidx);
     }
-    emit(a, kind, y, tidx, kAxiomLink | (first + (uint32_t)i), 0u);
+    emit_resolved(a, sm, kind, y, tidx, kAxiomLink | (first + (uint32_t)i), 0u, a.stage != 0);
+    __syncthreads();
+    if (sm.stageCount) process_chunk(a, sm, 0, 0, true);
   }
 }
 
-// Expands the queued shapes of one warp-wide chunk [base, base + 32) ∩ [.., hi).
-__device__ __forceinline__ void expand_chunk(const DeriveArgs& a, unsigned long long base, unsigned long long hi) {
-  const unsigned lane = threadIdx.x & 31u;
-  unsigned long long i = base + lane;
-  Expander E;
-  uint32_t n = 0;
-  if (i < hi) {
-    load_node(a.nodes, i, E.base);
-    int32_t e = E.base.entry;
-    if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
-      raise_error(a.st, PGA_ERR_BAD_OPCODE, e);
-    } else {
-      E.r = a.tab.rules[e];
-      E.base.kind = E.r.shape;
-      n = expander_init(a, E);
-    }
+// Copies the rule table into shared memory when it fits (set at launch).
+__device__ __forceinline__ void setup_block(const DeriveArgs& a, Smem& sm) {
+  if (threadIdx.x == 0) sm.stageCount = 0;
+  if (a.tableInSmem) {
+    DevRule* rules = reinterpret_cast<DevRule*>(smem_raw + sizeof(Smem));
+    DevParam* params = reinterpret_cast<DevParam*>(rules + a.tab.numEntries);
+    int32_t* succ = reinterpret_cast<int32_t*>(params + a.numParams);
+    for (uint32_t i = threadIdx.x; i < a.tab.numEntries; i += kThreads) rules[i] = a.tab.rules[i];
+    for (uint32_t i = threadIdx.x; i < a.numParams; i += kThreads) params[i] = a.tab.params[i];
+    for (uint32_t i = threadIdx.x; i < a.numSucc; i += kThreads) succ[i] = a.tab.succ[i];
   }
-  for (uint32_t c = 0; __any_sync(kFull, c < n); c++) {
-    int kind = kNone;
-    Shape y;
-    uint32_t tidx = 0, ordinal = 0;
-    if (c < n && expander_child(a, E, c, y, ordinal)) kind = resolve(a, y, tidx);
-    emit(a, kind, y, tidx, (uint32_t)i, ordinal);
-  }
+  __syncthreads();
 }
 
 // ---------------------------------------------------- bounded grid barrier
@@ -547,7 +761,7 @@ __device__ bool grid_barrier(const DeriveArgs& a, Leader leader) {
           ok = 0;
           break;
         }
-        __nanosleep(100);
+        __nanosleep(32);
       }
     }
     __threadfence();
@@ -582,8 +796,10 @@ __device__ __forceinline__ void level_snapshot(const DeriveArgs& a, uint32_t lev
   vs->stop = (!more || vs->status != 0) ? 1u : 0u;
 }
 
-__global__ void __launch_bounds__(256) k_derive_persistent(DeriveArgs a) {
-  seed_axioms(a, 0, a.numAxioms);
+__global__ void __launch_bounds__(kThreads, 3) k_derive_persistent(DeriveArgs a) {
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  setup_block(a, sm);
+  seed_axioms(a, sm, 0, a.numAxioms);
   if (!grid_barrier(a, [&] {
         volatile DevState* vs = a.st;
         vs->levelHi = 0;
@@ -595,27 +811,36 @@ __global__ void __launch_bounds__(256) k_derive_persistent(DeriveArgs a) {
     volatile DevState* vs = a.st;
     if (vs->stop) break;
     const unsigned long long hi = vs->levelHi;
-    const unsigned lane = threadIdx.x & 31u;
     for (;;) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(&a.st->cursor, 32ull);
-      base = __shfl_sync(kFull, base, 0);
+      if (threadIdx.x == 0) sm.chunkBase = atomicAdd(&a.st->cursor, (unsigned long long)kThreads);
+      __syncthreads();
+      const unsigned long long base = sm.chunkBase;
+      __syncthreads();
       if (base >= hi) break;
-      expand_chunk(a, base, hi);
+      process_chunk(a, sm, base, hi, false);
+      if (sm.stageCount) process_chunk(a, sm, 0, 0, true);
     }
     if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0 && a.outCount != nullptr) *a.outCount = a.st->termCount;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && a.outCount != nullptr)
+    *a.outCount = atomicAdd(&a.st->termCount, 0ull);
 }
 
-__global__ void __launch_bounds__(256) k_seed(DeriveArgs a, uint32_t first, uint32_t count) {
-  seed_axioms(a, first, count);
+__global__ void __launch_bounds__(kThreads, 3) k_seed(DeriveArgs a, uint32_t first, uint32_t count) {
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  setup_block(a, sm);
+  seed_axioms(a, sm, first, count);
 }
 
-__global__ void __launch_bounds__(256) k_expand_level(DeriveArgs a, unsigned long long lo, unsigned long long hi) {
-  unsigned long long warpId = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  unsigned long long base = lo + warpId * 32;
-  if (base < hi) expand_chunk(a, base, hi);
+__global__ void __launch_bounds__(kThreads, 3) k_expand_level(DeriveArgs a, unsigned long long lo,
+                                                              unsigned long long hi) {
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  setup_block(a, sm);
+  const unsigned long long base = lo + (unsigned long long)blockIdx.x * kThreads;
+  if (base < hi) {
+    process_chunk(a, sm, base, hi, false);
+    if (sm.stageCount) process_chunk(a, sm, 0, 0, true);
+  }
 }
 
 __global__ void k_write_count(const DevState* st, unsigned long long* out) { *out = st->termCount; }
@@ -656,6 +881,12 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.levelClock = e->dLevelClock;
   a.maxLevels = e->cfg.maxLevels;
   a.spinLimit = e->cfg.spinLimit;
+  a.subItem = e->cfg.subItem;
+  a.useSeeds = e->useSeeds ? 1u : 0u;
+  a.stage = (e->cfg.recordTape || (e->cfg.flags & PGA_FLAG_NO_STAGE)) ? 0u : 1u;
+  a.tableInSmem = e->tableInSmem ? 1u : 0u;
+  a.numParams = (uint32_t)e->hParams.size();
+  a.numSucc = (uint32_t)e->hSucc.size();
   a.st = e->dState;
   return a;
 }
@@ -710,6 +941,12 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   if (c.threadsPerBlock == 0) c.threadsPerBlock = 256;
   if (c.spinLimit == 0) c.spinLimit = 1u << 24;
   if (c.maxLevels == 0) c.maxLevels = 4096;
+  if (c.subItem == 0) c.subItem = 8;
+  if (c.subItem > 64) {
+    set_error("pga_engine_create: subItem must be at most 64");
+    delete e;
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
   if (c.threadsPerBlock != 256) {
     set_error("pga_engine_create: threadsPerBlock must be 256");
     delete e;
@@ -745,6 +982,16 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     }
     r.nParams = (uint8_t)en.numParameters;
     r.nSucc = (uint8_t)en.numSuccessors;
+    bool pure = true;
+    for (uint32_t k = 0; k < en.numParameters; k++) {
+      const PgaParameter& p = en.parameters[k];
+      if (p.type != PGA_PT_SCALAR && p.type != PGA_PT_BLOCK) pure = false;
+      // Seeds are observable only through random ranges, expressions and the
+      // seed attribute (Shape::at(15)); otherwise seed updates can be skipped.
+      if (p.type == PGA_PT_RAND || p.type == PGA_PT_EXP) e->useSeeds = true;
+      if (p.type == PGA_PT_SHAPE_ATTR && p.value[0] >= 15.0f && p.value[0] < 16.0f) e->useSeeds = true;
+    }
+    r.flags = pure ? kRulePure : 0;
     r.paramBase = (uint32_t)e->hParams.size();
     r.succBase = (uint32_t)e->hSucc.size();
     for (uint32_t k = 0; k < en.numParameters; k++) {
@@ -810,10 +1057,22 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   if (err == cudaSuccess) err = cudaMemset(e->dState, 0, sizeof(DevState));
   if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create upload"));
 
+  // Shared memory: the stage, plus the rule table when it is small.
+  size_t tableBytes = e->hRules.size() * sizeof(DevRule) + e->hParams.size() * sizeof(DevParam) +
+                      e->hSucc.size() * sizeof(int32_t);
+  e->tableInSmem = tableBytes <= 48 * 1024;
+  e->smemBytes = sizeof(Smem) + (e->tableInSmem ? ((tableBytes + 15) & ~size_t(15)) : 0);
   err = cudaGetDevice(&e->device);
   if (err == cudaSuccess) err = cudaDeviceGetAttribute(&e->numSMs, cudaDevAttrMultiProcessorCount, e->device);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_derive_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_expand_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
   int perSM = 0;
-  if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_derive_persistent, e->threads, 0);
+  if (err == cudaSuccess)
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_derive_persistent, e->threads, e->smemBytes);
   if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create occupancy"));
   if (c.blocksPerSM > 0 && (int)c.blocksPerSM < perSM) perSM = (int)c.blocksPerSM;
   if (perSM < 1) perSM = 1;
@@ -842,6 +1101,7 @@ PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, 
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)e->persistentBlocks);
   cfg.blockDim = dim3((unsigned)e->threads);
+  cfg.dynamicSmemBytes = e->smemBytes;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -867,11 +1127,12 @@ PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAx
   DeriveArgs a = make_args(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
   a.nodeLinks = nullptr;  // the arena is reused per axiom: no tape
   a.termLinks = nullptr;
+  a.stage = 0;            // one thread per shape, every branching shape through the queue
   const unsigned threads = (unsigned)e->threads;
   for (uint32_t ax = 0; ax < numAxioms; ax++) {
     // One grammar (axiom) at a time: reset the queue, seed, expand level by level.
     PGA_CUDA_TRY(cudaMemsetAsync(&e->dState->nodeNext, 0, sizeof(unsigned long long), s));
-    k_seed<<<1, 32, 0, s>>>(a, ax, 1);
+    k_seed<<<1, threads, e->smemBytes, s>>>(a, ax, 1);
     PGA_CUDA_TRY(cudaGetLastError());
     unsigned long long lo = 0, hi = 0;
     int32_t status = 0;
@@ -888,7 +1149,7 @@ PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAx
       }
       unsigned long long n = hi - lo;
       unsigned long long blocks = (n + threads - 1) / threads;
-      k_expand_level<<<(unsigned)blocks, threads, 0, s>>>(a, lo, hi);
+      k_expand_level<<<(unsigned)blocks, threads, e->smemBytes, s>>>(a, lo, hi);
       PGA_CUDA_TRY(cudaGetLastError());
       lo = hi;
     }

@@ -11,6 +11,13 @@
 // offset o, column permutations/negations of R, and R[:,j] * s_j (the other
 // terms are products with exact zeros and ones).  Only the sign of a zero can
 // differ, which no output distinguishes.
+//
+// Axioms start with the identity rotation (the reference's axiom generators
+// only place and size them, Grid.cuh:199-204) and the operators of this path
+// only permute and negate columns, so every rotation is a signed permutation.
+// A shape therefore carries a 9-bit frame code instead of nine floats: column
+// j of R is sign_j * e_{perm_j}.  fl(R[i][a] * o) is then exactly +-o in row
+// perm_a and a signed zero elsewhere, so a translation is one rounded add.
 #pragma once
 
 #include <cstdint>
@@ -36,10 +43,12 @@ struct __align__(16) DevRule {
   uint8_t shape;     // PgaShape the procedure expects
   uint8_t nParams;
   uint8_t nSucc;
-  uint32_t nChildren;  // PGA_OP_SUBDIVIDE_STATIC
+  uint16_t nChildren;  // PGA_OP_SUBDIVIDE_STATIC
+  uint16_t flags;      // kRulePure: no parameter reads the shape (scalar or block values only)
   uint32_t paramBase;  // into DevParam[]
   uint32_t succBase;   // into int32 successor entries
 };
+constexpr uint16_t kRulePure = 1;
 
 struct DevTables {
   const DevRule* rules;
@@ -49,11 +58,14 @@ struct DevTables {
   uint32_t numEntries;
 };
 
-// 80-byte queued shape: model rows (rotation | translation), size + seed, meta.
+// 64-byte queued work item: a shape plus the range of its children that this
+// item produces (a branching shape with many children is queued as several
+// items of at most `subItem` children each).
 struct __align__(16) Node {
-  float4 r0, r1, r2;
-  float4 sz;     // size.xyz, seed
+  float4 ts;     // translation xyz, size x
+  float4 sf;     // size y, size z, seed, frame code (bits)
   uint4 meta;    // entry, axiom, path lo, path hi
+  uint4 ext;     // first child, end child, tape link (parent item or kAxiomLink | axiom), ordinal
 };
 
 struct DevState {
@@ -86,21 +98,40 @@ struct DeriveArgs {
   unsigned long long* levelClock;  // %globaltimer when each level's range was fixed
   uint32_t maxLevels;
   uint32_t spinLimit;
+  uint32_t subItem;     // children per queued item (1..8)
+  uint32_t useSeeds;    // 0: no parameter of the grammar reads a seed, skip seed updates
+  uint32_t stage;       // 1: stage one generation of children in shared memory
+  uint32_t tableInSmem; // 1: rule table copied to shared memory at launch
+  uint32_t numParams, numSucc;
   DevState* st;
 };
 
 // ------------------------------------------------------------ shape state
 
 struct Shape {
-  float r[3][3];   // rotation (model columns 0..2)
   float t[3];      // translation (model column 3)
   float s[3];      // size
   float seed;
+  uint32_t frame;  // rotation: bits 2j..2j+1 = row of column j's nonzero, bit 6+j = column j negated
   int32_t entry;
   uint32_t axiom;
   uint32_t kind;   // PgaShape
   uint64_t path;
 };
+
+constexpr uint32_t kIdentityFrame = 0u | (1u << 2) | (2u << 4);
+
+__device__ __forceinline__ uint32_t frame_row(uint32_t f, uint32_t col) { return (f >> (2 * col)) & 3u; }
+__device__ __forceinline__ uint32_t frame_neg(uint32_t f, uint32_t col) { return (f >> (6 + col)) & 1u; }
+// Column `col` of the result is column `src` of f, negated when `flip`.
+__device__ __forceinline__ uint32_t frame_set(uint32_t g, uint32_t col, uint32_t f, uint32_t src, uint32_t flip) {
+  g &= ~((3u << (2 * col)) | (1u << (6 + col)));
+  return g | (frame_row(f, src) << (2 * col)) | ((frame_neg(f, src) ^ flip) << (6 + col));
+}
+// R[row][col] of a frame: 0, 1 or -1.
+__device__ __forceinline__ float frame_entry(uint32_t f, uint32_t row, uint32_t col) {
+  return frame_row(f, col) == row ? (frame_neg(f, col) ? -1.0f : 1.0f) : 0.0f;
+}
 
 __device__ __forceinline__ void raise_error(DevState* st, int code, int detail) {
   if (atomicCAS(&st->status, 0, code) == 0) atomicExch(&st->detail, detail);
@@ -155,9 +186,7 @@ __device__ __forceinline__ void put3(float v[3], uint32_t k, float x) {
 __device__ __forceinline__ float shape_attr(const Shape& x, uint32_t i, float custom) {
   if (i < 12) {
     uint32_t row = i >> 2, col = i & 3;
-    float rr[3] = {pick3(x.r[0], col), pick3(x.r[1], col), pick3(x.r[2], col)};
-    float tt = pick3(x.t, row);
-    return col == 3 ? tt : pick3(rr, row);
+    return col == 3 ? pick3(x.t, row) : frame_entry(x.frame, row, col);
   }
   if (i < 15) return pick3(x.s, i - 12);
   if (i == 15) return x.seed;

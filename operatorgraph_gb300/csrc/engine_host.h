@@ -25,6 +25,9 @@ struct PgaEngine {
   int numSMs = 0;
   int persistentBlocks = 0;
   int threads = 256;
+  bool useSeeds = false;
+  bool tableInSmem = false;
+  size_t smemBytes = 0;
 
   // Work storage (allocated once in pga_engine_create).
   pga::DevState* dState = nullptr;
