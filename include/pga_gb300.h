@@ -145,7 +145,8 @@ typedef enum PgaStatus {
   PGA_ERR_CUDA = 6,             /* a CUDA runtime call failed */
   PGA_ERR_INVALID_ARGUMENT = 7, /* bad host-side argument */
   PGA_ERR_NO_TAPE = 8,          /* pga_adjoint without a recorded tape */
-  PGA_ERR_DEPTH = 9             /* maxLevels exceeded (likely a recursive grammar) */
+  PGA_ERR_DEPTH = 9,            /* maxLevels exceeded (likely a recursive grammar) */
+  PGA_ERR_INTERNAL = 10         /* a bounds check of a checked build failed (detail = check site) */
 } PgaStatus;
 
 /* Result of the last derivation, read back by pga_engine_sync_report. */

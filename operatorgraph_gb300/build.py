@@ -12,12 +12,18 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
-LIB = os.path.join(HERE, "libpga_gb300.so")
+# PGA_CHECKS=1 builds the bounds-checked variant (every table, queue and output
+# access checked; a failed check raises PGA_ERR_INTERNAL instead of accessing).
+CHECKED = os.environ.get("PGA_CHECKS") == "1"
+LIB = os.path.join(HERE, "libpga_gb300_checked.so" if CHECKED else "libpga_gb300.so")
 SOURCES = ["derive.cu", "lbvh.cu", "adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: no FMA contraction anywhere in the derivation path (the kernels
 # also use explicit round-to-nearest intrinsics).
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+if CHECKED:
+    FLAGS += ["-DPGA_CHECKS=1"]
+    BUILD = BUILD + "_checked"
 
 
 def nvcc():

@@ -54,18 +54,42 @@ struct __align__(16) Smem {
 
 extern __shared__ __align__(16) unsigned char smem_raw[];
 
+// Checked builds (-DPGA_CHECKS) test every table, queue, stage and axiom index
+// before the access; a failure raises PGA_ERR_INTERNAL with the site number and
+// skips the access.
+#ifdef PGA_CHECKS
+#define PGA_GUARD(cond, site, ...)                  \
+  do {                                              \
+    if (!(cond)) {                                  \
+      raise_error(a.st, PGA_ERR_INTERNAL, (site));  \
+      __VA_ARGS__;                                  \
+    }                                               \
+  } while (0)
+#else
+#define PGA_GUARD(cond, site, ...) \
+  do {                             \
+  } while (0)
+#endif
+
 // Rule-table reads: from the block's shared-memory copy when the table fits
 // (tableInSmem), else from global memory.
 __device__ __forceinline__ DevRule rule_at(const DeriveArgs& a, uint32_t e) {
+  PGA_GUARD(e < a.tab.numEntries, 1, {
+    DevRule bad{};
+    bad.op = 0xFF;
+    return bad;
+  });
   if (a.tableInSmem) return reinterpret_cast<const DevRule*>(smem_raw + sizeof(Smem))[e];
   return a.tab.rules[e];
 }
 __device__ __forceinline__ DevParam param_at(const DeriveArgs& a, uint32_t k) {
+  PGA_GUARD(k < a.numParams, 2, return DevParam{});
   if (a.tableInSmem)
     return reinterpret_cast<const DevParam*>(smem_raw + sizeof(Smem) + (size_t)a.tab.numEntries * sizeof(DevRule))[k];
   return a.tab.params[k];
 }
 __device__ __forceinline__ int32_t succ_at(const DeriveArgs& a, uint32_t k) {
+  PGA_GUARD(k < a.numSucc, 3, return -1);
   if (a.tableInSmem)
     return reinterpret_cast<const int32_t*>(smem_raw + sizeof(Smem) + (size_t)a.tab.numEntries * sizeof(DevRule) +
                                             (size_t)a.numParams * sizeof(DevParam))[k];
@@ -102,6 +126,7 @@ __device__ __noinline__ float eval_param_slow(const DeriveArgs& a, DevParam p, S
       return rand_range(x.seed, p.v0, p.v1);
     case PGA_PT_SHAPE_ATTR: {
       uint32_t i = f2u(p.v0);
+      PGA_GUARD(x.axiom < a.numAxioms, 7, return 0.0f);
       float custom = (i == 16) ? __ldg(&a.axioms[x.axiom].custom) : 0.0f;
       return shape_attr(x, i, custom);
     }
@@ -549,6 +574,7 @@ __device__ __forceinline__ void store_stage(Node* stage, uint32_t i, const Shape
 __device__ __forceinline__ void store_terminal(const DeriveArgs& a, unsigned long long slot, const Shape& x,
                                                uint32_t tidx) {
   float4* p = reinterpret_cast<float4*>(a.out + slot);
+  PGA_GUARD(x.axiom < a.numAxioms && slot < a.cap, 8, return);
   float custom = __ldg(&a.axioms[x.axiom].custom);
   uint32_t rule = ((uint32_t)x.entry & 0xFFFFFFu) | (tidx << 24) | (x.kind == PGA_SHAPE_QUAD ? 0x80000000u : 0u);
   // R[i][j] * s_j is exactly +-s_j in row perm_j and zero elsewhere.
@@ -622,8 +648,10 @@ __device__ __forceinline__ void block_emit(const DeriveArgs& a, Smem& sm, int ki
   } else if (kind == kNode) {
     if (want && myFit) {
       const uint32_t at = stage0 + myStage + eW;
-      for (uint32_t j = 0; j < m; j++)
+      for (uint32_t j = 0; j < m; j++) {
+        PGA_GUARD(at + j < kStageCap, 11, break);
         store_stage(sm.stage, at + j, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
+      }
     } else {
       const unsigned long long at = sm.nodeBase + myGlob + (myFit ? eG : eWG);
       for (uint32_t j = 0; j < m; j++) {
@@ -668,8 +696,10 @@ __device__ void process_chunk(const DeriveArgs& a, Smem& sm, unsigned long long 
   bool valid = fromStage ? ((uint32_t)tid < sm.stageCount) : (base + tid < hi);
   if (valid) {
     if (fromStage) {
+      PGA_GUARD(tid < (int)kStageCap, 9, return);
       load_stage(sm.stage, tid, E.base, ext);
     } else {
+      PGA_GUARD(base + tid < a.nodeCap, 10, return);
       load_node(a.nodes, base + tid, E.base, ext);
       link = (uint32_t)(base + tid);
     }

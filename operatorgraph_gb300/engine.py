@@ -15,12 +15,12 @@ import numpy as np
 from . import grammar as G
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpga_gb300.so")
+LIB_PATH = os.environ.get("PGA_LIB") or os.path.join(HERE, "libpga_gb300.so")
 
 STATUS = {
     0: "PGA_OK", 1: "PGA_ERR_QUEUE_OVERFLOW", 2: "PGA_ERR_OUTPUT_OVERFLOW", 3: "PGA_ERR_TIMEOUT",
     4: "PGA_ERR_BAD_OPCODE", 5: "PGA_ERR_BAD_PARAM", 6: "PGA_ERR_CUDA", 7: "PGA_ERR_INVALID_ARGUMENT",
-    8: "PGA_ERR_NO_TAPE", 9: "PGA_ERR_DEPTH",
+    8: "PGA_ERR_NO_TAPE", 9: "PGA_ERR_DEPTH", 10: "PGA_ERR_INTERNAL",
 }
 
 # Every symbol include/pga_gb300.h declares.
