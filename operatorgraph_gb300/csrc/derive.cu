@@ -46,6 +46,11 @@ enum Kind { kNone = 0, kTerm = 1, kNode = 2 };
 
 struct __align__(16) Smem {
   Node stage[kStageCap];
+  // Rule table of this block: generic pointers to the shared-memory copy or to
+  // global memory, fixed once in setup_block (no per-access address-space choice).
+  const DevRule* rules;
+  const DevParam* params;
+  const int32_t* succ;
   unsigned long long termBase, nodeBase, chunkBase;
   uint32_t warpW[kWarps], warpG[kWarps], warpT[kWarps];
   uint32_t stageCount;
@@ -71,29 +76,25 @@ extern __shared__ __align__(16) unsigned char smem_raw[];
   } while (0)
 #endif
 
-// Rule-table reads: from the block's shared-memory copy when the table fits
-// (tableInSmem), else from global memory.
+__device__ __forceinline__ Smem& block_smem() { return *reinterpret_cast<Smem*>(smem_raw); }
+
+// Rule-table reads through the block's table pointers (shared-memory copy when
+// the table fits, else global memory).
 __device__ __forceinline__ DevRule rule_at(const DeriveArgs& a, uint32_t e) {
   PGA_GUARD(e < a.tab.numEntries, 1, {
     DevRule bad{};
     bad.op = 0xFF;
     return bad;
   });
-  if (a.tableInSmem) return reinterpret_cast<const DevRule*>(smem_raw + sizeof(Smem))[e];
-  return a.tab.rules[e];
+  return block_smem().rules[e];
 }
 __device__ __forceinline__ DevParam param_at(const DeriveArgs& a, uint32_t k) {
   PGA_GUARD(k < a.numParams, 2, return DevParam{});
-  if (a.tableInSmem)
-    return reinterpret_cast<const DevParam*>(smem_raw + sizeof(Smem) + (size_t)a.tab.numEntries * sizeof(DevRule))[k];
-  return a.tab.params[k];
+  return block_smem().params[k];
 }
 __device__ __forceinline__ int32_t succ_at(const DeriveArgs& a, uint32_t k) {
   PGA_GUARD(k < a.numSucc, 3, return -1);
-  if (a.tableInSmem)
-    return reinterpret_cast<const int32_t*>(smem_raw + sizeof(Smem) + (size_t)a.tab.numEntries * sizeof(DevRule) +
-                                            (size_t)a.numParams * sizeof(DevParam))[k];
-  return succ_at(a, k);
+  return block_smem().succ[k];
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -748,17 +749,32 @@ __device__ void seed_axioms(const DeriveArgs& a, Smem& sm, uint32_t first, uint3
   }
 }
 
-// Copies the rule table into shared memory when it fits (set at launch).
+// Copies the rule table into shared memory when it fits (decided at engine
+// creation, which sized the dynamic shared memory for it) and fixes the block's
+// table pointers.
 __device__ __forceinline__ void setup_block(const DeriveArgs& a, Smem& sm) {
-  if (threadIdx.x == 0) sm.stageCount = 0;
-  if (a.tableInSmem) {
+  uint32_t dynBytes;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dynBytes));
+  const size_t tableBytes = (size_t)a.tab.numEntries * sizeof(DevRule) + (size_t)a.numParams * sizeof(DevParam) +
+                            (size_t)a.numSucc * sizeof(int32_t);
+  if (a.tableInSmem && sizeof(Smem) + tableBytes <= dynBytes) {
     DevRule* rules = reinterpret_cast<DevRule*>(smem_raw + sizeof(Smem));
     DevParam* params = reinterpret_cast<DevParam*>(rules + a.tab.numEntries);
     int32_t* succ = reinterpret_cast<int32_t*>(params + a.numParams);
     for (uint32_t i = threadIdx.x; i < a.tab.numEntries; i += kThreads) rules[i] = a.tab.rules[i];
     for (uint32_t i = threadIdx.x; i < a.numParams; i += kThreads) params[i] = a.tab.params[i];
     for (uint32_t i = threadIdx.x; i < a.numSucc; i += kThreads) succ[i] = a.tab.succ[i];
+    if (threadIdx.x == 0) {
+      sm.rules = rules;
+      sm.params = params;
+      sm.succ = succ;
+    }
+  } else if (threadIdx.x == 0) {
+    sm.rules = a.tab.rules;
+    sm.params = a.tab.params;
+    sm.succ = a.tab.succ;
   }
+  if (threadIdx.x == 0) sm.stageCount = 0;
   __syncthreads();
 }
 
