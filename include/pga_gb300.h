@@ -130,10 +130,13 @@ typedef struct PgaEngineConfig {
   uint32_t maxLevels;        /* derivation depth limit (0 = default 4096) */
   uint32_t flags;            /* PGA_FLAG_* */
   uint32_t subItem;          /* children per queued work item, 1..64 (0 = default 8) */
+  uint32_t inlineMax;        /* expand branching children with at most this many children in
+                                place, one generation deep (0 = default 8) */
+  uint32_t reserved;
 } PgaEngineConfig;
 
 /* PgaEngineConfig.flags */
-#define PGA_FLAG_NO_STAGE 1u /* queue every branching shape (no shared-memory staging) */
+#define PGA_FLAG_NO_INLINE 1u /* queue every branching shape (no in-place expansion) */
 
 typedef enum PgaStatus {
   PGA_OK = 0,

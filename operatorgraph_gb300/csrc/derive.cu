@@ -8,13 +8,13 @@
 // 1 -> 1 rules (IfSizeLess, Extrude) and ends as a terminal (Generate: written
 // out directly), a discard, or a branching shape that is queued as work items.
 //
-// A block works on 256 items at a time and emits in block-synchronous rounds:
-// one child per thread per round, block-wide prefix sums, one global atomic per
-// round for the terminals and one for the queued items, so each round writes a
-// contiguous run of 64-byte terminal records.  Small branching children are
-// staged in shared memory and expanded by the same block right after the
-// current chunk (their own branching children go to the next level), which
-// halves the queue traffic and the number of levels.
+// A block works on 256 items at a time, in two passes over the same children:
+// the first counts the terminals and queued items each thread produces, a
+// block-wide prefix sum and one global atomic per counter reserve contiguous
+// slots for the whole block, the second recomputes the children and writes
+// them.  A branching child with at most `inlineMax` children (a window
+// Subdivide, a ComponentSplit, a Menger sub-step) is expanded in place, one
+// generation deep, instead of being queued.
 //
 // pga_derive runs every level of every axiom in ONE persistent cooperative
 // launch (a bounded grid barrier between levels, blocks pulling 256 items at a
@@ -41,25 +41,21 @@ namespace pga {
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr uint32_t kStageCap = kThreads;
 enum Kind { kNone = 0, kTerm = 1, kNode = 2 };
 
 struct __align__(16) Smem {
-  Node stage[kStageCap];
   // Rule table of this block: generic pointers to the shared-memory copy or to
   // global memory, fixed once in setup_block (no per-access address-space choice).
   const DevRule* rules;
   const DevParam* params;
   const int32_t* succ;
   unsigned long long termBase, nodeBase, chunkBase;
-  uint32_t warpW[kWarps], warpG[kWarps], warpT[kWarps];
-  uint32_t stageCount;
-  uint32_t pad;
+  unsigned long long warpT[kWarps], warpG[kWarps];
 };
 
 extern __shared__ __align__(16) unsigned char smem_raw[];
 
-// Checked builds (-DPGA_CHECKS) test every table, queue, stage and axiom index
+// Checked builds (-DPGA_CHECKS) test every table, queue and axiom index
 // before the access; a failure raises PGA_ERR_INTERNAL with the site number and
 // skips the access.
 #ifdef PGA_CHECKS
@@ -541,12 +537,6 @@ __device__ __forceinline__ void load_node(const Node* nodes, unsigned long long 
   unpack_node(a, b, m, x);
 }
 
-__device__ __forceinline__ void load_stage(const Node* stage, uint32_t i, Shape& x, uint4& ext) {
-  const Node& n = stage[i];
-  unpack_node(n.ts, n.sf, n.meta, x);
-  ext = n.ext;
-}
-
 __device__ __forceinline__ void pack_node(const Shape& x, float4& a, float4& b, uint4& m) {
   a = make_float4(x.t[0], x.t[1], x.t[2], x.s[0]);
   b = make_float4(x.s[1], x.s[2], x.seed, __uint_as_float(x.frame));
@@ -562,12 +552,6 @@ __device__ __forceinline__ void store_node(Node* nodes, unsigned long long i, co
   __stcg(p + 1, b);
   __stcg(reinterpret_cast<uint4*>(p + 2), m);
   __stcg(reinterpret_cast<uint4*>(p + 3), ext);
-}
-
-__device__ __forceinline__ void store_stage(Node* stage, uint32_t i, const Shape& x, uint4 ext) {
-  Node& n = stage[i];
-  pack_node(x, n.ts, n.sf, n.meta);
-  n.ext = ext;
 }
 
 // GenerationFunction<.., 1>::perShape (GenerationFunctions.cuh:158-188):
@@ -594,83 +578,107 @@ __device__ __forceinline__ void store_terminal(const DeriveArgs& a, unsigned lon
          make_uint4(rule, __float_as_uint(custom), (uint32_t)x.path, (uint32_t)(x.path >> 32)));
 }
 
-// Block-collective emission of one shape per thread.  kind: kNone, kTerm or
-// kNode (a branching shape with `nChild` children, queued as ceil(nChild /
-// subItem) items).  Small nodes go to the shared-memory stage when allowed.
-// One global atomic per round for terminals and one for queued items.
-__device__ __forceinline__ void block_emit(const DeriveArgs& a, Smem& sm, int kind, const Shape& y, uint32_t tidx,
-                                           uint32_t nChild, uint32_t link, uint32_t ordinal, bool canStage) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t S = a.subItem;
-  uint32_t m = (kind == kNode) ? (nChild + S - 1) / S : 0u;
-  const bool want = canStage && m != 0 && m <= 2;
-  const uint32_t mW = want ? m : 0u, mG = want ? 0u : m, t = (kind == kTerm) ? 1u : 0u;
-  uint32_t totW, totG, totWG, totT;
-  const uint32_t eW = warp_excl_scan(mW, totW);
-  const uint32_t eG = warp_excl_scan(mG, totG);
-  const uint32_t eWG = warp_excl_scan(mW + mG, totWG);
-  const uint32_t eT = warp_excl_scan(t, totT);
-  if (lane == 0) {
-    sm.warpW[warp] = totW;
-    sm.warpG[warp] = totG;
-    sm.warpT[warp] = totT;
-  }
-  __syncthreads();
-  const uint32_t stage0 = sm.stageCount;
-  const uint32_t room = kStageCap - stage0;
-  uint32_t used = 0, glob = 0, term = 0, myStage = 0, myGlob = 0, myTerm = 0;
-  bool myFit = false;
-#pragma unroll
-  for (int w = 0; w < kWarps; w++) {
-    const uint32_t W = sm.warpW[w], Gw = sm.warpG[w], T = sm.warpT[w];
-    const bool fit = W != 0 && used + W <= room;
-    if (w == warp) {
-      myFit = fit;
-      myStage = used;
-      myGlob = glob;
-      myTerm = term;
-    }
-    if (fit) used += W;
-    glob += Gw + (fit ? 0u : W);
-    term += T;
-  }
-  if (tid == 0) {
-    if (term) sm.termBase = atomicAdd(&a.st->termCount, (unsigned long long)term);
-    if (glob) sm.nodeBase = atomicAdd(&a.st->nodeNext, (unsigned long long)glob);
-  }
-  __syncthreads();
-  if (tid == 0) sm.stageCount = stage0 + used;
+// Output cursor of one thread: in the counting pass it only counts, in the
+// writing pass it writes at consecutive slots reserved for the thread.
+struct Emit {
+  bool write;
+  unsigned long long term;  // terminals: count, or next slot
+  unsigned long long node;  // queued items: count, or next slot
+};
+
+// Emits one resolved shape: a terminal, or a branching shape queued as
+// ceil(nChild / subItem) work items.
+__device__ __forceinline__ void emit_one(const DeriveArgs& a, Emit& em, int kind, const Shape& y, uint32_t tidx,
+                                         uint32_t nChild, uint32_t link, uint32_t ordinal) {
   if (kind == kTerm) {
-    unsigned long long slot = sm.termBase + myTerm + eT;
-    if (slot < a.cap) {
-      store_terminal(a, slot, y, tidx);
-      if (a.termLinks != nullptr && slot < a.termLinkCap) a.termLinks[slot] = make_uint2(link, ordinal);
+    if (em.write && em.term < a.cap) {
+      store_terminal(a, em.term, y, tidx);
+      if (a.termLinks != nullptr && em.term < a.termLinkCap) a.termLinks[em.term] = make_uint2(link, ordinal);
     }
+    em.term++;
   } else if (kind == kNode) {
-    if (want && myFit) {
-      const uint32_t at = stage0 + myStage + eW;
+    const uint32_t S = a.subItem;
+    const uint32_t m = (nChild + S - 1) / S;
+    if (em.write) {
       for (uint32_t j = 0; j < m; j++) {
-        PGA_GUARD(at + j < kStageCap, 11, break);
-        store_stage(sm.stage, at + j, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
-      }
-    } else {
-      const unsigned long long at = sm.nodeBase + myGlob + (myFit ? eG : eWG);
-      for (uint32_t j = 0; j < m; j++) {
-        if (at + j < a.nodeCap) {
-          store_node(a.nodes, at + j, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
-        } else {
+        if (em.node + j >= a.nodeCap) {
           raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, -1);
           break;
         }
+        store_node(a.nodes, em.node + j, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
       }
     }
+    em.node += m;
   }
 }
 
-__device__ __forceinline__ void emit_resolved(const DeriveArgs& a, Smem& sm, int kind, const Shape& y,
-                                              uint32_t tidx, uint32_t link, uint32_t ordinal, bool canStage) {
-  uint32_t nChild = (kind == kNode) ? count_children(a, y) : 0u;
-  block_emit(a, sm, kind, y, tidx, nChild, link, ordinal, canStage);
+// Resolves a new child and emits it.  A branching child with at most
+// inlineMax children is expanded in place, one generation deep: its children
+// are resolved and emitted instead of the child itself (no queue round trip).
+__device__ __forceinline__ void emit_child(const DeriveArgs& a, Emit& em, Shape& y, uint32_t link, uint32_t ordinal) {
+  uint32_t tidx = 0;
+  int kind = resolve(a, y, tidx);
+  if (kind != kNode) {
+    emit_one(a, em, kind, y, tidx, 0, link, ordinal);
+    return;
+  }
+  const uint32_t n = count_children(a, y);
+  if (n > a.inlineMax) {
+    emit_one(a, em, kNode, y, 0, n, link, ordinal);
+    return;
+  }
+  Expander F;
+  F.base = y;
+  F.r = rule_at(a, (uint32_t)y.entry);
+  F.base.kind = F.r.shape;
+  const uint32_t n2 = expander_init(a, F);
+  for (uint32_t c = 0; c < n2; c++) {
+    Shape z;
+    uint32_t ord2, t2 = 0;
+    if (!expander_child(a, F, c, z, ord2)) continue;
+    const int k2 = resolve(a, z, t2);
+    emit_one(a, em, k2, z, t2, k2 == kNode ? count_children(a, z) : 0u, link, ordinal);
+  }
+}
+
+// Reserves, for every thread of the block, `nT` terminal and `nG` item slots
+// with one global atomic each for the whole block.
+__device__ __forceinline__ void block_reserve(const DeriveArgs& a, Smem& sm, unsigned long long nT,
+                                              unsigned long long nG, unsigned long long& tSlot,
+                                              unsigned long long& gSlot) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  unsigned long long xT = nT, xG = nG;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    unsigned long long yT = __shfl_up_sync(kFull, xT, d), yG = __shfl_up_sync(kFull, xG, d);
+    if (lane >= d) {
+      xT += yT;
+      xG += yG;
+    }
+  }
+  if (lane == 31) {
+    sm.warpT[warp] = xT;
+    sm.warpG[warp] = xG;
+  }
+  __syncthreads();
+  unsigned long long preT = 0, preG = 0, totT = 0, totG = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) {
+    const unsigned long long T = sm.warpT[w], Gw = sm.warpG[w];
+    if (w < warp) {
+      preT += T;
+      preG += Gw;
+    }
+    totT += T;
+    totG += Gw;
+  }
+  if (tid == 0) {
+    sm.termBase = totT ? atomicAdd(&a.st->termCount, totT) : 0ull;
+    sm.nodeBase = totG ? atomicAdd(&a.st->nodeNext, totG) : 0ull;
+  }
+  __syncthreads();
+  tSlot = sm.termBase + preT + (xT - nT);
+  gSlot = sm.nodeBase + preG + (xG - nG);
 }
 
 // Root shape of axiom i, as Grid::...::generateAxiom builds it (Grid.cuh:199-204).
@@ -686,32 +694,36 @@ __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Sha
   x.path = mix64((uint64_t)i + 0x9E3779B97F4A7C15ULL);
 }
 
-// Expands 256 work items: from the level queue [base, base + 256) ∩ [.., hi),
-// or (fromStage) the block's staged items.
-__device__ void process_chunk(const DeriveArgs& a, Smem& sm, unsigned long long base, unsigned long long hi,
-                              bool fromStage) {
+// Produces the children [c0, c0 + n) of one work item.
+__device__ __forceinline__ void traverse(const DeriveArgs& a, Expander& E, uint32_t c0, uint32_t n, uint32_t link,
+                                         Emit& em) {
+  for (uint32_t c = c0; c < c0 + n; c++) {
+    Shape y;
+    uint32_t ordinal;
+    if (expander_child(a, E, c, y, ordinal)) emit_child(a, em, y, link, ordinal);
+  }
+}
+
+// Expands the work items [base, base + 256) ∩ [.., hi), one per thread, in two
+// passes over the same children: count, reserve (one atomic per block), write.
+__device__ void process_chunk(const DeriveArgs& a, Smem& sm, unsigned long long base, unsigned long long hi) {
   const int tid = threadIdx.x;
   Expander E;
-  uint4 ext = make_uint4(0, 0, 0, 0);
-  uint32_t c0 = 0, n = 0, link = 0;
-  bool valid = fromStage ? ((uint32_t)tid < sm.stageCount) : (base + tid < hi);
+  uint32_t c0 = 0, n = 0;
+  const uint32_t link = (uint32_t)(base + tid);
+  bool valid = base + tid < hi;
+  PGA_GUARD(!valid || base + tid < a.nodeCap, 10, valid = false);
   if (valid) {
-    if (fromStage) {
-      PGA_GUARD(tid < (int)kStageCap, 9, return);
-      load_stage(sm.stage, tid, E.base, ext);
-    } else {
-      PGA_GUARD(base + tid < a.nodeCap, 10, return);
-      load_node(a.nodes, base + tid, E.base, ext);
-      link = (uint32_t)(base + tid);
-    }
+    uint4 ext;
+    load_node(a.nodes, base + tid, E.base, ext);
     const int32_t e = E.base.entry;
     if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
       raise_error(a.st, PGA_ERR_BAD_OPCODE, e);
     } else {
       E.r = rule_at(a, (uint32_t)e);
       E.base.kind = E.r.shape;
-      uint32_t all = expander_init(a, E);
-      uint32_t c1 = min(ext.y, all);
+      const uint32_t all = expander_init(a, E);
+      const uint32_t c1 = min(ext.y, all);
       c0 = ext.x;
       if (c0 < c1) {
         expander_skip(a, E, c0);
@@ -719,15 +731,17 @@ __device__ void process_chunk(const DeriveArgs& a, Smem& sm, unsigned long long 
       }
     }
   }
-  __syncthreads();  // the stage has been read
-  if (fromStage && tid == 0) sm.stageCount = 0;
-  const bool canStage = a.stage != 0 && !fromStage;
-  for (uint32_t r = 0; __syncthreads_or(r < n); r++) {
-    int kind = kNone;
-    Shape y;
-    uint32_t tidx = 0, ordinal = 0;
-    if (r < n && expander_child(a, E, c0 + r, y, ordinal)) kind = resolve(a, y, tidx);
-    emit_resolved(a, sm, kind, y, tidx, link, ordinal, canStage);
+  const float off0 = E.offset, ps0 = E.prevSize, po0 = E.prevOff;
+  Emit em{false, 0ull, 0ull};
+  if (n) traverse(a, E, c0, n, link, em);
+  unsigned long long tSlot, gSlot;
+  block_reserve(a, sm, em.term, em.node, tSlot, gSlot);
+  if (n) {
+    E.offset = off0;
+    E.prevSize = ps0;
+    E.prevOff = po0;
+    Emit wr{true, tSlot, gSlot};
+    traverse(a, E, c0, n, link, wr);
   }
 }
 
@@ -736,16 +750,20 @@ __device__ void seed_axioms(const DeriveArgs& a, Smem& sm, uint32_t first, uint3
   for (unsigned long long b = (unsigned long long)blockIdx.x * kThreads; b < count;
        b += (unsigned long long)gridDim.x * kThreads) {
     const unsigned long long i = b + threadIdx.x;
-    int kind = kNone;
+    const uint32_t link = kAxiomLink | (first + (uint32_t)i);
+    Emit em{false, 0ull, 0ull};
     Shape y;
-    uint32_t tidx = 0;
     if (i < count) {
       axiom_shape(a, first + (uint32_t)i, y);
-      kind = resolve(a, y, tidx);
+      emit_child(a, em, y, link, 0u);
     }
-    emit_resolved(a, sm, kind, y, tidx, kAxiomLink | (first + (uint32_t)i), 0u, a.stage != 0);
-    __syncthreads();
-    if (sm.stageCount) process_chunk(a, sm, 0, 0, true);
+    unsigned long long tSlot, gSlot;
+    block_reserve(a, sm, em.term, em.node, tSlot, gSlot);
+    if (i < count) {
+      Emit wr{true, tSlot, gSlot};
+      axiom_shape(a, first + (uint32_t)i, y);
+      emit_child(a, wr, y, link, 0u);
+    }
   }
 }
 
@@ -774,7 +792,6 @@ __device__ __forceinline__ void setup_block(const DeriveArgs& a, Smem& sm) {
     sm.params = a.tab.params;
     sm.succ = a.tab.succ;
   }
-  if (threadIdx.x == 0) sm.stageCount = 0;
   __syncthreads();
 }
 
@@ -842,7 +859,7 @@ __device__ __forceinline__ void level_snapshot(const DeriveArgs& a, uint32_t lev
   vs->stop = (!more || vs->status != 0) ? 1u : 0u;
 }
 
-__global__ void __launch_bounds__(kThreads, 3) k_derive_persistent(DeriveArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
   seed_axioms(a, sm, 0, a.numAxioms);
@@ -863,8 +880,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_derive_persistent(DeriveArgs a)
       const unsigned long long base = sm.chunkBase;
       __syncthreads();
       if (base >= hi) break;
-      process_chunk(a, sm, base, hi, false);
-      if (sm.stageCount) process_chunk(a, sm, 0, 0, true);
+      process_chunk(a, sm, base, hi);
     }
     if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
   }
@@ -872,21 +888,18 @@ __global__ void __launch_bounds__(kThreads, 3) k_derive_persistent(DeriveArgs a)
     *a.outCount = atomicAdd(&a.st->termCount, 0ull);
 }
 
-__global__ void __launch_bounds__(kThreads, 3) k_seed(DeriveArgs a, uint32_t first, uint32_t count) {
+__global__ void __launch_bounds__(kThreads, 2) k_seed(DeriveArgs a, uint32_t first, uint32_t count) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
   seed_axioms(a, sm, first, count);
 }
 
-__global__ void __launch_bounds__(kThreads, 3) k_expand_level(DeriveArgs a, unsigned long long lo,
+__global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsigned long long lo,
                                                               unsigned long long hi) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
   const unsigned long long base = lo + (unsigned long long)blockIdx.x * kThreads;
-  if (base < hi) {
-    process_chunk(a, sm, base, hi, false);
-    if (sm.stageCount) process_chunk(a, sm, 0, 0, true);
-  }
+  if (base < hi) process_chunk(a, sm, base, hi);
 }
 
 __global__ void k_write_count(const DevState* st, unsigned long long* out) { *out = st->termCount; }
@@ -929,7 +942,7 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.spinLimit = e->cfg.spinLimit;
   a.subItem = e->cfg.subItem;
   a.useSeeds = e->useSeeds ? 1u : 0u;
-  a.stage = (e->cfg.recordTape || (e->cfg.flags & PGA_FLAG_NO_STAGE)) ? 0u : 1u;
+  a.inlineMax = (e->cfg.recordTape || (e->cfg.flags & PGA_FLAG_NO_INLINE)) ? 0u : e->cfg.inlineMax;
   a.tableInSmem = e->tableInSmem ? 1u : 0u;
   a.numParams = (uint32_t)e->hParams.size();
   a.numSucc = (uint32_t)e->hSucc.size();
@@ -988,6 +1001,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   if (c.spinLimit == 0) c.spinLimit = 1u << 24;
   if (c.maxLevels == 0) c.maxLevels = 4096;
   if (c.subItem == 0) c.subItem = 8;
+  if (c.inlineMax == 0) c.inlineMax = 8;
   if (c.subItem > 64) {
     set_error("pga_engine_create: subItem must be at most 64");
     delete e;
@@ -1103,7 +1117,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   if (err == cudaSuccess) err = cudaMemset(e->dState, 0, sizeof(DevState));
   if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create upload"));
 
-  // Shared memory: the stage, plus the rule table when it is small.
+  // Shared memory: block scratch, plus the rule table when it is small.
   size_t tableBytes = e->hRules.size() * sizeof(DevRule) + e->hParams.size() * sizeof(DevParam) +
                       e->hSucc.size() * sizeof(int32_t);
   e->tableInSmem = tableBytes <= 48 * 1024;
@@ -1173,7 +1187,7 @@ PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAx
   DeriveArgs a = make_args(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
   a.nodeLinks = nullptr;  // the arena is reused per axiom: no tape
   a.termLinks = nullptr;
-  a.stage = 0;            // one thread per shape, every branching shape through the queue
+  a.inlineMax = 0;        // every branching shape through the queue
   const unsigned threads = (unsigned)e->threads;
   for (uint32_t ax = 0; ax < numAxioms; ax++) {
     // One grammar (axiom) at a time: reset the queue, seed, expand level by level.

@@ -48,7 +48,7 @@ def test_version_and_default_procs(lib):
 def test_struct_layouts_match_header():
     import ctypes
 
-    assert ctypes.sizeof(engine.PgaEngineConfig) == 48
+    assert ctypes.sizeof(engine.PgaEngineConfig) == 56
     assert ctypes.sizeof(engine.PgaDeriveReport) == 40
     assert G.ENTRY_DT.itemsize == 1332 and G.AXIOM_DT.itemsize == 48 and G.TERMINAL_DT.itemsize == 64
 
