@@ -128,15 +128,12 @@ typedef struct PgaEngineConfig {
   uint32_t recordTape;       /* 1 = keep the derivation tape so pga_adjoint can run */
   uint32_t spinLimit;        /* iterations before a bounded wait gives up (0 = default) */
   uint32_t maxLevels;        /* derivation depth limit (0 = default 4096) */
-  uint32_t flags;            /* PGA_FLAG_* */
+  uint32_t flags;            /* reserved, 0 */
   uint32_t subItem;          /* children per queued work item, 1..64 (0 = default 8) */
-  uint32_t inlineMax;        /* expand branching children with at most this many children in
-                                place, one generation deep (0 = default 8) */
+  uint32_t itemsPerLane;     /* work items per lane in one warp chunk (0 = default 2) */
   uint32_t reserved;
 } PgaEngineConfig;
 
-/* PgaEngineConfig.flags */
-#define PGA_FLAG_NO_INLINE 1u /* queue every branching shape (no in-place expansion) */
 
 typedef enum PgaStatus {
   PGA_OK = 0,

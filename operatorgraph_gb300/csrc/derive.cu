@@ -8,13 +8,13 @@
 // 1 -> 1 rules (IfSizeLess, Extrude) and ends as a terminal (Generate: written
 // out directly), a discard, or a branching shape that is queued as work items.
 //
-// A block works on 256 items at a time, in two passes over the same children:
-// the first counts the terminals and queued items each thread produces, a
-// block-wide prefix sum and one global atomic per counter reserve contiguous
-// slots for the whole block, the second recomputes the children and writes
-// them.  A branching child with at most `inlineMax` children (a window
-// Subdivide, a ComponentSplit, a Menger sub-step) is expanded in place, one
-// generation deep, instead of being queued.
+// A warp works on a chunk of 32 x itemsPerLane work items in two passes over
+// the same children: the first counts the terminals and queued items the
+// chunk produces, one global atomic per counter reserves contiguous slots for
+// the whole chunk, the second recomputes the children and writes them; each
+// emission round writes a contiguous run of records in lane order.  Warps take
+// chunks in a static grid-stride order: no shared work counter, no block-wide
+// barrier inside a level.
 //
 // pga_derive runs every level of every axiom in ONE persistent cooperative
 // launch (a bounded grid barrier between levels, blocks pulling 256 items at a
@@ -49,8 +49,6 @@ struct __align__(16) Smem {
   const DevRule* rules;
   const DevParam* params;
   const int32_t* succ;
-  unsigned long long termBase, nodeBase, chunkBase;
-  unsigned long long warpT[kWarps], warpG[kWarps];
 };
 
 extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -176,7 +174,7 @@ __device__ __forceinline__ void translate_axis(Shape& y, const Shape& x, uint32_
 // Resolves a freshly created shape through IfSizeLess / Extrude rules
 // (If.cuh:65-89, Extrude.cuh:29-56) until it reaches a Generate (terminal),
 // a Discard, or a branching rule (queued).
-__device__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
+__device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
   for (int step = 0; step < kMaxChain; step++) {
     if (x.entry < 0 || (uint32_t)x.entry >= a.tab.numEntries) {
       raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry);
@@ -247,44 +245,51 @@ struct Expander {
   float prevSize, prevOff;  // Subdivide<DynParams>: the previous child, i.e. the symbol as updated in place
 };
 
-// Repeat<false, ...> set-up (Repeat.cuh:70-146); false on an argument the reference rejects.
-__device__ __noinline__ bool repeat_setup(const DeriveArgs& a, const DevRule& r, const Shape& x, uint32_t& axis,
-                                             uint32_t& reps, float& e1, float& e2, float& e3, bool& start,
-                                             bool raise) {
+// Repeat<false, ...> set-up (Repeat.cuh:70-146).  Out of line (it is needed
+// once per Repeat shape) and returned by value so that callers keep their
+// state in registers.
+struct RepeatSetup {
+  uint32_t axis, reps;
+  float e1, e2, e3;
+  uint32_t flags;  // bit 0: arguments valid, bit 1: anchored to start
+};
+
+__device__ __noinline__ RepeatSetup repeat_setup(const DeriveArgs& a, DevRule r, Shape x, bool raise) {
+  RepeatSetup R{0u, 0u, 0.0f, 0.0f, 0.0f, 0u};
   if (r.nParams < 3 || r.nSucc < 1) {
     if (raise) raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
-    return false;
+    return R;
   }
-  axis = f2u(param(a, r, 0, x));
-  if (axis > 2) {
+  R.axis = f2u(param(a, r, 0, x));
+  if (R.axis > 2) {
     if (raise) raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
-    return false;
+    return R;
   }
-  uint32_t mode = f2u(param(a, r, 2, x));
-  float ext = param(a, r, 1, x);
-  float total = pick3(x.s, axis);
-  float extent = __fadd_rn(__fmul_rn(__fmul_rn((float)(ext < 0.0f), total), fabsf(ext)),
-                           __fmul_rn((float)(ext > 0.0f), ext));
+  const uint32_t mode = f2u(param(a, r, 2, x));
+  const float ext = param(a, r, 1, x);
+  const float total = pick3(x.s, R.axis);
+  const float extent = __fadd_rn(__fmul_rn(__fmul_rn((float)(ext < 0.0f), total), fabsf(ext)),
+                                 __fmul_rn((float)(ext > 0.0f), ext));
   if (extent <= 0.0f || total < 0.0f) {
     if (raise) raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
-    return false;
+    return R;
   }
-  float division = __fdiv_rn(total, extent);
+  const float division = __fdiv_rn(total, extent);
   if (mode == 0u || mode == 1u) {
-    float rest = fmodf(total, extent);
-    bool exact = (rest == 0.0f);
-    reps = f2u(ceilf(division));
-    e1 = __fadd_rn(__fmul_rn((float)exact, extent), __fmul_rn((float)(!exact), rest));
-    e2 = e3 = extent;
+    const float rest = fmodf(total, extent);
+    const bool exact = (rest == 0.0f);
+    R.reps = f2u(ceilf(division));
+    R.e1 = __fadd_rn(__fmul_rn((float)exact, extent), __fmul_rn((float)(!exact), rest));
+    R.e2 = R.e3 = extent;
   } else if (mode == 2u) {
-    reps = f2u(floorf(division));
-    e1 = e2 = e3 = (reps > 0) ? __fdiv_rn(total, __uint2float_rn(reps)) : 0.0f;
+    R.reps = f2u(floorf(division));
+    R.e1 = R.e2 = R.e3 = (R.reps > 0) ? __fdiv_rn(total, __uint2float_rn(R.reps)) : 0.0f;
   } else {
     if (raise) raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
-    return false;
+    return R;
   }
-  start = (mode == 0u);
-  return true;
+  R.flags = 1u | (mode == 0u ? 2u : 0u);
+  return R;
 }
 
 // Number of children a branching shape produces (decides how many work items
@@ -299,11 +304,9 @@ __device__ __forceinline__ uint32_t count_children(const DeriveArgs& a, const Sh
     case PGA_OP_COMPONENT_SPLIT:
       return 6u;
     case PGA_OP_REPEAT: {
-      uint32_t axis, reps;
-      float e1, e2, e3;
-      bool start;
-      if (!repeat_setup(a, r, y, axis, reps, e1, e2, e3, start, false)) return 1u;
-      return reps > 1 ? reps : 1u;
+      const RepeatSetup R = repeat_setup(a, r, y, false);
+      if (!(R.flags & 1u)) return 1u;
+      return R.reps > 1 ? R.reps : 1u;
     }
     default:
       return 1u;  // raises BAD_OPCODE when executed
@@ -311,7 +314,7 @@ __device__ __forceinline__ uint32_t count_children(const DeriveArgs& a, const Sh
 }
 
 // Operator set-up; returns the number of child slots (0 on error).
-__device__ uint32_t expander_init(const DeriveArgs& a, Expander& E) {
+__device__ __forceinline__ uint32_t expander_init(const DeriveArgs& a, Expander& E) {
   const Shape& x = E.base;
   const DevRule& r = E.r;
   switch (r.op) {
@@ -338,9 +341,13 @@ __device__ uint32_t expander_init(const DeriveArgs& a, Expander& E) {
       return n;
     }
     case PGA_OP_REPEAT: {
-      float e1, e3;
-      bool start;
-      if (!repeat_setup(a, r, x, E.axis, E.reps, e1, E.e2, e3, start, true)) return 0;
+      const RepeatSetup R = repeat_setup(a, r, x, true);
+      if (!(R.flags & 1u)) return 0;
+      E.axis = R.axis;
+      E.reps = R.reps;
+      E.e2 = R.e2;
+      const float e1 = R.e1, e3 = R.e3;
+      const bool start = (R.flags & 2u) != 0;
       E.startExt = __fadd_rn(__fmul_rn((float)start, e1), __fmul_rn((float)(!start), e3));
       E.endExt = __fadd_rn(__fmul_rn((float)start, e3), __fmul_rn((float)(!start), e1));
       E.halfMid = __fmul_rn(E.e2, 0.5f);
@@ -375,7 +382,7 @@ __device__ __forceinline__ float subdivide_size(float f, float scale) {
 }
 
 // Advances the running state past children [0, c0) without producing them.
-__device__ void expander_skip(const DeriveArgs& a, Expander& E, uint32_t c0) {
+__device__ __forceinline__ void expander_skip(const DeriveArgs& a, Expander& E, uint32_t c0) {
   const DevRule& r = E.r;
   if (c0 == 0) return;
   switch (r.op) {
@@ -406,7 +413,8 @@ __device__ void expander_skip(const DeriveArgs& a, Expander& E, uint32_t c0) {
 
 // Produces child slot c (slots are produced in increasing order).  Returns
 // false when the slot yields no child (a zero factor of a static Subdivide).
-__device__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Shape& y, uint32_t& ordinal) {
+__device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Shape& y,
+                                               uint32_t& ordinal) {
   const Shape& x = E.base;
   const DevRule& r = E.r;
   switch (r.op) {
@@ -578,107 +586,52 @@ __device__ __forceinline__ void store_terminal(const DeriveArgs& a, unsigned lon
          make_uint4(rule, __float_as_uint(custom), (uint32_t)x.path, (uint32_t)(x.path >> 32)));
 }
 
-// Output cursor of one thread: in the counting pass it only counts, in the
-// writing pass it writes at consecutive slots reserved for the thread.
-struct Emit {
-  bool write;
-  unsigned long long term;  // terminals: count, or next slot
-  unsigned long long node;  // queued items: count, or next slot
-};
-
-// Emits one resolved shape: a terminal, or a branching shape queued as
-// ceil(nChild / subItem) work items.
-__device__ __forceinline__ void emit_one(const DeriveArgs& a, Emit& em, int kind, const Shape& y, uint32_t tidx,
-                                         uint32_t nChild, uint32_t link, uint32_t ordinal) {
-  if (kind == kTerm) {
-    if (em.write && em.term < a.cap) {
-      store_terminal(a, em.term, y, tidx);
-      if (a.termLinks != nullptr && em.term < a.termLinkCap) a.termLinks[em.term] = make_uint2(link, ordinal);
+// Warp-collective emission of one shape per lane (kind kNone / kTerm / kNode,
+// a branching shape with nChild children queued as ceil(nChild / subItem)
+// work items).  tCur / nCur are the warp's next terminal and item slots
+// (warp-uniform).  WRITE = false only advances them (the counting pass).
+// Each round writes a contiguous run: lanes in lane order.
+template <bool WRITE>
+__device__ __forceinline__ void emit_round(const DeriveArgs& a, int kind, const Shape& y, uint32_t tidx,
+                                           uint32_t nChild, uint32_t link, uint32_t ordinal,
+                                           unsigned long long& tCur, unsigned long long& nCur) {
+  const unsigned tm = __ballot_sync(kFull, kind == kTerm);
+  if (WRITE && kind == kTerm) {
+    const unsigned long long slot = tCur + __popc(tm & lanemask_lt());
+    if (slot < a.cap) {
+      store_terminal(a, slot, y, tidx);
+      if (a.termLinks != nullptr && slot < a.termLinkCap) a.termLinks[slot] = make_uint2(link, ordinal);
     }
-    em.term++;
-  } else if (kind == kNode) {
+  }
+  tCur += __popc(tm);
+  const unsigned nm = __ballot_sync(kFull, kind == kNode);
+  if (nm) {
     const uint32_t S = a.subItem;
-    const uint32_t m = (nChild + S - 1) / S;
-    if (em.write) {
+    const uint32_t m = (kind == kNode) ? (nChild + S - 1) / S : 0u;
+    uint32_t total;
+    const uint32_t pre = warp_excl_scan(m, total);
+    if (WRITE) {
       for (uint32_t j = 0; j < m; j++) {
-        if (em.node + j >= a.nodeCap) {
+        const unsigned long long slot = nCur + pre + j;
+        if (slot >= a.nodeCap) {
           raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, -1);
           break;
         }
-        store_node(a.nodes, em.node + j, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
+        store_node(a.nodes, slot, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
       }
     }
-    em.node += m;
+    nCur += total;
   }
 }
 
-// Resolves a new child and emits it.  A branching child with at most
-// inlineMax children is expanded in place, one generation deep: its children
-// are resolved and emitted instead of the child itself (no queue round trip).
-__device__ __forceinline__ void emit_child(const DeriveArgs& a, Emit& em, Shape& y, uint32_t link, uint32_t ordinal) {
-  uint32_t tidx = 0;
-  int kind = resolve(a, y, tidx);
-  if (kind != kNode) {
-    emit_one(a, em, kind, y, tidx, 0, link, ordinal);
-    return;
-  }
-  const uint32_t n = count_children(a, y);
-  if (n > a.inlineMax) {
-    emit_one(a, em, kNode, y, 0, n, link, ordinal);
-    return;
-  }
-  Expander F;
-  F.base = y;
-  F.r = rule_at(a, (uint32_t)y.entry);
-  F.base.kind = F.r.shape;
-  const uint32_t n2 = expander_init(a, F);
-  for (uint32_t c = 0; c < n2; c++) {
-    Shape z;
-    uint32_t ord2, t2 = 0;
-    if (!expander_child(a, F, c, z, ord2)) continue;
-    const int k2 = resolve(a, z, t2);
-    emit_one(a, em, k2, z, t2, k2 == kNode ? count_children(a, z) : 0u, link, ordinal);
-  }
-}
-
-// Reserves, for every thread of the block, `nT` terminal and `nG` item slots
-// with one global atomic each for the whole block.
-__device__ __forceinline__ void block_reserve(const DeriveArgs& a, Smem& sm, unsigned long long nT,
-                                              unsigned long long nG, unsigned long long& tSlot,
-                                              unsigned long long& gSlot) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  unsigned long long xT = nT, xG = nG;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    unsigned long long yT = __shfl_up_sync(kFull, xT, d), yG = __shfl_up_sync(kFull, xG, d);
-    if (lane >= d) {
-      xT += yT;
-      xG += yG;
-    }
-  }
-  if (lane == 31) {
-    sm.warpT[warp] = xT;
-    sm.warpG[warp] = xG;
-  }
-  __syncthreads();
-  unsigned long long preT = 0, preG = 0, totT = 0, totG = 0;
-#pragma unroll
-  for (int w = 0; w < kWarps; w++) {
-    const unsigned long long T = sm.warpT[w], Gw = sm.warpG[w];
-    if (w < warp) {
-      preT += T;
-      preG += Gw;
-    }
-    totT += T;
-    totG += Gw;
-  }
-  if (tid == 0) {
-    sm.termBase = totT ? atomicAdd(&a.st->termCount, totT) : 0ull;
-    sm.nodeBase = totG ? atomicAdd(&a.st->nodeNext, totG) : 0ull;
-  }
-  __syncthreads();
-  tSlot = sm.termBase + preT + (xT - nT);
-  gSlot = sm.nodeBase + preG + (xG - nG);
+// Emits a new child per lane (kind from resolve); a branching child is queued
+// as ceil(children / subItem) work items.
+template <bool WRITE>
+__device__ __forceinline__ void emit_child(const DeriveArgs& a, int kind, const Shape& y, uint32_t tidx,
+                                           uint32_t link, uint32_t ordinal, unsigned long long& tCur,
+                                           unsigned long long& nCur) {
+  const uint32_t nY = (kind == kNode) ? count_children(a, y) : 0u;
+  emit_round<WRITE>(a, kind, y, tidx, nY, link, ordinal, tCur, nCur);
 }
 
 // Root shape of axiom i, as Grid::...::generateAxiom builds it (Grid.cuh:199-204).
@@ -694,77 +647,106 @@ __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Sha
   x.path = mix64((uint64_t)i + 0x9E3779B97F4A7C15ULL);
 }
 
-// Produces the children [c0, c0 + n) of one work item.
-__device__ __forceinline__ void traverse(const DeriveArgs& a, Expander& E, uint32_t c0, uint32_t n, uint32_t link,
-                                         Emit& em) {
-  for (uint32_t c = c0; c < c0 + n; c++) {
-    Shape y;
-    uint32_t ordinal;
-    if (expander_child(a, E, c, y, ordinal)) emit_child(a, em, y, link, ordinal);
-  }
-}
-
-// Expands the work items [base, base + 256) ∩ [.., hi), one per thread, in two
-// passes over the same children: count, reserve (one atomic per block), write.
-__device__ void process_chunk(const DeriveArgs& a, Smem& sm, unsigned long long base, unsigned long long hi) {
-  const int tid = threadIdx.x;
-  Expander E;
-  uint32_t c0 = 0, n = 0;
-  const uint32_t link = (uint32_t)(base + tid);
-  bool valid = base + tid < hi;
-  PGA_GUARD(!valid || base + tid < a.nodeCap, 10, valid = false);
-  if (valid) {
-    uint4 ext;
-    load_node(a.nodes, base + tid, E.base, ext);
-    const int32_t e = E.base.entry;
-    if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
-      raise_error(a.st, PGA_ERR_BAD_OPCODE, e);
-    } else {
-      E.r = rule_at(a, (uint32_t)e);
-      E.base.kind = E.r.shape;
-      const uint32_t all = expander_init(a, E);
-      const uint32_t c1 = min(ext.y, all);
-      c0 = ext.x;
-      if (c0 < c1) {
-        expander_skip(a, E, c0);
-        n = c1 - c0;
+// One pass of a warp over the work items first + 32 k + lane (k < K, item < hi).
+template <bool WRITE>
+__device__ __forceinline__ void warp_items(const DeriveArgs& a, unsigned long long first, unsigned long long hi,
+                                           uint32_t K, unsigned long long& tCur, unsigned long long& nCur) {
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint32_t k = 0; k < K; k++) {
+    const unsigned long long item = first + 32ull * k + lane;
+    if (!__any_sync(kFull, item < hi)) break;
+    Expander E;
+    uint32_t c0 = 0, n = 0;
+    bool valid = item < hi;
+    PGA_GUARD(!valid || item < a.nodeCap, 10, valid = false);
+    if (valid) {
+      uint4 ext;
+      load_node(a.nodes, item, E.base, ext);
+      const int32_t e = E.base.entry;
+      if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
+        raise_error(a.st, PGA_ERR_BAD_OPCODE, e);
+      } else {
+        E.r = rule_at(a, (uint32_t)e);
+        E.base.kind = E.r.shape;
+        const uint32_t all = expander_init(a, E);
+        const uint32_t c1 = min(ext.y, all);
+        c0 = ext.x;
+        if (c0 < c1) {
+          expander_skip(a, E, c0);
+          n = c1 - c0;
+        }
       }
     }
-  }
-  const float off0 = E.offset, ps0 = E.prevSize, po0 = E.prevOff;
-  Emit em{false, 0ull, 0ull};
-  if (n) traverse(a, E, c0, n, link, em);
-  unsigned long long tSlot, gSlot;
-  block_reserve(a, sm, em.term, em.node, tSlot, gSlot);
-  if (n) {
-    E.offset = off0;
-    E.prevSize = ps0;
-    E.prevOff = po0;
-    Emit wr{true, tSlot, gSlot};
-    traverse(a, E, c0, n, link, wr);
+    for (uint32_t c = 0; __any_sync(kFull, c < n); c++) {
+      int kind = kNone;
+      Shape y;
+      uint32_t tidx = 0, ordinal = 0;
+      if (c < n && expander_child(a, E, c0 + c, y, ordinal)) kind = resolve(a, y, tidx);
+      emit_child<WRITE>(a, kind, y, tidx, (uint32_t)item, ordinal, tCur, nCur);
+    }
   }
 }
 
-// Seeds the axioms [first, first + count): one axiom per thread, block-wide.
-__device__ void seed_axioms(const DeriveArgs& a, Smem& sm, uint32_t first, uint32_t count) {
-  for (unsigned long long b = (unsigned long long)blockIdx.x * kThreads; b < count;
-       b += (unsigned long long)gridDim.x * kThreads) {
-    const unsigned long long i = b + threadIdx.x;
-    const uint32_t link = kAxiomLink | (first + (uint32_t)i);
-    Emit em{false, 0ull, 0ull};
-    Shape y;
-    if (i < count) {
-      axiom_shape(a, first + (uint32_t)i, y);
-      emit_child(a, em, y, link, 0u);
-    }
-    unsigned long long tSlot, gSlot;
-    block_reserve(a, sm, em.term, em.node, tSlot, gSlot);
-    if (i < count) {
-      Emit wr{true, tSlot, gSlot};
-      axiom_shape(a, first + (uint32_t)i, y);
-      emit_child(a, wr, y, link, 0u);
-    }
+// Expands the warp's chunk of 32 K work items: count, reserve (one atomic per
+// counter per chunk), write.
+__device__ __forceinline__ void warp_chunk(const DeriveArgs& a, unsigned long long first, unsigned long long hi,
+                                           uint32_t K) {
+  unsigned long long tCur = 0, nCur = 0;
+  warp_items<false>(a, first, hi, K, tCur, nCur);
+  unsigned long long tBase = 0, nBase = 0;
+  if ((threadIdx.x & 31u) == 0) {
+    if (tCur) tBase = atomicAdd(&a.st->termCount, tCur);
+    if (nCur) nBase = atomicAdd(&a.st->nodeNext, nCur);
   }
+  tBase = __shfl_sync(kFull, tBase, 0);
+  nBase = __shfl_sync(kFull, nBase, 0);
+  warp_items<true>(a, first, hi, K, tBase, nBase);
+}
+
+// Seeds the axioms [first, first + count): 32 K axioms per warp chunk.
+template <bool WRITE>
+__device__ __forceinline__ void warp_axioms(const DeriveArgs& a, unsigned long long first, unsigned long long end,
+                                            uint32_t K, unsigned long long& tCur, unsigned long long& nCur) {
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint32_t k = 0; k < K; k++) {
+    const unsigned long long i = first + 32ull * k + lane;
+    if (!__any_sync(kFull, i < end)) break;
+    int kind = kNone;
+    Shape y;
+    uint32_t tidx = 0;
+    if (i < end) {
+      axiom_shape(a, (uint32_t)i, y);
+      kind = resolve(a, y, tidx);
+    }
+    emit_child<WRITE>(a, kind, y, tidx, kAxiomLink | (uint32_t)i, 0u, tCur, nCur);
+  }
+}
+
+__device__ void seed_axioms(const DeriveArgs& a, uint32_t first, uint32_t count, uint32_t K) {
+  const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
+  const unsigned long long end = (unsigned long long)first + count;
+  for (unsigned long long b = first + warpId * 32ull * K; b < end; b += numWarps * 32ull * K) {
+    unsigned long long tCur = 0, nCur = 0;
+    warp_axioms<false>(a, b, end, K, tCur, nCur);
+    unsigned long long tBase = 0, nBase = 0;
+    if ((threadIdx.x & 31u) == 0) {
+      if (tCur) tBase = atomicAdd(&a.st->termCount, tCur);
+      if (nCur) nBase = atomicAdd(&a.st->nodeNext, nCur);
+    }
+    tBase = __shfl_sync(kFull, tBase, 0);
+    nBase = __shfl_sync(kFull, nBase, 0);
+    warp_axioms<true>(a, b, end, K, tBase, nBase);
+  }
+}
+
+// All items of one level [lo, hi), warp chunks of 32 K items assigned
+// statically (grid-stride): no shared counters.
+__device__ __forceinline__ void expand_level(const DeriveArgs& a, unsigned long long lo, unsigned long long hi,
+                                             uint32_t K) {
+  const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
+  for (unsigned long long b = lo + warpId * 32ull * K; b < hi; b += numWarps * 32ull * K) warp_chunk(a, b, hi, K);
 }
 
 // Copies the rule table into shared memory when it fits (decided at engine
@@ -862,7 +844,7 @@ __device__ __forceinline__ void level_snapshot(const DeriveArgs& a, uint32_t lev
 __global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
-  seed_axioms(a, sm, 0, a.numAxioms);
+  seed_axioms(a, 0, a.numAxioms, a.itemsPerLane);
   if (!grid_barrier(a, [&] {
         volatile DevState* vs = a.st;
         vs->levelHi = 0;
@@ -873,15 +855,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a)
   for (uint32_t level = 0;; level++) {
     volatile DevState* vs = a.st;
     if (vs->stop) break;
-    const unsigned long long hi = vs->levelHi;
-    for (;;) {
-      if (threadIdx.x == 0) sm.chunkBase = atomicAdd(&a.st->cursor, (unsigned long long)kThreads);
-      __syncthreads();
-      const unsigned long long base = sm.chunkBase;
-      __syncthreads();
-      if (base >= hi) break;
-      process_chunk(a, sm, base, hi);
-    }
+    expand_level(a, vs->levelLo, vs->levelHi, a.itemsPerLane);
     if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && a.outCount != nullptr)
@@ -891,15 +865,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a)
 __global__ void __launch_bounds__(kThreads, 2) k_seed(DeriveArgs a, uint32_t first, uint32_t count) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
-  seed_axioms(a, sm, first, count);
+  seed_axioms(a, first, count, 1);
 }
 
 __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsigned long long lo,
                                                               unsigned long long hi) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
-  const unsigned long long base = lo + (unsigned long long)blockIdx.x * kThreads;
-  if (base < hi) process_chunk(a, sm, base, hi);
+  expand_level(a, lo, hi, 1);
 }
 
 __global__ void k_write_count(const DevState* st, unsigned long long* out) { *out = st->termCount; }
@@ -942,7 +915,7 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.spinLimit = e->cfg.spinLimit;
   a.subItem = e->cfg.subItem;
   a.useSeeds = e->useSeeds ? 1u : 0u;
-  a.inlineMax = (e->cfg.recordTape || (e->cfg.flags & PGA_FLAG_NO_INLINE)) ? 0u : e->cfg.inlineMax;
+  a.itemsPerLane = e->cfg.itemsPerLane;
   a.tableInSmem = e->tableInSmem ? 1u : 0u;
   a.numParams = (uint32_t)e->hParams.size();
   a.numSucc = (uint32_t)e->hSucc.size();
@@ -1001,7 +974,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   if (c.spinLimit == 0) c.spinLimit = 1u << 24;
   if (c.maxLevels == 0) c.maxLevels = 4096;
   if (c.subItem == 0) c.subItem = 8;
-  if (c.inlineMax == 0) c.inlineMax = 8;
+  if (c.itemsPerLane == 0) c.itemsPerLane = 2;
   if (c.subItem > 64) {
     set_error("pga_engine_create: subItem must be at most 64");
     delete e;
@@ -1187,7 +1160,6 @@ PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAx
   DeriveArgs a = make_args(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
   a.nodeLinks = nullptr;  // the arena is reused per axiom: no tape
   a.termLinks = nullptr;
-  a.inlineMax = 0;        // every branching shape through the queue
   const unsigned threads = (unsigned)e->threads;
   for (uint32_t ax = 0; ax < numAxioms; ax++) {
     // One grammar (axiom) at a time: reset the queue, seed, expand level by level.

@@ -100,7 +100,7 @@ struct DeriveArgs {
   uint32_t spinLimit;
   uint32_t subItem;     // children per queued item (1..8)
   uint32_t useSeeds;    // 0: no parameter of the grammar reads a seed, skip seed updates
-  uint32_t inlineMax;   // expand branching children with at most this many children in place
+  uint32_t itemsPerLane;  // work items per lane in one warp chunk
   uint32_t tableInSmem; // 1: rule table copied to shared memory at launch
   uint32_t numParams, numSucc;
   DevState* st;
