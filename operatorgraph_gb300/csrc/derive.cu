@@ -564,10 +564,10 @@ __device__ __forceinline__ void store_node(Node* nodes, unsigned long long i, co
 
 // GenerationFunction<.., 1>::perShape (GenerationFunctions.cuh:158-188):
 // model4 * scale(size) and the custom attribute, as four 16-byte stores.
-__device__ __forceinline__ void store_terminal(const DeriveArgs& a, unsigned long long slot, const Shape& x,
-                                               uint32_t tidx) {
-  float4* p = reinterpret_cast<float4*>(a.out + slot);
-  PGA_GUARD(x.axiom < a.numAxioms && slot < a.cap, 8, return);
+__device__ __forceinline__ void store_terminal(const DeriveArgs& a, PgaTerminal* dst, unsigned long long slot,
+                                               const Shape& x, uint32_t tidx) {
+  float4* p = reinterpret_cast<float4*>(dst + slot);
+  PGA_GUARD(x.axiom < a.numAxioms, 8, return);
   float custom = __ldg(&a.axioms[x.axiom].custom);
   uint32_t rule = ((uint32_t)x.entry & 0xFFFFFFu) | (tidx << 24) | (x.kind == PGA_SHAPE_QUAD ? 0x80000000u : 0u);
   // R[i][j] * s_j is exactly +-s_j in row perm_j and zero elsewhere.
@@ -586,52 +586,145 @@ __device__ __forceinline__ void store_terminal(const DeriveArgs& a, unsigned lon
          make_uint4(rule, __float_as_uint(custom), (uint32_t)x.path, (uint32_t)(x.path >> 32)));
 }
 
+// Output of the persistent engine: every warp owns a page of kTermPage
+// terminal slots and a page of kNodePage item slots at a time, taken with one
+// atomic on a page counter; a round's lanes write consecutive slots of the
+// warp's page.  This cuts the same-address atomics on the output counters by
+// the page size.  Item pages are closed at every level end (their unused slots
+// marked empty); the warps' last terminal pages leave holes that a compaction
+// at the end of the launch fills, so the output is dense.
+constexpr uint32_t kTermPage = 256;
+constexpr uint32_t kNodePage = 64;
+constexpr uint32_t kEmptyItem = 0xFFFFFFFFu;
+
+struct WarpOut {
+  unsigned long long tPage, nPage;
+  uint32_t tFill, nFill;  // slots used in the current page (page size when there is none)
+};
+
+__device__ __forceinline__ void warpout_init(WarpOut& w) {
+  w.tPage = w.nPage = ~0ull;
+  w.tFill = kTermPage;
+  w.nFill = kNodePage;
+}
+
+// Reserves cnt consecutive slots (warp-uniform) of a paged stream: a lane's
+// rank r < cnt maps to first + r (r < rem) or next + (r - rem).
+struct Span {
+  unsigned long long first, next;
+  uint32_t rem;
+};
+
+__device__ __forceinline__ Span page_reserve(unsigned long long* counter, uint32_t pageSize,
+                                             unsigned long long& page, uint32_t& fill, uint32_t cnt) {
+  Span sp;
+  sp.rem = min(pageSize - fill, cnt);
+  sp.first = page * pageSize + fill;
+  sp.next = 0;
+  if (cnt > sp.rem) {
+    const uint32_t need = cnt - sp.rem;
+    const uint32_t np = (need + pageSize - 1) / pageSize;
+    unsigned long long p0 = 0;
+    if ((threadIdx.x & 31u) == 0) p0 = atomicAdd(counter, (unsigned long long)np);
+    p0 = __shfl_sync(kFull, p0, 0);
+    sp.next = p0 * pageSize;
+    page = p0 + np - 1;
+    fill = need - (np - 1) * pageSize;
+  } else {
+    fill += cnt;
+  }
+  return sp;
+}
+
+__device__ __forceinline__ unsigned long long span_slot(const Span& sp, uint32_t r) {
+  return r < sp.rem ? sp.first + r : sp.next + (r - sp.rem);
+}
+
+// Terminal slot s: the caller's buffer below `cap`, the engine's tail buffer above.
+__device__ __forceinline__ void write_terminal(const DeriveArgs& a, unsigned long long s, const Shape& y, uint32_t tidx,
+                                               uint32_t link, uint32_t ordinal) {
+  if (s < a.cap) {
+    store_terminal(a, a.out, s, y, tidx);
+    if (a.termLinks != nullptr && s < a.termLinkCap) a.termLinks[s] = make_uint2(link, ordinal);
+  } else if (s - a.cap < a.tailCap) {
+    store_terminal(a, a.tail, s - a.cap, y, tidx);
+    if (a.tailLinks != nullptr) a.tailLinks[s - a.cap] = make_uint2(link, ordinal);
+  }
+}
+
 // Warp-collective emission of one shape per lane (kind kNone / kTerm / kNode,
 // a branching shape with nChild children queued as ceil(nChild / subItem)
-// work items).  tCur / nCur are the warp's next terminal and item slots
-// (warp-uniform).  WRITE = false only advances them (the counting pass).
-// Each round writes a contiguous run: lanes in lane order.
-template <bool WRITE>
-__device__ __forceinline__ void emit_round(const DeriveArgs& a, int kind, const Shape& y, uint32_t tidx,
-                                           uint32_t nChild, uint32_t link, uint32_t ordinal,
-                                           unsigned long long& tCur, unsigned long long& nCur) {
+// work items); each round writes a contiguous run in lane order.  PAGED: warp
+// pages; otherwise (the plain form) one atomic per round and kind.
+template <bool PAGED>
+__device__ __forceinline__ void emit_round(const DeriveArgs& a, WarpOut& w, int kind, const Shape& y, uint32_t tidx,
+                                           uint32_t nChild, uint32_t link, uint32_t ordinal) {
+  const unsigned lane = threadIdx.x & 31u;
   const unsigned tm = __ballot_sync(kFull, kind == kTerm);
-  if (WRITE && kind == kTerm) {
-    const unsigned long long slot = tCur + __popc(tm & lanemask_lt());
-    if (slot < a.cap) {
-      store_terminal(a, slot, y, tidx);
-      if (a.termLinks != nullptr && slot < a.termLinkCap) a.termLinks[slot] = make_uint2(link, ordinal);
+  if (tm) {
+    const uint32_t cnt = __popc(tm), rank = __popc(tm & lanemask_lt());
+    unsigned long long slot;
+    if (PAGED) {
+      const Span sp = page_reserve(&a.st->termPages, kTermPage, w.tPage, w.tFill, cnt);
+      slot = span_slot(sp, rank);
+    } else {
+      unsigned long long base = 0;
+      const unsigned leader = __ffs(tm) - 1;
+      if (lane == leader) base = atomicAdd(&a.st->termCount, (unsigned long long)cnt);
+      slot = __shfl_sync(kFull, base, leader) + rank;
     }
+    if (kind == kTerm) write_terminal(a, slot, y, tidx, link, ordinal);
   }
-  tCur += __popc(tm);
   const unsigned nm = __ballot_sync(kFull, kind == kNode);
   if (nm) {
     const uint32_t S = a.subItem;
     const uint32_t m = (kind == kNode) ? (nChild + S - 1) / S : 0u;
     uint32_t total;
     const uint32_t pre = warp_excl_scan(m, total);
-    if (WRITE) {
-      for (uint32_t j = 0; j < m; j++) {
-        const unsigned long long slot = nCur + pre + j;
-        if (slot >= a.nodeCap) {
-          raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, -1);
-          break;
-        }
-        store_node(a.nodes, slot, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
-      }
+    Span sp;
+    if (PAGED) {
+      sp = page_reserve(&a.st->nodePages, kNodePage, w.nPage, w.nFill, total);
+    } else {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&a.st->nodeNext, (unsigned long long)total);
+      sp.first = __shfl_sync(kFull, base, 0);
+      sp.rem = total;
+      sp.next = 0;
     }
-    nCur += total;
+    for (uint32_t j = 0; j < m; j++) {
+      const unsigned long long slot = span_slot(sp, pre + j);
+      if (slot >= a.nodeCap) {
+        raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, -1);
+        break;
+      }
+      store_node(a.nodes, slot, y, make_uint4(j * S, min((j + 1) * S, nChild), link, ordinal));
+    }
   }
+}
+
+// Marks the unused slots of the warp's item page empty and gives the page up
+// (at the end of a level: the next level's items are exactly the pages handed
+// out during this one).
+__device__ __forceinline__ void close_node_page(const DeriveArgs& a, WarpOut& w) {
+  const unsigned lane = threadIdx.x & 31u;
+  if (w.nPage != ~0ull) {
+    for (uint32_t k = w.nFill + lane; k < kNodePage; k += 32) {
+      const unsigned long long slot = w.nPage * kNodePage + k;
+      if (slot < a.nodeCap)
+        __stcg(reinterpret_cast<uint4*>(a.nodes + slot) + 3, make_uint4(kEmptyItem, 0u, 0u, 0u));
+    }
+  }
+  w.nPage = ~0ull;
+  w.nFill = kNodePage;
 }
 
 // Emits a new child per lane (kind from resolve); a branching child is queued
 // as ceil(children / subItem) work items.
-template <bool WRITE>
-__device__ __forceinline__ void emit_child(const DeriveArgs& a, int kind, const Shape& y, uint32_t tidx,
-                                           uint32_t link, uint32_t ordinal, unsigned long long& tCur,
-                                           unsigned long long& nCur) {
+template <bool PAGED>
+__device__ __forceinline__ void emit_child(const DeriveArgs& a, WarpOut& w, int kind, const Shape& y, uint32_t tidx,
+                                           uint32_t link, uint32_t ordinal) {
   const uint32_t nY = (kind == kNode) ? count_children(a, y) : 0u;
-  emit_round<WRITE>(a, kind, y, tidx, nY, link, ordinal, tCur, nCur);
+  emit_round<PAGED>(a, w, kind, y, tidx, nY, link, ordinal);
 }
 
 // Root shape of axiom i, as Grid::...::generateAxiom builds it (Grid.cuh:199-204).
@@ -647,10 +740,10 @@ __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Sha
   x.path = mix64((uint64_t)i + 0x9E3779B97F4A7C15ULL);
 }
 
-// One pass of a warp over the work items first + 32 k + lane (k < K, item < hi).
-template <bool WRITE>
-__device__ __forceinline__ void warp_items(const DeriveArgs& a, unsigned long long first, unsigned long long hi,
-                                           uint32_t K, unsigned long long& tCur, unsigned long long& nCur) {
+// Expands the work items first + 32 k + lane (k < K, item < hi) of one warp.
+template <bool PAGED>
+__device__ __forceinline__ void warp_items(const DeriveArgs& a, WarpOut& w, unsigned long long first,
+                                           unsigned long long hi, uint32_t K) {
   const unsigned lane = threadIdx.x & 31u;
   for (uint32_t k = 0; k < K; k++) {
     const unsigned long long item = first + 32ull * k + lane;
@@ -663,7 +756,9 @@ __device__ __forceinline__ void warp_items(const DeriveArgs& a, unsigned long lo
       uint4 ext;
       load_node(a.nodes, item, E.base, ext);
       const int32_t e = E.base.entry;
-      if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
+      if (ext.x == kEmptyItem) {
+        // an unused slot of an item page
+      } else if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
         raise_error(a.st, PGA_ERR_BAD_OPCODE, e);
       } else {
         E.r = rule_at(a, (uint32_t)e);
@@ -682,35 +777,20 @@ __device__ __forceinline__ void warp_items(const DeriveArgs& a, unsigned long lo
       Shape y;
       uint32_t tidx = 0, ordinal = 0;
       if (c < n && expander_child(a, E, c0 + c, y, ordinal)) kind = resolve(a, y, tidx);
-      emit_child<WRITE>(a, kind, y, tidx, (uint32_t)item, ordinal, tCur, nCur);
+      emit_child<PAGED>(a, w, kind, y, tidx, (uint32_t)item, ordinal);
     }
   }
 }
 
-// Expands the warp's chunk of 32 K work items: count, reserve (one atomic per
-// counter per chunk), write.
-__device__ __forceinline__ void warp_chunk(const DeriveArgs& a, unsigned long long first, unsigned long long hi,
-                                           uint32_t K) {
-  unsigned long long tCur = 0, nCur = 0;
-  warp_items<false>(a, first, hi, K, tCur, nCur);
-  unsigned long long tBase = 0, nBase = 0;
-  if ((threadIdx.x & 31u) == 0) {
-    if (tCur) tBase = atomicAdd(&a.st->termCount, tCur);
-    if (nCur) nBase = atomicAdd(&a.st->nodeNext, nCur);
-  }
-  tBase = __shfl_sync(kFull, tBase, 0);
-  nBase = __shfl_sync(kFull, nBase, 0);
-  warp_items<true>(a, first, hi, K, tBase, nBase);
-}
-
-// Seeds the axioms [first, first + count): 32 K axioms per warp chunk.
-template <bool WRITE>
-__device__ __forceinline__ void warp_axioms(const DeriveArgs& a, unsigned long long first, unsigned long long end,
-                                            uint32_t K, unsigned long long& tCur, unsigned long long& nCur) {
+// Seeds the axioms [first, first + count) with a warp-uniform grid-stride loop.
+template <bool PAGED>
+__device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uint32_t count) {
   const unsigned lane = threadIdx.x & 31u;
-  for (uint32_t k = 0; k < K; k++) {
-    const unsigned long long i = first + 32ull * k + lane;
-    if (!__any_sync(kFull, i < end)) break;
+  const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
+  const unsigned long long end = (unsigned long long)first + count;
+  for (unsigned long long b = first + warpId * 32ull; b < end; b += numWarps * 32ull) {
+    const unsigned long long i = b + lane;
     int kind = kNone;
     Shape y;
     uint32_t tidx = 0;
@@ -718,35 +798,19 @@ __device__ __forceinline__ void warp_axioms(const DeriveArgs& a, unsigned long l
       axiom_shape(a, (uint32_t)i, y);
       kind = resolve(a, y, tidx);
     }
-    emit_child<WRITE>(a, kind, y, tidx, kAxiomLink | (uint32_t)i, 0u, tCur, nCur);
+    emit_child<PAGED>(a, w, kind, y, tidx, kAxiomLink | (uint32_t)i, 0u);
   }
 }
 
-__device__ void seed_axioms(const DeriveArgs& a, uint32_t first, uint32_t count, uint32_t K) {
+// All items of one level [lo, hi): warp chunks of 32 K items in a static
+// grid-stride order (no shared work counter).
+template <bool PAGED>
+__device__ __forceinline__ void expand_level(const DeriveArgs& a, WarpOut& w, unsigned long long lo,
+                                             unsigned long long hi, uint32_t K) {
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
   const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
-  const unsigned long long end = (unsigned long long)first + count;
-  for (unsigned long long b = first + warpId * 32ull * K; b < end; b += numWarps * 32ull * K) {
-    unsigned long long tCur = 0, nCur = 0;
-    warp_axioms<false>(a, b, end, K, tCur, nCur);
-    unsigned long long tBase = 0, nBase = 0;
-    if ((threadIdx.x & 31u) == 0) {
-      if (tCur) tBase = atomicAdd(&a.st->termCount, tCur);
-      if (nCur) nBase = atomicAdd(&a.st->nodeNext, nCur);
-    }
-    tBase = __shfl_sync(kFull, tBase, 0);
-    nBase = __shfl_sync(kFull, nBase, 0);
-    warp_axioms<true>(a, b, end, K, tBase, nBase);
-  }
-}
-
-// All items of one level [lo, hi), warp chunks of 32 K items assigned
-// statically (grid-stride): no shared counters.
-__device__ __forceinline__ void expand_level(const DeriveArgs& a, unsigned long long lo, unsigned long long hi,
-                                             uint32_t K) {
-  const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
-  const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
-  for (unsigned long long b = lo + warpId * 32ull * K; b < hi; b += numWarps * 32ull * K) warp_chunk(a, b, hi, K);
+  for (unsigned long long b = lo + warpId * 32ull * K; b < hi; b += numWarps * 32ull * K)
+    warp_items<PAGED>(a, w, b, hi, K);
 }
 
 // Copies the rule table into shared memory when it fits (decided at engine
@@ -819,8 +883,9 @@ __device__ __forceinline__ void level_snapshot(const DeriveArgs& a, uint32_t lev
   DevState* st = a.st;
   volatile DevState* vs = st;
   unsigned long long lo = vs->levelHi;
-  unsigned long long hi = atomicAdd(&st->nodeNext, 0ull);
+  unsigned long long hi = atomicAdd(&st->nodePages, 0ull) * kNodePage;
   if (hi > a.nodeCap) hi = a.nodeCap;
+  vs->nodeNext = hi;
   vs->levelLo = lo;
   vs->levelHi = hi;
   vs->cursor = lo;
@@ -841,10 +906,158 @@ __device__ __forceinline__ void level_snapshot(const DeriveArgs& a, uint32_t lev
   vs->stop = (!more || vs->status != 0) ? 1u : 0u;
 }
 
+// Compaction of the terminal output after the last level.  Every warp's last
+// terminal page may be partly filled: N = pages * kTermPage - holes terminals
+// exist, some at positions >= N.  The k-th hole below N (in position order)
+// receives the k-th filled position at or above N.  Partial pages are sorted by
+// rank (each warp counts the entries below its own), one block turns them into
+// hole and source segments with prefix sums, every thread then moves records.
+__device__ void compact_terminals(const DeriveArgs& a, WarpOut& w) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t W = a.numWarps;
+  const unsigned long long gw = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
+  unsigned long long* part = a.scratch;              // W entries: page << 9 | fill, or ~0
+  unsigned long long* sorted = part + W;             // W
+  unsigned long long* holeStart = sorted + W;        // W + 1
+  unsigned long long* holePre = holeStart + W + 1;   // W + 2
+  unsigned long long* srcStart = holePre + W + 2;    // W + 1
+  unsigned long long* srcPre = srcStart + W + 1;     // W + 2
+  DevState* st = a.st;
+  // 1. publish the warp's partly filled page
+  unsigned long long mine = ~0ull;
+  if (w.tPage != ~0ull && w.tFill < kTermPage) mine = (w.tPage << 9) | w.tFill;
+  if (lane == 0 && gw < W) {
+    part[gw] = mine;
+    if (mine != ~0ull) {
+      atomicAdd(&st->holes, (unsigned long long)(kTermPage - w.tFill));
+      atomicAdd(&st->partials, 1ull);
+    }
+  }
+  if (!grid_barrier(a, [&] {
+        volatile DevState* vs = st;
+        const unsigned long long total = atomicAdd(&st->termPages, 0ull) * kTermPage - atomicAdd(&st->holes, 0ull);
+        vs->termCount = total;
+        vs->stop = (vs->status != 0 || total > a.cap || atomicAdd(&st->partials, 0ull) == 0) ? 1u : 0u;
+      }))
+    return;
+  volatile DevState* vs = st;
+  const unsigned long long N = vs->termCount;
+  if (vs->stop == 0) {
+    // 2. sort the partial pages: rank = number of smaller entries
+    if (gw < W && mine != ~0ull) {
+      uint32_t rank = 0;
+      for (uint32_t j = 0; j < W; j += 32) {
+        const unsigned long long other = (j + lane < W) ? __ldcg(&part[j + lane]) : ~0ull;
+        rank += __popc(__ballot_sync(kFull, other < mine));
+      }
+      if (lane == 0) sorted[rank] = mine;
+    }
+    if (!grid_barrier(a, [] {})) return;
+    // 3. hole and source segments (block 0)
+    const uint32_t Q = (uint32_t)vs->partials;
+    const unsigned long long G = atomicAdd(&st->termPages, 0ull);
+    if (blockIdx.x == 0) {
+      __shared__ unsigned long long carryH, carryS;
+      if (threadIdx.x == 0) carryH = carryS = 0;
+      __syncthreads();
+      for (uint32_t base = 0; base <= Q; base += kThreads) {
+        const uint32_t i = base + threadIdx.x;
+        unsigned long long h = 0, sLen = 0, hs = 0, ss = 0;
+        if (i <= Q) {
+          unsigned long long prevEnd = N;
+          if (i > 0) {
+            const unsigned long long e = __ldcg(&sorted[i - 1]);
+            prevEnd = max(((e >> 9) + 1) * kTermPage, N);
+          }
+          unsigned long long vs0 = G * kTermPage;
+          if (i < Q) {
+            const unsigned long long e = __ldcg(&sorted[i]);
+            const unsigned long long start = (e >> 9) * kTermPage + (e & 511ull);
+            const unsigned long long end = ((e >> 9) + 1) * kTermPage;
+            vs0 = max(start, N);
+            hs = start;
+            h = start < N ? min(end, N) - start : 0ull;
+          }
+          ss = prevEnd;
+          sLen = vs0 - prevEnd;
+        }
+        // block-wide inclusive scans of h and sLen
+        unsigned long long xh = h, xs = sLen;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const unsigned long long yh = __shfl_up_sync(kFull, xh, d), ys = __shfl_up_sync(kFull, xs, d);
+          if ((int)lane >= d) { xh += yh; xs += ys; }
+        }
+        __shared__ unsigned long long wh[kWarps], wsum[kWarps];
+        if (lane == 31) { wh[threadIdx.x >> 5] = xh; wsum[threadIdx.x >> 5] = xs; }
+        __syncthreads();
+        unsigned long long ph = carryH, ps = carryS, th = 0, ts = 0;
+        for (int k = 0; k < kWarps; k++) {
+          if (k < (int)(threadIdx.x >> 5)) { ph += wh[k]; ps += wsum[k]; }
+          th += wh[k];
+          ts += wsum[k];
+        }
+        if (i <= Q) {
+          if (i < Q) {
+            holeStart[i] = hs;
+            holePre[i] = ph + xh - h;
+          }
+          srcStart[i] = ss;
+          srcPre[i] = ps + xs - sLen;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) { carryH += th; carryS += ts; }
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        holePre[Q] = carryH;
+        srcPre[Q + 1] = carryS;
+      }
+    }
+    if (!grid_barrier(a, [] {})) return;
+    // 4. move the k-th source record into the k-th hole
+    const unsigned long long H = __ldcg(&holePre[Q]);
+    for (unsigned long long k = (unsigned long long)blockIdx.x * kThreads + threadIdx.x; k < H;
+         k += (unsigned long long)gridDim.x * kThreads) {
+      uint32_t lo = 0, hi = Q;  // last hole segment with holePre <= k
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldcg(&holePre[mid]) <= k) lo = mid; else hi = mid;
+      }
+      const unsigned long long dst = __ldcg(&holeStart[lo]) + (k - __ldcg(&holePre[lo]));
+      uint32_t slo = 0, shi = Q + 1;
+      while (shi - slo > 1) {
+        const uint32_t mid = (slo + shi) >> 1;
+        if (__ldcg(&srcPre[mid]) <= k) slo = mid; else shi = mid;
+      }
+      const unsigned long long src = __ldcg(&srcStart[slo]) + (k - __ldcg(&srcPre[slo]));
+      if (dst >= a.cap) continue;
+      const bool inTail = src >= a.cap;
+      if (inTail && src - a.cap >= a.tailCap) continue;
+      const uint4* from = reinterpret_cast<const uint4*>(inTail ? a.tail + (src - a.cap) : a.out + src);
+      uint4* to = reinterpret_cast<uint4*>(a.out + dst);
+#pragma unroll
+      for (int q = 0; q < 4; q++) to[q] = __ldcg(from + q);
+      if (a.termLinks != nullptr && dst < a.termLinkCap) {
+        uint2 l = make_uint2(0u, 0u);
+        if (inTail) {
+          if (a.tailLinks != nullptr) l = a.tailLinks[src - a.cap];
+        } else if (src < a.termLinkCap) {
+          l = a.termLinks[src];
+        }
+        a.termLinks[dst] = l;
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
-  seed_axioms(a, 0, a.numAxioms, a.itemsPerLane);
+  WarpOut w;
+  warpout_init(w);
+  seed_axioms<true>(a, w, 0, a.numAxioms);
+  close_node_page(a, w);
   if (!grid_barrier(a, [&] {
         volatile DevState* vs = a.st;
         vs->levelHi = 0;
@@ -855,24 +1068,29 @@ __global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a)
   for (uint32_t level = 0;; level++) {
     volatile DevState* vs = a.st;
     if (vs->stop) break;
-    expand_level(a, vs->levelLo, vs->levelHi, a.itemsPerLane);
+    expand_level<true>(a, w, vs->levelLo, vs->levelHi, a.itemsPerLane);
+    close_node_page(a, w);
     if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0 && a.outCount != nullptr)
-    *a.outCount = atomicAdd(&a.st->termCount, 0ull);
+  compact_terminals(a, w);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && a.outCount != nullptr) *a.outCount = ((volatile DevState*)a.st)->termCount;
 }
 
 __global__ void __launch_bounds__(kThreads, 2) k_seed(DeriveArgs a, uint32_t first, uint32_t count) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
-  seed_axioms(a, first, count, 1);
+  WarpOut w;
+  warpout_init(w);
+  seed_axioms<false>(a, w, first, count);
 }
 
 __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsigned long long lo,
                                                               unsigned long long hi) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
-  expand_level(a, lo, hi, 1);
+  WarpOut w;
+  warpout_init(w);
+  expand_level<false>(a, w, lo, hi, 1);
 }
 
 __global__ void k_write_count(const DevState* st, unsigned long long* out) { *out = st->termCount; }
@@ -916,6 +1134,11 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.subItem = e->cfg.subItem;
   a.useSeeds = e->useSeeds ? 1u : 0u;
   a.itemsPerLane = e->cfg.itemsPerLane;
+  a.tail = e->dTail;
+  a.tailLinks = e->dTailLinks;
+  a.tailCap = e->tailCap;
+  a.scratch = e->dScratch;
+  a.numWarps = (uint32_t)e->persistentBlocks * (uint32_t)(e->threads / 32);
   a.tableInSmem = e->tableInSmem ? 1u : 0u;
   a.numParams = (uint32_t)e->hParams.size();
   a.numSucc = (uint32_t)e->hSucc.size();
@@ -950,6 +1173,7 @@ const PgaProc* pga_default_procs(uint32_t* numProcs) {
 
 static void free_engine(PgaEngine* e) {
   void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dNodeLinks, e->dLevelClock,
+                  e->dTail, e->dTailLinks, e->dScratch,
                   e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA, e->dKeysB,
                   e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dNodeGrad, e->dAxiomGrad};
   for (void* p : ptrs)
@@ -1110,6 +1334,17 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   if (c.blocksPerSM > 0 && (int)c.blocksPerSM < perSM) perSM = (int)c.blocksPerSM;
   if (perSM < 1) perSM = 1;
   e->persistentBlocks = perSM * e->numSMs;
+  {
+    // Paged output of the persistent engine: every warp may leave one partly
+    // filled terminal page, so up to warps * kTermPage slots can lie past the
+    // caller's capacity before compaction; they go to a tail buffer.
+    const unsigned long long warps = (unsigned long long)e->persistentBlocks * (e->threads / 32);
+    e->tailCap = warps * kTermPage;
+    err = cudaMalloc((void**)&e->dTail, e->tailCap * sizeof(PgaTerminal));
+    if (err == cudaSuccess && c.recordTape) err = cudaMalloc((void**)&e->dTailLinks, e->tailCap * sizeof(uint2));
+    if (err == cudaSuccess) err = cudaMalloc((void**)&e->dScratch, 6 * (warps + 2) * sizeof(unsigned long long));
+    if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create tail"));
+  }
   *out = e;
   return PGA_OK;
 }

@@ -69,8 +69,12 @@ struct __align__(16) Node {
 };
 
 struct DevState {
-  unsigned long long termCount;
-  unsigned long long nodeNext;
+  unsigned long long termCount;   // terminals emitted (exact, after compaction in the paged engine)
+  unsigned long long nodeNext;    // queued item slots handed out (plain form)
+  unsigned long long termPages;   // terminal pages handed out (paged engine)
+  unsigned long long nodePages;   // item pages handed out (paged engine)
+  unsigned long long holes;       // unused slots of the warps' last terminal pages
+  unsigned long long partials;    // warps holding a partly filled terminal page
   unsigned long long cursor;
   unsigned long long levelLo, levelHi;
   unsigned long long maxLevelNodes;
@@ -101,6 +105,11 @@ struct DeriveArgs {
   uint32_t subItem;     // children per queued item (1..8)
   uint32_t useSeeds;    // 0: no parameter of the grammar reads a seed, skip seed updates
   uint32_t itemsPerLane;  // work items per lane in one warp chunk
+  PgaTerminal* tail;      // terminal slots at or beyond `cap` (pages straddling the end of the output)
+  uint2* tailLinks;
+  unsigned long long tailCap;
+  unsigned long long* scratch;  // compaction: 6 x (warps + 2) words
+  uint32_t numWarps;
   uint32_t tableInSmem; // 1: rule table copied to shared memory at launch
   uint32_t numParams, numSucc;
   DevState* st;

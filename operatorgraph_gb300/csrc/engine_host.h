@@ -37,6 +37,11 @@ struct PgaEngine {
   unsigned long long* dLevelStart = nullptr;
   unsigned long long* dLevelClock = nullptr;
   unsigned long long* dScratchCount = nullptr;
+  // Paged output: tail slots past the caller's capacity and compaction scratch.
+  PgaTerminal* dTail = nullptr;
+  uint2* dTailLinks = nullptr;
+  unsigned long long tailCap = 0;
+  unsigned long long* dScratch = nullptr;
 
   // LBVH scratch.
   void* dSortTemp = nullptr;
