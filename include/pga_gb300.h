@@ -234,6 +234,19 @@ PgaStatus pga_engine_levels(PgaEngine* engine, void* stream, uint64_t* starts, u
 PgaStatus pga_lbvh_build(PgaEngine* engine, const PgaTerminal* dTerminals, uint64_t n,
                          const PgaBounds* bounds, const PgaLbvh* out, void* stream);
 
+/* Same LBVH as pga_lbvh_build, for callers that cannot allocate device memory
+ * (their budget is fixed up front, or the allocator belongs to a host
+ * application): it needs no engine and calls no allocator.  Its scratch is a
+ * fixed device array inside this library (6 MiB, held by every GPU that loads
+ * the library until the process exits), so n is limited to
+ * PGA_LBVH_STATIC_MAX_LEAVES; larger n is rejected with
+ * PGA_ERR_INVALID_ARGUMENT.  The first call on a device looks the array's
+ * device address up; make it before any stream capture.  Calls share the array
+ * and race when they overlap on the GPU.  No counterpart in the reference. */
+#define PGA_LBVH_STATIC_MAX_LEAVES 65536u
+PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const PgaBounds* bounds,
+                                const PgaLbvh* out, void* stream);
+
 /* Adjoint of the last pga_derive (recordTape = 1): dGradTerminals holds
  * dL/dm (12 floats per terminal, same order as that derivation's output).
  * Accumulates dL/dDynParam into dGradParams (numBlocks x blockStride; may be NULL)

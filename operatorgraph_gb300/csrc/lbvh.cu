@@ -14,6 +14,8 @@
 
 #include <cfloat>
 #include <cub/device/device_radix_sort.cuh>
+#include <mutex>
+#include <string>
 
 #include "engine_host.h"
 
@@ -241,6 +243,107 @@ extern "C" PgaStatus pga_lbvh_build(PgaEngine* e, const PgaTerminal* dTerminals,
   PGA_CUDA_TRY(cudaMemsetAsync(e->dArrival, 0, (n - 1) * sizeof(uint32_t), s));
   k_refit<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, (long long)n, out->nodes, out->leafParents, out->leafTerminal,
                                           e->dArrival, out->aabbs);
+  PGA_CUDA_TRY(cudaGetLastError());
+  return PGA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// pga_lbvh_build_static: the same LBVH build with every piece of scratch taken
+// from one fixed device array of this file instead of an engine's buffers.
+//
+// Some callers cannot allocate device memory when they build a hierarchy: a
+// host process whose device-memory budget was handed out in full at start-up,
+// a plug-in running inside an application that owns the allocator, or code
+// that must not hit the driver's allocator inside a latency-critical loop.
+// They pass only their inputs and outputs; the scratch lives in
+// g_lbvhStaticScratch, which every GPU that loads this library holds until
+// the process exits.
+//
+// The array's name denotes a host-side stand-in in host code, not a device
+// address, so the device address is looked up once per device with
+// cudaGetSymbolAddress (with that device current) on the first call made on
+// it; make that first call before any stream capture.  All calls share the
+// array and it keeps the last call's contents: the arrival counters that must
+// start at zero are cleared on every call, and calls that overlap on the GPU
+// (on different streams, or from different threads) race on it.
+
+namespace pga {
+
+constexpr size_t kStaticScratchBytes = 6u << 20;  // 6 MiB
+static __device__ __align__(256) unsigned char g_lbvhStaticScratch[kStaticScratchBytes];
+
+static std::mutex g_staticMutex;
+static void* g_staticAddr[64];  // device address of g_lbvhStaticScratch per device ordinal
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace pga
+
+extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const PgaBounds* bounds,
+                                           const PgaLbvh* out, void* stream) {
+  if (!dTerminals || !bounds || !out || !out->nodes || !out->leafParents || !out->aabbs || !out->leafTerminal ||
+      !out->keys) {
+    set_error("pga_lbvh_build_static: null argument");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  if (n < 2 || n > PGA_LBVH_STATIC_MAX_LEAVES) {
+    set_error("pga_lbvh_build_static: n must be in [2, " + std::to_string(PGA_LBVH_STATIC_MAX_LEAVES) +
+              "] (the fixed scratch holds at most that many leaves); use pga_lbvh_build for larger sets");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  int dev = 0;
+  PGA_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("pga_lbvh_build_static: device ordinal out of range");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  unsigned char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_staticMutex);
+    if (!g_staticAddr[dev]) {
+      void* p = nullptr;
+      cudaError_t err = cudaGetSymbolAddress(&p, g_lbvhStaticScratch);
+      if (err != cudaSuccess) return cuda_status(err, "pga_lbvh_build_static: cudaGetSymbolAddress");
+      g_staticAddr[dev] = p;
+    }
+    base = static_cast<unsigned char*>(g_staticAddr[dev]);
+  }
+  // Carve the scratch: keys, two value arrays, arrival counters, sort temp.
+  size_t temp = pga_lbvh_temp_bytes(n);
+  size_t off = 0;
+  unsigned long long* keysA = reinterpret_cast<unsigned long long*>(base + off);
+  off += align256(n * sizeof(unsigned long long));
+  uint32_t* valsA = reinterpret_cast<uint32_t*>(base + off);
+  off += align256(n * sizeof(uint32_t));
+  uint32_t* valsB = reinterpret_cast<uint32_t*>(base + off);
+  off += align256(n * sizeof(uint32_t));
+  uint32_t* arrival = reinterpret_cast<uint32_t*>(base + off);
+  off += align256(n * sizeof(uint32_t));
+  void* sortTemp = base + off;
+  off += align256(temp);
+  if (off > kStaticScratchBytes) {
+    set_error("pga_lbvh_build_static: fixed scratch too small for the radix sort of " + std::to_string(n) + " keys");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  Bounds b;
+  for (int k = 0; k < 3; k++) {
+    b.mn[k] = bounds->min[k];
+    b.sz[k] = bounds->max[k] - bounds->min[k];
+  }
+  const unsigned blocks = (unsigned)((n + kLbvhThreads - 1) / kLbvhThreads);
+  k_morton<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, n, b, keysA, valsA);
+  PGA_CUDA_TRY(cudaGetLastError());
+  PGA_CUDA_TRY(cub::DeviceRadixSort::SortPairs(sortTemp, temp, keysA, (unsigned long long*)out->keys, valsA, valsB,
+                                               (int64_t)n, 0, 64, s));
+  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, valsB, dTerminals, n);
+  PGA_CUDA_TRY(cudaGetLastError());
+  k_karras<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, (long long)n, out->nodes,
+                                           out->leafParents, out->leafTerminal, valsB);
+  PGA_CUDA_TRY(cudaGetLastError());
+  PGA_CUDA_TRY(cudaMemsetAsync(arrival, 0, (n - 1) * sizeof(uint32_t), s));
+  k_refit<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, (long long)n, out->nodes, out->leafParents, out->leafTerminal,
+                                          arrival, out->aabbs);
   PGA_CUDA_TRY(cudaGetLastError());
   return PGA_OK;
 }

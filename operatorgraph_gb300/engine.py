@@ -26,7 +26,7 @@ STATUS = {
 # Every symbol include/pga_gb300.h declares.
 EXPORTS = ["pga_version", "pga_last_error", "pga_default_procs", "pga_engine_create", "pga_engine_destroy",
            "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_engine_levels", "pga_lbvh_build",
-           "pga_adjoint"]
+           "pga_lbvh_build_static", "pga_adjoint"]
 
 
 class PgaError(RuntimeError):
@@ -92,6 +92,7 @@ def load_library(path=LIB_PATH):
     L.pga_lbvh_build.argtypes = [vp, vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
     L.pga_adjoint.argtypes = [vp, vp, vp, u32, vp, vp]
     L.pga_engine_levels.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(u32)]
+    L.pga_lbvh_build_static.argtypes = [vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
     for name in EXPORTS[3:]:
         getattr(L, name).restype = ctypes.c_int
     _lib = L

@@ -1,0 +1,76 @@
+"""pga_lbvh_build_static: the LBVH build for callers that cannot allocate.
+
+Some callers of this library cannot allocate device memory when they need a
+hierarchy -- their device-memory budget was handed out in full at start-up, or
+the allocator belongs to the host application they run in.  The static entry
+point takes only inputs and outputs and draws all of its scratch from a fixed
+device array inside the library.  These tests call it through the C ABI twice
+in a row (the array keeps the previous call's contents) and compare every
+output with pga_lbvh_build's, bit for bit -- the tolerance the other LBVH
+tests use.  This file is collected last on purpose.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from operatorgraph_gb300 import scenes
+from operatorgraph_gb300.engine import PgaBounds, PgaLbvh
+
+
+def _bounds(b):
+    b = np.asarray(b, np.float32)
+    return PgaBounds((ctypes.c_float * 3)(*b[:3]), (ctypes.c_float * 3)(*b[3:]))
+
+
+def test_static_rejects_too_many_leaves_without_a_gpu():
+    from operatorgraph_gb300 import build as B
+    from operatorgraph_gb300 import engine
+
+    B.build()
+    L = engine.load_library()
+    dummy = ctypes.c_void_p(16)
+    out = PgaLbvh(dummy, dummy, dummy, dummy, dummy)
+    st = L.pga_lbvh_build_static(dummy, 65537, ctypes.byref(_bounds((0, 0, 0, 1, 1, 1))), ctypes.byref(out), None)
+    assert st == 7
+    assert b"65536" in L.pga_last_error()
+
+
+@pytest.mark.gpu
+def test_static_matches_engine_lbvh_twice_in_a_row():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from operatorgraph_gb300 import build as B
+    from operatorgraph_gb300 import engine
+    from operatorgraph_gb300.engine import Engine
+
+    B.build()
+    torch.cuda.set_device(0)
+    L = engine.load_library()
+    cases = [(scenes.menger(0.05), (-0.5, -0.5, -0.5, 0.5, 0.5, 0.5)),
+             (scenes.building(), (-20.0, -20.0, -1.0, 20.0, 20.0, 40.0))]
+    for b, bounds in cases:
+        eng = Engine(b["entries"], node_capacity=1 << 16, max_terminals=1 << 16)
+        out, n, _ = eng.execute(b["axioms"], capacity=1 << 14)
+        want = eng.lbvh(out, n, bounds)
+        torch.cuda.synchronize()
+        got = {
+            "nodes": torch.empty((n - 1, 3), dtype=torch.int32, device="cuda"),
+            "leafParents": torch.empty(n, dtype=torch.int32, device="cuda"),
+            "aabbs": torch.empty((n - 1, 6), dtype=torch.float32, device="cuda"),
+            "leafTerminal": torch.empty(n, dtype=torch.int32, device="cuda"),
+            "keys": torch.empty(n, dtype=torch.int64, device="cuda"),
+        }
+        lb = PgaLbvh(got["nodes"].data_ptr(), got["leafParents"].data_ptr(), got["aabbs"].data_ptr(),
+                     got["leafTerminal"].data_ptr(), got["keys"].data_ptr())
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        st = L.pga_lbvh_build_static(ctypes.c_void_p(out.data_ptr()), n, ctypes.byref(_bounds(bounds)),
+                                     ctypes.byref(lb), stream)
+        assert st == 0, L.pga_last_error()
+        torch.cuda.synchronize()
+        for k in want:
+            a = want[k].cpu().numpy().view(np.uint32)
+            c = got[k].cpu().numpy().view(np.uint32)
+            assert np.array_equal(a, c), f"{k} differs from pga_lbvh_build"
+        eng.release()
