@@ -415,6 +415,34 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["menger_d5_ms"] = statistics.median(ts)
     res["menger_d5_terminals_per_s"] = 3.2e6 / (res["menger_d5_ms"] * 1e-3)
     em.release()
+    # Facades (1024 axioms x 16 block parameters, 393,216 terminals): derivation
+    # with the tape recorded, then the adjoint to the block parameters and sizes.
+    f = scenes.facades(1024)
+    ef = Engine(f["entries"], node_capacity=1 << 20, max_terminals=1 << 20, block_stride=f["block_stride"],
+                record_tape=True)
+    d_f = torch.from_numpy(f["axioms"].view(np.uint8).copy()).to(dev)
+    d_blk = torch.from_numpy(f["blocks"]).to(dev)
+    n_f = 1024 * 384
+    g_term = torch.randn((n_f, 12), dtype=torch.float32, device=dev)
+    g_blk = torch.empty_like(d_blk)
+    g_sz = torch.empty((1024, 3), dtype=torch.float32, device=dev)
+    fw, bw = [], []
+    for it in range(8):
+        flush.fill_(3)
+        a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        a.record(stream)
+        ef.derive_raw(d_f.data_ptr(), 1024, d_blk.data_ptr(), out.data_ptr(), out.shape[0], count.data_ptr())
+        b.record(stream)
+        ef.adjoint_raw(g_term.data_ptr(), g_blk.data_ptr(), 1024, g_sz.data_ptr())
+        c.record(stream)
+        torch.cuda.synchronize()
+        if it >= 3:
+            fw.append(a.elapsed_time(b))
+            bw.append(b.elapsed_time(c))
+    assert int(count.item()) == n_f
+    res["facades1024_forward_tape_ms"] = statistics.median(fw)
+    res["facades1024_adjoint_ms"] = statistics.median(bw)
+    ef.release()
     return res
 
 

@@ -1,0 +1,422 @@
+// Adjoint of the derivation (no reference counterpart).
+//
+// With the discrete derivation frozen -- every IfSizeLess branch, Repeat count,
+// discard and the rule of every shape as recorded by the forward pass -- a
+// terminal's transform is a smooth function of the continuous inputs: the
+// per-axiom parameter blocks (PGA_PT_BLOCK parameters) and the axiom sizes.
+// Rotations are signed permutations that no continuous input changes, so the
+// state that carries gradient is a shape's translation t and size s.
+//
+// Tape: every queued work item stores (parent item or kAxiomLink | axiom,
+// child ordinal) in its ext field, every terminal the same pair in termLinks.
+// The reverse sweep first visits every terminal, then the levels from the
+// deepest up: a record recomputes its creating child from the parent item (or
+// the axiom), replays the 1 -> 1 chain to itself, and pushes its gradient
+// through the chain and the operator that created it into the parent item's
+// accumulator (atomicAdd) and the parameter / axiom-size gradients.
+//
+// Operator VJPs (o = offset along the split axis a, S = size[a]):
+//  Subdivide  size_c = N_c, o_c = -S/2 + sum_{i<c} N_i + N_c/2, N_i = f_i (f > 0)
+//             or scale * -f_i (f < 0), scale = (S - sum_abs) / sum_rel.
+//  Repeat     size / offset linear in (S, startExt, e2, endExt); extent
+//             E = e or S * |e|, the remainder fmod(S, E) = S - k E with k frozen.
+//  ComponentSplit  t_f = t + R[:,k] * (+-s_k / 2), face size picks two of s.
+//  Extrude    size (s0, extent, s1).
+//  Generate   M[:, j] = R[:, j] s_j, M[:, 3] = t.
+
+namespace pga {
+
+struct Grad {
+  float t[3], s[3];
+};
+
+__device__ __forceinline__ void grad_zero(Grad& g) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) g.t[k] = g.s[k] = 0.0f;
+}
+
+struct AdjArgs {
+  const float* gradTerminals;  // 12 per terminal
+  float* gradParams;           // numBlocks * blockStride
+  uint32_t numBlocks;
+  float* gradSizes;            // 3 per axiom
+  float* nodeGrad;             // 6 per item: d/dt, d/ds
+  unsigned long long numTerminals;
+};
+
+// Gradient g of a parameter evaluated on shape x: a block value feeds the
+// parameter gradient; a size attribute (Shape::at 12..14) feeds gs of x;
+// every other kind is a constant of the grammar.
+__device__ __forceinline__ void param_grad(const DeriveArgs& a, const AdjArgs& j, const DevRule& r, uint32_t k,
+                                           const Shape& x, float g, float* gsOfX) {
+  if (g == 0.0f) return;
+  const DevParam p = param_at(a, r.paramBase + k);
+  if (p.type == PGA_PT_BLOCK) {
+    const uint32_t slot = f2u(p.v0);
+    const uint32_t b = __ldg(&a.axioms[x.axiom].block);
+    if (j.gradParams != nullptr && slot < a.blockStride && b < j.numBlocks)
+      atomicAdd(&j.gradParams[(size_t)b * a.blockStride + slot], g);
+  } else if (p.type == PGA_PT_SHAPE_ATTR && gsOfX != nullptr) {
+    const uint32_t i = f2u(p.v0);
+    if (i >= 12 && i < 15) gsOfX[i - 12] += g;
+  }
+}
+
+// d(offset along the split axis) seen through the translation: R[:,a] has one
+// nonzero entry, +-1 in row perm_a.
+__device__ __forceinline__ float axis_dot(const Shape& x, uint32_t ax, const float gt[3]) {
+  const float v = pick3(gt, frame_row(x.frame, ax));
+  return frame_neg(x.frame, ax) ? -v : v;
+}
+
+// VJP of child c of the item held in E (state before producing children,
+// i.e. right after expander_init).  gc is the gradient of the child's state;
+// the parent's gradient is accumulated into gp.
+__device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander& E0, uint32_t c, const Grad& gc,
+                          Grad& gp) {
+  const Shape& x = E0.base;
+  const DevRule& r = E0.r;
+#pragma unroll
+  for (int k = 0; k < 3; k++) gp.t[k] += gc.t[k];
+  switch (r.op) {
+    case PGA_OP_SUBDIVIDE:
+    case PGA_OP_SUBDIVIDE_STATIC: {
+      const bool dyn = r.op == PGA_OP_SUBDIVIDE;
+      const uint32_t n = dyn ? r.nParams - 1u : r.nChildren;
+      const uint32_t ax = E0.axis;
+      const float go = axis_dot(x, ax, gc.t);
+      for (uint32_t k = 0; k < 3; k++)
+        if (k != ax) gp.s[k] += gc.s[k];
+      // gN_i: go for i < c, go / 2 + gs_c[a] for i = c.  Child sizes use the
+      // factors as the forward pass read them (a dynamic Subdivide reads factor
+      // i from the symbol left by child i - 1); the scale uses the factors read
+      // from the unmodified symbol.  Shape reads of a dynamic factor past the
+      // first (on the updated symbol) carry no gradient.
+      float gS = -0.5f * go;
+      float gscale = 0.0f;
+      Expander W = E0;
+      for (uint32_t i = 0; i <= c && i < n; i++) {
+        const float f = dyn ? dyn_factor(a, W, i) : param(a, r, i + 1, x);
+        if (dyn) {
+          const float sz = subdivide_size(f, W.scale);
+          W.prevOff = __fadd_rn(W.offset, __fmul_rn(sz, 0.5f));
+          W.prevSize = sz;
+          W.offset = __fadd_rn(W.offset, sz);
+        }
+        if (!dyn && f == 0.0f) continue;
+        float* gsx = (dyn && i > 0) ? nullptr : gp.s;
+        const float gN = (i < c) ? go : 0.5f * go + pick3(gc.s, ax);
+        if (f < 0.0f) {
+          gscale += gN * (-f);
+          param_grad(a, j, r, i + 1, x, gN * (-E0.scale), gsx);
+        } else if (f > 0.0f) {
+          param_grad(a, j, r, i + 1, x, gN, gsx);
+        }
+      }
+      if (gscale != 0.0f) {
+        float relSum = 0.0f;
+        for (uint32_t i = 0; i < n; i++) {
+          const float f = param(a, r, i + 1, x);
+          if (f < 0.0f) relSum += -f;
+        }
+        if (relSum != 0.0f) {
+          // scale = (S - sum_{f>0} f) / sum_{f<0} -f
+          gS += gscale / relSum;
+          const float gA = -gscale / relSum, gR = gscale * E0.scale / relSum;
+          for (uint32_t i = 0; i < n; i++) {
+            const float f = param(a, r, i + 1, x);
+            if (f > 0.0f) param_grad(a, j, r, i + 1, x, gA, gp.s);
+            if (f < 0.0f) param_grad(a, j, r, i + 1, x, gR, gp.s);
+          }
+        }
+      }
+      gp.s[0] += (ax == 0) ? gS : 0.0f;
+      gp.s[1] += (ax == 1) ? gS : 0.0f;
+      gp.s[2] += (ax == 2) ? gS : 0.0f;
+      return;
+    }
+    case PGA_OP_REPEAT: {
+      const RepeatSetup R = repeat_setup(a, r, x, false);
+      const uint32_t ax = R.axis, reps = R.reps;
+      const bool start = (R.flags & 2u) != 0;
+      const uint32_t mode = f2u(param(a, r, 2, x));
+      const float go = axis_dot(x, ax, gc.t);
+      const float gsize = pick3(gc.s, ax);
+      for (uint32_t k = 0; k < 3; k++)
+        if (k != ax) gp.s[k] += gc.s[k];
+      const bool first = (c == 0), last = (c > 0 && c + 1 >= reps), middle = !first && !last;
+      float gStart = first ? (0.5f * go + gsize) : go;
+      float gE2 = middle ? (go * ((float)c - 0.5f) + gsize) : (last ? go * (float)(reps - 2) : 0.0f);
+      float gEnd = last ? (0.5f * go + gsize) : 0.0f;
+      if (first && reps <= 1) gE2 = 0.0f;
+      float gS = -0.5f * go, gE = 0.0f;
+      const float S = pick3(x.s, ax);
+      const float ext = param(a, r, 1, x);
+      const float E = ext < 0.0f ? S * fabsf(ext) : ext;
+      if (mode == 2u) {
+        if (reps > 0) gS += (gStart + gE2 + gEnd) / (float)reps;
+      } else {
+        const float ge1 = start ? gStart : gEnd;
+        gE += (start ? gEnd : gStart) + gE2;
+        const float rest = fmodf(S, E);
+        if (rest == 0.0f) {
+          gE += ge1;
+        } else {
+          gS += ge1;
+          gE += -truncf(S / E) * ge1;
+        }
+      }
+      if (ext < 0.0f) {
+        gS += gE * fabsf(ext);
+        param_grad(a, j, r, 1, x, gE * (-S), gp.s);
+      } else {
+        param_grad(a, j, r, 1, x, gE, gp.s);
+      }
+      gp.s[0] += (ax == 0) ? gS : 0.0f;
+      gp.s[1] += (ax == 1) ? gS : 0.0f;
+      gp.s[2] += (ax == 2) ? gS : 0.0f;
+      return;
+    }
+    case PGA_OP_COMPONENT_SPLIT: {
+      // face c: translation axis k and sign, face size (x, y) from parent components.
+      uint32_t k, m0, m1;
+      float sgn;
+      switch (c) {
+        case 0: k = 2; sgn = -1.0f; m0 = 0; m1 = 1; break;
+        case 1: k = 2; sgn = 1.0f; m0 = 0; m1 = 1; break;
+        case 2: k = 0; sgn = -1.0f; m0 = 2; m1 = 1; break;
+        case 3: k = 0; sgn = 1.0f; m0 = 2; m1 = 1; break;
+        case 4: k = 1; sgn = -1.0f; m0 = 0; m1 = 2; break;
+        default: k = 1; sgn = 1.0f; m0 = 0; m1 = 2; break;
+      }
+      const float go = axis_dot(x, k, gc.t);
+      float add[3] = {0.0f, 0.0f, 0.0f};
+      add[k] += sgn * 0.5f * go;
+      add[m0] += gc.s[0];
+      add[m1] += gc.s[1];
+#pragma unroll
+      for (int q = 0; q < 3; q++) gp.s[q] += add[q];
+      return;
+    }
+    default:
+      return;
+  }
+}
+
+// Recomputes the shape created as child `ordinal` of `link` (an item or an
+// axiom) and replays its 1 -> 1 chain until `stopAt` (a terminal: the Generate
+// rule; an item: its branching rule).  Extrude steps are recorded so that the
+// reverse pass can undo them.
+struct Chain {
+  uint32_t n;             // Extrude steps
+  int32_t entry[4];       // rule of each step
+  Shape before[4];        // state entering each step
+};
+
+__device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, bool toTerminal, Expander& E,
+                       bool& fromAxiom, uint32_t& c, Shape& y0, Chain& ch, Shape& yEnd) {
+  fromAxiom = (link & kAxiomLink) != 0;
+  if (fromAxiom) {
+    axiom_shape(a, link & ~kAxiomLink, y0);
+    c = 0;
+  } else {
+    uint4 ext;
+    load_node(a.nodes, link, E.base, ext);
+    const int32_t e = E.base.entry;
+    if (e < 0 || (uint32_t)e >= a.tab.numEntries) return false;
+    E.r = rule_at(a, (uint32_t)e);
+    E.base.kind = E.r.shape;
+    const uint32_t all = expander_init(a, E);
+    c = (E.r.op == PGA_OP_REPEAT) ? ordinal - 1u : ordinal;
+    if (c >= all) return false;
+    Expander W = E;
+    expander_skip(a, W, c);
+    uint32_t ord;
+    if (!expander_child(a, W, c, y0, ord)) return false;
+  }
+  ch.n = 0;
+  Shape x = y0;
+  for (int step = 0; step < kMaxChain; step++) {
+    if (x.entry < 0 || (uint32_t)x.entry >= a.tab.numEntries) return false;
+    const DevRule r = rule_at(a, (uint32_t)x.entry);
+    if (r.op == PGA_OP_IF_SIZE_LESS) {
+      uint32_t axis;
+      if (!axis_param(a, r, x, axis)) return false;
+      const float size = param(a, r, 1, x);
+      const uint32_t branch = (pick3(x.s, axis) < size) ? 0u : 1u;
+      x.path = child_path(x.path, branch, succ_at(a, r.succBase + branch));
+      x.entry = succ_at(a, r.succBase + branch);
+      continue;
+    }
+    if (r.op == PGA_OP_EXTRUDE) {
+      if (ch.n >= 4) return false;
+      ch.entry[ch.n] = x.entry;
+      ch.before[ch.n] = x;
+      ch.n++;
+      const float extent = param(a, r, 1, x);
+      const uint32_t f = x.frame;
+      x.frame = frame_set(frame_set(f, 1, f, 2, 0), 2, f, 1, 1);
+      x.s[2] = x.s[1];
+      x.s[1] = extent;
+      x.seed = seed_of(a, x.seed, 0u);
+      x.kind = PGA_SHAPE_BOX;
+      const int32_t nxt = succ_at(a, r.succBase);
+      x.path = child_path(x.path, 0u, nxt);
+      x.entry = nxt;
+      continue;
+    }
+    const bool isTerm = r.op == PGA_OP_GENERATE;
+    yEnd = x;
+    return isTerm == toTerminal;
+  }
+  return false;
+}
+
+// Pushes the gradient g of the recorded record back to its parent.
+__device__ void push_back(const DeriveArgs& a, const AdjArgs& j, uint32_t link, uint32_t ordinal, bool toTerminal,
+                          Grad g) {
+  Expander E;
+  bool fromAxiom;
+  uint32_t c;
+  Shape y0, yEnd;
+  Chain ch;
+  if (!replay(a, link, ordinal, toTerminal, E, fromAxiom, c, y0, ch, yEnd)) {
+    raise_error(a.st, PGA_ERR_NO_TAPE, (int)link);
+    return;
+  }
+  // Undo the Extrude steps, last first: after = (s0, extent, s1).
+  for (int k = (int)ch.n - 1; k >= 0; k--) {
+    const Shape& xb = ch.before[k];
+    const DevRule r = rule_at(a, (uint32_t)ch.entry[k]);
+    Grad gb;
+#pragma unroll
+    for (int q = 0; q < 3; q++) gb.t[q] = g.t[q];
+    gb.s[0] = g.s[0];
+    gb.s[1] = g.s[2];
+    gb.s[2] = 0.0f;
+    param_grad(a, j, r, 1, xb, g.s[1], gb.s);
+    g = gb;
+  }
+  if (fromAxiom) {
+    const uint32_t ax = link & ~kAxiomLink;
+    if (j.gradSizes != nullptr)
+      for (int q = 0; q < 3; q++)
+        if (g.s[q] != 0.0f) atomicAdd(&j.gradSizes[(size_t)ax * 3 + q], g.s[q]);
+    return;
+  }
+  Grad gp;
+  grad_zero(gp);
+  child_vjp(a, j, E, c, g, gp);
+  float* dst = j.nodeGrad + (size_t)link * 6;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    if (gp.t[q] != 0.0f) atomicAdd(dst + q, gp.t[q]);
+    if (gp.s[q] != 0.0f) atomicAdd(dst + 3 + q, gp.s[q]);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_adj_terminals(DeriveArgs a, AdjArgs j) {
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  setup_block(a, sm);
+  for (unsigned long long t = (unsigned long long)blockIdx.x * kThreads + threadIdx.x; t < j.numTerminals;
+       t += (unsigned long long)gridDim.x * kThreads) {
+    const float* gm = j.gradTerminals + t * 12;
+    const uint2 link = a.termLinks[t];
+    Grad g;
+    float G[12];
+#pragma unroll
+    for (int q = 0; q < 12; q++) G[q] = __ldg(gm + q);
+    // Generate: M[:, k] = R[:, k] s_k and M[:, 3] = t, with R from the replayed state.
+    Expander E;
+    bool fromAxiom;
+    uint32_t c;
+    Shape y0, yEnd;
+    Chain ch;
+    if (!replay(a, link.x, link.y, true, E, fromAxiom, c, y0, ch, yEnd)) {
+      raise_error(a.st, PGA_ERR_NO_TAPE, (int)t);
+      continue;
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      g.t[q] = G[q * 4 + 3];
+      const uint32_t row = frame_row(yEnd.frame, q);
+      const float v = G[row * 4 + q];
+      g.s[q] = frame_neg(yEnd.frame, q) ? -v : v;
+    }
+    push_back(a, j, link.x, link.y, true, g);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_adj_items(DeriveArgs a, AdjArgs j, unsigned long long lo,
+                                                        unsigned long long hi) {
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  setup_block(a, sm);
+  for (unsigned long long i = lo + (unsigned long long)blockIdx.x * kThreads + threadIdx.x; i < hi;
+       i += (unsigned long long)gridDim.x * kThreads) {
+    const uint4 ext = __ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3);
+    if (ext.x == kEmptyItem) continue;
+    Grad g;
+    const float* src = j.nodeGrad + i * 6;
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      g.t[q] = __ldcg(src + q);
+      g.s[q] = __ldcg(src + 3 + q);
+      any |= (g.t[q] != 0.0f) || (g.s[q] != 0.0f);
+    }
+    if (any) push_back(a, j, ext.z, ext.w, false, g);
+  }
+}
+
+}  // namespace pga
+
+extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, float* dGradParams, uint32_t numBlocks,
+                                 float* dGradAxiomSizes, void* stream) {
+  using namespace pga;
+  if (!e || !dGradTerminals) {
+    set_error("pga_adjoint: null engine or gradient");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  if (!e->cfg.recordTape || !e->lastWasBatched || !e->dTermLinks || !e->lastOut) {
+    set_error("pga_adjoint: the last derivation was not a pga_derive on an engine created with recordTape = 1");
+    return PGA_ERR_NO_TAPE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  DevState snap;
+  PGA_CUDA_TRY(cudaMemcpyAsync(&snap, e->dState, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+  PGA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (snap.status != 0) {
+    set_error("pga_adjoint: the last derivation failed");
+    return (PgaStatus)snap.status;
+  }
+  if (snap.termCount > e->lastCap || snap.termCount > e->cfg.maxTerminals) {
+    set_error("pga_adjoint: more terminals than the tape holds (maxTerminals)");
+    return PGA_ERR_NO_TAPE;
+  }
+  const uint32_t levels = snap.levels + 1;
+  std::vector<unsigned long long> starts(levels + 1, 0);
+  PGA_CUDA_TRY(cudaMemcpy(starts.data(), e->dLevelStart, (levels + 1) * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost));
+  const unsigned long long nodes = std::min<unsigned long long>(snap.nodeNext, e->cfg.nodeCapacity);
+  PGA_CUDA_TRY(cudaMemsetAsync(e->dNodeGrad, 0, nodes * 6 * sizeof(float), s));
+  if (dGradParams) PGA_CUDA_TRY(cudaMemsetAsync(dGradParams, 0, (size_t)numBlocks * e->cfg.blockStride * sizeof(float), s));
+  if (dGradAxiomSizes) PGA_CUDA_TRY(cudaMemsetAsync(dGradAxiomSizes, 0, (size_t)e->lastNumAxioms * 3 * sizeof(float), s));
+  DeriveArgs a = make_args(e, e->lastAxioms, e->lastNumAxioms, e->lastBlocks, e->lastOut, e->lastCap, nullptr);
+  AdjArgs j;
+  j.gradTerminals = dGradTerminals;
+  j.gradParams = dGradParams;
+  j.numBlocks = numBlocks;
+  j.gradSizes = dGradAxiomSizes;
+  j.nodeGrad = e->dNodeGrad;
+  j.numTerminals = snap.termCount;
+  const unsigned blocks = (unsigned)std::max(1, e->numSMs * 4);
+  k_adj_terminals<<<blocks, kThreads, e->smemBytes, s>>>(a, j);
+  PGA_CUDA_TRY(cudaGetLastError());
+  for (int L = (int)levels - 1; L >= 0; L--) {
+    const unsigned long long lo = starts[L], hi = std::min(starts[L + 1], nodes);
+    if (hi <= lo) continue;
+    k_adj_items<<<blocks, kThreads, e->smemBytes, s>>>(a, j, lo, hi);
+    PGA_CUDA_TRY(cudaGetLastError());
+  }
+  return PGA_OK;
+}

@@ -1124,7 +1124,6 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.outCount = count;
   a.nodes = e->dNodes;
   a.nodeCap = e->cfg.nodeCapacity;
-  a.nodeLinks = e->dNodeLinks;
   a.termLinks = e->dTermLinks;
   a.termLinkCap = e->dTermLinks ? e->cfg.maxTerminals : 0;
   a.levelStart = e->dLevelStart;
@@ -1172,7 +1171,7 @@ const PgaProc* pga_default_procs(uint32_t* numProcs) {
 }
 
 static void free_engine(PgaEngine* e) {
-  void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dNodeLinks, e->dLevelClock,
+  void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dLevelClock,
                   e->dTail, e->dTailLinks, e->dScratch,
                   e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA, e->dKeysB,
                   e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dNodeGrad, e->dAxiomGrad};
@@ -1291,7 +1290,6 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   ALLOC(e->dLevelClock, (c.maxLevels + 2) * sizeof(unsigned long long));
   ALLOC(e->dScratchCount, sizeof(unsigned long long));
   if (c.recordTape) {
-    ALLOC(e->dNodeLinks, c.nodeCapacity * sizeof(uint2));
     ALLOC(e->dTermLinks, c.maxTerminals * sizeof(uint2));
     ALLOC(e->dNodeGrad, c.nodeCapacity * 6 * sizeof(float));
   }
@@ -1380,6 +1378,8 @@ PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, 
   e->lastAxioms = dAxioms;
   e->lastNumAxioms = numAxioms;
   e->lastBlocks = dParamBlocks;
+  e->lastOut = dOut;
+  e->lastCap = capacity;
   e->lastWasBatched = true;
   return PGA_OK;
 }
@@ -1393,7 +1393,6 @@ PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAx
   cudaStream_t s = (cudaStream_t)stream;
   PGA_CUDA_TRY(cudaMemsetAsync(e->dState, 0, sizeof(DevState), s));
   DeriveArgs a = make_args(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
-  a.nodeLinks = nullptr;  // the arena is reused per axiom: no tape
   a.termLinks = nullptr;
   const unsigned threads = (unsigned)e->threads;
   for (uint32_t ax = 0; ax < numAxioms; ax++) {
@@ -1463,3 +1462,5 @@ PgaStatus pga_engine_levels(PgaEngine* e, void* stream, uint64_t* starts, uint64
 }
 
 }  // extern "C"
+
+#include "adjoint.cuh"

@@ -95,7 +95,6 @@ struct DeriveArgs {
   unsigned long long* outCount;
   Node* nodes;
   unsigned long long nodeCap;
-  uint2* nodeLinks;          // tape: parent node (or kAxiomLink | axiom), ordinal
   uint2* termLinks;
   unsigned long long termLinkCap;
   unsigned long long* levelStart;

@@ -32,7 +32,6 @@ struct PgaEngine {
   // Work storage (allocated once in pga_engine_create).
   pga::DevState* dState = nullptr;
   pga::Node* dNodes = nullptr;
-  uint2* dNodeLinks = nullptr;
   uint2* dTermLinks = nullptr;
   unsigned long long* dLevelStart = nullptr;
   unsigned long long* dLevelClock = nullptr;
@@ -61,6 +60,8 @@ struct PgaEngine {
   const PgaAxiom* lastAxioms = nullptr;
   uint32_t lastNumAxioms = 0;
   const float* lastBlocks = nullptr;
+  PgaTerminal* lastOut = nullptr;
+  unsigned long long lastCap = 0;
   bool lastWasBatched = false;
 };
 

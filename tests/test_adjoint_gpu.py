@@ -1,0 +1,191 @@
+"""Adjoint (pga_adjoint / torch.autograd) against FP64 central differences.
+
+The derivation tree is frozen by the forward pass.  For a linear loss
+L = sum(W * M) over the terminal transforms (W random, matched to terminals by
+derivation-path hash) the gradient with respect to the per-axiom parameter
+blocks and the axiom sizes is compared with central finite differences
+(h = 1e-4) of the oracle's double-precision derivation.  Perturbations that
+change the set of derivation paths (a branch or a repetition count flips) are
+skipped: the derivative is only defined away from those boundaries.
+Tolerance: FP32 forward and adjoint against FP64 differences, relative 2e-3 of
+the gradient's scale.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from operatorgraph_gb300 import grammar as G
+from operatorgraph_gb300 import scenes
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+H = 1e-4
+RTOL = 2e-3
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from operatorgraph_gb300 import build as B
+
+    B.build()
+    torch.cuda.set_device(0)
+
+
+def _loss64(batch, weights_by_path, blocks64=None, sizes64=None):
+    """sum over terminals of W . M in FP64 (oracle) and the set of derivation paths."""
+    M, P = oracle.derive_f64(G.DEFAULT_PROCS, batch["entries"], batch["axioms"], blocks64, batch["block_stride"],
+                             sizes64)
+    total, keys = 0.0, []
+    for m, p in zip(M, P):
+        w = weights_by_path.get(int(p))
+        if w is None:
+            return None, None
+        total += float(np.dot(w, m))
+        keys.append(int(p))
+    return total, frozenset(keys)
+
+
+def _gpu_grad(batch, weights_seed=3):
+    from operatorgraph_gb300.autograd import axioms_tensor, derive_transforms
+    from operatorgraph_gb300.engine import Engine
+
+    n_ref = len(oracle.derive(G.DEFAULT_PROCS, batch["entries"], batch["axioms"], batch["blocks"],
+                              batch["block_stride"]))
+    eng = Engine(batch["entries"], block_stride=batch["block_stride"], record_tape=True, node_capacity=1 << 20,
+                 max_terminals=1 << 20)
+    d_ax = axioms_tensor(batch["axioms"])
+    blocks = None
+    if batch["blocks"] is not None:
+        blocks = torch.tensor(batch["blocks"], dtype=torch.float32, device="cuda", requires_grad=True)
+    sizes = torch.tensor(batch["axioms"]["size"], dtype=torch.float32, device="cuda", requires_grad=True)
+    M, paths = derive_transforms(eng, d_ax, blocks, sizes, n_ref)
+    assert M.shape[0] == n_ref
+    rng = np.random.default_rng(weights_seed)
+    W = rng.standard_normal((n_ref, 12))
+    loss = (M * torch.tensor(W, dtype=torch.float32, device="cuda")).sum()
+    loss.backward()
+    by_path = {int(p): W[i] for i, p in enumerate(paths.cpu().numpy().view(np.uint64))}
+    gb = None if blocks is None else blocks.grad.detach().cpu().numpy().astype(np.float64)
+    gs = sizes.grad.detach().cpu().numpy().astype(np.float64)
+    eng.release()
+    return by_path, gb, gs
+
+
+def _central(batch, by_path, keys0, base, b64, s64, perturb):
+    """(central difference, forward difference, backward difference) or None
+    when the perturbation changes the set of derivation paths."""
+    bp, sp = perturb(b64, s64, +H)
+    bm, sm = perturb(b64, s64, -H)
+    lp, kp = _loss64(batch, by_path, bp, sp)
+    lm, km = _loss64(batch, by_path, bm, sm)
+    if lp is None or lm is None or kp != keys0 or km != keys0:
+        return None  # a branch, a repetition count or a discard flips within +-H
+    return (lp - lm) / (2 * H), (lp - base) / H, (base - lm) / H
+
+
+def _compare(label, got, diffs):
+    """Checks every smooth entry of diffs (None: skipped); returns how many.
+
+    An input sitting on a kink (an exact Repeat division, where the remainder
+    piece switches between zero and a full extent while the extra piece is
+    discarded) keeps its path set but has different one-sided slopes: the
+    central difference is no derivative there, so entries whose forward and
+    backward differences disagree are skipped too."""
+    fds = [d[0] for d in diffs if d is not None]
+    scale = max(max((abs(f) for f in fds), default=0.0), 1.0)
+    checked = 0
+    for k, d in enumerate(diffs):
+        if d is None or abs(d[1] - d[2]) > 0.5 * RTOL * scale:
+            continue
+        _check(f"{label}[{k}]", got[k], d[0], scale)
+        checked += 1
+    return checked
+
+
+def _check(name, got, fd, scale):
+    err = abs(got - fd)
+    assert err <= RTOL * scale + 1e-6, f"{name}: adjoint {got:.6g} vs FD {fd:.6g} (scale {scale:.3g})"
+
+
+def test_facade_block_and_size_gradients_match_fp64_central_differences():
+    batch = scenes.facades(8, seed=7)
+    by_path, gb, gs = _gpu_grad(batch)
+    b64 = batch["blocks"].astype(np.float64)
+    s64 = batch["axioms"]["size"].astype(np.float64)
+    base, keys0 = _loss64(batch, by_path, b64, s64)
+    assert base is not None and len(keys0) == len(by_path)
+
+    def block_at(k):
+        def f(b, s, h):
+            b = b.copy()
+            b[k] += h
+            return b, s
+        return f
+
+    def size_at(k):
+        def f(b, s, h):
+            s = s.copy()
+            s.reshape(-1)[k] += h
+            return b, s
+        return f
+
+    diffs = [_central(batch, by_path, keys0, base, b64, s64, block_at(k)) for k in range(len(b64))]
+    assert _compare("block", gb, diffs) >= len(b64) * 0.9
+    diffs = [_central(batch, by_path, keys0, base, b64, s64, size_at(k)) for k in range(s64.size)]
+    assert _compare("size", gs.reshape(-1), diffs) == s64.size
+
+
+def _size_cases():
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).parent / "golden"))
+    import cases as C
+
+    out = C.cases()
+    for mode in (G.ANCHOR_TO_START, G.ANCHOR_TO_END, G.ADJUST_TO_FILL):
+        out.append((f"building_off_grid_m{mode}", scenes.building(w=25.3, d=19.7, h=31.0, mode=mode)))
+    return out
+
+
+_SIZE_CASES = _size_cases()
+
+
+@pytest.mark.parametrize("name,batch", _SIZE_CASES, ids=[c[0] for c in _SIZE_CASES])
+def test_axiom_size_gradients_match_fp64_central_differences(name, batch):
+    """Every operator's VJP through the axiom sizes: Subdivide (static, dynamic,
+    absolute / relative / zero factors), Repeat (three modes, relative and
+    absolute extents), ComponentSplit, Extrude, IfSizeLess chains."""
+    by_path, _, gs = _gpu_grad(batch)
+    b64 = None if batch["blocks"] is None else batch["blocks"].astype(np.float64)
+    s64 = batch["axioms"]["size"].astype(np.float64)
+    base, keys0 = _loss64(batch, by_path, b64, s64)
+    assert base is not None and len(keys0) == len(by_path)
+
+    def size_at(k):
+        def f(b, s, h):
+            s = s.copy()
+            s.reshape(-1)[k] += h
+            return b, s
+        return f
+
+    diffs = [_central(batch, by_path, keys0, base, b64, s64, size_at(k)) for k in range(s64.size)]
+    checked = _compare(name, gs.reshape(-1), diffs)
+    if checked == 0:
+        pytest.skip("every axiom size sits on a kink or a discrete boundary")
+
+
+def test_adjoint_requires_tape():
+    from operatorgraph_gb300.engine import Engine, PgaError
+
+    b = scenes.menger(0.15)
+    eng = Engine(b["entries"])
+    out, n, _ = eng.execute(b["axioms"], capacity=1024)
+    g = torch.zeros((n, 12), dtype=torch.float32, device="cuda")
+    with pytest.raises(PgaError) as e:
+        eng.adjoint_raw(g.data_ptr(), None, 0, None)
+    assert e.value.status == 8
+    eng.release()
