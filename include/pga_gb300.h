@@ -220,10 +220,13 @@ PgaStatus pga_derive_plain(PgaEngine* engine, const PgaAxiom* dAxioms, uint32_t 
 PgaStatus pga_engine_sync_report(PgaEngine* engine, void* stream, PgaDeriveReport* report);
 
 /* Per-level profile of the last pga_derive: starts[l] = first node of level l
- * (starts[l+1] its end), nanos[l] = device clock (ns) when level l's range was
- * fixed, for up to `capacity` levels; *numLevels receives the level count.
- * Synchronises `stream`.  Counterpart of the reference's per-subgraph clock
- * instrumentation (include/pga/core/Instrumentation.cuh:44-74). */
+ * (starts[l+1] its end) for up to `capacity` levels; device clock (ns)
+ * nanos[0] = launch start, nanos[l + 1] = when level l's range was fixed (after
+ * the axioms were seeded for l = 0), nanos[numLevels + 1] = launch end (after
+ * the output compaction), as far as `capacity` entries reach; *numLevels
+ * receives the level count.  Synchronises `stream`.  Counterpart of the
+ * reference's per-subgraph clock instrumentation
+ * (include/pga/core/Instrumentation.cuh:44-74). */
 PgaStatus pga_engine_levels(PgaEngine* engine, void* stream, uint64_t* starts, uint64_t* nanos,
                             uint32_t capacity, uint32_t* numLevels);
 

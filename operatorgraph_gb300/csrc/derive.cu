@@ -906,153 +906,173 @@ __device__ __forceinline__ void level_snapshot(const DeriveArgs& a, uint32_t lev
   vs->stop = (!more || vs->status != 0) ? 1u : 0u;
 }
 
+// Exclusive prefix sum of x[0, n) in place (shared memory, whole block);
+// x[n] receives the total.  Every thread takes a contiguous run.
+__device__ void block_exclusive_scan(uint32_t* x, uint32_t n) {
+  __shared__ uint32_t warpSum[kWarps];
+  const unsigned lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  const uint32_t per = (n + kThreads - 1) / kThreads;
+  const uint32_t b = min(n, threadIdx.x * per), e = min(n, b + per);
+  uint32_t sum = 0;
+  for (uint32_t i = b; i < e; i++) sum += x[i];
+  uint32_t total;
+  const uint32_t pre = warp_excl_scan(sum, total);
+  if (lane == 0) warpSum[wid] = total;
+  __syncthreads();
+  uint32_t off = 0, all = 0;
+#pragma unroll
+  for (int k = 0; k < kWarps; k++) {
+    off += (k < (int)wid) ? warpSum[k] : 0u;
+    all += warpSum[k];
+  }
+  uint32_t run = off + pre;
+  for (uint32_t i = b; i < e; i++) {
+    const uint32_t v = x[i];
+    x[i] = run;
+    run += v;
+  }
+  if (threadIdx.x == 0) x[n] = all;
+  __syncthreads();
+}
+
+// Shared-memory bytes the compaction needs for W warps.
+__host__ __device__ constexpr size_t compact_smem_bytes(uint32_t W) {
+  return ((sizeof(Smem) + 15) & ~size_t(15)) + 8ull * W + 4ull * (W + 1) + 4ull * (W + 2);
+}
+
 // Compaction of the terminal output after the last level.  Every warp's last
-// terminal page may be partly filled: N = pages * kTermPage - holes terminals
-// exist, some at positions >= N.  The k-th hole below N (in position order)
-// receives the k-th filled position at or above N.  Partial pages are sorted by
-// rank (each warp counts the entries below its own), one block turns them into
-// hole and source segments with prefix sums, every thread then moves records.
+// terminal page may be partly filled, so with G pages handed out and `holes`
+// unused slots in them, N = G * kTermPage - holes terminals exist and some lie
+// at positions >= N.  Holes below N and filled slots at or above N are equally
+// many; the k-th hole (warps in index order) receives the k-th such record
+// (positions in increasing order).  Only the pages from the one holding N to
+// the last can hold records >= N: fewer than W + 1 pages, all full except the
+// partial pages among them.  After one grid barrier every block rebuilds both
+// enumerations in shared memory from the W published partial pages (no sort,
+// no further barrier) and moves its share of the records.
 __device__ void compact_terminals(const DeriveArgs& a, WarpOut& w) {
   const unsigned lane = threadIdx.x & 31u;
   const uint32_t W = a.numWarps;
   const unsigned long long gw = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
-  unsigned long long* part = a.scratch;              // W entries: page << 9 | fill, or ~0
-  unsigned long long* sorted = part + W;             // W
-  unsigned long long* holeStart = sorted + W;        // W + 1
-  unsigned long long* holePre = holeStart + W + 1;   // W + 2
-  unsigned long long* srcStart = holePre + W + 2;    // W + 1
-  unsigned long long* srcPre = srcStart + W + 1;     // W + 2
+  unsigned long long* part = a.scratch;  // W entries: page << 9 | fill, or ~0
   DevState* st = a.st;
-  // 1. publish the warp's partly filled page
   unsigned long long mine = ~0ull;
   if (w.tPage != ~0ull && w.tFill < kTermPage) mine = (w.tPage << 9) | w.tFill;
-  if (lane == 0 && gw < W) {
-    part[gw] = mine;
-    if (mine != ~0ull) {
-      atomicAdd(&st->holes, (unsigned long long)(kTermPage - w.tFill));
-      atomicAdd(&st->partials, 1ull);
-    }
-  }
-  if (!grid_barrier(a, [&] {
-        volatile DevState* vs = st;
-        const unsigned long long total = atomicAdd(&st->termPages, 0ull) * kTermPage - atomicAdd(&st->holes, 0ull);
-        vs->termCount = total;
-        vs->stop = (vs->status != 0 || total > a.cap || atomicAdd(&st->partials, 0ull) == 0) ? 1u : 0u;
-      }))
+  if (lane == 0 && gw < W) part[gw] = mine;
+  if (!grid_barrier(a, [] {})) return;
+  uint32_t dynBytes;  // the same in every thread of the launch
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dynBytes));
+  if (dynBytes < compact_smem_bytes(W)) {
+    if (threadIdx.x == 0) raise_error(st, PGA_ERR_INTERNAL, 11);
     return;
-  volatile DevState* vs = st;
-  const unsigned long long N = vs->termCount;
-  if (vs->stop == 0) {
-    // 2. sort the partial pages: rank = number of smaller entries
-    if (gw < W && mine != ~0ull) {
-      uint32_t rank = 0;
-      for (uint32_t j = 0; j < W; j += 32) {
-        const unsigned long long other = (j + lane < W) ? __ldcg(&part[j + lane]) : ~0ull;
-        rank += __popc(__ballot_sync(kFull, other < mine));
-      }
-      if (lane == 0) sorted[rank] = mine;
-    }
-    if (!grid_barrier(a, [] {})) return;
-    // 3. hole and source segments (block 0)
-    const uint32_t Q = (uint32_t)vs->partials;
-    const unsigned long long G = atomicAdd(&st->termPages, 0ull);
-    if (blockIdx.x == 0) {
-      __shared__ unsigned long long carryH, carryS;
-      if (threadIdx.x == 0) carryH = carryS = 0;
-      __syncthreads();
-      for (uint32_t base = 0; base <= Q; base += kThreads) {
-        const uint32_t i = base + threadIdx.x;
-        unsigned long long h = 0, sLen = 0, hs = 0, ss = 0;
-        if (i <= Q) {
-          unsigned long long prevEnd = N;
-          if (i > 0) {
-            const unsigned long long e = __ldcg(&sorted[i - 1]);
-            prevEnd = max(((e >> 9) + 1) * kTermPage, N);
-          }
-          unsigned long long vs0 = G * kTermPage;
-          if (i < Q) {
-            const unsigned long long e = __ldcg(&sorted[i]);
-            const unsigned long long start = (e >> 9) * kTermPage + (e & 511ull);
-            const unsigned long long end = ((e >> 9) + 1) * kTermPage;
-            vs0 = max(start, N);
-            hs = start;
-            h = start < N ? min(end, N) - start : 0ull;
-          }
-          ss = prevEnd;
-          sLen = vs0 - prevEnd;
-        }
-        // block-wide inclusive scans of h and sLen
-        unsigned long long xh = h, xs = sLen;
+  }
+  unsigned long long* ps = reinterpret_cast<unsigned long long*>(smem_raw + ((sizeof(Smem) + 15) & ~size_t(15)));
+  uint32_t* hPre = reinterpret_cast<uint32_t*>(ps + W);  // W + 1: holes below N per warp, then prefix
+  uint32_t* sPre = hPre + W + 1;                        // W + 2: records >= N per page, then prefix
+  __shared__ unsigned long long blockHoles[kWarps];
+  unsigned long long holes = 0;
+  for (uint32_t i = threadIdx.x; i < W; i += kThreads) {
+    const unsigned long long e = __ldcg(&part[i]);
+    ps[i] = e;
+    if (e != ~0ull) holes += kTermPage - (e & 511ull);
+  }
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const unsigned long long yh = __shfl_up_sync(kFull, xh, d), ys = __shfl_up_sync(kFull, xs, d);
-          if ((int)lane >= d) { xh += yh; xs += ys; }
-        }
-        __shared__ unsigned long long wh[kWarps], wsum[kWarps];
-        if (lane == 31) { wh[threadIdx.x >> 5] = xh; wsum[threadIdx.x >> 5] = xs; }
-        __syncthreads();
-        unsigned long long ph = carryH, ps = carryS, th = 0, ts = 0;
-        for (int k = 0; k < kWarps; k++) {
-          if (k < (int)(threadIdx.x >> 5)) { ph += wh[k]; ps += wsum[k]; }
-          th += wh[k];
-          ts += wsum[k];
-        }
-        if (i <= Q) {
-          if (i < Q) {
-            holeStart[i] = hs;
-            holePre[i] = ph + xh - h;
-          }
-          srcStart[i] = ss;
-          srcPre[i] = ps + xs - sLen;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) { carryH += th; carryS += ts; }
-        __syncthreads();
-      }
-      if (threadIdx.x == 0) {
-        holePre[Q] = carryH;
-        srcPre[Q + 1] = carryS;
-      }
-    }
-    if (!grid_barrier(a, [] {})) return;
-    // 4. move the k-th source record into the k-th hole
-    const unsigned long long H = __ldcg(&holePre[Q]);
-    for (unsigned long long k = (unsigned long long)blockIdx.x * kThreads + threadIdx.x; k < H;
-         k += (unsigned long long)gridDim.x * kThreads) {
-      uint32_t lo = 0, hi = Q;  // last hole segment with holePre <= k
-      while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldcg(&holePre[mid]) <= k) lo = mid; else hi = mid;
-      }
-      const unsigned long long dst = __ldcg(&holeStart[lo]) + (k - __ldcg(&holePre[lo]));
-      uint32_t slo = 0, shi = Q + 1;
-      while (shi - slo > 1) {
-        const uint32_t mid = (slo + shi) >> 1;
-        if (__ldcg(&srcPre[mid]) <= k) slo = mid; else shi = mid;
-      }
-      const unsigned long long src = __ldcg(&srcStart[slo]) + (k - __ldcg(&srcPre[slo]));
-      if (dst >= a.cap) continue;
-      const bool inTail = src >= a.cap;
-      if (inTail && src - a.cap >= a.tailCap) continue;
-      const uint4* from = reinterpret_cast<const uint4*>(inTail ? a.tail + (src - a.cap) : a.out + src);
-      uint4* to = reinterpret_cast<uint4*>(a.out + dst);
+  for (int d = 16; d > 0; d >>= 1) holes += __shfl_xor_sync(kFull, holes, d);
+  if (lane == 0) blockHoles[threadIdx.x >> 5] = holes;
+  __syncthreads();
+  holes = 0;
 #pragma unroll
-      for (int q = 0; q < 4; q++) to[q] = __ldcg(from + q);
-      if (a.termLinks != nullptr && dst < a.termLinkCap) {
-        uint2 l = make_uint2(0u, 0u);
-        if (inTail) {
-          if (a.tailLinks != nullptr) l = a.tailLinks[src - a.cap];
-        } else if (src < a.termLinkCap) {
-          l = a.termLinks[src];
-        }
-        a.termLinks[dst] = l;
+  for (int k = 0; k < kWarps; k++) holes += blockHoles[k];
+  // One thread decides for the block, so that every thread takes the same path
+  // through the block-wide steps below.
+  __shared__ unsigned long long blockPages;
+  __shared__ int blockGo;
+  if (threadIdx.x == 0) {
+    volatile DevState* vs = st;
+    const unsigned long long G = vs->termPages;
+    const unsigned long long N = G * kTermPage - holes;
+    if (blockIdx.x == 0) vs->termCount = N;
+    int go = (vs->status == 0 && N <= a.cap && holes != 0) ? 1 : 0;
+    // G * kTermPage - N = holes < W * kTermPage, so at most W + 1 pages hold records >= N.
+    if (go && (G <= N / kTermPage || G - N / kTermPage > W + 1)) {
+      raise_error(st, PGA_ERR_INTERNAL, 11);
+      go = 0;
+    }
+    blockPages = G;
+    blockGo = go;
+  }
+  __syncthreads();
+  if (!blockGo) return;
+  const unsigned long long G = blockPages;
+  const unsigned long long N = G * kTermPage - holes;
+  const unsigned long long qN = N / kTermPage;
+  const uint32_t P = (uint32_t)(G - qN);  // pages qN .. G-1
+  for (uint32_t q = threadIdx.x; q < P; q += kThreads) sPre[q] = kTermPage;
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < W; i += kThreads) {
+    const unsigned long long e = ps[i];
+    uint32_t h = 0;
+    if (e != ~0ull) {
+      const unsigned long long page = e >> 9, start = page * kTermPage + (e & 511ull);
+      if (page >= qN) sPre[page - qN] = (uint32_t)(e & 511ull);
+      if (start < N) h = (uint32_t)(min((page + 1) * kTermPage, N) - start);
+    }
+    hPre[i] = h;
+  }
+  __syncthreads();
+  for (uint32_t q = threadIdx.x; q < P; q += kThreads) {
+    const unsigned long long base = (qN + q) * kTermPage, lo = max(base, N), end = base + sPre[q];
+    sPre[q] = end > lo ? (uint32_t)(end - lo) : 0u;
+  }
+  __syncthreads();
+  block_exclusive_scan(hPre, W);
+  block_exclusive_scan(sPre, P);
+  const uint32_t H = hPre[W];
+  for (uint32_t k = blockIdx.x * kThreads + threadIdx.x; k < H; k += gridDim.x * kThreads) {
+    uint32_t lo = 0, hi = W;  // last warp with hPre <= k
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (hPre[mid] <= k) lo = mid; else hi = mid;
+    }
+    const unsigned long long e = ps[lo];
+    const unsigned long long dst = (e >> 9) * kTermPage + (e & 511ull) + (k - hPre[lo]);
+    uint32_t slo = 0, shi = P;  // last page with sPre <= k
+    while (shi - slo > 1) {
+      const uint32_t mid = (slo + shi) >> 1;
+      if (sPre[mid] <= k) slo = mid; else shi = mid;
+    }
+    const unsigned long long src = max((qN + slo) * kTermPage, N) + (k - sPre[slo]);
+    PGA_GUARD(dst < N && src >= N && e != ~0ull, 12, continue);
+    const bool inTail = src >= a.cap;
+    if (inTail && src - a.cap >= a.tailCap) continue;
+    const uint4* from = reinterpret_cast<const uint4*>(inTail ? a.tail + (src - a.cap) : a.out + src);
+    uint4* to = reinterpret_cast<uint4*>(a.out + dst);
+    uint4 r[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) r[q] = __ldcg(from + q);
+#pragma unroll
+    for (int q = 0; q < 4; q++) to[q] = r[q];
+    if (a.termLinks != nullptr && dst < a.termLinkCap) {
+      uint2 l = make_uint2(0u, 0u);
+      if (inTail) {
+        if (a.tailLinks != nullptr) l = a.tailLinks[src - a.cap];
+      } else if (src < a.termLinkCap) {
+        l = a.termLinks[src];
       }
+      a.termLinks[dst] = l;
     }
   }
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+  return now;
+}
+
 __global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.st->clockStart = global_ns();
   setup_block(a, sm);
   WarpOut w;
   warpout_init(w);
@@ -1074,6 +1094,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a)
   }
   compact_terminals(a, w);
   if (blockIdx.x == 0 && threadIdx.x == 0 && a.outCount != nullptr) *a.outCount = ((volatile DevState*)a.st)->termCount;
+  __syncthreads();
+  if (threadIdx.x == 0) atomicMax(&a.st->clockEnd, global_ns());
 }
 
 __global__ void __launch_bounds__(kThreads, 2) k_seed(DeriveArgs a, uint32_t first, uint32_t count) {
@@ -1331,6 +1353,24 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create occupancy"));
   if (c.blocksPerSM > 0 && (int)c.blocksPerSM < perSM) perSM = (int)c.blocksPerSM;
   if (perSM < 1) perSM = 1;
+  {
+    // The end-of-launch compaction keeps per-warp tables in the same dynamic
+    // shared memory (the rule table is no longer read by then).
+    const size_t need = compact_smem_bytes((uint32_t)(perSM * e->numSMs * (e->threads / 32)));
+    if (need > e->smemBytes) {
+      e->smemBytes = (need + 15) & ~size_t(15);
+      err = cudaFuncSetAttribute(k_derive_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
+      if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
+      if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(k_expand_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
+      int again = 0;
+      if (err == cudaSuccess)
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&again, k_derive_persistent, e->threads, e->smemBytes);
+      if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create occupancy"));
+      perSM = std::max(1, std::min(perSM, again));  // fewer warps need fewer bytes
+    }
+  }
   e->persistentBlocks = perSM * e->numSMs;
   {
     // Paged output of the persistent engine: every warp may leave one partly
@@ -1340,7 +1380,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     e->tailCap = warps * kTermPage;
     err = cudaMalloc((void**)&e->dTail, e->tailCap * sizeof(PgaTerminal));
     if (err == cudaSuccess && c.recordTape) err = cudaMalloc((void**)&e->dTailLinks, e->tailCap * sizeof(uint2));
-    if (err == cudaSuccess) err = cudaMalloc((void**)&e->dScratch, 6 * (warps + 2) * sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMalloc((void**)&e->dScratch, (warps + 2) * sizeof(unsigned long long));
     if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create tail"));
   }
   *out = e;
@@ -1457,7 +1497,12 @@ PgaStatus pga_engine_levels(PgaEngine* e, void* stream, uint64_t* starts, uint64
   *numLevels = n;
   uint32_t k = std::min(n, capacity);
   if (k && starts) PGA_CUDA_TRY(cudaMemcpy(starts, e->dLevelStart, k * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-  if (k && nanos) PGA_CUDA_TRY(cudaMemcpy(nanos, e->dLevelClock, k * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  if (nanos && capacity) {
+    nanos[0] = snap.clockStart;
+    const uint32_t kc = std::min(n, capacity - 1);
+    if (kc) PGA_CUDA_TRY(cudaMemcpy(nanos + 1, e->dLevelClock, kc * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    if (n + 1 < capacity) nanos[n + 1] = snap.clockEnd;
+  }
   return PGA_OK;
 }
 

@@ -73,14 +73,14 @@ struct DevState {
   unsigned long long nodeNext;    // queued item slots handed out (plain form)
   unsigned long long termPages;   // terminal pages handed out (paged engine)
   unsigned long long nodePages;   // item pages handed out (paged engine)
-  unsigned long long holes;       // unused slots of the warps' last terminal pages
-  unsigned long long partials;    // warps holding a partly filled terminal page
   unsigned long long cursor;
   unsigned long long levelLo, levelHi;
   unsigned long long maxLevelNodes;
   int32_t status, detail;
   uint32_t barrierArrive, barrierGen;
   uint32_t levels, stop;
+  unsigned long long clockStart;  // %globaltimer when block 0 started (paged engine)
+  unsigned long long clockEnd;    // %globaltimer when the last block finished
 };
 
 struct DeriveArgs {

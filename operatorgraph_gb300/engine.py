@@ -158,15 +158,19 @@ class Engine:
                 "levels": rep.levels, "max_level_nodes": rep.maxLevelNodes}
 
     def levels(self, stream=None, capacity=4096):
-        """Per-level node ranges and device clock of the last pga_derive."""
+        """Per-level node ranges and device clocks of the last pga_derive.
+
+        Returns (starts, nanos): starts[l] is the first item of level l; nanos[0]
+        the launch start, nanos[l + 1] the time level l's range was fixed and
+        nanos[-1] the launch end."""
         L = load_library()
         starts = np.zeros(capacity, np.uint64)
-        nanos = np.zeros(capacity, np.uint64)
+        nanos = np.zeros(capacity + 2, np.uint64)
         n = ctypes.c_uint32()
         _check(L.pga_engine_levels(self.handle, _stream_handle(stream), starts.ctypes.data, nanos.ctypes.data,
-                                   capacity, ctypes.byref(n)), "pga_engine_levels")
+                                   capacity + 2, ctypes.byref(n)), "pga_engine_levels")
         k = min(n.value, capacity)
-        return starts[: k + 1], nanos[:k]
+        return starts[:k], nanos[: k + 2]
 
     # -- convenience on torch tensors --------------------------------------------------------
     def execute(self, axioms, blocks=None, capacity=None, plain=False, out=None, stream=None, check=True):

@@ -73,8 +73,10 @@ def main(argv=None):
     if not args.plain:
         starts, nanos = eng.levels()
         nanos = nanos.astype(np.int64)
+        d = np.diff(nanos) / 1e3
         lv = {"level_nodes": np.diff(starts.astype(np.int64)).tolist(),
-              "level_us": (np.diff(nanos) / 1e3).round(2).tolist()}
+              "seed_us": round(float(d[0]), 2), "level_us": d[1:-1].round(2).tolist(),
+              "compact_us": round(float(d[-1]), 2)}
     res = {"scene": args.scene, "n": args.n, "plain": args.plain, "terminals": int(count.item()),
            "ms": times, "ms_median": statistics.median(times), "report": rep, **lv}
     if lb:
