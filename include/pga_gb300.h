@@ -130,8 +130,9 @@ typedef struct PgaEngineConfig {
   uint32_t maxLevels;        /* derivation depth limit (0 = default 4096) */
   uint32_t flags;            /* reserved, 0 */
   uint32_t subItem;          /* children per queued work item, 1..64 (0 = default 8) */
-  uint32_t itemsPerLane;     /* work items per lane in one warp chunk (0 = default 2) */
-  uint32_t reserved;
+  uint32_t itemsPerLane;     /* work items per lane in one warp chunk (0 = default 1) */
+  uint32_t narrowSubItem;    /* children per work item queued while the level being expanded has fewer
+                                items than the grid has threads, 1..64 (0 = default) */
 } PgaEngineConfig;
 
 

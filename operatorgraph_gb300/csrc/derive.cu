@@ -8,18 +8,21 @@
 // 1 -> 1 rules (IfSizeLess, Extrude) and ends as a terminal (Generate: written
 // out directly), a discard, or a branching shape that is queued as work items.
 //
-// A warp works on a chunk of 32 x itemsPerLane work items in two passes over
-// the same children: the first counts the terminals and queued items the
-// chunk produces, one global atomic per counter reserves contiguous slots for
-// the whole chunk, the second recomputes the children and writes them; each
-// emission round writes a contiguous run of records in lane order.  Warps take
-// chunks in a static grid-stride order: no shared work counter, no block-wide
-// barrier inside a level.
+// A warp works on a chunk of 32 x itemsPerLane work items; warps take chunks
+// in a static grid-stride order (no shared work counter, no block-wide barrier
+// inside a level).  Output is paged per warp: a warp holds a page of kTermPage
+// terminal slots and a page of kNodePage item slots, each taken with one
+// atomic, and every emission round writes a contiguous run of its page in lane
+// order.  A branching child is queued as ceil(children / S) work items, with S
+// = narrowSubItem while the level being expanded is narrower than the grid and
+// subItem otherwise.
 //
 // pga_derive runs every level of every axiom in ONE persistent cooperative
-// launch (a bounded grid barrier between levels, blocks pulling 256 items at a
-// time from a level cursor); pga_derive_plain is the plain GPU form: one axiom
-// at a time, one launch per level, the host reading each level's size back.
+// launch: a bounded grid barrier between levels, item pages closed at each
+// level end, and one compaction at the end that moves the records past the
+// final count into the holes the warps' last terminal pages left.
+// pga_derive_plain is the plain GPU form: one axiom at a time, one launch per
+// level, the host reading each level's size back, one atomic per round.
 //
 // The reference executes the same operators from per-procedure queues in a
 // Whippletree megakernel (deps/whippletree/include/techniqueMegakernel.cuh:374-473)
@@ -600,12 +603,20 @@ constexpr uint32_t kEmptyItem = 0xFFFFFFFFu;
 struct WarpOut {
   unsigned long long tPage, nPage;
   uint32_t tFill, nFill;  // slots used in the current page (page size when there is none)
+  uint32_t sub;           // children per queued work item for the level being expanded
 };
 
-__device__ __forceinline__ void warpout_init(WarpOut& w) {
+__device__ __forceinline__ void warpout_init(const DeriveArgs& a, WarpOut& w) {
   w.tPage = w.nPage = ~0ull;
   w.tFill = kTermPage;
   w.nFill = kNodePage;
+  w.sub = a.subItem;
+}
+
+// A level with fewer items than the grid has threads leaves most lanes idle:
+// its children are queued in finer work items (more parallelism next level).
+__device__ __forceinline__ void warpout_level(const DeriveArgs& a, WarpOut& w, unsigned long long items) {
+  w.sub = items < (unsigned long long)gridDim.x * kThreads ? a.narrowSubItem : a.subItem;
 }
 
 // Reserves cnt consecutive slots (warp-uniform) of a paged stream: a lane's
@@ -677,7 +688,7 @@ __device__ __forceinline__ void emit_round(const DeriveArgs& a, WarpOut& w, int 
   }
   const unsigned nm = __ballot_sync(kFull, kind == kNode);
   if (nm) {
-    const uint32_t S = a.subItem;
+    const uint32_t S = w.sub;
     const uint32_t m = (kind == kNode) ? (nChild + S - 1) / S : 0u;
     uint32_t total;
     const uint32_t pre = warp_excl_scan(m, total);
@@ -1070,12 +1081,18 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return now;
 }
 
-__global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a) {
+// Resident blocks per SM the persistent kernel is compiled for (register budget).
+#ifndef PGA_PERSISTENT_MIN_BLOCKS
+#define PGA_PERSISTENT_MIN_BLOCKS 2
+#endif
+
+__global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   if (blockIdx.x == 0 && threadIdx.x == 0) a.st->clockStart = global_ns();
   setup_block(a, sm);
   WarpOut w;
-  warpout_init(w);
+  warpout_init(a, w);
+  warpout_level(a, w, a.numAxioms);
   seed_axioms<true>(a, w, 0, a.numAxioms);
   close_node_page(a, w);
   if (!grid_barrier(a, [&] {
@@ -1088,7 +1105,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_derive_persistent(DeriveArgs a)
   for (uint32_t level = 0;; level++) {
     volatile DevState* vs = a.st;
     if (vs->stop) break;
-    expand_level<true>(a, w, vs->levelLo, vs->levelHi, a.itemsPerLane);
+    const unsigned long long lo = vs->levelLo, hi = vs->levelHi;
+    warpout_level(a, w, hi - lo);
+    expand_level<true>(a, w, lo, hi, a.itemsPerLane);
     close_node_page(a, w);
     if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
   }
@@ -1102,7 +1121,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_seed(DeriveArgs a, uint32_t fir
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
   WarpOut w;
-  warpout_init(w);
+  warpout_init(a, w);
   seed_axioms<false>(a, w, first, count);
 }
 
@@ -1111,7 +1130,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsi
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
   WarpOut w;
-  warpout_init(w);
+  warpout_init(a, w);
   expand_level<false>(a, w, lo, hi, 1);
 }
 
@@ -1155,6 +1174,7 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.subItem = e->cfg.subItem;
   a.useSeeds = e->useSeeds ? 1u : 0u;
   a.itemsPerLane = e->cfg.itemsPerLane;
+  a.narrowSubItem = e->cfg.narrowSubItem;
   a.tail = e->dTail;
   a.tailLinks = e->dTailLinks;
   a.tailCap = e->tailCap;
@@ -1219,9 +1239,10 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   if (c.spinLimit == 0) c.spinLimit = 1u << 24;
   if (c.maxLevels == 0) c.maxLevels = 4096;
   if (c.subItem == 0) c.subItem = 8;
-  if (c.itemsPerLane == 0) c.itemsPerLane = 2;
-  if (c.subItem > 64) {
-    set_error("pga_engine_create: subItem must be at most 64");
+  if (c.itemsPerLane == 0) c.itemsPerLane = 1;
+  if (c.narrowSubItem == 0) c.narrowSubItem = c.subItem;
+  if (c.subItem > 64 || c.narrowSubItem > 64) {
+    set_error("pga_engine_create: subItem and narrowSubItem must be at most 64");
     delete e;
     return PGA_ERR_INVALID_ARGUMENT;
   }

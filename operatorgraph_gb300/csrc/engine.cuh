@@ -103,7 +103,8 @@ struct DeriveArgs {
   uint32_t spinLimit;
   uint32_t subItem;     // children per queued item (1..8)
   uint32_t useSeeds;    // 0: no parameter of the grammar reads a seed, skip seed updates
-  uint32_t itemsPerLane;  // work items per lane in one warp chunk
+  uint32_t itemsPerLane;
+  uint32_t narrowSubItem;  // work items per lane in one warp chunk
   PgaTerminal* tail;      // terminal slots at or beyond `cap` (pages straddling the end of the output)
   uint2* tailLinks;
   unsigned long long tailCap;

@@ -50,7 +50,7 @@ class PgaEngineConfig(ctypes.Structure):
                 ("blockStride", ctypes.c_uint32), ("threadsPerBlock", ctypes.c_uint32),
                 ("blocksPerSM", ctypes.c_uint32), ("recordTape", ctypes.c_uint32), ("spinLimit", ctypes.c_uint32),
                 ("maxLevels", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("subItem", ctypes.c_uint32),
-                ("itemsPerLane", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("itemsPerLane", ctypes.c_uint32), ("narrowSubItem", ctypes.c_uint32)]
 
 
 class PgaDeriveReport(ctypes.Structure):
@@ -130,14 +130,15 @@ class Engine:
     """A dispatch table lowered to the device, plus all of its work storage."""
 
     def __init__(self, entries, procs=None, node_capacity=1 << 22, max_terminals=1 << 22, block_stride=0,
-                 record_tape=False, blocks_per_sm=0, spin_limit=0, max_levels=0, sub_item=0, items_per_lane=0):
+                 record_tape=False, blocks_per_sm=0, spin_limit=0, max_levels=0, sub_item=0, items_per_lane=0,
+                 narrow_sub_item=0):
         L = load_library()
         self.entries = np.ascontiguousarray(entries, dtype=G.ENTRY_DT)
         self.procs = np.ascontiguousarray(G.DEFAULT_PROCS if procs is None else procs, dtype=G.PROC_DT)
         table = PgaRuleTable(self.procs.ctypes.data, len(self.procs), self.entries.ctypes.data, len(self.entries))
         self.config = PgaEngineConfig(node_capacity, max_terminals, block_stride, 256, blocks_per_sm,
                                       1 if record_tape else 0, spin_limit, max_levels, 0, sub_item,
-                                      items_per_lane, 0)
+                                      items_per_lane, narrow_sub_item)
         h = ctypes.c_void_p()
         _check(L.pga_engine_create(ctypes.byref(table), ctypes.byref(self.config), ctypes.byref(h)),
                "pga_engine_create")

@@ -41,11 +41,18 @@ def main(argv=None):
     ap.add_argument("--lbvh", action="store_true", help="also build the LBVH after each derivation")
     ap.add_argument("--capacity", type=int, default=0)
     ap.add_argument("--nodes", type=int, default=1 << 22)
+    ap.add_argument("--sub-item", type=int, default=0, help="children per work item (engine default 8)")
+    ap.add_argument("--items-per-lane", type=int, default=0, help="work items per lane per chunk (default 2)")
+    ap.add_argument("--narrow-sub-item", type=int, default=0,
+                    help="children per work item queued from levels narrower than the grid (default subItem)")
+    ap.add_argument("--blocks-per-sm", type=int, default=0, help="cap on resident blocks per SM (0: occupancy)")
     args = ap.parse_args(argv)
 
     b, bounds = make_scene(args.scene, args.n)
     cap = args.capacity or 8_000_000
-    eng = Engine(b["entries"], node_capacity=args.nodes, max_terminals=cap, block_stride=b["block_stride"])
+    eng = Engine(b["entries"], node_capacity=args.nodes, max_terminals=cap, block_stride=b["block_stride"],
+                 sub_item=args.sub_item, items_per_lane=args.items_per_lane, blocks_per_sm=args.blocks_per_sm,
+                 narrow_sub_item=args.narrow_sub_item)
     dev = torch.device("cuda", torch.cuda.current_device())
     d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).to(dev)
     d_blk = None if b["blocks"] is None else torch.from_numpy(np.asarray(b["blocks"], np.float32)).to(dev)
@@ -77,7 +84,9 @@ def main(argv=None):
         lv = {"level_nodes": np.diff(starts.astype(np.int64)).tolist(),
               "seed_us": round(float(d[0]), 2), "level_us": d[1:-1].round(2).tolist(),
               "compact_us": round(float(d[-1]), 2)}
-    res = {"scene": args.scene, "n": args.n, "plain": args.plain, "terminals": int(count.item()),
+    res = {"scene": args.scene, "n": args.n, "plain": args.plain, "sub_item": args.sub_item,
+           "items_per_lane": args.items_per_lane, "narrow_sub_item": args.narrow_sub_item,
+           "terminals": int(count.item()),
            "ms": times, "ms_median": statistics.median(times), "report": rep, **lv}
     if lb:
         res["lbvh_ms"] = lb
