@@ -217,7 +217,10 @@ PgaStatus pga_derive_plain(PgaEngine* engine, const PgaAxiom* dAxioms, uint32_t 
                            const float* dParamBlocks, PgaTerminal* dOut, uint64_t capacity,
                            uint64_t* dCount, void* stream);
 
-/* Synchronises `stream` and reports the device status of the last derivation. */
+/* Synchronises `stream` and reports the device status of the last derivation:
+ * PGA_ERR_OUTPUT_OVERFLOW when it produced more terminals than the capacity it
+ * was given (report->terminals holds the full count; records past the
+ * capacity were dropped, never wrapped around). */
 PgaStatus pga_engine_sync_report(PgaEngine* engine, void* stream, PgaDeriveReport* report);
 
 /* Per-level profile of the last pga_derive: starts[l] = first node of level l

@@ -1482,6 +1482,7 @@ PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAx
     }
     if (status != 0) break;
   }
+  e->lastCap = capacity;
   if (dCount) {
     k_write_count<<<1, 1, 0, s>>>(e->dState, (unsigned long long*)dCount);
     PGA_CUDA_TRY(cudaGetLastError());
@@ -1498,6 +1499,9 @@ PgaStatus pga_engine_sync_report(PgaEngine* e, void* stream, PgaDeriveReport* re
   PGA_CUDA_TRY(cudaMemcpyAsync(&snap, e->dState, sizeof(DevState), cudaMemcpyDeviceToHost, s));
   PGA_CUDA_TRY(cudaStreamSynchronize(s));
   memset(report, 0, sizeof *report);
+  // Terminals past the caller's capacity were dropped (never wrapped around):
+  // that is an output overflow, reported with the full count.
+  if (snap.status == 0 && snap.termCount > e->lastCap) snap.status = PGA_ERR_OUTPUT_OVERFLOW;
   report->status = snap.status;
   report->detail = snap.detail;
   report->terminals = snap.termCount;

@@ -227,3 +227,40 @@ def test_bounded_barrier_timeout_is_a_status():
     out, n, rep = eng.execute(b["axioms"], capacity=8000)
     assert n == 8000
     eng.release()
+
+
+def test_derive_is_graph_capturable():
+    """pga_derive (a state reset plus one cooperative launch on the caller's
+    stream) captured in a CUDA graph and replayed gives the same terminals."""
+    import torch
+
+    b = scenes.city(64)
+    eng = _engine(b["entries"])
+    d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).cuda()
+    cap = 200_000
+    out = torch.zeros((cap, 64), dtype=torch.uint8, device="cuda")
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    want, n, _ = eng.execute(b["axioms"], capacity=cap)
+    want = want[:n].cpu().numpy().copy()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):  # warm-up outside the capture
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None, out.data_ptr(), cap, count.data_ptr(), stream=s)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None, out.data_ptr(), cap, count.data_ptr(),
+                       stream=torch.cuda.current_stream())
+    for _ in range(3):
+        out.zero_()
+        count.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert int(count.item()) == n
+        got = out[:n].cpu().numpy()
+        ka = np.sort(got.view(np.dtype((np.void, 64))).ravel())
+        kb = np.sort(want.view(np.dtype((np.void, 64))).ravel())
+        assert (ka == kb).all()
+    assert eng.report()["status"] == 0
+    eng.release()
