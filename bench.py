@@ -7,6 +7,9 @@ IfSizeLess, window Subdivide) derived in one pga_derive call -> 5,856,274
 instanced terminals (375 MB of 64-byte records, larger than the 129 MB L2;
 L2 is also flushed with a 256 MB write before every timed step).
 
+schedule: before timing, the engine knobs are autotuned on this workload
+         (operatorgraph_gb300/autotune.py, 24 candidates); the fastest drives
+         the timed engine ("batched + autotuned").
 value  : terminals/s with axioms and grammar resident in HBM (CUDA events on
          the launching stream around pga_derive).
 e2e    : the same through the C ABI with host buffers: pinned-host -> device
@@ -16,7 +19,8 @@ roofline: algorithmic bytes of the derivation kernel (64 B per terminal
          written + 48 B per axiom read) / kernel time, against the measured
          HBM copy bandwidth.
 extra  : the plain one-grammar-per-launch GPU form on the same city, the
-         Menger sponge at depth 5 and the LBVH over the city's terminals.
+         Menger sponge at depth 5, the LBVH over the city's terminals, the
+         facades with tape + adjoint, and the 65,536-axiom mixed batch.
 
 `--impl reference` times the reference's own CPU derivation (oracle/_ref,
 built from the reference sources) on the same workload, sharded by axiom
@@ -234,6 +238,7 @@ def reference_arm(args):
 def our_arm(args):
     import torch
 
+    from operatorgraph_gb300 import autotune
     from operatorgraph_gb300 import build as B
     from operatorgraph_gb300.engine import Engine, load_library
 
@@ -254,7 +259,11 @@ def our_arm(args):
     batch = scenes.city(4096)
     n_ax = len(batch["axioms"])
     cap = 6_000_000
-    eng = Engine(batch["entries"], node_capacity=1 << 22, max_terminals=cap)
+    # Schedule autotuning (the reference's per-grammar schedule search): the
+    # fastest knob set on this workload drives the timed engine.
+    best, tuned_ms, tuning = autotune.tune(batch, cap, node_capacity=1 << 22, runs=5)
+    default_ms = next((r["ms"] for r in tuning if r["config"] == autotune.DEFAULT_CONFIG), None)
+    eng = Engine(batch["entries"], node_capacity=1 << 22, max_terminals=cap, **best)
     d_ax = torch.from_numpy(batch["axioms"].view(np.uint8).copy()).to(dev)
     out = torch.empty((cap, 64), dtype=torch.uint8, device=dev)
     count = torch.zeros(1, dtype=torch.int64, device=dev)
@@ -343,6 +352,8 @@ def our_arm(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_derive_persistent", "algorithmic_bytes": alg_bytes},
+            "schedule": {"autotuned": best, "candidates": len(tuning), "tuned_ms": tuned_ms,
+                         "default_ms": default_ms},
             "gpu_launches": args.steps,
             "clocks": clocks.summary(),
             "extra": extra,
@@ -443,6 +454,31 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["facades1024_forward_tape_ms"] = statistics.median(fw)
     res["facades1024_adjoint_ms"] = statistics.median(bw)
     ef.release()
+    del out
+    # The mixed batch: 65,536 axioms (40 % Menger depth 1-3, 40 % city
+    # buildings, 20 % random grammars), about 152M terminals in one launch.
+    mx = scenes.mixed(65536)
+    mcap = 160_000_000
+    em = Engine(mx["entries"], node_capacity=1 << 27, max_terminals=mcap)
+    d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
+    mout = torch.empty((mcap, 64), dtype=torch.uint8, device=dev)
+    ts = []
+    for it in range(6):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        em.derive_raw(d_mx.data_ptr(), 65536, None, mout.data_ptr(), mcap, count.data_ptr())
+        b.record(stream)
+        torch.cuda.synchronize()
+        if it >= 2:
+            ts.append(a.elapsed_time(b))
+    rep = em.report()
+    assert rep["status"] == 0, rep
+    n_mx = int(count.item())
+    res["mixed65536_terminals"] = n_mx
+    res["mixed65536_ms"] = statistics.median(ts)
+    res["mixed65536_terminals_per_s"] = n_mx / (res["mixed65536_ms"] * 1e-3)
+    em.release()
+    del mout
     return res
 
 

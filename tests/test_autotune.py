@@ -1,0 +1,61 @@
+"""Schedule autotuner: candidate space and selection on CPU (fake timings),
+one real sweep on the GPU whose winner must still derive bit-exactly."""
+import numpy as np
+import pytest
+
+import oracle
+from operatorgraph_gb300 import autotune as A
+from operatorgraph_gb300 import grammar as G
+from operatorgraph_gb300 import scenes
+
+
+def test_candidates_cover_the_space_without_duplicates():
+    c = A.candidates({"sub_item": (4, 8), "narrow_sub_item": (0, 4, 8), "items_per_lane": (1,)})
+    keys = {tuple(sorted(x.items())) for x in c}
+    assert len(keys) == len(c)
+    # narrow == sub is the same schedule as narrow = 0
+    assert {"sub_item": 4, "narrow_sub_item": 0, "items_per_lane": 1} in c
+    assert {"sub_item": 4, "narrow_sub_item": 4, "items_per_lane": 1} not in c
+    assert len(c) == 4  # (4,0) (4,8) (8,0) (8,4)
+
+
+def test_tune_picks_the_fastest_successful_candidate():
+    space = {"sub_item": (4, 8, 16), "items_per_lane": (1, 2)}
+    fake = {(4, 1): (0.30, 1), (8, 1): (0.31, 0), (16, 1): (0.29, 2), (4, 2): (0.35, 0), (8, 2): (0.33, 0),
+            (16, 2): (0.40, 0)}
+
+    def measure(cfg):
+        ms, st = fake[(cfg["sub_item"], cfg["items_per_lane"])]
+        return (ms if st == 0 else None), st
+
+    best, ms, results = A.tune(None, 0, space=space, measure_fn=measure)
+    assert best == {"sub_item": 8, "items_per_lane": 1} and ms == pytest.approx(0.31)
+    assert len(results) == 6 and sum(r["status"] != 0 for r in results) == 2
+
+
+def test_tune_fails_loudly_when_nothing_runs():
+    with pytest.raises(RuntimeError):
+        A.tune(None, 0, space={"sub_item": (8,)}, measure_fn=lambda cfg: (None, 1))
+
+
+@pytest.mark.gpu
+def test_tuned_schedule_derives_the_same_terminals():
+    torch = pytest.importorskip("torch")
+    from operatorgraph_gb300 import build as B
+    from operatorgraph_gb300.engine import Engine
+
+    B.build()
+    b = scenes.city(256)
+    want = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    cap = len(want) + 4096
+    best, ms, results = A.tune(b, cap, node_capacity=1 << 20, runs=2,
+                               space={"sub_item": (4, 8), "narrow_sub_item": (0, 2), "items_per_lane": (1, 2)})
+    assert ms > 0 and len(results) == 8
+    eng = Engine(b["entries"], node_capacity=1 << 20, max_terminals=cap, **best)
+    out, n, _ = eng.execute(b["axioms"], capacity=cap)
+    got = out[:n].cpu().numpy()
+    eng.release()
+    ka = np.sort(got.view(np.dtype((np.void, 64))).ravel())
+    kb = np.sort(want.view(np.uint8).reshape(len(want), 64).view(np.dtype((np.void, 64))).ravel())
+    assert n == len(want) and (ka == kb).all()
+    assert torch.cuda.is_available()

@@ -264,3 +264,42 @@ def test_derive_is_graph_capturable():
         assert (ka == kb).all()
     assert eng.report()["status"] == 0
     eng.release()
+
+
+def test_mixed_65536_full_size_properties():
+    """The C5 mix at full size (65,536 axioms: Menger depths 1-3, city buildings,
+    random grammars; about 152M terminals) in one launch, against the oracle run
+    in axiom shards: the exact count, the exact histogram of emitting rules
+    (entry, mesh index, shape), float64 sums of every transform component, and
+    unique path hashes.  Bit-exact per-record parity is covered on the smaller
+    cases; here the shard runs renumber the axioms, so path hashes differ."""
+    import torch
+
+    b = scenes.mixed(65536)
+    want_n, want_sum, want_rules = 0, np.zeros(12), {}
+    for lo in range(0, 65536, 4096):
+        t = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"][lo:lo + 4096])
+        want_n += len(t)
+        want_sum += t["m"].astype(np.float64).sum(axis=0)
+        r, c = np.unique(t["rule"], return_counts=True)
+        for k, v in zip(r.tolist(), c.tolist()):
+            want_rules[k] = want_rules.get(k, 0) + v
+        del t
+    cap = want_n + (1 << 20)
+    eng = _engine(b["entries"], node_capacity=1 << 27, max_terminals=cap)
+    out, n, rep = eng.execute(b["axioms"], capacity=cap)
+    assert rep["status"] == 0 and n == want_n
+    got_sum = torch.zeros(12, dtype=torch.float64, device="cuda")
+    rules, paths = [], []
+    for lo in range(0, n, 1 << 23):
+        chunk = out[lo:min(n, lo + (1 << 23))]
+        f = chunk.view(torch.float32).view(-1, 16)
+        got_sum += f[:, :12].double().sum(dim=0)
+        rules.append(chunk.view(torch.int32).view(-1, 16)[:, 12])
+        paths.append(chunk.view(torch.int64).view(-1, 8)[:, 7])
+    r, c = torch.unique(torch.cat(rules), return_counts=True)
+    got_rules = {int(k) & 0xFFFFFFFF: int(v) for k, v in zip(r.cpu().tolist(), c.cpu().tolist())}
+    assert got_rules == want_rules
+    np.testing.assert_allclose(got_sum.cpu().numpy(), want_sum, rtol=1e-9, atol=1e-3)
+    assert torch.unique(torch.cat(paths)).numel() == n
+    eng.release()
