@@ -261,8 +261,12 @@ def our_arm(args):
     cap = 6_000_000
     # Schedule autotuning (the reference's per-grammar schedule search): the
     # fastest knob set on this workload drives the timed engine.
-    best, tuned_ms, tuning = autotune.tune(batch, cap, node_capacity=1 << 22, runs=5)
-    default_ms = next((r["ms"] for r in tuning if r["config"] == autotune.DEFAULT_CONFIG), None)
+    if args.schedule:
+        best = {k: int(v) for k, v in (kv.split("=") for kv in args.schedule.split(","))}
+        tuned_ms, tuning, default_ms = None, [], None
+    else:
+        best, tuned_ms, tuning = autotune.tune(batch, cap, node_capacity=1 << 22, runs=5)
+        default_ms = next((r["ms"] for r in tuning if r["config"] == autotune.DEFAULT_CONFIG), None)
     eng = Engine(batch["entries"], node_capacity=1 << 22, max_terminals=cap, **best)
     d_ax = torch.from_numpy(batch["axioms"].view(np.uint8).copy()).to(dev)
     out = torch.empty((cap, 64), dtype=torch.uint8, device=dev)
@@ -488,6 +492,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--schedule", default="",
+                    help="fixed engine knobs instead of autotuning, e.g. sub_item=16,narrow_sub_item=2")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -165,11 +165,13 @@ __device__ __forceinline__ float seed_of(const DeriveArgs& a, float base, uint32
 
 // Translation by o along model axis `ax`: t' = fl(fl(R[:,ax] * o) + t), which
 // for a signed-permutation R is one rounded add in row perm_ax.
-__device__ __forceinline__ void translate_axis(Shape& y, const Shape& x, uint32_t ax, float o) {
-  const uint32_t row = frame_row(x.frame, ax);
-  const float v = frame_neg(x.frame, ax) ? -o : o;
+__device__ __forceinline__ void translate_row(Shape& y, const Shape& x, uint32_t row, float sign, float o) {
+  const float v = __fmul_rn(sign, o);  // exact: sign is +-1
 #pragma unroll
   for (uint32_t i = 0; i < 3; i++) y.t[i] = (i == row) ? __fadd_rn(v, x.t[i]) : x.t[i];
+}
+__device__ __forceinline__ void translate_axis(Shape& y, const Shape& x, uint32_t ax, float o) {
+  translate_row(y, x, frame_row(x.frame, ax), frame_neg(x.frame, ax) ? -1.0f : 1.0f, o);
 }
 
 // ------------------------------------------------- 1 -> 1 chain resolution
@@ -219,6 +221,10 @@ __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& 
         continue;
       }
       case PGA_OP_GENERATE: {
+        if (r.flags & kRuleConstTerminal) {
+          tidx = r.nChildren;
+          return kTerm;
+        }
         if (r.nParams < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
         tidx = f2u(param(a, r, 0, x));
         if (tidx > 127u) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
@@ -241,6 +247,8 @@ struct Expander {
   Shape base;       // the executing shape
   DevRule r;
   uint32_t axis;
+  uint32_t axisRow;  // row of the split axis in the frame (Subdivide, Repeat)
+  float axisSign;    // its sign, +-1
   float offset;     // running offset along the axis
   float scale;
   uint32_t reps;
@@ -329,6 +337,8 @@ __device__ __forceinline__ uint32_t expander_init(const DeriveArgs& a, Expander&
       uint32_t n = dyn ? (r.nParams >= 1 ? r.nParams - 1u : 0u) : r.nChildren;
       if (r.nParams < n + 1 || r.nParams < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
       if (!axis_param(a, r, x, E.axis)) return 0;
+      E.axisRow = frame_row(x.frame, E.axis);
+      E.axisSign = frame_neg(x.frame, E.axis) ? -1.0f : 1.0f;
       float total = pick3(x.s, E.axis);
       E.offset = __fmul_rn(total, -0.5f);
       float absSum = 0.0f, relSum = 0.0f;
@@ -347,6 +357,8 @@ __device__ __forceinline__ uint32_t expander_init(const DeriveArgs& a, Expander&
       const RepeatSetup R = repeat_setup(a, r, x, true);
       if (!(R.flags & 1u)) return 0;
       E.axis = R.axis;
+      E.axisRow = frame_row(x.frame, R.axis);
+      E.axisSign = frame_neg(x.frame, R.axis) ? -1.0f : 1.0f;
       E.reps = R.reps;
       E.e2 = R.e2;
       const float e1 = R.e1, e3 = R.e3;
@@ -432,7 +444,7 @@ __device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E,
       int32_t nxt = succ_at(a, r.succBase + c);
       y = x;
       put3(y.s, E.axis, newSize);
-      translate_axis(y, x, E.axis, o);
+      translate_row(y, x, E.axisRow, E.axisSign, o);
       y.seed = seed_of(a, x.seed, c);
       y.entry = nxt;
       y.path = child_path(x.path, c, nxt);
@@ -465,7 +477,7 @@ __device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E,
       }
       y = x;
       put3(y.s, E.axis, size);
-      translate_axis(y, x, E.axis, o);
+      translate_row(y, x, E.axisRow, E.axisSign, o);
       y.seed = seed_of(a, x.seed, mod);
       y.entry = nxt;
       y.path = child_path(x.path, mod, nxt);
@@ -1291,6 +1303,13 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
       if (p.type == PGA_PT_SHAPE_ATTR && p.value[0] >= 15.0f && p.value[0] < 16.0f) e->useSeeds = true;
     }
     r.flags = pure ? kRulePure : 0;
+    // A scalar terminal index is decided here once (the device truncates it
+    // toward zero like __float2uint_rz; only 0..127 are valid mesh indices).
+    if (r.op == PGA_OP_GENERATE && en.numParameters >= 1 && en.parameters[0].type == PGA_PT_SCALAR &&
+        en.parameters[0].value[0] >= 0.0f && en.parameters[0].value[0] < 128.0f) {
+      r.flags |= kRuleConstTerminal;
+      r.nChildren = (uint16_t)(uint32_t)en.parameters[0].value[0];
+    }
     r.paramBase = (uint32_t)e->hParams.size();
     r.succBase = (uint32_t)e->hSucc.size();
     for (uint32_t k = 0; k < en.numParameters; k++) {

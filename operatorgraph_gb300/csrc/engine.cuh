@@ -49,6 +49,7 @@ struct __align__(16) DevRule {
   uint32_t succBase;   // into int32 successor entries
 };
 constexpr uint16_t kRulePure = 1;
+constexpr uint16_t kRuleConstTerminal = 2;  // Generate with a scalar terminal index, kept in nChildren
 
 struct DevTables {
   const DevRule* rules;
