@@ -119,6 +119,13 @@ typedef struct PgaTerminal {
   uint64_t path;         /* derivation-path hash */
 } PgaTerminal;
 
+/* PgaEngineConfig.flags.  By default a child whose rule is a Subdivide with
+ * shape-independent factors and only constant-index Generate or Discard
+ * successors is expanded by the thread that created it (its terminals written
+ * at once) instead of being queued as a work item; engines with recordTape = 1
+ * never do this.  PGA_FLAG_NO_INLINE turns it off. */
+#define PGA_FLAG_NO_INLINE 1u
+
 typedef struct PgaEngineConfig {
   uint64_t nodeCapacity;     /* non-terminal shapes held per derivation (queue storage) */
   uint64_t maxTerminals;     /* sizes the LBVH / adjoint scratch */
@@ -128,7 +135,7 @@ typedef struct PgaEngineConfig {
   uint32_t recordTape;       /* 1 = keep the derivation tape so pga_adjoint can run */
   uint32_t spinLimit;        /* iterations before a bounded wait gives up (0 = default) */
   uint32_t maxLevels;        /* derivation depth limit (0 = default 4096) */
-  uint32_t flags;            /* reserved, 0 */
+  uint32_t flags;            /* PGA_FLAG_* */
   uint32_t subItem;          /* children per queued work item, 1..64 (0 = default 8) */
   uint32_t itemsPerLane;     /* work items per lane in one warp chunk (0 = default 1) */
   uint32_t narrowSubItem;    /* children per work item queued while the level being expanded has fewer

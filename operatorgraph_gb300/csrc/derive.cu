@@ -324,6 +324,30 @@ __device__ __forceinline__ uint32_t count_children(const DeriveArgs& a, const Sh
   }
 }
 
+// Subdivide set-up shared by the work-item expander and the in-place leaf
+// expansion: axis, starting offset -size/2 and the scale of relative factors
+// (size - sum of absolute) / sum of relative; returns the child count, 0 on error.
+// Subdivide<DynParams>::execute (Subdivide.cuh:177-216) and the static form
+// Subdivide<Axis, Pair<DynParam<k+1>, DCall<k>>...> (Subdivide.cuh:139-156).
+__device__ __forceinline__ uint32_t subdivide_setup(const DeriveArgs& a, const DevRule& r, const Shape& x,
+                                                    uint32_t& axis, float& offset, float& scale) {
+  const bool dyn = r.op == PGA_OP_SUBDIVIDE;
+  uint32_t n = dyn ? (r.nParams >= 1 ? r.nParams - 1u : 0u) : r.nChildren;
+  if (r.nParams < n + 1 || r.nParams < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+  if (!axis_param(a, r, x, axis)) return 0;
+  float total = pick3(x.s, axis);
+  offset = __fmul_rn(total, -0.5f);
+  float absSum = 0.0f, relSum = 0.0f;
+  for (uint32_t i = 1; i <= n; i++) {
+    float f = param(a, r, i, x);
+    absSum = __fadd_rn(absSum, __fmul_rn((float)(f > 0.0f), f));
+    relSum = __fadd_rn(relSum, __fmul_rn((float)(f < 0.0f), __fmul_rn(f, -1.0f)));
+  }
+  scale = (relSum == 0.0f) ? 0.0f : __fdiv_rn(__fsub_rn(total, absSum), relSum);
+  if (dyn && scale < 0.0f) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
+  return n;
+}
+
 // Operator set-up; returns the number of child slots (0 on error).
 __device__ __forceinline__ uint32_t expander_init(const DeriveArgs& a, Expander& E) {
   const Shape& x = E.base;
@@ -331,24 +355,10 @@ __device__ __forceinline__ uint32_t expander_init(const DeriveArgs& a, Expander&
   switch (r.op) {
     case PGA_OP_SUBDIVIDE:
     case PGA_OP_SUBDIVIDE_STATIC: {
-      // Subdivide<DynParams>::execute (Subdivide.cuh:177-216) and the static
-      // form Subdivide<Axis, Pair<DynParam<k+1>, DCall<k>>...> (Subdivide.cuh:139-156).
-      const bool dyn = r.op == PGA_OP_SUBDIVIDE;
-      uint32_t n = dyn ? (r.nParams >= 1 ? r.nParams - 1u : 0u) : r.nChildren;
-      if (r.nParams < n + 1 || r.nParams < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
-      if (!axis_param(a, r, x, E.axis)) return 0;
+      const uint32_t n = subdivide_setup(a, r, x, E.axis, E.offset, E.scale);
+      if (n == 0) return 0;
       E.axisRow = frame_row(x.frame, E.axis);
       E.axisSign = frame_neg(x.frame, E.axis) ? -1.0f : 1.0f;
-      float total = pick3(x.s, E.axis);
-      E.offset = __fmul_rn(total, -0.5f);
-      float absSum = 0.0f, relSum = 0.0f;
-      for (uint32_t i = 1; i <= n; i++) {
-        float f = param(a, r, i, x);
-        absSum = __fadd_rn(absSum, __fmul_rn((float)(f > 0.0f), f));
-        relSum = __fadd_rn(relSum, __fmul_rn((float)(f < 0.0f), __fmul_rn(f, -1.0f)));
-      }
-      E.scale = (relSum == 0.0f) ? 0.0f : __fdiv_rn(__fsub_rn(total, absSum), relSum);
-      if (dyn && E.scale < 0.0f) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return 0; }
       E.prevSize = 0.0f;
       E.prevOff = 0.0f;
       return n;
@@ -750,6 +760,70 @@ __device__ __forceinline__ void emit_child(const DeriveArgs& a, WarpOut& w, int 
   emit_round<PAGED>(a, w, kind, y, tidx, nY, link, ordinal);
 }
 
+// In-place expansion of leaf children.  A leaf rule (flagged at engine
+// creation) is a Subdivide whose factors do not read the shape and whose
+// successors are all Generates with a constant terminal index or Discards, so
+// its children are known to end right away.  The lane that created such a
+// child emits the child's terminals itself instead of queuing a work item for
+// the next level: the same arithmetic (subdivide_setup, subdivide_size, the
+// running offset, translate_row, child seeds and path hashes) in a loop that
+// holds only the Subdivide's state.
+template <bool PAGED>
+__device__ __forceinline__ void emit_leaf(const DeriveArgs& a, WarpOut& w, bool leaf, const Shape& y, uint32_t link) {
+  DevRule r;
+  uint32_t n = 0, axis = 0, row = 0;
+  float sign = 1.0f, offset = 0.0f, scale = 0.0f;
+  if (leaf) {
+    r = rule_at(a, (uint32_t)y.entry);
+    n = subdivide_setup(a, r, y, axis, offset, scale);
+    row = frame_row(y.frame, axis);
+    sign = frame_neg(y.frame, axis) ? -1.0f : 1.0f;
+  }
+  for (uint32_t g = 0; __any_sync(kFull, g < n); g++) {
+    int kind = kNone;
+    Shape z;
+    uint32_t tidx = 0;
+    if (g < n) {
+      const float f = param(a, r, g + 1, y);
+      if (r.op == PGA_OP_SUBDIVIDE || f != 0.0f) {
+        const float newSize = subdivide_size(f, scale);
+        const float o = __fadd_rn(offset, __fmul_rn(newSize, 0.5f));
+        offset = __fadd_rn(offset, newSize);
+        const int32_t nxt = succ_at(a, r.succBase + g);
+        const DevRule sr = rule_at(a, (uint32_t)nxt);
+        if (sr.op == PGA_OP_GENERATE) {
+          z = y;
+          put3(z.s, axis, newSize);
+          translate_row(z, y, row, sign, o);
+          z.seed = seed_of(a, y.seed, g);
+          z.entry = nxt;
+          z.path = child_path(y.path, g, nxt);
+          tidx = sr.nChildren;
+          kind = kTerm;
+        }
+      }
+    }
+    emit_round<PAGED>(a, w, kind, z, tidx, 0u, link, g);
+  }
+}
+
+// Emits a lane's new child: with LEAF, leaf children in place and the others
+// as terminals or work items; without, everything as terminals or work items.
+// LEAF is a separate instantiation of the persistent kernel, launched only for
+// grammars that have leaf rules, so the others do not carry its registers.
+template <bool PAGED, bool LEAF>
+__device__ __forceinline__ void emit_new(const DeriveArgs& a, WarpOut& w, int kind, const Shape& y, uint32_t tidx,
+                                         uint32_t link, uint32_t ordinal) {
+  if (!LEAF) {
+    emit_child<PAGED>(a, w, kind, y, tidx, link, ordinal);
+    return;
+  }
+  bool leaf = false;
+  if (kind == kNode) leaf = (rule_at(a, (uint32_t)y.entry).flags & kRuleLeaf) != 0;
+  emit_child<PAGED>(a, w, leaf ? (int)kNone : kind, y, tidx, link, ordinal);
+  if (__any_sync(kFull, leaf)) emit_leaf<PAGED>(a, w, leaf, y, link);
+}
+
 // Root shape of axiom i, as Grid::...::generateAxiom builds it (Grid.cuh:199-204).
 __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Shape& x) {
   const PgaAxiom* ax = a.axioms + i;
@@ -764,7 +838,7 @@ __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Sha
 }
 
 // Expands the work items first + 32 k + lane (k < K, item < hi) of one warp.
-template <bool PAGED>
+template <bool PAGED, bool LEAF>
 __device__ __forceinline__ void warp_items(const DeriveArgs& a, WarpOut& w, unsigned long long first,
                                            unsigned long long hi, uint32_t K) {
   const unsigned lane = threadIdx.x & 31u;
@@ -800,13 +874,13 @@ __device__ __forceinline__ void warp_items(const DeriveArgs& a, WarpOut& w, unsi
       Shape y;
       uint32_t tidx = 0, ordinal = 0;
       if (c < n && expander_child(a, E, c0 + c, y, ordinal)) kind = resolve(a, y, tidx);
-      emit_child<PAGED>(a, w, kind, y, tidx, (uint32_t)item, ordinal);
+      emit_new<PAGED, LEAF>(a, w, kind, y, tidx, (uint32_t)item, ordinal);
     }
   }
 }
 
 // Seeds the axioms [first, first + count) with a warp-uniform grid-stride loop.
-template <bool PAGED>
+template <bool PAGED, bool LEAF>
 __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uint32_t count) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
@@ -821,19 +895,19 @@ __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uin
       axiom_shape(a, (uint32_t)i, y);
       kind = resolve(a, y, tidx);
     }
-    emit_child<PAGED>(a, w, kind, y, tidx, kAxiomLink | (uint32_t)i, 0u);
+    emit_new<PAGED, LEAF>(a, w, kind, y, tidx, kAxiomLink | (uint32_t)i, 0u);
   }
 }
 
 // All items of one level [lo, hi): warp chunks of 32 K items in a static
 // grid-stride order (no shared work counter).
-template <bool PAGED>
+template <bool PAGED, bool LEAF>
 __device__ __forceinline__ void expand_level(const DeriveArgs& a, WarpOut& w, unsigned long long lo,
                                              unsigned long long hi, uint32_t K) {
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
   const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
   for (unsigned long long b = lo + warpId * 32ull * K; b < hi; b += numWarps * 32ull * K)
-    warp_items<PAGED>(a, w, b, hi, K);
+    warp_items<PAGED, LEAF>(a, w, b, hi, K);
 }
 
 // Copies the rule table into shared memory when it fits (decided at engine
@@ -1098,6 +1172,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 #define PGA_PERSISTENT_MIN_BLOCKS 2
 #endif
 
+template <bool LEAF>
 __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   if (blockIdx.x == 0 && threadIdx.x == 0) a.st->clockStart = global_ns();
@@ -1105,7 +1180,7 @@ __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_
   WarpOut w;
   warpout_init(a, w);
   warpout_level(a, w, a.numAxioms);
-  seed_axioms<true>(a, w, 0, a.numAxioms);
+  seed_axioms<true, LEAF>(a, w, 0, a.numAxioms);
   close_node_page(a, w);
   if (!grid_barrier(a, [&] {
         volatile DevState* vs = a.st;
@@ -1119,7 +1194,7 @@ __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_
     if (vs->stop) break;
     const unsigned long long lo = vs->levelLo, hi = vs->levelHi;
     warpout_level(a, w, hi - lo);
-    expand_level<true>(a, w, lo, hi, a.itemsPerLane);
+    expand_level<true, LEAF>(a, w, lo, hi, a.itemsPerLane);
     close_node_page(a, w);
     if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
   }
@@ -1134,7 +1209,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_seed(DeriveArgs a, uint32_t fir
   setup_block(a, sm);
   WarpOut w;
   warpout_init(a, w);
-  seed_axioms<false>(a, w, first, count);
+  seed_axioms<false, false>(a, w, first, count);
 }
 
 __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsigned long long lo,
@@ -1143,7 +1218,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsi
   setup_block(a, sm);
   WarpOut w;
   warpout_init(a, w);
-  expand_level<false>(a, w, lo, hi, 1);
+  expand_level<false, false>(a, w, lo, hi, 1);
 }
 
 __global__ void k_write_count(const DevState* st, unsigned long long* out) { *out = st->termCount; }
@@ -1202,6 +1277,23 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
 }  // namespace pga
 
 using namespace pga;
+
+// Both instantiations of the persistent kernel get the same dynamic shared
+// memory limit; the launch uses the smaller of their occupancies, so either can
+// run co-resident.
+static cudaError_t set_persistent_smem(size_t bytes) {
+  cudaError_t err = cudaFuncSetAttribute(k_derive_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_derive_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return err;
+}
+static cudaError_t persistent_occupancy(int* perSM, int threads, size_t smem) {
+  int a = 0, b = 0;
+  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_derive_persistent<false>, threads, smem);
+  if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_derive_persistent<true>, threads, smem);
+  *perSM = std::min(a, b);
+  return err;
+}
 
 static const PgaProc kDefaultProcs[14] = {
     {PGA_OP_SUBDIVIDE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SUBDIVIDE, PGA_SHAPE_QUAD, 0, 1},
@@ -1328,6 +1420,29 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     for (uint32_t k = 0; k < en.numSuccessors; k++) e->hSucc.push_back(en.successors[k].entryIndex);
     e->hRules.push_back(r);
   }
+  // Leaf rules: a Subdivide with shape-independent factors whose every child
+  // successor is a Generate with a constant terminal index or a Discard, both
+  // of the Subdivide's own shape (children keep the parent's shape kind).
+  for (DevRule& r : e->hRules) {
+    if ((r.op != PGA_OP_SUBDIVIDE && r.op != PGA_OP_SUBDIVIDE_STATIC) || !(r.flags & kRulePure)) continue;
+    const uint32_t n = r.op == PGA_OP_SUBDIVIDE ? (r.nParams >= 1 ? r.nParams - 1u : 0u) : r.nChildren;
+    if (n == 0 || n > r.nSucc || r.nParams < n + 1) continue;
+    bool leaf = true;
+    for (uint32_t k = 0; k < n && leaf; k++) {
+      const int32_t s = e->hSucc[r.succBase + k];
+      if (s < 0 || (size_t)s >= e->hRules.size()) {
+        leaf = false;
+        break;
+      }
+      const DevRule& sr = e->hRules[(size_t)s];
+      leaf = sr.shape == r.shape &&
+             ((sr.op == PGA_OP_GENERATE && (sr.flags & kRuleConstTerminal)) || sr.op == PGA_OP_DISCARD);
+    }
+    if (leaf) r.flags |= kRuleLeaf;
+    // Leaf children are expanded in place, except with a tape (the adjoint
+    // replays one work item per branching shape) or when disabled.
+    if (leaf && !c.recordTape && !(c.flags & PGA_FLAG_NO_INLINE)) e->leafKernel = true;
+  }
   if (e->hParams.empty()) e->hParams.push_back(DevParam{0, 0.f, 0.f, 0});
   if (e->hSucc.empty()) e->hSucc.push_back(-1);
   if (e->hExpPool.empty()) e->hExpPool.push_back(0.f);
@@ -1382,14 +1497,14 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   err = cudaGetDevice(&e->device);
   if (err == cudaSuccess) err = cudaDeviceGetAttribute(&e->numSMs, cudaDevAttrMultiProcessorCount, e->device);
   if (err == cudaSuccess)
-    err = cudaFuncSetAttribute(k_derive_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
+    err = set_persistent_smem(e->smemBytes);
   if (err == cudaSuccess)
     err = cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
   if (err == cudaSuccess)
     err = cudaFuncSetAttribute(k_expand_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
   int perSM = 0;
   if (err == cudaSuccess)
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_derive_persistent, e->threads, e->smemBytes);
+    err = persistent_occupancy(&perSM, e->threads, e->smemBytes);
   if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create occupancy"));
   if (c.blocksPerSM > 0 && (int)c.blocksPerSM < perSM) perSM = (int)c.blocksPerSM;
   if (perSM < 1) perSM = 1;
@@ -1399,14 +1514,14 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     const size_t need = compact_smem_bytes((uint32_t)(perSM * e->numSMs * (e->threads / 32)));
     if (need > e->smemBytes) {
       e->smemBytes = (need + 15) & ~size_t(15);
-      err = cudaFuncSetAttribute(k_derive_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
+      err = set_persistent_smem(e->smemBytes);
       if (err == cudaSuccess)
         err = cudaFuncSetAttribute(k_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
       if (err == cudaSuccess)
         err = cudaFuncSetAttribute(k_expand_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes);
       int again = 0;
       if (err == cudaSuccess)
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&again, k_derive_persistent, e->threads, e->smemBytes);
+        err = persistent_occupancy(&again, e->threads, e->smemBytes);
       if (err != cudaSuccess) return fail(cuda_status(err, "pga_engine_create occupancy"));
       perSM = std::max(1, std::min(perSM, again));  // fewer warps need fewer bytes
     }
@@ -1454,7 +1569,8 @@ PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, 
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, (const void*)k_derive_persistent, args));
+  const void* kernel = e->leafKernel ? (const void*)k_derive_persistent<true> : (const void*)k_derive_persistent<false>;
+  PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, kernel, args));
   e->lastAxioms = dAxioms;
   e->lastNumAxioms = numAxioms;
   e->lastBlocks = dParamBlocks;

@@ -50,6 +50,7 @@ struct __align__(16) DevRule {
 };
 constexpr uint16_t kRulePure = 1;
 constexpr uint16_t kRuleConstTerminal = 2;  // Generate with a scalar terminal index, kept in nChildren
+constexpr uint16_t kRuleLeaf = 4;           // Subdivide whose children all end at once (expanded in place)
 
 struct DevTables {
   const DevRule* rules;
@@ -105,7 +106,8 @@ struct DeriveArgs {
   uint32_t subItem;     // children per queued item (1..8)
   uint32_t useSeeds;    // 0: no parameter of the grammar reads a seed, skip seed updates
   uint32_t itemsPerLane;
-  uint32_t narrowSubItem;  // work items per lane in one warp chunk
+  uint32_t narrowSubItem;
+  uint32_t inlineLeaves;      // expand kRuleLeaf children in the lane that creates them  // work items per lane in one warp chunk
   PgaTerminal* tail;      // terminal slots at or beyond `cap` (pages straddling the end of the output)
   uint2* tailLinks;
   unsigned long long tailCap;

@@ -62,6 +62,7 @@ struct PgaEngine {
   const float* lastBlocks = nullptr;
   PgaTerminal* lastOut = nullptr;
   unsigned long long lastCap = 0;
+  bool leafKernel = false;  // launch the instantiation that expands leaf children in place
   bool lastWasBatched = false;
 };
 

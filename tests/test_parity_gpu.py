@@ -77,16 +77,19 @@ def _load(path):
     return b, z
 
 
-@pytest.mark.parametrize("plain", [False, True], ids=["persistent", "plain"])
+@pytest.mark.parametrize("form", ["persistent", "queued", "plain"])
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
-def test_golden_case(path, plain):
+def test_golden_case(path, form):
+    """persistent: the batched launch (leaf children expanded in place);
+    queued: the same with every branching child queued (PGA_FLAG_NO_INLINE);
+    plain: one axiom and one launch per level."""
     import sys
 
     sys.path.insert(0, os.path.join(HERE, "golden"))
     import cases
 
     b, z = _load(path)
-    eng, out, got, rep = _run(b, plain=plain)
+    eng, out, got, rep = _run(b, plain=form == "plain", no_inline=form == "queued")
     assert rep["status"] == 0
     n_base = len(b["entries"]) if b["blocks"] is not None else None
     canon = cases.canonical(got, n_base)
@@ -97,8 +100,10 @@ def test_golden_case(path, plain):
     eng.release()
 
 
-@pytest.mark.parametrize("name", ["menger_d5", "city_4096", "facades_1024", "random_16"])
+@pytest.mark.parametrize("name", ["menger_d5", "city_4096", "facades_1024", "random_16", "city_4096_queued"])
 def test_full_size_bit_exact(name):
+    kw = {"no_inline": True} if name.endswith("_queued") else {}
+    name = name.replace("_queued", "")
     if name == "menger_d5":
         b = scenes.menger(0.005)
     elif name == "city_4096":
@@ -113,7 +118,7 @@ def test_full_size_bit_exact(name):
         ax["entry"] = [offs[i % 16] for i in range(64)]
         b = {"entries": entries, "axioms": ax, "blocks": None, "block_stride": 0}
     ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"], b["blocks"], b["block_stride"])
-    eng, out, got, rep = _run(b, capacity=len(ref), node_capacity=1 << 23, max_terminals=1 << 23)
+    eng, out, got, rep = _run(b, capacity=len(ref), node_capacity=1 << 23, max_terminals=1 << 23, **kw)
     assert rep["status"] == 0
     _assert_same(got, ref)
     eng.release()
