@@ -1319,8 +1319,8 @@ const PgaProc* pga_default_procs(uint32_t* numProcs) {
 static void free_engine(PgaEngine* e) {
   void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dLevelClock,
                   e->dTail, e->dTailLinks, e->dScratch,
-                  e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA, e->dKeysB,
-                  e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dNodeGrad, e->dAxiomGrad};
+                  e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA,
+                  e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dLeafAabbSorted, e->dNodeGrad, e->dAxiomGrad};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete e;
@@ -1474,7 +1474,8 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   e->sortTempBytes = pga_lbvh_temp_bytes(c.maxTerminals);
   ALLOC(e->dSortTemp, e->sortTempBytes);
   ALLOC(e->dKeysA, c.maxTerminals * sizeof(unsigned long long));
-  ALLOC(e->dKeysB, c.maxTerminals * sizeof(unsigned long long));
+  ALLOC(e->dLeafAabb, c.maxTerminals * 6 * sizeof(float));
+  ALLOC(e->dLeafAabbSorted, c.maxTerminals * 6 * sizeof(float));
   ALLOC(e->dValsA, c.maxTerminals * sizeof(uint32_t));
   ALLOC(e->dValsB, c.maxTerminals * sizeof(uint32_t));
   ALLOC(e->dArrival, c.maxTerminals * sizeof(uint32_t));

@@ -46,11 +46,11 @@ struct PgaEngine {
   void* dSortTemp = nullptr;
   size_t sortTempBytes = 0;
   unsigned long long* dKeysA = nullptr;
-  unsigned long long* dKeysB = nullptr;
   uint32_t* dValsA = nullptr;
   uint32_t* dValsB = nullptr;
   uint32_t* dArrival = nullptr;
-  float* dLeafAabb = nullptr;
+  float* dLeafAabb = nullptr;        // LBVH leaf boxes in terminal order
+  float* dLeafAabbSorted = nullptr;  // the same in sorted (leaf) order
 
   // Adjoint scratch: per-node gradient of (translation, size).
   float* dNodeGrad = nullptr;

@@ -37,16 +37,45 @@ struct Bounds {
   float sz[3];
 };
 
+// Leaf AABB: corners of the terminal box (8) or quad (4), as
+// BoundingVolumeConstructor<AABB>::construct (BoundingVolumeConstructor.cuh:22-76)
+// with the scale folded into the terminal matrix.
+__device__ __forceinline__ void leaf_aabb(const float4 r[3], bool quad, float mn[3], float mx[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) { mn[k] = FLT_MAX; mx[k] = -FLT_MAX; }
+  for (int cz = 0; cz < (quad ? 1 : 2); cz++)
+#pragma unroll
+    for (int cy = 0; cy < 2; cy++)
+#pragma unroll
+      for (int cx = 0; cx < 2; cx++) {
+        float x = cx ? 0.5f : -0.5f, y = cy ? 0.5f : -0.5f, z = quad ? 0.0f : (cz ? 0.5f : -0.5f);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          float v = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r[k].x, x), __fmul_rn(r[k].y, y)), __fmul_rn(r[k].z, z)), r[k].w);
+          mn[k] = fminf(mn[k], v);
+          mx[k] = fmaxf(mx[k], v);
+        }
+      }
+}
+
 // generateMortonCodes (GPUBVHConstructor.cuh:66-86) on terminal centres.
+// Also writes each terminal's AABB (6 floats, terminal order) while its record
+// is in registers.
 __global__ void __launch_bounds__(kLbvhThreads) k_morton(const PgaTerminal* __restrict__ t, unsigned long long n,
                                                          Bounds b, unsigned long long* __restrict__ keys,
-                                                         uint32_t* __restrict__ vals) {
+                                                         uint32_t* __restrict__ vals, float* __restrict__ leafBox) {
   unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4* p = reinterpret_cast<const float4*>(t + i);
-  float4 r0 = __ldg(p + 0), r1 = __ldg(p + 1), r2 = __ldg(p + 2);
+  float4 r[3] = {__ldg(p + 0), __ldg(p + 1), __ldg(p + 2)};
   uint4 meta = __ldg(reinterpret_cast<const uint4*>(p + 3));
-  float c[3] = {r0.w, r1.w, r2.w};
+  float mn[3], mx[3];
+  leaf_aabb(r, (meta.x >> 31) != 0, mn, mx);
+  float2* lb = reinterpret_cast<float2*>(leafBox + i * 6);
+  lb[0] = make_float2(mn[0], mn[1]);
+  lb[1] = make_float2(mn[2], mx[0]);
+  lb[2] = make_float2(mx[1], mx[2]);
+  float c[3] = {r[0].w, r[1].w, r[2].w};
   uint32_t code = 0;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
@@ -63,15 +92,23 @@ __device__ __forceinline__ uint64_t term_path(const PgaTerminal* t, uint32_t i) 
   return ((uint64_t)v.y << 32) | v.x;
 }
 
-// Orders runs of equal keys by the full path hash (then terminal index).
-__global__ void k_fix_ties(const unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
+// The radix sort orders the keys' top bits [kSortLowBit, 64) only (the Morton
+// code and the path hash's top 10 bits), which leaves runs of equal top bits
+// in input order.  Each such run -- rare and short, since its members share a
+// Morton cell and 10 hash bits -- is ordered here by the full path hash, then
+// terminal index, and its keys are rewritten to match.  The result is the
+// order a full 64-bit sort plus tie fix gives: lexicographic in (Morton code,
+// path hash, terminal).
+constexpr int kSortLowBit = 24;  // 5 radix passes of 8 bits instead of 8
+
+__global__ void k_fix_ties(unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
                            const PgaTerminal* __restrict__ t, unsigned long long n) {
   unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i + 1 >= n) return;
-  unsigned long long k = keys[i];
-  if (keys[i + 1] != k || (i > 0 && keys[i - 1] == k)) return;
+  const unsigned long long k = keys[i] >> kSortLowBit;
+  if ((keys[i + 1] >> kSortLowBit) != k || (i > 0 && (keys[i - 1] >> kSortLowBit) == k)) return;
   unsigned long long j = i + 1;
-  while (j < n && keys[j] == k) j++;
+  while (j < n && (keys[j] >> kSortLowBit) == k) j++;
   for (unsigned long long a = i + 1; a < j; a++) {
     uint32_t v = vals[a];
     uint64_t pv = term_path(t, v);
@@ -85,6 +122,8 @@ __global__ void k_fix_ties(const unsigned long long* __restrict__ keys, uint32_t
     }
     vals[b] = v;
   }
+  const unsigned long long morton = (keys[i] >> 34) << 34;
+  for (unsigned long long a = i; a < j; a++) keys[a] = morton | (term_path(t, vals[a]) >> 30);
 }
 
 __device__ __forceinline__ unsigned long long karras_code(const unsigned long long* keys, long long j) {
@@ -93,11 +132,24 @@ __device__ __forceinline__ unsigned long long karras_code(const unsigned long lo
 
 // buildRadixTree (GPUBVHConstructor.cuh:88-213), one thread per internal node,
 // with bounds checks on every probe.
+// Also gathers the leaf boxes into sorted order (one independent load per
+// leaf here instead of a dependent one inside the refit's climb).
 __global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long long* __restrict__ keys, long long n,
                                                          int32_t* __restrict__ nodes, uint32_t* __restrict__ leafParents,
-                                                         uint32_t* __restrict__ sortedVals, const uint32_t* __restrict__ vals) {
+                                                         uint32_t* __restrict__ sortedVals, const uint32_t* __restrict__ vals,
+                                                         const float* __restrict__ leafBox,
+                                                         float* __restrict__ sortedBox) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) sortedVals[i] = vals[i];
+  if (i < n) {
+    const uint32_t v = vals[i];
+    sortedVals[i] = v;
+    const float2* src = reinterpret_cast<const float2*>(leafBox + (size_t)v * 6);
+    float2* dst = reinterpret_cast<float2*>(sortedBox + (size_t)i * 6);
+    const float2 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
+    dst[0] = a;
+    dst[1] = b;
+    dst[2] = c;
+  }
   if (i >= n - 1) return;
   const unsigned long long ci = karras_code(keys, i);
   auto delta = [&](long long j) -> int { return __clzll(ci ^ karras_code(keys, j)); };
@@ -140,63 +192,61 @@ __global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long lon
   if (i == 0) nodes[0] = -1;
 }
 
-// Leaf AABB: corners of the terminal box (8) or quad (4), as
-// BoundingVolumeConstructor<AABB>::construct (BoundingVolumeConstructor.cuh:22-76)
-// with the scale folded into the terminal matrix.
-__device__ __forceinline__ void leaf_aabb(const PgaTerminal* t, uint32_t idx, float mn[3], float mx[3]) {
-  const float4* p = reinterpret_cast<const float4*>(t + idx);
-  float4 r[3] = {__ldg(p + 0), __ldg(p + 1), __ldg(p + 2)};
-  uint32_t rule = __ldg(reinterpret_cast<const uint32_t*>(p + 3));
-  bool quad = (rule >> 31) != 0;
-#pragma unroll
-  for (int k = 0; k < 3; k++) { mn[k] = FLT_MAX; mx[k] = -FLT_MAX; }
-  for (int cz = 0; cz < (quad ? 1 : 2); cz++)
-#pragma unroll
-    for (int cy = 0; cy < 2; cy++)
-#pragma unroll
-      for (int cx = 0; cx < 2; cx++) {
-        float x = cx ? 0.5f : -0.5f, y = cy ? 0.5f : -0.5f, z = quad ? 0.0f : (cz ? 0.5f : -0.5f);
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          float v = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r[k].x, x), __fmul_rn(r[k].y, y)), __fmul_rn(r[k].z, z)), r[k].w);
-          mn[k] = fminf(mn[k], v);
-          mx[k] = fmaxf(mx[k], v);
-        }
-      }
+// Arrival counter bump with acquire-release order at GPU scope: the climber
+// that stops at a node has published its child's AABB (release), the one that
+// goes on sees it (acquire).  One atomic per step and no separate fences.
+__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t* p) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
 }
 
-// propagateBVH (GPUBVHConstructor.cuh:215-261): the second thread to reach a
-// node merges its children and climbs on.
-__global__ void __launch_bounds__(kLbvhThreads) k_refit(const PgaTerminal* __restrict__ t, long long n,
+__device__ __forceinline__ void load_box(const float* p, float mn[3], float mx[3]) {
+  const float2* q = reinterpret_cast<const float2*>(p);
+  const float2 a = __ldcg(q), b = __ldcg(q + 1), c = __ldcg(q + 2);
+  mn[0] = a.x; mn[1] = a.y; mn[2] = b.x; mx[0] = b.y; mx[1] = c.x; mx[2] = c.y;
+}
+
+// propagateBVH (GPUBVHConstructor.cuh:215-261): one thread per leaf climbs;
+// the second thread to reach a node merges its children and goes on.  The
+// climber keeps the box of the child it comes from in registers and reads
+// only the sibling's (a leaf's from the sorted leaf boxes, an internal node's
+// from aabbs); the union is min/max(left, right) in that order.  A node's
+// links and a leaf sibling's box are fixed before this kernel, so they are
+// read ahead of the arrival atomic.
+__global__ void __launch_bounds__(kLbvhThreads) k_refit(const float* __restrict__ sortedBox, long long n,
                                                         const int32_t* __restrict__ nodes,
                                                         const uint32_t* __restrict__ leafParents,
-                                                        const uint32_t* __restrict__ sortedVals,
                                                         uint32_t* __restrict__ arrival, float* __restrict__ aabbs) {
   long long leaf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (leaf >= n) return;
+  float mn[3], mx[3];
+  load_box(sortedBox + (size_t)leaf * 6, mn, mx);
   long long cur = leafParents[leaf];
+  int32_t from = (int32_t)leaf;  // child id as the node table stores it: leaf j -> j, internal k -> -k
   for (long long guard = 0; guard < n; guard++) {
-    __threadfence();
-    if (atomicAdd(&arrival[cur], 1u) == 0) return;
-    __threadfence();
-    int32_t l = __ldcg(&nodes[cur * 3 + 1]), r = __ldcg(&nodes[cur * 3 + 2]);
-    float amn[3], amx[3], bmn[3], bmx[3];
-    if (l < 0) {
-      for (int k = 0; k < 3; k++) { amn[k] = __ldcg(&aabbs[(long long)(-l) * 6 + k]); amx[k] = __ldcg(&aabbs[(long long)(-l) * 6 + 3 + k]); }
-    } else {
-      leaf_aabb(t, sortedVals[l], amn, amx);
-    }
-    if (r < 0) {
-      for (int k = 0; k < 3; k++) { bmn[k] = __ldcg(&aabbs[(long long)(-r) * 6 + k]); bmx[k] = __ldcg(&aabbs[(long long)(-r) * 6 + 3 + k]); }
-    } else {
-      leaf_aabb(t, sortedVals[r], bmn, bmx);
-    }
+    const int32_t l = __ldg(&nodes[cur * 3 + 1]), r = __ldg(&nodes[cur * 3 + 2]);
+    const int32_t parent = __ldg(&nodes[cur * 3 + 0]);
+    const bool fromLeft = l == from;
+    const int32_t sib = fromLeft ? r : l;
+    float smn[3], smx[3];
+    if (sib >= 0) load_box(sortedBox + (size_t)sib * 6, smn, smx);
+    if (arrive_acq_rel(&arrival[cur]) == 0) return;
+    if (sib < 0) load_box(aabbs + (size_t)(-(long long)sib) * 6, smn, smx);
+#pragma unroll
     for (int k = 0; k < 3; k++) {
-      __stcg(&aabbs[cur * 6 + k], fminf(amn[k], bmn[k]));
-      __stcg(&aabbs[cur * 6 + 3 + k], fmaxf(amx[k], bmx[k]));
+      const float lmn = fromLeft ? mn[k] : smn[k], rmn = fromLeft ? smn[k] : mn[k];
+      const float lmx = fromLeft ? mx[k] : smx[k], rmx = fromLeft ? smx[k] : mx[k];
+      mn[k] = fminf(lmn, rmn);
+      mx[k] = fmaxf(lmx, rmx);
     }
+    float2* o = reinterpret_cast<float2*>(aabbs + (size_t)cur * 6);
+    __stcg(o + 0, make_float2(mn[0], mn[1]));
+    __stcg(o + 1, make_float2(mn[2], mx[0]));
+    __stcg(o + 2, make_float2(mx[1], mx[2]));
     if (cur == 0) return;
-    cur = __ldcg(&nodes[cur * 3 + 0]);
+    from = -(int32_t)cur;
+    cur = parent;
     if (cur < 0) return;
   }
 }
@@ -230,19 +280,20 @@ extern "C" PgaStatus pga_lbvh_build(PgaEngine* e, const PgaTerminal* dTerminals,
     b.sz[k] = bounds->max[k] - bounds->min[k];
   }
   unsigned blocks = (unsigned)((n + kLbvhThreads - 1) / kLbvhThreads);
-  k_morton<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, n, b, e->dKeysA, e->dValsA);
+  k_morton<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, n, b, e->dKeysA, e->dValsA, e->dLeafAabb);
   PGA_CUDA_TRY(cudaGetLastError());
   size_t temp = e->sortTempBytes;
   PGA_CUDA_TRY(cub::DeviceRadixSort::SortPairs(e->dSortTemp, temp, e->dKeysA, (unsigned long long*)out->keys,
-                                               e->dValsA, e->dValsB, (int64_t)n, 0, 64, s));
-  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, e->dValsB, dTerminals, n);
+                                               e->dValsA, e->dValsB, (int64_t)n, kSortLowBit, 64, s));
+  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>((unsigned long long*)out->keys, e->dValsB, dTerminals, n);
   PGA_CUDA_TRY(cudaGetLastError());
   k_karras<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, (long long)n, out->nodes,
-                                           out->leafParents, out->leafTerminal, e->dValsB);
+                                           out->leafParents, out->leafTerminal, e->dValsB, e->dLeafAabb,
+                                           e->dLeafAabbSorted);
   PGA_CUDA_TRY(cudaGetLastError());
   PGA_CUDA_TRY(cudaMemsetAsync(e->dArrival, 0, (n - 1) * sizeof(uint32_t), s));
-  k_refit<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, (long long)n, out->nodes, out->leafParents, out->leafTerminal,
-                                          e->dArrival, out->aabbs);
+  k_refit<<<blocks, kLbvhThreads, 0, s>>>(e->dLeafAabbSorted, (long long)n, out->nodes, out->leafParents, e->dArrival,
+                                          out->aabbs);
   PGA_CUDA_TRY(cudaGetLastError());
   return PGA_OK;
 }
@@ -308,7 +359,8 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
     }
     base = static_cast<unsigned char*>(g_staticAddr[dev]);
   }
-  // Carve the scratch: keys, two value arrays, arrival counters, sort temp.
+  // Carve the scratch: keys, two value arrays, arrival counters, leaf boxes
+  // (terminal and sorted order), sort temp.
   size_t temp = pga_lbvh_temp_bytes(n);
   size_t off = 0;
   unsigned long long* keysA = reinterpret_cast<unsigned long long*>(base + off);
@@ -319,6 +371,10 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
   off += align256(n * sizeof(uint32_t));
   uint32_t* arrival = reinterpret_cast<uint32_t*>(base + off);
   off += align256(n * sizeof(uint32_t));
+  float* leafBox = reinterpret_cast<float*>(base + off);
+  off += align256(n * 6 * sizeof(float));
+  float* sortedBox = reinterpret_cast<float*>(base + off);
+  off += align256(n * 6 * sizeof(float));
   void* sortTemp = base + off;
   off += align256(temp);
   if (off > kStaticScratchBytes) {
@@ -332,18 +388,17 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
     b.sz[k] = bounds->max[k] - bounds->min[k];
   }
   const unsigned blocks = (unsigned)((n + kLbvhThreads - 1) / kLbvhThreads);
-  k_morton<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, n, b, keysA, valsA);
+  k_morton<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, n, b, keysA, valsA, leafBox);
   PGA_CUDA_TRY(cudaGetLastError());
   PGA_CUDA_TRY(cub::DeviceRadixSort::SortPairs(sortTemp, temp, keysA, (unsigned long long*)out->keys, valsA, valsB,
-                                               (int64_t)n, 0, 64, s));
-  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, valsB, dTerminals, n);
+                                               (int64_t)n, kSortLowBit, 64, s));
+  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>((unsigned long long*)out->keys, valsB, dTerminals, n);
   PGA_CUDA_TRY(cudaGetLastError());
   k_karras<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, (long long)n, out->nodes,
-                                           out->leafParents, out->leafTerminal, valsB);
+                                           out->leafParents, out->leafTerminal, valsB, leafBox, sortedBox);
   PGA_CUDA_TRY(cudaGetLastError());
   PGA_CUDA_TRY(cudaMemsetAsync(arrival, 0, (n - 1) * sizeof(uint32_t), s));
-  k_refit<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, (long long)n, out->nodes, out->leafParents, out->leafTerminal,
-                                          arrival, out->aabbs);
+  k_refit<<<blocks, kLbvhThreads, 0, s>>>(sortedBox, (long long)n, out->nodes, out->leafParents, arrival, out->aabbs);
   PGA_CUDA_TRY(cudaGetLastError());
   return PGA_OK;
 }
