@@ -51,6 +51,7 @@ struct PgaEngine {
   uint32_t* dArrival = nullptr;
   float* dLeafAabb = nullptr;        // LBVH leaf boxes in terminal order
   float* dLeafAabbSorted = nullptr;  // the same in sorted (leaf) order
+  int2* dNodeRange = nullptr;        // LBVH internal node leaf ranges [lo, hi]
 
   // Adjoint scratch: per-node gradient of (translation, size).
   float* dNodeGrad = nullptr;

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long lon
                                                          int32_t* __restrict__ nodes, uint32_t* __restrict__ leafParents,
                                                          uint32_t* __restrict__ sortedVals, const uint32_t* __restrict__ vals,
                                                          const float* __restrict__ leafBox,
-                                                         float* __restrict__ sortedBox) {
+                                                         float* __restrict__ sortedBox, int2* __restrict__ nodeRange) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     const uint32_t v = vals[i];
@@ -190,14 +190,36 @@ __global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long lon
   if (right < 0) nodes[(-right) * 3 + 0] = (int32_t)i;
   else leafParents[right] = (uint32_t)i;
   if (i == 0) nodes[0] = -1;
+  nodeRange[i] = make_int2((int)min(i, j), (int)max(i, j));
 }
 
-// Arrival counter bump with acquire-release order at GPU scope: the climber
-// that stops at a node has published its child's AABB (release), the one that
-// goes on sees it (acquire).  One atomic per step and no separate fences.
-__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t* p) {
+// Arrival counter bump at GPU scope with only the ordering the step needs.
+// A climber publishes a box through memory only when it comes from an
+// internal node (it stored that node's box itself): release.  A climber that
+// goes on reads its sibling's box through memory only when the sibling is an
+// internal node (stored by another thread): acquire.  Leaf boxes come from an
+// earlier kernel and need neither, so a step between two leaves is relaxed.
+__device__ __forceinline__ uint32_t arrive(uint32_t* p, bool release, bool acquire) {
   uint32_t old;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  if (release && acquire)
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  else if (release)
+    asm volatile("atom.release.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  else if (acquire)
+    asm volatile("atom.acquire.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  else
+    asm volatile("atom.relaxed.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
+// The same for a node whose two climbers are threads of one block: the
+// counter and the boxes live in shared memory, ordered at block scope.
+__device__ __forceinline__ uint32_t arrive_block(uint32_t* p) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], 1;"
+               : "=r"(old)
+               : "r"((uint32_t)__cvta_generic_to_shared(p))
+               : "memory");
   return old;
 }
 
@@ -210,15 +232,28 @@ __device__ __forceinline__ void load_box(const float* p, float mn[3], float mx[3
 // propagateBVH (GPUBVHConstructor.cuh:215-261): one thread per leaf climbs;
 // the second thread to reach a node merges its children and goes on.  The
 // climber keeps the box of the child it comes from in registers and reads
-// only the sibling's (a leaf's from the sorted leaf boxes, an internal node's
-// from aabbs); the union is min/max(left, right) in that order.  A node's
-// links and a leaf sibling's box are fixed before this kernel, so they are
-// read ahead of the arrival atomic.
+// only the sibling's; the union is min/max(left, right) in that order.
+//
+// Thread j handles sorted leaf j, so a block holds leaves [B, B + 256).  A node
+// whose leaf range lies inside that span is reached only by threads of the
+// block: its arrival counter and box sit in shared memory (index node - B;
+// a Karras node's index is one end of its range) with block-scope ordering.
+// Only nodes whose range crosses a block boundary -- a few percent -- use
+// global counters at GPU scope (`arrive`).  Every node's box is also stored
+// to aabbs, the output.  A node's links, its range and a leaf sibling's box
+// are fixed before this kernel, so they are read ahead of the arrival.
 __global__ void __launch_bounds__(kLbvhThreads) k_refit(const float* __restrict__ sortedBox, long long n,
                                                         const int32_t* __restrict__ nodes,
+                                                        const int2* __restrict__ nodeRange,
                                                         const uint32_t* __restrict__ leafParents,
                                                         uint32_t* __restrict__ arrival, float* __restrict__ aabbs) {
-  long long leaf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ uint32_t blockArrive[kLbvhThreads];
+  __shared__ float blockBox[kLbvhThreads * 6];
+  blockArrive[threadIdx.x] = 0u;
+  __syncthreads();
+  const long long B = (long long)blockIdx.x * kLbvhThreads;
+  const long long E = min(B + kLbvhThreads, n);
+  long long leaf = B + threadIdx.x;
   if (leaf >= n) return;
   float mn[3], mx[3];
   load_box(sortedBox + (size_t)leaf * 6, mn, mx);
@@ -227,12 +262,22 @@ __global__ void __launch_bounds__(kLbvhThreads) k_refit(const float* __restrict_
   for (long long guard = 0; guard < n; guard++) {
     const int32_t l = __ldg(&nodes[cur * 3 + 1]), r = __ldg(&nodes[cur * 3 + 2]);
     const int32_t parent = __ldg(&nodes[cur * 3 + 0]);
+    const int2 range = __ldg(&nodeRange[cur]);
+    const bool local = range.x >= B && range.y < E;  // then B <= cur < E
     const bool fromLeft = l == from;
     const int32_t sib = fromLeft ? r : l;
     float smn[3], smx[3];
     if (sib >= 0) load_box(sortedBox + (size_t)sib * 6, smn, smx);
-    if (arrive_acq_rel(&arrival[cur]) == 0) return;
-    if (sib < 0) load_box(aabbs + (size_t)(-(long long)sib) * 6, smn, smx);
+    if (local) {
+      if (arrive_block(&blockArrive[cur - B]) == 0) return;
+      if (sib < 0) {  // an internal sibling of a local node is local too
+        const float* q = &blockBox[(-(long long)sib - B) * 6];
+        smn[0] = q[0]; smn[1] = q[1]; smn[2] = q[2]; smx[0] = q[3]; smx[1] = q[4]; smx[2] = q[5];
+      }
+    } else {
+      if (arrive(&arrival[cur], from < 0, sib < 0) == 0) return;
+      if (sib < 0) load_box(aabbs + (size_t)(-(long long)sib) * 6, smn, smx);
+    }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       const float lmn = fromLeft ? mn[k] : smn[k], rmn = fromLeft ? smn[k] : mn[k];
@@ -244,6 +289,10 @@ __global__ void __launch_bounds__(kLbvhThreads) k_refit(const float* __restrict_
     __stcg(o + 0, make_float2(mn[0], mn[1]));
     __stcg(o + 1, make_float2(mn[2], mx[0]));
     __stcg(o + 2, make_float2(mx[1], mx[2]));
+    if (local) {
+      float* q = &blockBox[(cur - B) * 6];
+      q[0] = mn[0]; q[1] = mn[1]; q[2] = mn[2]; q[3] = mx[0]; q[4] = mx[1]; q[5] = mx[2];
+    }
     if (cur == 0) return;
     from = -(int32_t)cur;
     cur = parent;
@@ -289,11 +338,11 @@ extern "C" PgaStatus pga_lbvh_build(PgaEngine* e, const PgaTerminal* dTerminals,
   PGA_CUDA_TRY(cudaGetLastError());
   k_karras<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, (long long)n, out->nodes,
                                            out->leafParents, out->leafTerminal, e->dValsB, e->dLeafAabb,
-                                           e->dLeafAabbSorted);
+                                           e->dLeafAabbSorted, e->dNodeRange);
   PGA_CUDA_TRY(cudaGetLastError());
   PGA_CUDA_TRY(cudaMemsetAsync(e->dArrival, 0, (n - 1) * sizeof(uint32_t), s));
-  k_refit<<<blocks, kLbvhThreads, 0, s>>>(e->dLeafAabbSorted, (long long)n, out->nodes, out->leafParents, e->dArrival,
-                                          out->aabbs);
+  k_refit<<<blocks, kLbvhThreads, 0, s>>>(e->dLeafAabbSorted, (long long)n, out->nodes, e->dNodeRange,
+                                          out->leafParents, e->dArrival, out->aabbs);
   PGA_CUDA_TRY(cudaGetLastError());
   return PGA_OK;
 }
@@ -360,7 +409,7 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
     base = static_cast<unsigned char*>(g_staticAddr[dev]);
   }
   // Carve the scratch: keys, two value arrays, arrival counters, leaf boxes
-  // (terminal and sorted order), sort temp.
+  // (terminal and sorted order), node ranges, sort temp.
   size_t temp = pga_lbvh_temp_bytes(n);
   size_t off = 0;
   unsigned long long* keysA = reinterpret_cast<unsigned long long*>(base + off);
@@ -375,6 +424,8 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
   off += align256(n * 6 * sizeof(float));
   float* sortedBox = reinterpret_cast<float*>(base + off);
   off += align256(n * 6 * sizeof(float));
+  int2* nodeRange = reinterpret_cast<int2*>(base + off);
+  off += align256(n * sizeof(int2));
   void* sortTemp = base + off;
   off += align256(temp);
   if (off > kStaticScratchBytes) {
@@ -395,10 +446,11 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
   k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>((unsigned long long*)out->keys, valsB, dTerminals, n);
   PGA_CUDA_TRY(cudaGetLastError());
   k_karras<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, (long long)n, out->nodes,
-                                           out->leafParents, out->leafTerminal, valsB, leafBox, sortedBox);
+                                           out->leafParents, out->leafTerminal, valsB, leafBox, sortedBox, nodeRange);
   PGA_CUDA_TRY(cudaGetLastError());
   PGA_CUDA_TRY(cudaMemsetAsync(arrival, 0, (n - 1) * sizeof(uint32_t), s));
-  k_refit<<<blocks, kLbvhThreads, 0, s>>>(sortedBox, (long long)n, out->nodes, out->leafParents, arrival, out->aabbs);
+  k_refit<<<blocks, kLbvhThreads, 0, s>>>(sortedBox, (long long)n, out->nodes, nodeRange, out->leafParents, arrival,
+                                          out->aabbs);
   PGA_CUDA_TRY(cudaGetLastError());
   return PGA_OK;
 }
