@@ -8,13 +8,14 @@ instanced terminals (375 MB of 64-byte records, larger than the 129 MB L2;
 L2 is also flushed with a 256 MB write before every timed step).
 
 schedule: before timing, the engine knobs are autotuned on this workload
-         (operatorgraph_gb300/autotune.py, 24 candidates); the fastest drives
+         (operatorgraph_gb300/autotune.py, 32 candidates); the fastest drives
          the timed engine ("batched + autotuned").
 value  : terminals/s with axioms and grammar resident in HBM (CUDA events on
          the launching stream around pga_derive).
-e2e    : the same through the C ABI with host buffers: pinned-host -> device
-         copy of the axioms, derivation, device -> pinned-host copy of the
-         count and of every terminal record, all inside the timed region.
+e2e    : the same through the C ABI with host buffers (pga_derive_to_host):
+         pinned-host -> device copy of the axioms, derivation in axiom ranges,
+         device -> pinned-host copy of every terminal record overlapped with
+         the next range's derivation, all inside the timed region.
 roofline: algorithmic bytes of the derivation kernel (64 B per terminal
          written + 48 B per axiom read) / kernel time, against the measured
          HBM copy bandwidth.
@@ -313,17 +314,15 @@ def our_arm(args):
         ms = float(t.item())
     value = world * n_term / (ms * 1e-3)
 
-    # ---- end-to-end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers: pga_derive_to_host
+    # copies the pinned host axioms in, derives in axiom ranges and copies each
+    # range's terminals back to pinned host memory while the next one derives.
     h_ax = torch.from_numpy(batch["axioms"].view(np.uint8).copy()).pin_memory()
-    h_out = torch.empty((n_term, 64), dtype=torch.uint8).pin_memory()
-    h_cnt = torch.empty(1, dtype=torch.int64).pin_memory()
-    d_ax2 = torch.empty_like(d_ax)
+    h_out = torch.empty((cap, 64), dtype=torch.uint8).pin_memory()
 
     def e2e_step():
-        d_ax2.copy_(h_ax, non_blocking=True)
-        eng.derive_raw(d_ax2.data_ptr(), n_ax, None, out.data_ptr(), cap, count.data_ptr())
-        h_cnt.copy_(count, non_blocking=True)
-        h_out.copy_(out[:n_term], non_blocking=True)
+        n, _ = eng.derive_to_host(h_ax.data_ptr(), n_ax, h_out.data_ptr(), cap)
+        return n
 
     for _ in range(2):
         e2e_step()
@@ -332,12 +331,32 @@ def our_arm(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(e2e_steps):
-        e2e_step()
+        n_host = e2e_step()
     e1.record(stream)
     barrier()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    assert int(h_cnt.item()) == n_term
+    assert n_host == n_term
     e2e_value = world * n_term / (e2e_ms * 1e-3)
+
+    # The same with one launch, then one copy of the whole output (for comparison).
+    h_cnt = torch.empty(1, dtype=torch.int64).pin_memory()
+    d_ax2 = torch.empty_like(d_ax)
+
+    def single_step():
+        d_ax2.copy_(h_ax, non_blocking=True)
+        eng.derive_raw(d_ax2.data_ptr(), n_ax, None, out.data_ptr(), cap, count.data_ptr())
+        h_cnt.copy_(count, non_blocking=True)
+        h_out[:n_term].copy_(out[:n_term], non_blocking=True)
+
+    single_step()
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(e2e_steps):
+        single_step()
+    s1.record(stream)
+    torch.cuda.synchronize()
+    single_ms = s0.elapsed_time(s1) / e2e_steps
 
     line = None
     if rank == 0:
@@ -352,7 +371,8 @@ def our_arm(args):
             "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": WORKLOAD,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h_ax.numel()),
-                    "d2h_bytes_per_step": int(h_out.numel() + h_cnt.numel() * 8), "ms_per_step": e2e_ms},
+                    "d2h_bytes_per_step": int(n_term * 64), "ms_per_step": e2e_ms,
+                    "api": "pga_derive_to_host (pinned host buffers)", "single_launch_then_copy_ms": single_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_derive_persistent", "algorithmic_bytes": alg_bytes},

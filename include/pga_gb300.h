@@ -202,7 +202,8 @@ const PgaProc* pga_default_procs(uint32_t* numProcs);
 /* Replaces SinglePhaseEvaluator::initialize(DispatchTableEntry*, n)
  * (include/pga/core/GPUEvaluator.cuh:475-506, CPUEvaluator.h:444-451):
  * validates and lowers the table to the device rule table and allocates all
- * work storage. No later call allocates device memory. */
+ * work storage. No later call allocates device memory, except the staging
+ * buffers of pga_derive_to_host on its first use. */
 PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* config, PgaEngine** engine);
 
 /* Replaces SinglePhaseEvaluator::release() (GPUEvaluator.cuh:528-536). */
@@ -216,6 +217,21 @@ PgaStatus pga_engine_destroy(PgaEngine* engine);
 PgaStatus pga_derive(PgaEngine* engine, const PgaAxiom* dAxioms, uint32_t numAxioms,
                      const float* dParamBlocks, PgaTerminal* dOut, uint64_t capacity,
                      uint64_t* dCount, void* stream);
+
+/* SinglePhaseEvaluator::execute (GPUEvaluator.cuh:508-521) for callers whose
+ * axioms and terminal buffer live in host memory (pinned memory is fastest):
+ * copies the axioms in, derives them in four axiom ranges (a small first one,
+ * then three equal ones) and copies each range's terminals out on a second
+ * stream while the next range derives, so most of the derivation hides behind
+ * the device-to-host copy.  Terminals are the same records as pga_derive's
+ * (path hashes use absolute axiom indices), range after range.  dParamBlocks
+ * stays a device pointer.  Returns when hOut holds *hCount terminals;
+ * PGA_ERR_OUTPUT_OVERFLOW when they do not fit in capacity.  Its staging
+ * buffers are allocated on first use and kept by the engine; it leaves no
+ * tape for pga_adjoint. */
+PgaStatus pga_derive_to_host(PgaEngine* engine, const PgaAxiom* hAxioms, uint32_t numAxioms,
+                             const float* dParamBlocks, PgaTerminal* hOut, uint64_t capacity, uint64_t* hCount,
+                             void* stream);
 
 /* The plain GPU form: one axiom (grammar) per launch sequence, one kernel
  * launch per derivation level, the host reading the level size back each time.

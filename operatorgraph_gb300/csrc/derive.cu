@@ -1179,8 +1179,8 @@ __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_
   setup_block(a, sm);
   WarpOut w;
   warpout_init(a, w);
-  warpout_level(a, w, a.numAxioms);
-  seed_axioms<true, LEAF>(a, w, 0, a.numAxioms);
+  warpout_level(a, w, a.numAxioms - a.axiomBase);
+  seed_axioms<true, LEAF>(a, w, a.axiomBase, a.numAxioms - a.axiomBase);
   close_node_page(a, w);
   if (!grid_barrier(a, [&] {
         volatile DevState* vs = a.st;
@@ -1323,6 +1323,11 @@ static void free_engine(PgaEngine* e) {
                   e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dLeafAabbSorted, e->dNodeRange, e->dNodeGrad, e->dAxiomGrad};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (e->dStageAxioms) cudaFree(e->dStageAxioms);
+  if (e->dStageOut) cudaFree(e->dStageOut);
+  if (e->dStageCount) cudaFree(e->dStageCount);
+  if (e->copyStream) cudaStreamDestroy(e->copyStream);
+  if (e->evDerived) cudaEventDestroy(e->evDerived);
   delete e;
 }
 
@@ -1551,15 +1556,17 @@ PgaStatus pga_engine_destroy(PgaEngine* e) {
   return PGA_OK;
 }
 
-PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dParamBlocks,
-                     PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount, void* stream) {
-  if (!e || (!dAxioms && numAxioms) || (!dOut && capacity)) {
-    set_error("pga_derive: null engine or buffers");
-    return PGA_ERR_INVALID_ARGUMENT;
-  }
-  cudaStream_t s = (cudaStream_t)stream;
+}  // extern "C"
+
+// One persistent launch over axioms [first, end) of dAxioms (path hashes are
+// seeded from the absolute axiom index, so a batch derived in ranges gives the
+// same terminals as one launch).
+static PgaStatus launch_persistent(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t first, uint32_t end,
+                                   const float* dParamBlocks, PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount,
+                                   cudaStream_t s) {
   PGA_CUDA_TRY(cudaMemsetAsync(e->dState, 0, sizeof(DevState), s));
-  DeriveArgs a = make_args(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
+  DeriveArgs a = make_args(e, dAxioms, end, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
+  a.axiomBase = first;
   void* args[] = {&a};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)e->persistentBlocks);
@@ -1574,12 +1581,93 @@ PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, 
   const void* kernel = e->leafKernel ? (const void*)k_derive_persistent<true> : (const void*)k_derive_persistent<false>;
   PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, kernel, args));
   e->lastAxioms = dAxioms;
-  e->lastNumAxioms = numAxioms;
+  e->lastNumAxioms = end;
   e->lastBlocks = dParamBlocks;
   e->lastOut = dOut;
   e->lastCap = capacity;
-  e->lastWasBatched = true;
+  e->lastWasBatched = first == 0;
   return PGA_OK;
+}
+
+extern "C" {
+
+PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dParamBlocks,
+                     PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount, void* stream) {
+  if (!e || (!dAxioms && numAxioms) || (!dOut && capacity)) {
+    set_error("pga_derive: null engine or buffers");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  return launch_persistent(e, dAxioms, 0, numAxioms, dParamBlocks, dOut, capacity, dCount, (cudaStream_t)stream);
+}
+
+// Grows an engine-owned device buffer (kept until the engine is destroyed).
+static cudaError_t ensure_buffer(void** p, size_t* have, size_t need) {
+  if (*have >= need && *p) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  cudaError_t err = cudaMalloc(p, need);
+  if (err == cudaSuccess) *have = need;
+  return err;
+}
+
+PgaStatus pga_derive_to_host(PgaEngine* e, const PgaAxiom* hAxioms, uint32_t numAxioms, const float* dParamBlocks,
+                             PgaTerminal* hOut, uint64_t capacity, uint64_t* hCount, void* stream) {
+  if (!e || (!hAxioms && numAxioms) || (!hOut && capacity) || !hCount) {
+    set_error("pga_derive_to_host: null engine, buffers or count");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  *hCount = 0;
+  PGA_CUDA_TRY(ensure_buffer((void**)&e->dStageAxioms, &e->stageAxiomBytes, std::max<size_t>(numAxioms, 1) * sizeof(PgaAxiom)));
+  PGA_CUDA_TRY(ensure_buffer((void**)&e->dStageOut, &e->stageOutBytes, std::max<uint64_t>(capacity, 1) * sizeof(PgaTerminal)));
+  PGA_CUDA_TRY(ensure_buffer((void**)&e->dStageCount, &e->stageCountBytes, sizeof(uint64_t)));
+  if (!e->copyStream) PGA_CUDA_TRY(cudaStreamCreateWithFlags(&e->copyStream, cudaStreamNonBlocking));
+  if (!e->evDerived) PGA_CUDA_TRY(cudaEventCreateWithFlags(&e->evDerived, cudaEventDisableTiming));
+  if (numAxioms == 0) return PGA_OK;
+  PGA_CUDA_TRY(cudaMemcpyAsync(e->dStageAxioms, hAxioms, (size_t)numAxioms * sizeof(PgaAxiom), cudaMemcpyHostToDevice, s));
+  // A small first range gets the copy engine going early; the rest follows in
+  // three equal ranges, each derived while the previous one is copied out.
+  uint32_t bounds[5];
+  uint32_t nr = 0;
+  bounds[nr++] = 0;
+  if (numAxioms >= 64) {
+    const uint32_t first = std::max<uint32_t>(numAxioms / 16, 1);
+    bounds[nr++] = first;
+    for (uint32_t k = 1; k <= 3; k++) bounds[nr++] = first + (uint32_t)((uint64_t)(numAxioms - first) * k / 3);
+  } else {
+    bounds[nr++] = numAxioms;
+  }
+  uint64_t offset = 0;
+  PgaStatus status = PGA_OK;
+  for (uint32_t r = 0; r + 1 < nr && status == PGA_OK; r++) {
+    if (bounds[r + 1] == bounds[r]) continue;
+    PgaStatus st = launch_persistent(e, e->dStageAxioms, bounds[r], bounds[r + 1], dParamBlocks, e->dStageOut + offset,
+                                     capacity - offset, e->dStageCount, s);
+    if (st != PGA_OK) {
+      status = st;
+      break;
+    }
+    PgaDeriveReport rep;
+    st = pga_engine_sync_report(e, s, &rep);  // waits for this range; OUTPUT_OVERFLOW past the capacity left
+    const uint64_t n = std::min<uint64_t>(rep.terminals, capacity - offset);
+    if (n) {
+      PGA_CUDA_TRY(cudaEventRecord(e->evDerived, s));
+      PGA_CUDA_TRY(cudaStreamWaitEvent(e->copyStream, e->evDerived, 0));
+      PGA_CUDA_TRY(cudaMemcpyAsync(hOut + offset, e->dStageOut + offset, n * sizeof(PgaTerminal), cudaMemcpyDeviceToHost,
+                                   e->copyStream));
+    }
+    if (st != PGA_OK) {
+      *hCount = offset + rep.terminals;
+      status = st;
+      break;
+    }
+    offset += n;
+    *hCount = offset;
+  }
+  PGA_CUDA_TRY(cudaStreamSynchronize(e->copyStream));
+  e->lastWasBatched = false;  // the staging ranges leave no tape for pga_adjoint
+  return status;
 }
 
 PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dParamBlocks,

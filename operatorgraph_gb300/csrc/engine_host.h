@@ -65,6 +65,13 @@ struct PgaEngine {
   unsigned long long lastCap = 0;
   bool leafKernel = false;  // launch the instantiation that expands leaf children in place
   bool lastWasBatched = false;
+  // pga_derive_to_host staging (allocated on first use, grown as needed)
+  PgaAxiom* dStageAxioms = nullptr;
+  PgaTerminal* dStageOut = nullptr;
+  uint64_t* dStageCount = nullptr;
+  size_t stageAxiomBytes = 0, stageOutBytes = 0, stageCountBytes = 0;
+  cudaStream_t copyStream = nullptr;
+  cudaEvent_t evDerived = nullptr;
 };
 
 namespace pga {

@@ -26,7 +26,7 @@ STATUS = {
 # Every symbol include/pga_gb300.h declares.
 EXPORTS = ["pga_version", "pga_last_error", "pga_default_procs", "pga_engine_create", "pga_engine_destroy",
            "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_engine_levels", "pga_lbvh_build",
-           "pga_lbvh_build_static", "pga_adjoint"]
+           "pga_lbvh_build_static", "pga_adjoint", "pga_derive_to_host"]
 
 
 class PgaError(RuntimeError):
@@ -96,6 +96,7 @@ def load_library(path=LIB_PATH):
     L.pga_adjoint.argtypes = [vp, vp, vp, u32, vp, vp]
     L.pga_engine_levels.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(u32)]
     L.pga_lbvh_build_static.argtypes = [vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
+    L.pga_derive_to_host.argtypes = [vp, vp, u32, vp, vp, u64, ctypes.POINTER(u64), vp]
     for name in EXPORTS[3:]:
         getattr(L, name).restype = ctypes.c_int
     _lib = L
@@ -155,6 +156,15 @@ class Engine:
         fn = L.pga_derive_plain if plain else L.pga_derive
         _check(fn(self.handle, d_axioms, n_axioms, d_blocks, d_out, capacity, d_count, _stream_handle(stream)),
                "pga_derive_plain" if plain else "pga_derive")
+
+    def derive_to_host(self, h_axioms, n_axioms, h_out, capacity, d_blocks=None, stream=None, check=True):
+        """pga_derive_to_host on host pointers (pinned memory is fastest); returns (count, status)."""
+        n = ctypes.c_uint64()
+        st = load_library().pga_derive_to_host(self.handle, h_axioms, n_axioms, d_blocks, h_out, capacity,
+                                                ctypes.byref(n), _stream_handle(stream))
+        if check:
+            _check(st, "pga_derive_to_host")
+        return n.value, st
 
     def report(self, stream=None):
         rep = PgaDeriveReport()

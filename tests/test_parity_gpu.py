@@ -308,3 +308,38 @@ def test_mixed_65536_full_size_properties():
     np.testing.assert_allclose(got_sum.cpu().numpy(), want_sum, rtol=1e-9, atol=1e-3)
     assert torch.unique(torch.cat(paths)).numel() == n
     eng.release()
+
+
+@pytest.mark.parametrize("scene", ["city_4096", "menger_d3"])
+def test_derive_to_host_matches_device_derive(scene):
+    """pga_derive_to_host (host axioms in, host terminals out, derived in axiom
+    ranges whose copies overlap the next range's derivation) gives the same
+    terminal records as one pga_derive, path hashes included."""
+    b = scenes.city(4096) if scene == "city_4096" else scenes.menger(0.05)
+    ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    cap = len(ref) + 4096
+    eng = _engine(b["entries"], node_capacity=1 << 23, max_terminals=1 << 23)
+    h_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).pin_memory()
+    h_out = torch.empty((cap, 64), dtype=torch.uint8).pin_memory()
+    for _ in range(2):  # staging is allocated on the first call and reused on the second
+        h_out.zero_()
+        n, st = eng.derive_to_host(h_ax.data_ptr(), len(b["axioms"]), h_out.data_ptr(), cap)
+        assert st == 0 and n == len(ref)
+        _assert_same(h_out[:n].numpy().reshape(-1).view(G.TERMINAL_DT), ref)
+    out, n2, _ = eng.execute(b["axioms"], capacity=cap)
+    assert n2 == n
+    eng.release()
+
+
+def test_derive_to_host_reports_overflow():
+    from operatorgraph_gb300.engine import PgaError
+
+    b = scenes.city(256)
+    eng = _engine(b["entries"])
+    h_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).pin_memory()
+    h_out = torch.empty((1000, 64), dtype=torch.uint8).pin_memory()
+    n, st = eng.derive_to_host(h_ax.data_ptr(), len(b["axioms"]), h_out.data_ptr(), 1000, check=False)
+    assert st == 2 and n > 1000
+    with pytest.raises(PgaError):
+        eng.derive_to_host(h_ax.data_ptr(), len(b["axioms"]), h_out.data_ptr(), 1000)
+    eng.release()
