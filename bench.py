@@ -412,6 +412,8 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     plain_s = time.perf_counter() - t0
     assert int(count.item()) == n_term
     res["plain_city_terminals_per_s"] = n_term / plain_s
+    peak, _ = read_peaks()
+    res["plain_city_roofline_frac"] = (64.0 * n_term + 48.0 * n_ax) / plain_s / 1e9 / peak
     # Restore the batched output for the LBVH below.
     eng.derive_raw(d_ax.data_ptr(), n_ax, None, out.data_ptr(), out.shape[0], count.data_ptr())
     torch.cuda.synchronize()
@@ -477,6 +479,17 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     assert int(count.item()) == n_f
     res["facades1024_forward_tape_ms"] = statistics.median(fw)
     res["facades1024_adjoint_ms"] = statistics.median(bw)
+    # Algorithmic bytes of the adjoint: per terminal the 48-B gradient and the
+    # 64-B record's tape link (8 B); per queued item its 64-B record read twice
+    # (replay of the parent and of itself) and 24 B of gradient written and read;
+    # per parameter and axiom size 4 B written.
+    n_items = ef.report()["nodes"]
+    adj_bytes = n_f * (48 + 8) + n_items * (2 * 64 + 2 * 24) + 4 * (d_blk.numel() + 3 * 1024)
+    peak, _ = read_peaks()
+    res["facades1024_adjoint_items"] = int(n_items)
+    res["facades1024_adjoint_gbs"] = adj_bytes / (res["facades1024_adjoint_ms"] * 1e-3) / 1e9
+    res["facades1024_adjoint_roofline_frac"] = res["facades1024_adjoint_gbs"] / peak
+    res["facades1024_fwd_adjoint_step_ms"] = res["facades1024_forward_tape_ms"] + res["facades1024_adjoint_ms"]
     ef.release()
     del out
     # The mixed batch: 65,536 axioms (40 % Menger depth 1-3, 40 % city

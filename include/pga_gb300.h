@@ -281,7 +281,10 @@ PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const
  * dL/dm (12 floats per terminal, same order as that derivation's output).
  * Accumulates dL/dDynParam into dGradParams (numBlocks x blockStride; may be NULL)
  * and dL/d(axiom size) into dGradAxiomSizes (3 per axiom; may be NULL).
- * Both outputs are overwritten, not added to. No reference counterpart. */
+ * Both outputs are overwritten, not added to.  One cooperative launch on
+ * `stream`, asynchronous; if the last derivation failed or overflowed, the
+ * gradients are zero and pga_engine_sync_report gives the status.  No
+ * reference counterpart. */
 PgaStatus pga_adjoint(PgaEngine* engine, const float* dGradTerminals, float* dGradParams,
                       uint32_t numBlocks, float* dGradAxiomSizes, void* stream);
 

@@ -272,18 +272,10 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
   return false;
 }
 
-// Pushes the gradient g of the recorded record back to its parent.
-__device__ void push_back(const DeriveArgs& a, const AdjArgs& j, uint32_t link, uint32_t ordinal, bool toTerminal,
-                          Grad g) {
-  Expander E;
-  bool fromAxiom;
-  uint32_t c;
-  Shape y0, yEnd;
-  Chain ch;
-  if (!replay(a, link, ordinal, toTerminal, E, fromAxiom, c, y0, ch, yEnd)) {
-    raise_error(a.st, PGA_ERR_NO_TAPE, (int)link);
-    return;
-  }
+// Pushes the gradient g of a record, whose creation has been replayed into
+// (E, fromAxiom, c, ch), back to its parent.
+__device__ void push_back_replayed(const DeriveArgs& a, const AdjArgs& j, uint32_t link, const Expander& E,
+                                   bool fromAxiom, uint32_t c, const Chain& ch, Grad g) {
   // Undo the Extrude steps, last first: after = (s0, extent, s1).
   for (int k = (int)ch.n - 1; k >= 0; k--) {
     const Shape& xb = ch.before[k];
@@ -315,56 +307,101 @@ __device__ void push_back(const DeriveArgs& a, const AdjArgs& j, uint32_t link, 
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_adj_terminals(DeriveArgs a, AdjArgs j) {
-  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
-  setup_block(a, sm);
-  for (unsigned long long t = (unsigned long long)blockIdx.x * kThreads + threadIdx.x; t < j.numTerminals;
-       t += (unsigned long long)gridDim.x * kThreads) {
-    const float* gm = j.gradTerminals + t * 12;
-    const uint2 link = a.termLinks[t];
-    Grad g;
-    float G[12];
-#pragma unroll
-    for (int q = 0; q < 12; q++) G[q] = __ldg(gm + q);
-    // Generate: M[:, k] = R[:, k] s_k and M[:, 3] = t, with R from the replayed state.
-    Expander E;
-    bool fromAxiom;
-    uint32_t c;
-    Shape y0, yEnd;
-    Chain ch;
-    if (!replay(a, link.x, link.y, true, E, fromAxiom, c, y0, ch, yEnd)) {
-      raise_error(a.st, PGA_ERR_NO_TAPE, (int)t);
-      continue;
-    }
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      g.t[q] = G[q * 4 + 3];
-      const uint32_t row = frame_row(yEnd.frame, q);
-      const float v = G[row * 4 + q];
-      g.s[q] = frame_neg(yEnd.frame, q) ? -v : v;
-    }
-    push_back(a, j, link.x, link.y, true, g);
+// Pushes the gradient g of the recorded record back to its parent.
+__device__ void push_back(const DeriveArgs& a, const AdjArgs& j, uint32_t link, uint32_t ordinal, bool toTerminal,
+                          Grad g) {
+  Expander E;
+  bool fromAxiom;
+  uint32_t c;
+  Shape y0, yEnd;
+  Chain ch;
+  if (!replay(a, link, ordinal, toTerminal, E, fromAxiom, c, y0, ch, yEnd)) {
+    raise_error(a.st, PGA_ERR_NO_TAPE, (int)link);
+    return;
   }
+  push_back_replayed(a, j, link, E, fromAxiom, c, ch, g);
 }
 
-__global__ void __launch_bounds__(kThreads) k_adj_items(DeriveArgs a, AdjArgs j, unsigned long long lo,
-                                                        unsigned long long hi) {
+// Reverse step of terminal t: dL/dM (12 floats) to the gradient of the
+// Generate rule's shape, then back to its parent.
+__device__ __forceinline__ void adj_terminal(const DeriveArgs& a, const AdjArgs& j, unsigned long long t) {
+  const float* gm = j.gradTerminals + t * 12;
+  const uint2 link = a.termLinks[t];
+  Grad g;
+  float G[12];
+#pragma unroll
+  for (int q = 0; q < 12; q++) G[q] = __ldg(gm + q);
+  // Generate: M[:, k] = R[:, k] s_k and M[:, 3] = t, with R from the replayed state.
+  Expander E;
+  bool fromAxiom;
+  uint32_t c;
+  Shape y0, yEnd;
+  Chain ch;
+  if (!replay(a, link.x, link.y, true, E, fromAxiom, c, y0, ch, yEnd)) {
+    raise_error(a.st, PGA_ERR_NO_TAPE, (int)t);
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    g.t[q] = G[q * 4 + 3];
+    const uint32_t row = frame_row(yEnd.frame, q);
+    const float v = G[row * 4 + q];
+    g.s[q] = frame_neg(yEnd.frame, q) ? -v : v;
+  }
+  push_back_replayed(a, j, link.x, E, fromAxiom, c, ch, g);
+}
+
+// Reverse step of work item i: its accumulated gradient back to its parent.
+__device__ __forceinline__ void adj_item(const DeriveArgs& a, const AdjArgs& j, unsigned long long i) {
+  const uint4 ext = __ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3);
+  if (ext.x == kEmptyItem) return;
+  Grad g;
+  const float* src = j.nodeGrad + i * 6;
+  bool any = false;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    g.t[q] = __ldcg(src + q);
+    g.s[q] = __ldcg(src + 3 + q);
+    any |= (g.t[q] != 0.0f) || (g.s[q] != 0.0f);
+  }
+  if (any) push_back(a, j, ext.z, ext.w, false, g);
+}
+
+// The whole reverse sweep in one cooperative launch: zero the accumulators and
+// outputs, visit every terminal, then the levels from the deepest up, with a
+// bounded grid barrier after each phase.  The level bounds, the item and the
+// terminal counts are the forward launch's final state, read on the device,
+// so no host round trip is needed.  A failed or overflowed forward pass leaves
+// the gradients zero (the engine report keeps the forward's status; a tape
+// too short for the terminals raises PGA_ERR_NO_TAPE).
+__global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, unsigned long long numParamFloats,
+                                                      uint32_t numAxioms) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
-  for (unsigned long long i = lo + (unsigned long long)blockIdx.x * kThreads + threadIdx.x; i < hi;
-       i += (unsigned long long)gridDim.x * kThreads) {
-    const uint4 ext = __ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3);
-    if (ext.x == kEmptyItem) continue;
-    Grad g;
-    const float* src = j.nodeGrad + i * 6;
-    bool any = false;
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      g.t[q] = __ldcg(src + q);
-      g.s[q] = __ldcg(src + 3 + q);
-      any |= (g.t[q] != 0.0f) || (g.s[q] != 0.0f);
-    }
-    if (any) push_back(a, j, ext.z, ext.w, false, g);
+  volatile DevState* vs = a.st;
+  // Fixed by the forward launch; nothing below changes them before the first barrier.
+  const unsigned long long nodes = min((unsigned long long)vs->nodeNext, a.nodeCap);
+  const unsigned long long nTerm = vs->termCount;
+  const uint32_t levels = vs->levels;
+  const bool ok = vs->status == 0 && nTerm <= a.cap && nTerm <= a.termLinkCap;
+  const unsigned long long tid = (unsigned long long)blockIdx.x * kThreads + threadIdx.x;
+  const unsigned long long stride = (unsigned long long)gridDim.x * kThreads;
+  for (unsigned long long k = tid; k < nodes * 6; k += stride) j.nodeGrad[k] = 0.0f;
+  if (j.gradParams)
+    for (unsigned long long k = tid; k < numParamFloats; k += stride) j.gradParams[k] = 0.0f;
+  if (j.gradSizes)
+    for (unsigned long long k = tid; k < (unsigned long long)numAxioms * 3; k += stride) j.gradSizes[k] = 0.0f;
+  if (!grid_barrier(a, [] {})) return;
+  if (!ok) {
+    if (tid == 0 && vs->status == 0) raise_error(a.st, PGA_ERR_NO_TAPE, -1);
+    return;
+  }
+  for (unsigned long long t = tid; t < nTerm; t += stride) adj_terminal(a, j, t);
+  if (!grid_barrier(a, [] {})) return;
+  for (int L = (int)levels; L >= 0; L--) {
+    const unsigned long long lo = a.levelStart[L], hi = min(a.levelStart[L + 1], nodes);
+    for (unsigned long long i = lo + tid; i < hi; i += stride) adj_item(a, j, i);
+    if (!grid_barrier(a, [] {})) return;
   }
 }
 
@@ -381,26 +418,18 @@ extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, floa
     set_error("pga_adjoint: the last derivation was not a pga_derive on an engine created with recordTape = 1");
     return PGA_ERR_NO_TAPE;
   }
-  cudaStream_t s = (cudaStream_t)stream;
-  DevState snap;
-  PGA_CUDA_TRY(cudaMemcpyAsync(&snap, e->dState, sizeof(DevState), cudaMemcpyDeviceToHost, s));
-  PGA_CUDA_TRY(cudaStreamSynchronize(s));
-  if (snap.status != 0) {
-    set_error("pga_adjoint: the last derivation failed");
-    return (PgaStatus)snap.status;
+  if (e->adjointBlocks == 0) {
+    // One cooperative launch: as many blocks as can be resident with the
+    // engine's dynamic shared memory.
+    PGA_CUDA_TRY(cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes));
+    int perSM = 0;
+    PGA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_adjoint, kThreads, e->smemBytes));
+    if (perSM < 1) {
+      set_error("pga_adjoint: the adjoint kernel does not fit on an SM");
+      return PGA_ERR_CUDA;
+    }
+    e->adjointBlocks = perSM * e->numSMs;
   }
-  if (snap.termCount > e->lastCap || snap.termCount > e->cfg.maxTerminals) {
-    set_error("pga_adjoint: more terminals than the tape holds (maxTerminals)");
-    return PGA_ERR_NO_TAPE;
-  }
-  const uint32_t levels = snap.levels + 1;
-  std::vector<unsigned long long> starts(levels + 1, 0);
-  PGA_CUDA_TRY(cudaMemcpy(starts.data(), e->dLevelStart, (levels + 1) * sizeof(unsigned long long),
-                          cudaMemcpyDeviceToHost));
-  const unsigned long long nodes = std::min<unsigned long long>(snap.nodeNext, e->cfg.nodeCapacity);
-  PGA_CUDA_TRY(cudaMemsetAsync(e->dNodeGrad, 0, nodes * 6 * sizeof(float), s));
-  if (dGradParams) PGA_CUDA_TRY(cudaMemsetAsync(dGradParams, 0, (size_t)numBlocks * e->cfg.blockStride * sizeof(float), s));
-  if (dGradAxiomSizes) PGA_CUDA_TRY(cudaMemsetAsync(dGradAxiomSizes, 0, (size_t)e->lastNumAxioms * 3 * sizeof(float), s));
   DeriveArgs a = make_args(e, e->lastAxioms, e->lastNumAxioms, e->lastBlocks, e->lastOut, e->lastCap, nullptr);
   AdjArgs j;
   j.gradTerminals = dGradTerminals;
@@ -408,15 +437,20 @@ extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, floa
   j.numBlocks = numBlocks;
   j.gradSizes = dGradAxiomSizes;
   j.nodeGrad = e->dNodeGrad;
-  j.numTerminals = snap.termCount;
-  const unsigned blocks = (unsigned)std::max(1, e->numSMs * 4);
-  k_adj_terminals<<<blocks, kThreads, e->smemBytes, s>>>(a, j);
-  PGA_CUDA_TRY(cudaGetLastError());
-  for (int L = (int)levels - 1; L >= 0; L--) {
-    const unsigned long long lo = starts[L], hi = std::min(starts[L + 1], nodes);
-    if (hi <= lo) continue;
-    k_adj_items<<<blocks, kThreads, e->smemBytes, s>>>(a, j, lo, hi);
-    PGA_CUDA_TRY(cudaGetLastError());
-  }
+  j.numTerminals = 0;  // read on the device
+  unsigned long long numParamFloats = (unsigned long long)numBlocks * e->cfg.blockStride;
+  uint32_t numAxioms = e->lastNumAxioms;
+  void* args[] = {&a, &j, &numParamFloats, &numAxioms};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)e->adjointBlocks);
+  cfg.blockDim = dim3((unsigned)kThreads);
+  cfg.dynamicSmemBytes = e->smemBytes;
+  cfg.stream = (cudaStream_t)stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, (const void*)k_adjoint, args));
   return PGA_OK;
 }
