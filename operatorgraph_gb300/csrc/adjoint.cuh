@@ -44,11 +44,68 @@ struct AdjArgs {
   unsigned long long numTerminals;
 };
 
+// Dual-number evaluation of an expression program (eval_exp's postfix VM):
+// every stack entry carries its value and its partials with respect to the
+// shape's translation (d[0..2]) and size (d[3..5]).  Shape attributes 3, 7, 11
+// are translation rows, 12..14 the size; rotation entries, the seed, the custom
+// attribute, scalars and random ranges are constants here.  Comparisons and
+// logic are piecewise constant.  Adds g times the partials to gx.
+__device__ __noinline__ void exp_grad(const float* b, const Shape& x, float custom, float g, Grad& gx) {
+  float val[PGA_MAX_EXP_LEVELS];
+  float d[PGA_MAX_EXP_LEVELS][6];
+  uint32_t top = 0;
+  const uint32_t size = f2u(b[0]);
+  for (uint32_t i = 1; i <= size && i < PGA_MAX_NUM_PARAMETER_VALUES; i++) {
+    const uint32_t rbits = __float_as_uint(b[i]);
+    const uint32_t kind = rbits >> 30;
+    const float v = __uint_as_float(rbits << 2);
+    float cv = 0.0f, cd[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (kind == 0) {
+      cv = v;
+    } else if (kind == 1) {
+      const float hi = __fdiv_rn(fmodf(v, 4096.0f), 4095.0f);
+      const float lo = __fdiv_rn(floorf(__fdiv_rn(v, 4096.0f)), 4095.0f);
+      cv = rand_range(x.seed, lo, hi);
+    } else if (kind == 2) {
+      const uint32_t attr = f2u(roundf(v));
+      cv = shape_attr(x, attr, custom);
+      if (attr < 12 && (attr & 3u) == 3u) cd[attr >> 2] = 1.0f;
+      if (attr >= 12 && attr < 15) cd[3 + attr - 12] = 1.0f;
+    } else {
+      if (top < 2) return;
+      const uint32_t bi = --top, ai = --top;
+      const float p1 = val[ai], p2 = val[bi];
+      const uint32_t op = f2u(roundf(v));
+      switch (op) {
+        case 0: cv = p1 + p2; for (int q = 0; q < 6; q++) cd[q] = d[ai][q] + d[bi][q]; break;
+        case 1: cv = p1 - p2; for (int q = 0; q < 6; q++) cd[q] = d[ai][q] - d[bi][q]; break;
+        case 2:
+          cv = p1 / p2;
+          for (int q = 0; q < 6; q++) cd[q] = (d[ai][q] - cv * d[bi][q]) / p2;
+          break;
+        case 3: cv = p1 * p2; for (int q = 0; q < 6; q++) cd[q] = d[ai][q] * p2 + p1 * d[bi][q]; break;
+        default: cv = 0.0f; break;  // comparisons and logic: zero partials
+      }
+    }
+    if (top >= PGA_MAX_EXP_LEVELS) return;
+    val[top] = cv;
+    for (int q = 0; q < 6; q++) d[top][q] = cd[q];
+    top++;
+  }
+  if (top == 0) return;
+  for (int q = 0; q < 3; q++) {
+    gx.t[q] += g * d[top - 1][q];
+    gx.s[q] += g * d[top - 1][3 + q];
+  }
+}
+
 // Gradient g of a parameter evaluated on shape x: a block value feeds the
-// parameter gradient; a size attribute (Shape::at 12..14) feeds gs of x;
-// every other kind is a constant of the grammar.
+// parameter gradient; a translation or size attribute (Shape::at 3/7/11,
+// 12..14) and an expression reading them feed gx, the gradient of x (null
+// where x's reads carry no gradient); every other kind is a constant of the
+// grammar.
 __device__ __forceinline__ void param_grad(const DeriveArgs& a, const AdjArgs& j, const DevRule& r, uint32_t k,
-                                           const Shape& x, float g, float* gsOfX) {
+                                           const Shape& x, float g, Grad* gx) {
   if (g == 0.0f) return;
   const DevParam p = param_at(a, r.paramBase + k);
   if (p.type == PGA_PT_BLOCK) {
@@ -56,9 +113,12 @@ __device__ __forceinline__ void param_grad(const DeriveArgs& a, const AdjArgs& j
     const uint32_t b = __ldg(&a.axioms[x.axiom].block);
     if (j.gradParams != nullptr && slot < a.blockStride && b < j.numBlocks)
       atomicAdd(&j.gradParams[(size_t)b * a.blockStride + slot], g);
-  } else if (p.type == PGA_PT_SHAPE_ATTR && gsOfX != nullptr) {
+  } else if (p.type == PGA_PT_SHAPE_ATTR && gx != nullptr) {
     const uint32_t i = f2u(p.v0);
-    if (i >= 12 && i < 15) gsOfX[i - 12] += g;
+    if (i >= 12 && i < 15) gx->s[i - 12] += g;
+    if (i < 12 && (i & 3u) == 3u) gx->t[i >> 2] += g;
+  } else if (p.type == PGA_PT_EXP && gx != nullptr) {
+    exp_grad(a.tab.expPool + p.aux, x, __ldg(&a.axioms[x.axiom].custom), g, *gx);
   }
 }
 
@@ -87,32 +147,70 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
       const float go = axis_dot(x, ax, gc.t);
       for (uint32_t k = 0; k < 3; k++)
         if (k != ax) gp.s[k] += gc.s[k];
-      // gN_i: go for i < c, go / 2 + gs_c[a] for i = c.  Child sizes use the
-      // factors as the forward pass read them (a dynamic Subdivide reads factor
-      // i from the symbol left by child i - 1); the scale uses the factors read
-      // from the unmodified symbol.  Shape reads of a dynamic factor past the
-      // first (on the updated symbol) carry no gradient.
-      float gS = -0.5f * go;
-      float gscale = 0.0f;
+      // Reverse pass over the recurrence that produced child c:
+      //   offset_0 = -S/2;  N_i = size(f_i, scale);  o_i = offset_i + N_i/2;
+      //   offset_{i+1} = offset_i + N_i;  child c: size N_c, translation t + R_a o_c.
+      // Factor f_i is read on the base shape (static form, i = 0, or a rule
+      // whose factors do not read the shape) or, for a dynamic Subdivide, on the
+      // symbol as child i - 1 left it in place: size N_{i-1} along a and
+      // translation t + R_a o_{i-1}; its gradient then flows to N_{i-1},
+      // o_{i-1} and the base's other sizes and translation.  The scale uses
+      // the factors read from the base shape.
+      constexpr uint32_t kMaxN = PGA_MAX_NUM_PARAMETERS;
+      float fv[kMaxN], Nv[kMaxN], ov[kMaxN], gN[kMaxN], goI[kMaxN];
+      const uint32_t last = min(c, n - 1u);
       Expander W = E0;
-      for (uint32_t i = 0; i <= c && i < n; i++) {
+      for (uint32_t i = 0; i <= last && i < kMaxN; i++) {
         const float f = dyn ? dyn_factor(a, W, i) : param(a, r, i + 1, x);
-        if (dyn) {
-          const float sz = subdivide_size(f, W.scale);
-          W.prevOff = __fadd_rn(W.offset, __fmul_rn(sz, 0.5f));
-          W.prevSize = sz;
-          W.offset = __fadd_rn(W.offset, sz);
+        const float sz = subdivide_size(f, W.scale);
+        fv[i] = f;
+        Nv[i] = sz;
+        ov[i] = __fadd_rn(W.offset, __fmul_rn(sz, 0.5f));
+        W.prevOff = ov[i];
+        W.prevSize = sz;
+        W.offset = __fadd_rn(W.offset, sz);
+        gN[i] = 0.0f;
+        goI[i] = 0.0f;
+      }
+      if (last >= kMaxN) return;
+      gN[last] += pick3(gc.s, ax);
+      goI[last] += go;
+      const bool readsUpdated = dyn && !(r.flags & kRulePure);
+      float gS = 0.0f, gscale = 0.0f, gOffNext = 0.0f;
+      for (int i = (int)last; i >= 0; i--) {
+        // o_i = offset_i + N_i/2 and offset_{i+1} = offset_i + N_i
+        const float gOff = gOffNext + goI[i];
+        gN[i] += gOffNext + 0.5f * goI[i];
+        gOffNext = gOff;
+        const float f = fv[i];
+        if (!dyn && f == 0.0f) continue;  // a skipped static slot
+        float gf = 0.0f;
+        if (f > 0.0f) {
+          gf = gN[i];
+        } else if (f < 0.0f) {
+          gf = gN[i] * (-E0.scale);
+          gscale += gN[i] * (-f);
         }
-        if (!dyn && f == 0.0f) continue;
-        float* gsx = (dyn && i > 0) ? nullptr : gp.s;
-        const float gN = (i < c) ? go : 0.5f * go + pick3(gc.s, ax);
-        if (f < 0.0f) {
-          gscale += gN * (-f);
-          param_grad(a, j, r, i + 1, x, gN * (-E0.scale), gsx);
-        } else if (f > 0.0f) {
-          param_grad(a, j, r, i + 1, x, gN, gsx);
+        if (gf == 0.0f) continue;
+        if (!readsUpdated || i == 0) {
+          param_grad(a, j, r, i + 1, x, gf, &gp);
+        } else {
+          Shape cur = x;
+          put3(cur.s, ax, Nv[i - 1]);
+          translate_row(cur, x, E0.axisRow, E0.axisSign, ov[i - 1]);
+          cur.seed = seed_of(a, x.seed, (uint32_t)i - 1u);
+          Grad gst;
+          grad_zero(gst);
+          param_grad(a, j, r, i + 1, cur, gf, &gst);
+          gN[i - 1] += pick3(gst.s, ax);
+          for (uint32_t k = 0; k < 3; k++)
+            if (k != ax) gp.s[k] += gst.s[k];
+#pragma unroll
+          for (int q = 0; q < 3; q++) gp.t[q] += gst.t[q];
+          goI[i - 1] += axis_dot(x, ax, gst.t);
         }
       }
+      gS += -0.5f * gOffNext;  // offset_0 = -S/2
       if (gscale != 0.0f) {
         float relSum = 0.0f;
         for (uint32_t i = 0; i < n; i++) {
@@ -125,8 +223,8 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
           const float gA = -gscale / relSum, gR = gscale * E0.scale / relSum;
           for (uint32_t i = 0; i < n; i++) {
             const float f = param(a, r, i + 1, x);
-            if (f > 0.0f) param_grad(a, j, r, i + 1, x, gA, gp.s);
-            if (f < 0.0f) param_grad(a, j, r, i + 1, x, gR, gp.s);
+            if (f > 0.0f) param_grad(a, j, r, i + 1, x, gA, &gp);
+            if (f < 0.0f) param_grad(a, j, r, i + 1, x, gR, &gp);
           }
         }
       }
@@ -168,9 +266,9 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
       }
       if (ext < 0.0f) {
         gS += gE * fabsf(ext);
-        param_grad(a, j, r, 1, x, gE * (-S), gp.s);
+        param_grad(a, j, r, 1, x, gE * (-S), &gp);
       } else {
-        param_grad(a, j, r, 1, x, gE, gp.s);
+        param_grad(a, j, r, 1, x, gE, &gp);
       }
       gp.s[0] += (ax == 0) ? gS : 0.0f;
       gp.s[1] += (ax == 1) ? gS : 0.0f;
@@ -286,7 +384,7 @@ __device__ void push_back_replayed(const DeriveArgs& a, const AdjArgs& j, uint32
     gb.s[0] = g.s[0];
     gb.s[1] = g.s[2];
     gb.s[2] = 0.0f;
-    param_grad(a, j, r, 1, xb, g.s[1], gb.s);
+    param_grad(a, j, r, 1, xb, g.s[1], &gb);
     g = gb;
   }
   if (fromAxiom) {

@@ -138,6 +138,33 @@ def block(slot):
     return Parameter(PT_BLOCK, (slot,))
 
 
+# Operand kinds and operations of expression parameters
+# (include/pga/core/OperandType.h, OperationType.h).
+ORT_SCALAR, ORT_RAND, ORT_SHAPE_ATTR, ORT_OP = 0, 1, 2, 3
+OPT_ADD, OPT_SUB, OPT_DIV, OPT_MULTI, OPT_EQ, OPT_NEQ, OPT_LT, OPT_GT, OPT_LEQ, OPT_GEQ, OPT_AND, OPT_OR = range(12)
+
+
+def _pack_operand(kind, x):
+    """One program word: the operand kind in the top two bits, the value's
+    float32 bits shifted right by two below (PackUtils::packOperand, PackUtils.h:18-23)."""
+    r = int(np.float32(x).view(np.uint32))
+    return float(np.uint32((r >> 2) | (kind << 30)).view(np.float32))
+
+
+def exp(*program):
+    """Expression parameter (PT_EXP) from a postfix program of tokens:
+    ("s", value) scalar, ("a", index) shape attribute, ("op", OPT_*) binary
+    operation.  value[0] = program length, value[1..] = the packed words
+    (Parameters.cuh:459-483)."""
+    words = []
+    for tok in program:
+        kind, v = tok
+        words.append(_pack_operand({"s": ORT_SCALAR, "a": ORT_SHAPE_ATTR, "op": ORT_OP}[kind], float(v)))
+    if len(words) + 1 > MAX_VALUES:
+        raise ValueError("expression longer than a parameter holds")
+    return Parameter(PT_EXP, [float(len(words))] + words)
+
+
 def make_axioms(n):
     a = np.zeros(n, dtype=AXIOM_DT)
     a["size"] = 1.0

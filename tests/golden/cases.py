@@ -61,6 +61,106 @@ def random_small():
     return _single(tab, ax, "random_grammar")
 
 
+def rich_random(seed, depth=5, n_axioms=4):
+    """A random grammar over all eight operators and both shapes: a DAG of
+    rules `depth` levels deep (rules of a level reused with some probability),
+    with scalar, random-range, shape-attribute and expression parameters,
+    relative / absolute / zero Subdivide factors, the three Repeat modes with
+    relative and absolute extents, ComponentSplit, Extrude from the custom
+    attribute, IfSizeLess on scalars and expressions, constant and random
+    terminal indices.  Seeds >= 1 and custom attributes vary per axiom."""
+    rng = np.random.default_rng(seed)
+    BOX, QUAD = G.SHAPE_BOX, G.SHAPE_QUAD
+    GEN = {BOX: G.BOX_GENERATE, QUAD: G.QUAD_GENERATE}
+    DIS = {BOX: G.BOX_DISCARD, QUAD: G.QUAD_DISCARD}
+    SUB = {BOX: G.BOX_SUBDIVIDE, QUAD: G.QUAD_SUBDIVIDE}
+    SUB3 = {BOX: G.BOX_SUBDIVIDE3, QUAD: G.QUAD_SUBDIVIDE3}
+    REP = {BOX: G.BOX_REPEAT, QUAD: G.QUAD_REPEAT}
+    IFL = {BOX: G.BOX_IF_SIZE_LESS, QUAD: G.QUAD_IF_SIZE_LESS}
+    entries = []
+    made = {}
+
+    def add(e):
+        entries.append(e)
+        return len(entries) - 1
+
+    def axis(kind):
+        return scalar(int(rng.integers(0, 3 if kind == BOX else 2)))
+
+    def rel_factor():
+        u = rng.random()
+        if u < 0.6:
+            return scalar(-float(rng.uniform(0.5, 2.0)))
+        if u < 0.8:
+            return rand(-2.0, -0.5)
+        return G.exp(("a", 12 + int(rng.integers(0, 2))), ("s", -float(rng.uniform(0.2, 1.0))), ("op", G.OPT_MULTI))
+
+    def make(kind, level):
+        key = (kind, level)
+        if made.get(key) and rng.random() < 0.3:
+            return made[key][int(rng.integers(0, len(made[key])))]
+        if level >= depth or rng.random() < 0.1:
+            if rng.random() < 0.15:
+                e = add(Entry(DIS[kind], [], []))
+            else:
+                tidx = scalar(int(rng.integers(0, 4))) if rng.random() < 0.8 else rand(0.0, 3.9)
+                e = add(Entry(GEN[kind], [tidx], []))
+            made.setdefault(key, []).append(e)
+            return e
+        ops = ["sub", "sub3", "rep", "ifl"] + (["cs"] if kind == BOX else ["ext"])
+        op = ops[int(rng.integers(0, len(ops)))]
+        if op == "sub":
+            k = int(rng.integers(2, 5))
+            factors = [rel_factor() for _ in range(k)]
+            if rng.random() < 0.3:
+                factors[int(rng.integers(0, k))] = scalar(0.02)
+            succ = [(make(kind, level + 1), 0) for _ in range(k)]
+            e = add(Entry(SUB[kind], [axis(kind)] + factors, succ))
+        elif op == "sub3":
+            factors = [rel_factor() for _ in range(3)]
+            if rng.random() < 0.4:
+                factors[int(rng.integers(0, 3))] = scalar(0.0)
+            succ = [(make(kind, level + 1), 0) for _ in range(3)]
+            e = add(Entry(SUB3[kind], [axis(kind)] + factors, succ))
+        elif op == "rep":
+            ext = scalar(-float(rng.uniform(0.2, 0.5))) if rng.random() < 0.7 else scalar(float(rng.uniform(0.3, 0.8)))
+            e = add(Entry(REP[kind], [axis(kind), ext, scalar(int(rng.integers(0, 3)))], [(make(kind, level + 1), 0)]))
+        elif op == "ifl":
+            size = scalar(float(rng.uniform(0.1, 1.0))) if rng.random() < 0.7 else G.exp(
+                ("a", 12 + int(rng.integers(0, 2))), ("s", 0.5), ("op", G.OPT_MULTI))
+            e = add(Entry(IFL[kind], [axis(kind), size], [(make(kind, level + 1), 0), (make(kind, level + 1), 0)]))
+        elif op == "cs":
+            e = add(Entry(G.BOX_COMPONENT_SPLIT, [],
+                          [(make(QUAD, level + 1), 0), (make(QUAD, level + 1), 0), (make(QUAD, level + 1), 0)]))
+        else:  # ext
+            u = rng.random()
+            extent = scalar(float(rng.uniform(0.2, 2.0))) if u < 0.5 else (shape_attr(16) if u < 0.8 else rand(0.3, 1.5))
+            e = add(Entry(G.QUAD_EXTRUDE, [scalar(1), extent], [(make(BOX, level + 1), 0)]))
+        made.setdefault(key, []).append(e)
+        return e
+
+    root_kind = BOX if rng.random() < 0.6 else QUAD
+    root = make(root_kind, 0)
+    tab = DispatchTable(entries).to_array()
+    ax = G.make_axioms(n_axioms)
+    ax["shape"] = root_kind
+    ax["entry"] = root
+    ax["size"] = rng.uniform(0.5, 4.0, (n_axioms, 3)).astype(np.float32)
+    if root_kind == QUAD:
+        ax["size"][:, 2] = 1.0
+    ax["position"] = rng.uniform(-10.0, 10.0, (n_axioms, 3)).astype(np.float32)
+    ax["seed"] = rng.uniform(0.0, 3.0, n_axioms).astype(np.float32)
+    ax["custom"] = rng.uniform(0.5, 3.0, n_axioms).astype(np.float32)
+    return _single(tab, ax, f"rich_random_{seed}")
+
+
+# Seeds of rich_random() with golden fixtures: seeds among the first sixty
+# whose grammar derives without error (the reference throws on, e.g., a
+# Subdivide whose absolute factors exceed the size) and that together use
+# every operator, both shapes and every parameter kind.
+RICH_SEEDS = (3, 5, 6, 8, 20, 26, 29, 32, 36, 38, 53, 58)
+
+
 def cases():
     out = [
         ("menger_d1", scenes.menger(0.5)),
@@ -79,6 +179,9 @@ def cases():
         for ext in (-0.3, 0.7):
             b = edge_repeat(mode, ext)
             out.append((b["name"], b))
+    for seed in RICH_SEEDS:
+        b = rich_random(seed)
+        out.append((b["name"], b))
     return out
 
 

@@ -7,7 +7,8 @@ stores: the grammar batch, the terminal count, a SHA-256 digest and checksum
 of the canonical (sorted, path-free) terminal records, and -- for cases of at
 most 2,000 terminals -- the canonical records themselves.
 
-Usage: python tests/golden/make_golden.py   (needs oracle/_ref built)
+Usage: python tests/golden/make_golden.py [case-name-prefix ...]   (needs oracle/_ref built)
+With prefixes, only the matching cases are (re)written.
 """
 import os
 import sys
@@ -29,7 +30,10 @@ FULL_LIMIT = 2000
 
 def main():
     tmp = tempfile.mkdtemp()
+    only = sys.argv[1:]
     for name, b in C.cases():
+        if only and not any(name.startswith(p) for p in only):
+            continue
         entries, axioms = b["entries"], b["axioms"]
         n_base = None
         if b["blocks"] is not None:
