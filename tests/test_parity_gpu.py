@@ -343,3 +343,42 @@ def test_derive_to_host_reports_overflow():
     with pytest.raises(PgaError):
         eng.derive_to_host(h_ax.data_ptr(), len(b["axioms"]), h_out.data_ptr(), 1000)
     eng.release()
+
+
+def test_rich_random_grammars_fuzz():
+    """120 more seeds of the rich random grammar generator (all operators, both
+    shapes, every parameter kind), each derived by the batched engine with leaf
+    children in place, with every child queued, and in the plain form, and
+    compared bit for bit with the oracle.  Seeds the oracle rejects (grammars
+    the reference would throw on) are skipped; statuses must then agree."""
+    import sys
+
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import cases
+
+    from operatorgraph_gb300.engine import terminals_to_numpy
+
+    checked = 0
+    for seed in range(1000, 1120):
+        b = cases.rich_random(seed)
+        try:
+            ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+        except oracle.OracleError as err:
+            eng = _engine(b["entries"])
+            _, _, rep = eng.execute(b["axioms"], capacity=1 << 16, check=False)
+            assert rep["status"] == err.status, (seed, rep["status"], err.status)
+            eng.release()
+            continue
+        if len(ref) > 200_000:
+            continue
+        for form in ("persistent", "queued", "plain"):
+            eng = _engine(b["entries"], no_inline=form == "queued")
+            out, n, rep = eng.execute(b["axioms"], capacity=max(len(ref), 1), plain=form == "plain")
+            assert rep["status"] == 0, (seed, form, rep)
+            if len(ref) == 0:
+                assert n == 0, (seed, form, n)
+            else:
+                _assert_same(terminals_to_numpy(out, n), ref)
+            eng.release()
+        checked += 1
+    assert checked >= 100
