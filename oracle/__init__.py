@@ -13,6 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+# Where the reference sources live in the build container (absent elsewhere).
+REFERENCE_ROOT = os.environ.get("PGA_REFERENCE_ROOT", "/root/reference")
 
 _lib = None
 
@@ -27,7 +29,7 @@ def build(verbose=False):
     return LIB_PATH
 
 
-def build_ref(ref_root="/root/reference"):
+def build_ref(ref_root=REFERENCE_ROOT):
     """Build oracle/_ref (the reference's own evaluator); returns the path or None."""
     script = os.path.join(HERE, "make_ref.py")
     try:
