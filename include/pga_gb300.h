@@ -69,7 +69,7 @@ typedef struct PgaEntry {
 } PgaEntry;                                      /* 1332 B */
 
 /* Operator kinds of the hot path (include/pga/core/{Subdivide,Repeat,
- * ComponentSplit,Extrude,If,Generate,Discard}.cuh). */
+ * ComponentSplit,Extrude,If,Generate,Discard,Translate,Scale,RandomRule}.cuh). */
 typedef enum PgaOperator {
   PGA_OP_SUBDIVIDE = 0,        /* Subdivide<DynParams>: axis = p0, factors = p1.., successor j for factor j+1 */
   PGA_OP_SUBDIVIDE_STATIC = 1, /* Subdivide<DynParam<0>, Pair<DynParam<k+1>, DCall<k>>...>: numChildren pairs, zero factors skipped */
@@ -78,7 +78,10 @@ typedef enum PgaOperator {
   PGA_OP_EXTRUDE = 4,          /* Extrude<DynParam<0> axis (unused), DynParam<1> extent, DCall<0>> (Quad -> Box) */
   PGA_OP_IF_SIZE_LESS = 5,     /* IfSizeLess<DynParam<0> axis, DynParam<1> size, DCall<0> true, DCall<1> false> */
   PGA_OP_GENERATE = 6,         /* Generate<false, 1, DynParam<0> terminal index>: instanced terminal */
-  PGA_OP_DISCARD = 7           /* Discard */
+  PGA_OP_DISCARD = 7,          /* Discard */
+  PGA_OP_TRANSLATE = 8,        /* Translate<DynParam<0..2> x y z, DCall<0>>: model * translate(x, y, z), in place */
+  PGA_OP_SCALE = 9,            /* Scale<DynParam<0..2>, DCall<0>>: per axis, v < 0 scales the size by -v, v > 0 sets it */
+  PGA_OP_RANDOM_RULE = 10      /* RandomRule<DynParams>: p0 chance (fractional part), p1.. weights, successor per weight */
 } PgaOperator;
 
 typedef enum PgaShape { PGA_SHAPE_BOX = 0, PGA_SHAPE_QUAD = 1 } PgaShape;
@@ -196,7 +199,10 @@ const char* pga_last_error(void);
  *   6 Box  ComponentSplit                7 Quad Extrude
  *   8 Box  IfSizeLess                    9 Quad IfSizeLess
  *  10 Box  Generate (instanced)         11 Quad Generate (instanced)
- *  12 Box  Discard                      13 Quad Discard */
+ *  12 Box  Discard                      13 Quad Discard
+ *  14 Box  Translate                    15 Quad Translate
+ *  16 Box  Scale                        17 Quad Scale
+ *  18 Box  RandomRule<DynParams>        19 Quad RandomRule<DynParams> */
 const PgaProc* pga_default_procs(uint32_t* numProcs);
 
 /* Replaces SinglePhaseEvaluator::initialize(DispatchTableEntry*, n)

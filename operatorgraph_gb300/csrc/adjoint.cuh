@@ -22,6 +22,9 @@
 //             E = e or S * |e|, the remainder fmod(S, E) = S - k E with k frozen.
 //  ComponentSplit  t_f = t + R[:,k] * (+-s_k / 2), face size picks two of s.
 //  Extrude    size (s0, extent, s1).
+//  Translate  t' = t + R v: t and s pass through, dL/dv_k = R[:, k] . g_t.
+//  Scale      s'_k = -v_k s_k (v_k < 0), v_k (v_k > 0), 0 (v_k = 0).
+//  IfSizeLess, RandomRule  discrete: the gradient passes through unchanged.
 //  Generate   M[:, j] = R[:, j] s_j, M[:, 3] = t.
 
 namespace pga {
@@ -303,12 +306,14 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
 
 // Recomputes the shape created as child `ordinal` of `link` (an item or an
 // axiom) and replays its 1 -> 1 chain until `stopAt` (a terminal: the Generate
-// rule; an item: its branching rule).  Extrude steps are recorded so that the
-// reverse pass can undo them.
+// rule; an item: its branching rule).  The smooth steps (Extrude, Translate,
+// Scale) are recorded so that the reverse pass can undo them; a chain with
+// more than kChainSteps of them has no adjoint (PGA_ERR_NO_TAPE).
+constexpr int kChainSteps = 8;
 struct Chain {
-  uint32_t n;             // Extrude steps
-  int32_t entry[4];       // rule of each step
-  Shape before[4];        // state entering each step
+  uint32_t n;                   // smooth steps
+  int32_t entry[kChainSteps];   // rule of each step
+  Shape before[kChainSteps];    // state entering each step
 };
 
 __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, bool toTerminal, Expander& E,
@@ -346,8 +351,28 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
       x.entry = succ_at(a, r.succBase + branch);
       continue;
     }
+    if (r.op == PGA_OP_RANDOM_RULE) {
+      const int pick = random_pick(a, r, x);
+      if (pick < 0) return false;
+      const int32_t nxt = succ_at(a, r.succBase + (uint32_t)pick);
+      x.path = child_path(x.path, (uint32_t)pick, nxt);
+      x.entry = nxt;
+      continue;
+    }
+    if (r.op == PGA_OP_TRANSLATE || r.op == PGA_OP_SCALE) {
+      if (ch.n >= kChainSteps) return false;
+      ch.entry[ch.n] = x.entry;
+      ch.before[ch.n] = x;
+      ch.n++;
+      if (r.op == PGA_OP_TRANSLATE)
+        apply_translate(a, r, x);
+      else
+        apply_scale(a, r, x);
+      x.entry = succ_at(a, r.succBase);
+      continue;
+    }
     if (r.op == PGA_OP_EXTRUDE) {
-      if (ch.n >= 4) return false;
+      if (ch.n >= kChainSteps) return false;
       ch.entry[ch.n] = x.entry;
       ch.before[ch.n] = x;
       ch.n++;
@@ -374,17 +399,32 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
 // (E, fromAxiom, c, ch), back to its parent.
 __device__ void push_back_replayed(const DeriveArgs& a, const AdjArgs& j, uint32_t link, const Expander& E,
                                    bool fromAxiom, uint32_t c, const Chain& ch, Grad g) {
-  // Undo the Extrude steps, last first: after = (s0, extent, s1).
+  // Undo the smooth steps, last first.
   for (int k = (int)ch.n - 1; k >= 0; k--) {
     const Shape& xb = ch.before[k];
     const DevRule r = rule_at(a, (uint32_t)ch.entry[k]);
     Grad gb;
 #pragma unroll
     for (int q = 0; q < 3; q++) gb.t[q] = g.t[q];
-    gb.s[0] = g.s[0];
-    gb.s[1] = g.s[2];
-    gb.s[2] = 0.0f;
-    param_grad(a, j, r, 1, xb, g.s[1], &gb);
+    if (r.op == PGA_OP_TRANSLATE) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) gb.s[q] = g.s[q];
+      for (uint32_t q = 0; q < 3; q++) param_grad(a, j, r, q, xb, axis_dot(xb, q, g.t), &gb);
+    } else if (r.op == PGA_OP_SCALE) {
+      float v[3], dv[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        v[q] = param(a, r, (uint32_t)q, xb);
+        gb.s[q] = (v[q] < 0.0f) ? -v[q] * g.s[q] : 0.0f;
+        dv[q] = (v[q] < 0.0f) ? -xb.s[q] : (v[q] > 0.0f ? 1.0f : 0.0f);
+      }
+      for (uint32_t q = 0; q < 3; q++) param_grad(a, j, r, q, xb, g.s[q] * dv[q], &gb);
+    } else {  // Extrude: after = (s0, extent, s1)
+      gb.s[0] = g.s[0];
+      gb.s[1] = g.s[2];
+      gb.s[2] = 0.0f;
+      param_grad(a, j, r, 1, xb, g.s[1], &gb);
+    }
     g = gb;
   }
   if (fromAxiom) {

@@ -176,9 +176,48 @@ __device__ __forceinline__ void translate_axis(Shape& y, const Shape& x, uint32_
 
 // ------------------------------------------------- 1 -> 1 chain resolution
 
-// Resolves a freshly created shape through IfSizeLess / Extrude rules
-// (If.cuh:65-89, Extrude.cuh:29-56) until it reaches a Generate (terminal),
-// a Discard, or a branching rule (queued).
+// Translate<X, Y, Z, Next>::execute (Translate.cuh): model * translate(v) in
+// place; R is a signed permutation, so every row gets one rounded add.
+__device__ __forceinline__ void apply_translate(const DeriveArgs& a, const DevRule& r, Shape& x) {
+  const float v0 = param(a, r, 0, x), v1 = param(a, r, 1, x), v2 = param(a, r, 2, x);
+  translate_axis(x, x, 0, v0);
+  translate_axis(x, x, 1, v1);
+  translate_axis(x, x, 2, v2);
+}
+
+// Scale<X, Y, Z, Next>::execute (Scale.cuh): per axis
+// ((v < 0) * size * v * -1) + ((v > 0) * v): a negative value scales the size,
+// a positive one replaces it, zero makes it zero.
+__device__ __forceinline__ float scaled_size(float s, float v) {
+  return __fadd_rn(__fmul_rn(__fmul_rn(__fmul_rn((float)(v < 0.0f), s), v), -1.0f), __fmul_rn((float)(v > 0.0f), v));
+}
+
+__device__ __forceinline__ void apply_scale(const DeriveArgs& a, const DevRule& r, Shape& x) {
+  const float v[3] = {param(a, r, 0, x), param(a, r, 1, x), param(a, r, 2, x)};
+#pragma unroll
+  for (int k = 0; k < 3; k++) x.s[k] = scaled_size(x.s[k], v[k]);
+}
+
+// RandomRule<DynParams>::execute (RandomRule.cuh:100-125): chance = frac(p0);
+// the first successor whose running share of the weights p1.. reaches it, or
+// -1 when rounding leaves none (the shape is dropped).
+__device__ __forceinline__ int random_pick(const DeriveArgs& a, const DevRule& r, const Shape& x) {
+  const float c0 = param(a, r, 0, x);
+  const float chance = __fsub_rn(c0, floorf(c0));
+  float sum = 0.0f;
+  for (uint32_t i = 1; i < r.nParams; i++) sum = __fadd_rn(sum, param(a, r, i, x));
+  float acc = 0.0f;
+  for (uint32_t i = 1; i < r.nParams; i++) {
+    acc = __fadd_rn(acc, __fdiv_rn(param(a, r, i, x), sum));
+    if (chance <= acc) return (int)i - 1;
+  }
+  return -1;
+}
+
+// Resolves a freshly created shape through IfSizeLess / Extrude / Translate /
+// Scale / RandomRule rules (If.cuh:65-89, Extrude.cuh:29-56, Translate.cuh,
+// Scale.cuh, RandomRule.cuh) until it reaches a Generate (terminal), a
+// Discard, or a branching rule (queued).
 __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
   for (int step = 0; step < kMaxChain; step++) {
     if (x.entry < 0 || (uint32_t)x.entry >= a.tab.numEntries) {
@@ -229,6 +268,27 @@ __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& 
         tidx = f2u(param(a, r, 0, x));
         if (tidx > 127u) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
         return kTerm;
+      }
+      case PGA_OP_TRANSLATE: {
+        if (r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        apply_translate(a, r, x);
+        x.entry = succ_at(a, r.succBase);
+        continue;
+      }
+      case PGA_OP_SCALE: {
+        if (r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        apply_scale(a, r, x);
+        x.entry = succ_at(a, r.succBase);
+        continue;
+      }
+      case PGA_OP_RANDOM_RULE: {
+        if (r.nParams < 2 || r.nSucc + 1 < r.nParams) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        const int pick = random_pick(a, r, x);
+        if (pick < 0) return kNone;
+        const int32_t nxt = succ_at(a, r.succBase + (uint32_t)pick);
+        x.path = child_path(x.path, (uint32_t)pick, nxt);
+        x.entry = nxt;
+        continue;
       }
       case PGA_OP_DISCARD:
         return kNone;
@@ -1295,7 +1355,7 @@ static cudaError_t persistent_occupancy(int* perSM, int threads, size_t smem) {
   return err;
 }
 
-static const PgaProc kDefaultProcs[14] = {
+static const PgaProc kDefaultProcs[20] = {
     {PGA_OP_SUBDIVIDE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SUBDIVIDE, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_BOX, 3, 1}, {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_QUAD, 3, 1},
     {PGA_OP_REPEAT, PGA_SHAPE_BOX, 0, 1},           {PGA_OP_REPEAT, PGA_SHAPE_QUAD, 0, 1},
@@ -1303,6 +1363,9 @@ static const PgaProc kDefaultProcs[14] = {
     {PGA_OP_IF_SIZE_LESS, PGA_SHAPE_BOX, 0, 1},     {PGA_OP_IF_SIZE_LESS, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_GENERATE, PGA_SHAPE_BOX, 0, 1},         {PGA_OP_GENERATE, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_DISCARD, PGA_SHAPE_BOX, 0, 1},          {PGA_OP_DISCARD, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_TRANSLATE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_TRANSLATE, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_SCALE, PGA_SHAPE_BOX, 0, 1},            {PGA_OP_SCALE, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_RANDOM_RULE, PGA_SHAPE_BOX, 0, 1},      {PGA_OP_RANDOM_RULE, PGA_SHAPE_QUAD, 0, 1},
 };
 
 extern "C" {
@@ -1312,7 +1375,7 @@ const char* pga_version(void) { return "pga_gb300 0.1.0 (sm_103a)"; }
 const char* pga_last_error(void) { return g_error.c_str(); }
 
 const PgaProc* pga_default_procs(uint32_t* numProcs) {
-  if (numProcs) *numProcs = 14;
+  if (numProcs) *numProcs = 20;
   return kDefaultProcs;
 }
 
@@ -1372,7 +1435,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     r.op = 0xFF;
     if (en.operatorCode >= 0 && (uint32_t)en.operatorCode < table->numProcs) {
       const PgaProc& p = table->procs[en.operatorCode];
-      if (p.op <= PGA_OP_DISCARD && p.shape <= PGA_SHAPE_QUAD) {
+      if (p.op <= PGA_OP_RANDOM_RULE && p.shape <= PGA_SHAPE_QUAD) {
         r.op = (uint8_t)p.op;
         r.shape = (uint8_t)p.shape;
         r.nChildren = p.numChildren;

@@ -24,7 +24,9 @@ PT_BLOCK = 16
 # PgaOperator
 OP_SUBDIVIDE, OP_SUBDIVIDE_STATIC, OP_REPEAT, OP_COMPONENT_SPLIT = 0, 1, 2, 3
 OP_EXTRUDE, OP_IF_SIZE_LESS, OP_GENERATE, OP_DISCARD = 4, 5, 6, 7
-OP_NAMES = ["Subdivide", "SubdivideStatic", "Repeat", "ComponentSplit", "Extrude", "IfSizeLess", "Generate", "Discard"]
+OP_TRANSLATE, OP_SCALE, OP_RANDOM_RULE = 8, 9, 10
+OP_NAMES = ["Subdivide", "SubdivideStatic", "Repeat", "ComponentSplit", "Extrude", "IfSizeLess", "Generate", "Discard",
+            "Translate", "Scale", "RandomRule"]
 
 SHAPE_BOX, SHAPE_QUAD = 0, 1
 
@@ -39,6 +41,9 @@ BOX_COMPONENT_SPLIT, QUAD_EXTRUDE = 6, 7
 BOX_IF_SIZE_LESS, QUAD_IF_SIZE_LESS = 8, 9
 BOX_GENERATE, QUAD_GENERATE = 10, 11
 BOX_DISCARD, QUAD_DISCARD = 12, 13
+BOX_TRANSLATE, QUAD_TRANSLATE = 14, 15
+BOX_SCALE, QUAD_SCALE = 16, 17
+BOX_RANDOM_RULE, QUAD_RANDOM_RULE = 18, 19
 
 PARAM_DT = np.dtype([("type", "<i4"), ("value", "<f4", (MAX_VALUES,))])
 SUCC_DT = np.dtype([("entryIndex", "<i4"), ("phaseIndex", "<i4")])
@@ -63,6 +68,9 @@ DEFAULT_PROCS = np.array([
     (OP_IF_SIZE_LESS, SHAPE_BOX, 0, 1), (OP_IF_SIZE_LESS, SHAPE_QUAD, 0, 1),
     (OP_GENERATE, SHAPE_BOX, 0, 1), (OP_GENERATE, SHAPE_QUAD, 0, 1),
     (OP_DISCARD, SHAPE_BOX, 0, 1), (OP_DISCARD, SHAPE_QUAD, 0, 1),
+    (OP_TRANSLATE, SHAPE_BOX, 0, 1), (OP_TRANSLATE, SHAPE_QUAD, 0, 1),
+    (OP_SCALE, SHAPE_BOX, 0, 1), (OP_SCALE, SHAPE_QUAD, 0, 1),
+    (OP_RANDOM_RULE, SHAPE_BOX, 0, 1), (OP_RANDOM_RULE, SHAPE_QUAD, 0, 1),
 ], dtype=PROC_DT)
 
 

@@ -541,6 +541,55 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
       }
       return;
     }
+    case PGA_OP_TRANSLATE: {
+      // Translate<X, Y, Z, Next>::execute (Translate.cuh): setModel(model * translate(x, y, z)),
+      // then the successor on the same symbol.
+      if (!param_ok<F>(c, e, 2, s.entry)) return;
+      F x = dyn_eval(c, blk, s, e.parameters[0]), y = dyn_eval(c, blk, s, e.parameters[1]),
+        z = dyn_eval(c, blk, s, e.parameters[2]);
+      int32_t nxt;
+      if (!successor<F>(c, e, 0, s.entry, nxt)) return;
+      s.model = mul(s.model, translate<F>(x, y, z));
+      s.entry = nxt;
+      dispatch(c, o, s);
+      return;
+    }
+    case PGA_OP_SCALE: {
+      // Scale<X, Y, Z, Next>::execute (Scale.cuh): size component by component as
+      // ((v < 0) * size * v * -1) + ((v > 0) * v), then the successor.
+      if (!param_ok<F>(c, e, 2, s.entry)) return;
+      F v[3] = {dyn_eval(c, blk, s, e.parameters[0]), dyn_eval(c, blk, s, e.parameters[1]),
+                dyn_eval(c, blk, s, e.parameters[2])};
+      int32_t nxt;
+      if (!successor<F>(c, e, 0, s.entry, nxt)) return;
+      for (int k = 0; k < 3; k++) s.size[k] = F(v[k] < F(0)) * s.size[k] * v[k] * F(-1) + F(v[k] > F(0)) * v[k];
+      s.entry = nxt;
+      dispatch(c, o, s);
+      return;
+    }
+    case PGA_OP_RANDOM_RULE: {
+      // RandomRule<DynParams>::execute (RandomRule.cuh): chance = frac(p0) in
+      // float; weights summed in order; the first successor whose running
+      // normalised share reaches the chance, none if rounding leaves it short.
+      if (e.numParameters < 2) { fail(c, PGA_ERR_BAD_PARAM, s.entry); return; }
+      float c0 = float(dyn_eval(c, blk, s, e.parameters[0]));
+      float chance = c0 - std::floor(c0);
+      F sum = F(0);
+      for (uint32_t i = 1; i < e.numParameters; i++) sum += dyn_eval(c, blk, s, e.parameters[i]);
+      F acc = F(0);
+      for (uint32_t i = 1; i < e.numParameters; i++) {
+        acc += dyn_eval(c, blk, s, e.parameters[i]) / sum;
+        if (F(chance) <= acc) {
+          int32_t nxt;
+          if (!successor<F>(c, e, i - 1, s.entry, nxt)) return;
+          s.entry = nxt;
+          s.path = child_path(s.path, i - 1, nxt);
+          dispatch(c, o, s);
+          return;
+        }
+      }
+      return;
+    }
     case PGA_OP_DISCARD:
       return;
     default:

@@ -28,10 +28,13 @@
 #include <pga/core/Generate.cuh>
 #include <pga/core/If.cuh>
 #include <pga/core/Proc.cuh>
+#include <pga/core/RandomRule.cuh>
 #include <pga/core/Repeat.cuh>
+#include <pga/core/Scale.cuh>
 #include <pga/core/ShapeGenerator.cuh>
 #include <pga/core/Subdivide.cuh>
 #include <pga/core/TStdLib.h>
+#include <pga/core/Translate.cuh>
 
 #include <algorithm>
 #include <chrono>
@@ -89,7 +92,7 @@ template <> struct GenerationFunction<HarnessFilter, 1> {
 };
 }  // namespace PGA
 
-// Operator codes 0..13 (see pga_default_procs() in include/pga_gb300.h).
+// Operator codes 0..19 (see pga_default_procs() in include/pga_gb300.h).
 struct HarnessProcs : T::List<
   /* 0 */ Proc<Box, Subdivide<DynParams>, 1>,
   /* 1 */ Proc<Quad, Subdivide<DynParams>, 1>,
@@ -104,7 +107,13 @@ struct HarnessProcs : T::List<
   /* 10 */ Proc<Box, Generate<false, 1, DynParam<0>>, 1>,
   /* 11 */ Proc<Quad, Generate<false, 1, DynParam<0>>, 1>,
   /* 12 */ Proc<Box, Discard, 1>,
-  /* 13 */ Proc<Quad, Discard, 1>
+  /* 13 */ Proc<Quad, Discard, 1>,
+  /* 14 */ Proc<Box, Translate<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 15 */ Proc<Quad, Translate<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 16 */ Proc<Box, Scale<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 17 */ Proc<Quad, Scale<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 18 */ Proc<Box, RandomRule<DynParams>, 1>,
+  /* 19 */ Proc<Quad, RandomRule<DynParams>, 1>
 > {};
 
 #pragma pack(push, 1)

@@ -61,14 +61,62 @@ def random_small():
     return _single(tab, ax, "random_grammar")
 
 
-def rich_random(seed, depth=5, n_axioms=4):
+def affine_mix():
+    """Translate, Scale and RandomRule<DynParams> (Translate.cuh, Scale.cuh,
+    RandomRule.cuh:100-125) on both shapes: a seed-driven choice between a
+    translated, absolutely / relatively scaled box split into faces and a
+    scaled subdivision; a custom-attribute choice among three weights that do
+    not sum to one; a zero first weight (picked when the chance is exactly 0,
+    since the accumulated probability is then 0 <= 0); a chance from a random
+    range; seeds with fractional part 0 and near 1."""
+    tab = DispatchTable([
+        Entry(G.BOX_RANDOM_RULE, [shape_attr(15), scalar(0.5), scalar(0.5)], [(1, 0), (4, 0)]),       # 0
+        Entry(G.BOX_TRANSLATE, [scalar(1.0), scalar(-2.0), scalar(0.5)], [(2, 0)]),                    # 1
+        Entry(G.BOX_SCALE, [scalar(-0.8), scalar(-1), scalar(2.0)], [(3, 0)]),                         # 2
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(6, 0), (11, 0), (7, 0)]),                                   # 3
+        Entry(G.BOX_SCALE, [scalar(-1.0666), scalar(-1), scalar(-1.1333)], [(5, 0)]),                  # 4
+        Entry(G.BOX_SUBDIVIDE, [scalar(1), scalar(-1), scalar(-3)], [(9, 0), (10, 0)]),                # 5
+        Entry(G.QUAD_RANDOM_RULE, [shape_attr(16), scalar(0.333), scalar(0.333), scalar(0.334)],
+              [(8, 0), (12, 0), (13, 0)]),                                                              # 6
+        Entry(G.QUAD_RANDOM_RULE, [rand(0.0, 1.0), scalar(0.0), scalar(1.0)], [(12, 0), (13, 0)]),     # 7
+        Entry(G.QUAD_TRANSLATE, [scalar(0), scalar(0.1666), scalar(-0.25)], [(14, 0)]),                # 8
+        Entry(G.BOX_GENERATE, [scalar(0)], []),                                                        # 9
+        Entry(G.BOX_RANDOM_RULE, [shape_attr(15), scalar(0.0), scalar(2.0), scalar(1.0)],
+              [(9, 0), (15, 0), (16, 0)]),                                                              # 10
+        Entry(G.QUAD_DISCARD, [], []),                                                                 # 11
+        Entry(G.QUAD_GENERATE, [scalar(1)], []),                                                       # 12
+        Entry(G.QUAD_SCALE, [scalar(0.5), scalar(-0.5), scalar(1)], [(12, 0)]),                        # 13
+        Entry(G.QUAD_GENERATE, [scalar(2)], []),                                                       # 14
+        Entry(G.BOX_TRANSLATE, [G.exp(("a", 12), ("s", 0.5), ("op", G.OPT_MULTI)), scalar(0), scalar(0)],
+              [(17, 0)]),                                                                               # 15
+        Entry(G.BOX_SCALE, [scalar(3), scalar(-2), scalar(-0.5)], [(9, 0)]),                           # 16
+        Entry(G.BOX_GENERATE, [scalar(3)], []),                                                        # 17
+    ]).to_array()
+    ax = G.make_axioms(10)
+    ax["size"] = [(2.0, 3.0, 1.5), (1.0, 1.0, 1.0), (4.0, 2.0, 0.5), (0.7, 5.0, 2.2), (3.0, 3.0, 3.0),
+                  (1.5, 0.5, 2.5), (2.5, 4.5, 1.0), (0.9, 1.1, 1.3), (1.2, 0.8, 2.0), (2.0, 1.0, 1.0)]
+    ax["position"] = [(0, 0, 0), (5, 0, 0), (0, 5, 0), (-3, 2, 1), (1, -4, 7), (2, 2, -2), (-6, -1, 3), (4, 4, 4),
+                      (-2, 6, 0), (3, -3, 3)]
+    ax["seed"] = [0.25, 0.75, 2.0, 0.999, 1.5, 3.0, 0.5, 1.6, 0.6, 0.0]
+    ax["custom"] = [0.1, 0.5, 0.9, 0.333, 0.666, 1.0, 0.0, 2.7, 0.4, 0.2]
+    # the last two axioms start inside the grammar: a box at the three-way
+    # choice and a quad at the choice whose first weight is zero
+    ax["entry"][8] = 10
+    ax["entry"][9] = 7
+    ax["shape"][9] = G.SHAPE_QUAD
+    return _single(tab, ax, "affine_mix")
+
+
+def rich_random(seed, depth=5, n_axioms=4, affine=False):
     """A random grammar over all eight operators and both shapes: a DAG of
     rules `depth` levels deep (rules of a level reused with some probability),
     with scalar, random-range, shape-attribute and expression parameters,
     relative / absolute / zero Subdivide factors, the three Repeat modes with
     relative and absolute extents, ComponentSplit, Extrude from the custom
     attribute, IfSizeLess on scalars and expressions, constant and random
-    terminal indices.  Seeds >= 1 and custom attributes vary per axiom."""
+    terminal indices.  Seeds >= 1 and custom attributes vary per axiom.
+    With affine=True the grammar also draws Translate, Scale and RandomRule
+    rules (the default draws exactly the grammars it always drew)."""
     rng = np.random.default_rng(seed)
     BOX, QUAD = G.SHAPE_BOX, G.SHAPE_QUAD
     GEN = {BOX: G.BOX_GENERATE, QUAD: G.QUAD_GENERATE}
@@ -77,6 +125,9 @@ def rich_random(seed, depth=5, n_axioms=4):
     SUB3 = {BOX: G.BOX_SUBDIVIDE3, QUAD: G.QUAD_SUBDIVIDE3}
     REP = {BOX: G.BOX_REPEAT, QUAD: G.QUAD_REPEAT}
     IFL = {BOX: G.BOX_IF_SIZE_LESS, QUAD: G.QUAD_IF_SIZE_LESS}
+    TRA = {BOX: G.BOX_TRANSLATE, QUAD: G.QUAD_TRANSLATE}
+    SCA = {BOX: G.BOX_SCALE, QUAD: G.QUAD_SCALE}
+    RRU = {BOX: G.BOX_RANDOM_RULE, QUAD: G.QUAD_RANDOM_RULE}
     entries = []
     made = {}
 
@@ -108,6 +159,8 @@ def rich_random(seed, depth=5, n_axioms=4):
             made.setdefault(key, []).append(e)
             return e
         ops = ["sub", "sub3", "rep", "ifl"] + (["cs"] if kind == BOX else ["ext"])
+        if affine:
+            ops += ["tr", "sc", "rr"]
         op = ops[int(rng.integers(0, len(ops)))]
         if op == "sub":
             k = int(rng.integers(2, 5))
@@ -132,6 +185,26 @@ def rich_random(seed, depth=5, n_axioms=4):
         elif op == "cs":
             e = add(Entry(G.BOX_COMPONENT_SPLIT, [],
                           [(make(QUAD, level + 1), 0), (make(QUAD, level + 1), 0), (make(QUAD, level + 1), 0)]))
+        elif op == "tr":
+            v = [scalar(float(rng.uniform(-2.0, 2.0))) if rng.random() < 0.7 else rand(-1.0, 1.0) for _ in range(3)]
+            if rng.random() < 0.3:
+                v[int(rng.integers(0, 3))] = G.exp(("a", 12), ("s", 0.5), ("op", G.OPT_MULTI))
+            e = add(Entry(TRA[kind], v, [(make(kind, level + 1), 0)]))
+        elif op == "sc":
+            v = []
+            for _ in range(3):
+                u = rng.random()
+                v.append(scalar(-float(rng.uniform(0.5, 1.5))) if u < 0.6 else
+                         (scalar(float(rng.uniform(0.2, 3.0))) if u < 0.8 else scalar(-1)))
+            e = add(Entry(SCA[kind], v, [(make(kind, level + 1), 0)]))
+        elif op == "rr":
+            u = rng.random()
+            chance = shape_attr(15) if u < 0.4 else (shape_attr(16) if u < 0.7 else rand(0.0, 1.0))
+            k = int(rng.integers(2, 5))
+            weights = [scalar(float(rng.uniform(0.1, 1.0))) for _ in range(k)]
+            if rng.random() < 0.2:
+                weights[int(rng.integers(0, k))] = scalar(0.0)
+            e = add(Entry(RRU[kind], [chance] + weights, [(make(kind, level + 1), 0) for _ in range(k)]))
         else:  # ext
             u = rng.random()
             extent = scalar(float(rng.uniform(0.2, 2.0))) if u < 0.5 else (shape_attr(16) if u < 0.8 else rand(0.3, 1.5))
@@ -151,7 +224,7 @@ def rich_random(seed, depth=5, n_axioms=4):
     ax["position"] = rng.uniform(-10.0, 10.0, (n_axioms, 3)).astype(np.float32)
     ax["seed"] = rng.uniform(0.0, 3.0, n_axioms).astype(np.float32)
     ax["custom"] = rng.uniform(0.5, 3.0, n_axioms).astype(np.float32)
-    return _single(tab, ax, f"rich_random_{seed}")
+    return _single(tab, ax, f"rich_affine_{seed}" if affine else f"rich_random_{seed}")
 
 
 # Seeds of rich_random() with golden fixtures: seeds among the first sixty
@@ -159,6 +232,10 @@ def rich_random(seed, depth=5, n_axioms=4):
 # Subdivide whose absolute factors exceed the size) and that together use
 # every operator, both shapes and every parameter kind.
 RICH_SEEDS = (3, 5, 6, 8, 20, 26, 29, 32, 36, 38, 53, 58)
+
+# Seeds of rich_random(affine=True) with golden fixtures: together they use
+# Translate, Scale and RandomRule on both shapes, with every chance kind.
+AFFINE_SEEDS = (2, 3, 5, 12, 13, 19, 27, 29, 49, 58)
 
 
 def cases():
@@ -181,6 +258,10 @@ def cases():
             out.append((b["name"], b))
     for seed in RICH_SEEDS:
         b = rich_random(seed)
+        out.append((b["name"], b))
+    out.append(("affine_mix", affine_mix()))
+    for seed in AFFINE_SEEDS:
+        b = rich_random(seed, affine=True)
         out.append((b["name"], b))
     return out
 

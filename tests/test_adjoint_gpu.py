@@ -178,6 +178,67 @@ def test_axiom_size_gradients_match_fp64_central_differences(name, batch):
         pytest.skip("every axiom size sits on a kink or a discrete boundary")
 
 
+def _affine_blocks_batch(n=6, seed=5):
+    """Translate and Scale driven by per-axiom blocks: a RandomRule on the seed
+    picks a translated-and-scaled box (relative x, absolute y, expression z
+    translate) or an extruded face of it, so both smooth-step kinds and the
+    discrete choice sit in 1 -> 1 chains of up to four smooth steps."""
+    from operatorgraph_gb300.grammar import DispatchTable, Entry, block, scalar, shape_attr
+
+    tab = DispatchTable([
+        Entry(G.BOX_RANDOM_RULE, [shape_attr(15), scalar(0.5), scalar(0.5)], [(1, 0), (4, 0)]),
+        Entry(G.BOX_TRANSLATE, [block(0), block(1), G.exp(("a", 13), ("s", 0.25), ("op", G.OPT_MULTI))], [(2, 0)]),
+        Entry(G.BOX_SCALE, [block(2), block(3), scalar(-1)], [(3, 0)]),
+        Entry(G.BOX_GENERATE, [scalar(0)], []),
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(5, 0), (8, 0), (5, 0)]),
+        Entry(G.QUAD_SCALE, [block(2), scalar(-1), scalar(1)], [(6, 0)]),
+        Entry(G.QUAD_EXTRUDE, [scalar(0), block(4)], [(7, 0)]),
+        Entry(G.BOX_TRANSLATE, [scalar(0), block(5), scalar(0)], [(3, 0)]),
+        Entry(G.QUAD_DISCARD, [], []),
+    ]).to_array()
+    rng = np.random.default_rng(seed)
+    ax = G.make_axioms(n)
+    ax["size"] = rng.uniform(1.0, 3.0, (n, 3)).astype(np.float32)
+    ax["position"] = rng.uniform(-5, 5, (n, 3)).astype(np.float32)
+    ax["seed"] = np.linspace(0.05, 0.95, n).astype(np.float32)
+    ax["block"] = np.arange(n)
+    stride = 6
+    blocks = np.zeros(n * stride, np.float32)
+    for i in range(n):
+        blocks[i * stride:(i + 1) * stride] = [rng.uniform(-2, 2), rng.uniform(-2, 2), -rng.uniform(0.5, 1.5),
+                                               rng.uniform(0.5, 2.0), rng.uniform(0.2, 1.0), rng.uniform(-1, 1)]
+    return {"entries": tab, "axioms": ax, "blocks": blocks, "block_stride": stride, "name": "affine_blocks"}
+
+
+def test_translate_scale_block_and_size_gradients_match_fp64_central_differences():
+    batch = _affine_blocks_batch()
+    by_path, gb, gs = _gpu_grad(batch)
+    b64 = batch["blocks"].astype(np.float64)
+    s64 = batch["axioms"]["size"].astype(np.float64)
+    base, keys0 = _loss64(batch, by_path, b64, s64)
+    assert base is not None and len(keys0) == len(by_path)
+
+    def block_at(k):
+        def f(b, s, h):
+            b = b.copy()
+            b[k] += h
+            return b, s
+        return f
+
+    def size_at(k):
+        def f(b, s, h):
+            s = s.copy()
+            s.reshape(-1)[k] += h
+            return b, s
+        return f
+
+    diffs = [_central(batch, by_path, keys0, base, b64, s64, block_at(k)) for k in range(len(b64))]
+    assert _compare("block", gb, diffs) == len(b64)
+    assert np.count_nonzero(gb) >= len(b64) * 0.8  # every block slot reached by some axiom
+    diffs = [_central(batch, by_path, keys0, base, b64, s64, size_at(k)) for k in range(s64.size)]
+    assert _compare("size", gs.reshape(-1), diffs) == s64.size
+
+
 def test_adjoint_requires_tape():
     from operatorgraph_gb300.engine import Engine, PgaError
 
