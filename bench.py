@@ -82,7 +82,7 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
-        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+        q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
         try:
@@ -93,24 +93,35 @@ class ClockSampler:
             self.thread.start()
         except OSError:
             self.proc = None
+            return self
         return self
 
     def _read(self):
+        # nvidia-smi's own timestamp, not the arrival time: its output through a
+        # pipe is block-buffered and can arrive long after the sample was taken.
+        import datetime
+
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 7:
-                self.samples.append([time.time()] + parts)
+            if len(parts) >= 8:
+                try:
+                    t = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                except ValueError:
+                    t = time.time()
+                self.samples.append([t] + parts[1:])
 
     def mark(self, start, end):
         self.window = (start, end)
 
     def __exit__(self, *exc):
         if self.proc:
+            time.sleep(0.3)  # one more period, so that a sample follows the timed region
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            self.thread.join(timeout=5)
 
     def summary(self):
         """Median SM clock and throttle reasons of the samples taken while the

@@ -217,7 +217,11 @@ __device__ __forceinline__ int random_pick(const DeriveArgs& a, const DevRule& r
 // Resolves a freshly created shape through IfSizeLess / Extrude / Translate /
 // Scale / RandomRule rules (If.cuh:65-89, Extrude.cuh:29-56, Translate.cuh,
 // Scale.cuh, RandomRule.cuh) until it reaches a Generate (terminal), a
-// Discard, or a branching rule (queued).
+// Discard, or a branching rule (queued).  The Translate / Scale / RandomRule
+// steps are compiled in with AFF only: the persistent kernel has an
+// instantiation without them for grammars that use none, which keeps their
+// registers out of its expansion loops.
+template <bool AFF>
 __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
   for (int step = 0; step < kMaxChain; step++) {
     if (x.entry < 0 || (uint32_t)x.entry >= a.tab.numEntries) {
@@ -270,19 +274,22 @@ __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& 
         return kTerm;
       }
       case PGA_OP_TRANSLATE: {
-        if (r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        if (!AFF || r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
         apply_translate(a, r, x);
         x.entry = succ_at(a, r.succBase);
         continue;
       }
       case PGA_OP_SCALE: {
-        if (r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        if (!AFF || r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
         apply_scale(a, r, x);
         x.entry = succ_at(a, r.succBase);
         continue;
       }
       case PGA_OP_RANDOM_RULE: {
-        if (r.nParams < 2 || r.nSucc + 1 < r.nParams) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        if (!AFF || r.nParams < 2 || r.nSucc + 1 < r.nParams) {
+          raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+          return kNone;
+        }
         const int pick = random_pick(a, r, x);
         if (pick < 0) return kNone;
         const int32_t nxt = succ_at(a, r.succBase + (uint32_t)pick);
@@ -898,7 +905,7 @@ __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Sha
 }
 
 // Expands the work items first + 32 k + lane (k < K, item < hi) of one warp.
-template <bool PAGED, bool LEAF>
+template <bool PAGED, bool LEAF, bool AFF>
 __device__ __forceinline__ void warp_items(const DeriveArgs& a, WarpOut& w, unsigned long long first,
                                            unsigned long long hi, uint32_t K) {
   const unsigned lane = threadIdx.x & 31u;
@@ -933,14 +940,14 @@ __device__ __forceinline__ void warp_items(const DeriveArgs& a, WarpOut& w, unsi
       int kind = kNone;
       Shape y;
       uint32_t tidx = 0, ordinal = 0;
-      if (c < n && expander_child(a, E, c0 + c, y, ordinal)) kind = resolve(a, y, tidx);
+      if (c < n && expander_child(a, E, c0 + c, y, ordinal)) kind = resolve<AFF>(a, y, tidx);
       emit_new<PAGED, LEAF>(a, w, kind, y, tidx, (uint32_t)item, ordinal);
     }
   }
 }
 
 // Seeds the axioms [first, first + count) with a warp-uniform grid-stride loop.
-template <bool PAGED, bool LEAF>
+template <bool PAGED, bool LEAF, bool AFF>
 __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uint32_t count) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
@@ -953,7 +960,7 @@ __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uin
     uint32_t tidx = 0;
     if (i < end) {
       axiom_shape(a, (uint32_t)i, y);
-      kind = resolve(a, y, tidx);
+      kind = resolve<AFF>(a, y, tidx);
     }
     emit_new<PAGED, LEAF>(a, w, kind, y, tidx, kAxiomLink | (uint32_t)i, 0u);
   }
@@ -961,13 +968,13 @@ __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uin
 
 // All items of one level [lo, hi): warp chunks of 32 K items in a static
 // grid-stride order (no shared work counter).
-template <bool PAGED, bool LEAF>
+template <bool PAGED, bool LEAF, bool AFF>
 __device__ __forceinline__ void expand_level(const DeriveArgs& a, WarpOut& w, unsigned long long lo,
                                              unsigned long long hi, uint32_t K) {
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
   const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
   for (unsigned long long b = lo + warpId * 32ull * K; b < hi; b += numWarps * 32ull * K)
-    warp_items<PAGED, LEAF>(a, w, b, hi, K);
+    warp_items<PAGED, LEAF, AFF>(a, w, b, hi, K);
 }
 
 // Copies the rule table into shared memory when it fits (decided at engine
@@ -1232,7 +1239,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 #define PGA_PERSISTENT_MIN_BLOCKS 2
 #endif
 
-template <bool LEAF>
+template <bool LEAF, bool AFF>
 __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   if (blockIdx.x == 0 && threadIdx.x == 0) a.st->clockStart = global_ns();
@@ -1240,7 +1247,7 @@ __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_
   WarpOut w;
   warpout_init(a, w);
   warpout_level(a, w, a.numAxioms - a.axiomBase);
-  seed_axioms<true, LEAF>(a, w, a.axiomBase, a.numAxioms - a.axiomBase);
+  seed_axioms<true, LEAF, AFF>(a, w, a.axiomBase, a.numAxioms - a.axiomBase);
   close_node_page(a, w);
   if (!grid_barrier(a, [&] {
         volatile DevState* vs = a.st;
@@ -1254,7 +1261,7 @@ __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_
     if (vs->stop) break;
     const unsigned long long lo = vs->levelLo, hi = vs->levelHi;
     warpout_level(a, w, hi - lo);
-    expand_level<true, LEAF>(a, w, lo, hi, a.itemsPerLane);
+    expand_level<true, LEAF, AFF>(a, w, lo, hi, a.itemsPerLane);
     close_node_page(a, w);
     if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
   }
@@ -1269,7 +1276,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_seed(DeriveArgs a, uint32_t fir
   setup_block(a, sm);
   WarpOut w;
   warpout_init(a, w);
-  seed_axioms<false, false>(a, w, first, count);
+  seed_axioms<false, false, true>(a, w, first, count);
 }
 
 __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsigned long long lo,
@@ -1278,7 +1285,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsi
   setup_block(a, sm);
   WarpOut w;
   warpout_init(a, w);
-  expand_level<false, false>(a, w, lo, hi, 1);
+  expand_level<false, false, true>(a, w, lo, hi, 1);
 }
 
 __global__ void k_write_count(const DevState* st, unsigned long long* out) { *out = st->termCount; }
@@ -1338,20 +1345,30 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
 
 using namespace pga;
 
-// Both instantiations of the persistent kernel get the same dynamic shared
-// memory limit; the launch uses the smaller of their occupancies, so either can
-// run co-resident.
+// The instantiations of the persistent kernel: leaf children in place or not,
+// with or without the Translate / Scale / RandomRule steps.
+static const void* persistent_kernel(bool leaf, bool aff) {
+  if (leaf) return aff ? (const void*)k_derive_persistent<true, true> : (const void*)k_derive_persistent<true, false>;
+  return aff ? (const void*)k_derive_persistent<false, true> : (const void*)k_derive_persistent<false, false>;
+}
+
+// All instantiations get the same dynamic shared memory limit; the launch uses
+// the smallest of their occupancies, so any of them can run co-resident.
 static cudaError_t set_persistent_smem(size_t bytes) {
-  cudaError_t err = cudaFuncSetAttribute(k_derive_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (err == cudaSuccess)
-    err = cudaFuncSetAttribute(k_derive_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t err = cudaSuccess;
+  for (int k = 0; k < 4 && err == cudaSuccess; k++)
+    err = cudaFuncSetAttribute(persistent_kernel(k & 1, k & 2), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   return err;
 }
 static cudaError_t persistent_occupancy(int* perSM, int threads, size_t smem) {
-  int a = 0, b = 0;
-  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_derive_persistent<false>, threads, smem);
-  if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_derive_persistent<true>, threads, smem);
-  *perSM = std::min(a, b);
+  int best = 1 << 30;
+  cudaError_t err = cudaSuccess;
+  for (int k = 0; k < 4 && err == cudaSuccess; k++) {
+    int n = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, persistent_kernel(k & 1, k & 2), threads, smem);
+    best = std::min(best, n);
+  }
+  *perSM = best;
   return err;
 }
 
@@ -1511,6 +1528,8 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     // replays one work item per branching shape) or when disabled.
     if (leaf && !c.recordTape && !(c.flags & PGA_FLAG_NO_INLINE)) e->leafKernel = true;
   }
+  for (const DevRule& r : e->hRules)
+    if (r.op == PGA_OP_TRANSLATE || r.op == PGA_OP_SCALE || r.op == PGA_OP_RANDOM_RULE) e->affineKernel = true;
   if (e->hParams.empty()) e->hParams.push_back(DevParam{0, 0.f, 0.f, 0});
   if (e->hSucc.empty()) e->hSucc.push_back(-1);
   if (e->hExpPool.empty()) e->hExpPool.push_back(0.f);
@@ -1641,7 +1660,7 @@ static PgaStatus launch_persistent(PgaEngine* e, const PgaAxiom* dAxioms, uint32
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const void* kernel = e->leafKernel ? (const void*)k_derive_persistent<true> : (const void*)k_derive_persistent<false>;
+  const void* kernel = persistent_kernel(e->leafKernel, e->affineKernel);
   PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, kernel, args));
   e->lastAxioms = dAxioms;
   e->lastNumAxioms = end;

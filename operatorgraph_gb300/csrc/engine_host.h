@@ -64,6 +64,7 @@ struct PgaEngine {
   PgaTerminal* lastOut = nullptr;
   unsigned long long lastCap = 0;
   bool leafKernel = false;  // launch the instantiation that expands leaf children in place
+  bool affineKernel = false;  // the table has Translate / Scale / RandomRule rules
   bool lastWasBatched = false;
   int adjointBlocks = 0;  // grid of the cooperative adjoint launch (set on first use)
   // pga_derive_to_host staging (allocated on first use, grown as needed)

@@ -234,7 +234,9 @@ def test_translate_scale_block_and_size_gradients_match_fp64_central_differences
 
     diffs = [_central(batch, by_path, keys0, base, b64, s64, block_at(k)) for k in range(len(b64))]
     assert _compare("block", gb, diffs) == len(b64)
-    assert np.count_nonzero(gb) >= len(b64) * 0.8  # every block slot reached by some axiom
+    # an axiom's Translate/Scale branch reads slots 0..3, its face branch 2, 4, 5
+    for i in range(len(batch["axioms"])):
+        assert np.count_nonzero(gb[i * 6:(i + 1) * 6]) >= 3, i
     diffs = [_central(batch, by_path, keys0, base, b64, s64, size_at(k)) for k in range(s64.size)]
     assert _compare("size", gs.reshape(-1), diffs) == s64.size
 
