@@ -176,7 +176,7 @@ __device__ __forceinline__ void translate_axis(Shape& y, const Shape& x, uint32_
 
 // ------------------------------------------------- 1 -> 1 chain resolution
 
-// Translate<X, Y, Z, Next>::execute (Translate.cuh): model * translate(v) in
+// Translate<X, Y, Z, Next>::execute (Translate.cuh:24-43): model * translate(v) in
 // place; R is a signed permutation, so every row gets one rounded add.
 __device__ __forceinline__ void apply_translate(const DeriveArgs& a, const DevRule& r, Shape& x) {
   const float v0 = param(a, r, 0, x), v1 = param(a, r, 1, x), v2 = param(a, r, 2, x);
@@ -185,7 +185,7 @@ __device__ __forceinline__ void apply_translate(const DeriveArgs& a, const DevRu
   translate_axis(x, x, 2, v2);
 }
 
-// Scale<X, Y, Z, Next>::execute (Scale.cuh): per axis
+// Scale<X, Y, Z, Next>::execute (Scale.cuh:23-45): per axis
 // ((v < 0) * size * v * -1) + ((v > 0) * v): a negative value scales the size,
 // a positive one replaces it, zero makes it zero.
 __device__ __forceinline__ float scaled_size(float s, float v) {
@@ -198,7 +198,7 @@ __device__ __forceinline__ void apply_scale(const DeriveArgs& a, const DevRule& 
   for (int k = 0; k < 3; k++) x.s[k] = scaled_size(x.s[k], v[k]);
 }
 
-// RandomRule<DynParams>::execute (RandomRule.cuh:100-125): chance = frac(p0);
+// RandomRule<DynParams>::execute (RandomRule.cuh:121-150): chance = frac(p0);
 // the first successor whose running share of the weights p1.. reaches it, or
 // -1 when rounding leaves none (the shape is dropped).
 __device__ __forceinline__ int random_pick(const DeriveArgs& a, const DevRule& r, const Shape& x) {
@@ -215,8 +215,8 @@ __device__ __forceinline__ int random_pick(const DeriveArgs& a, const DevRule& r
 }
 
 // Resolves a freshly created shape through IfSizeLess / Extrude / Translate /
-// Scale / RandomRule rules (If.cuh:65-89, Extrude.cuh:29-56, Translate.cuh,
-// Scale.cuh, RandomRule.cuh) until it reaches a Generate (terminal), a
+// Scale / RandomRule rules (If.cuh:65-89, Extrude.cuh:29-56, Translate.cuh:24-43,
+// Scale.cuh:23-45, RandomRule.cuh:121-150) until it reaches a Generate (terminal), a
 // Discard, or a branching rule (queued).  The Translate / Scale / RandomRule
 // steps are compiled in with AFF only: the persistent kernel has an
 // instantiation without them for grammars that use none, which keeps their

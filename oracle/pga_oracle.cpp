@@ -542,7 +542,7 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
       return;
     }
     case PGA_OP_TRANSLATE: {
-      // Translate<X, Y, Z, Next>::execute (Translate.cuh): setModel(model * translate(x, y, z)),
+      // Translate<X, Y, Z, Next>::execute (Translate.cuh:24-43): setModel(model * translate(x, y, z)),
       // then the successor on the same symbol.
       if (!param_ok<F>(c, e, 2, s.entry)) return;
       F x = dyn_eval(c, blk, s, e.parameters[0]), y = dyn_eval(c, blk, s, e.parameters[1]),
@@ -555,7 +555,7 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
       return;
     }
     case PGA_OP_SCALE: {
-      // Scale<X, Y, Z, Next>::execute (Scale.cuh): size component by component as
+      // Scale<X, Y, Z, Next>::execute (Scale.cuh:23-45): size component by component as
       // ((v < 0) * size * v * -1) + ((v > 0) * v), then the successor.
       if (!param_ok<F>(c, e, 2, s.entry)) return;
       F v[3] = {dyn_eval(c, blk, s, e.parameters[0]), dyn_eval(c, blk, s, e.parameters[1]),
@@ -568,7 +568,7 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
       return;
     }
     case PGA_OP_RANDOM_RULE: {
-      // RandomRule<DynParams>::execute (RandomRule.cuh): chance = frac(p0) in
+      // RandomRule<DynParams>::execute (RandomRule.cuh:121-150): chance = frac(p0) in
       // float; weights summed in order; the first successor whose running
       // normalised share reaches the chance, none if rounding leaves it short.
       if (e.numParameters < 2) { fail(c, PGA_ERR_BAD_PARAM, s.entry); return; }

@@ -63,7 +63,7 @@ def random_small():
 
 def affine_mix():
     """Translate, Scale and RandomRule<DynParams> (Translate.cuh, Scale.cuh,
-    RandomRule.cuh:100-125) on both shapes: a seed-driven choice between a
+    RandomRule.cuh:121-150) on both shapes: a seed-driven choice between a
     translated, absolutely / relatively scaled box split into faces and a
     scaled subdivision; a custom-attribute choice among three weights that do
     not sum to one; a zero first weight (picked when the chance is exactly 0,
