@@ -81,7 +81,10 @@ typedef enum PgaOperator {
   PGA_OP_DISCARD = 7,          /* Discard */
   PGA_OP_TRANSLATE = 8,        /* Translate<DynParam<0..2> x y z, DCall<0>>: model * translate(x, y, z), in place */
   PGA_OP_SCALE = 9,            /* Scale<DynParam<0..2>, DCall<0>>: per axis, v < 0 scales the size by -v, v > 0 sets it */
-  PGA_OP_RANDOM_RULE = 10      /* RandomRule<DynParams>: p0 chance (fractional part), p1.. weights, successor per weight */
+  PGA_OP_RANDOM_RULE = 10,     /* RandomRule<DynParams>: p0 chance (fractional part), p1.. weights, successor per weight */
+  PGA_OP_ROTATE = 11,          /* Rotate<DynParam<0..2> degrees about x y z, DCall<0>>: model * rotateXYZ, in place;
+                                  the angles must be scalars (the rotation is built once, at engine creation) */
+  PGA_OP_REPLICATE = 12        /* Replicate<DynParams>: the shape, unchanged, once per successor */
 } PgaOperator;
 
 typedef enum PgaShape { PGA_SHAPE_BOX = 0, PGA_SHAPE_QUAD = 1 } PgaShape;
@@ -202,7 +205,9 @@ const char* pga_last_error(void);
  *  12 Box  Discard                      13 Quad Discard
  *  14 Box  Translate                    15 Quad Translate
  *  16 Box  Scale                        17 Quad Scale
- *  18 Box  RandomRule<DynParams>        19 Quad RandomRule<DynParams> */
+ *  18 Box  RandomRule<DynParams>        19 Quad RandomRule<DynParams>
+ *  20 Box  Rotate                       21 Quad Rotate
+ *  22 Box  Replicate<DynParams>         23 Quad Replicate<DynParams> */
 const PgaProc* pga_default_procs(uint32_t* numProcs);
 
 /* Replaces SinglePhaseEvaluator::initialize(DispatchTableEntry*, n)

@@ -16,11 +16,14 @@ BUILD = os.path.join(HERE, "_build")
 # access checked; a failed check raises PGA_ERR_INTERNAL instead of accessing).
 CHECKED = os.environ.get("PGA_CHECKS") == "1"
 LIB = os.path.join(HERE, "libpga_gb300_checked.so" if CHECKED else "libpga_gb300.so")
-SOURCES = ["derive.cu", "lbvh.cu"]
+SOURCES = ["derive.cu", "derive_gen.cu", "lbvh.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: no FMA contraction anywhere in the derivation path (the kernels
-# also use explicit round-to-nearest intrinsics).
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+# also use explicit round-to-nearest intrinsics); -ffp-contract=off for the
+# host code, which builds Rotate's matrices as the reference's host code does
+# (gcc contracts to FMA by default on aarch64).
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "-Xcompiler", "-ffp-contract=off"]
 if CHECKED:
     FLAGS += ["-DPGA_CHECKS=1"]
     BUILD = BUILD + "_checked"

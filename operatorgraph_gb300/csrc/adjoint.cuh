@@ -21,6 +21,7 @@
 //  Repeat     size / offset linear in (S, startExt, e2, endExt); extent
 //             E = e or S * |e|, the remainder fmod(S, E) = S - k E with k frozen.
 //  ComponentSplit  t_f = t + R[:,k] * (+-s_k / 2), face size picks two of s.
+//  Replicate  every child is the shape itself.
 //  Extrude    size (s0, extent, s1).
 //  Translate  t' = t + R v: t and s pass through, dL/dv_k = R[:, k] . g_t.
 //  Scale      s'_k = -v_k s_k (v_k < 0), v_k (v_k > 0), 0 (v_k = 0).
@@ -200,7 +201,7 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
         } else {
           Shape cur = x;
           put3(cur.s, ax, Nv[i - 1]);
-          translate_row(cur, x, E0.axisRow, E0.axisSign, ov[i - 1]);
+          translate_ref(cur, x, E0.axisRef, ov[i - 1]);
           cur.seed = seed_of(a, x.seed, (uint32_t)i - 1u);
           Grad gst;
           grad_zero(gst);
@@ -299,6 +300,10 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
       for (int q = 0; q < 3; q++) gp.s[q] += add[q];
       return;
     }
+    case PGA_OP_REPLICATE:
+#pragma unroll
+      for (int q = 0; q < 3; q++) gp.s[q] += gc.s[q];
+      return;
     default:
       return;
   }
@@ -324,7 +329,7 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
     c = 0;
   } else {
     uint4 ext;
-    load_node(a.nodes, link, E.base, ext);
+    load_node(a, link, E.base, ext);
     const int32_t e = E.base.entry;
     if (e < 0 || (uint32_t)e >= a.tab.numEntries) return false;
     E.r = rule_at(a, (uint32_t)e);

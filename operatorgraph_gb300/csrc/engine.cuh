@@ -18,12 +18,28 @@
 // A shape therefore carries a 9-bit frame code instead of nine floats: column
 // j of R is sign_j * e_{perm_j}.  fl(R[i][a] * o) is then exactly +-o in row
 // perm_a and a signed zero elsewhere, so a translation is one rounded add.
+//
+// Rotate (Rotate.cuh:24-41) leaves that set.  The device code is therefore
+// compiled twice: by default with frame codes, and with PGA_GENERAL_FRAMES
+// (derive_gen.cu, for tables with Rotate rules) with the rotation as nine
+// floats and the reference's 4x4 products written out term by term.  The shape
+// state and the kernels of each build live in an inline namespace of their
+// own (pga::perm, pga::gen), so the two sets of kernels have distinct names.
 #pragma once
 
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #include "../../include/pga_gb300.h"
+
+#ifndef PGA_GENERAL_FRAMES
+#define PGA_GENERAL_FRAMES 0
+#endif
+#if PGA_GENERAL_FRAMES
+#define PGA_FRAMES_NS gen
+#else
+#define PGA_FRAMES_NS perm
+#endif
 
 namespace pga {
 
@@ -97,6 +113,7 @@ struct DeriveArgs {
   unsigned long long* outCount;
   Node* nodes;
   unsigned long long nodeCap;
+  float4* nodeRot;           // general frames: rotation entries 0..7 of each item (2 x float4; entry 8 in Node::sf.w)
   uint2* termLinks;
   unsigned long long termLinkCap;
   unsigned long long* levelStart;
@@ -118,32 +135,12 @@ struct DeriveArgs {
   DevState* st;
 };
 
-// ------------------------------------------------------------ shape state
-
-struct Shape {
-  float t[3];      // translation (model column 3)
-  float s[3];      // size
-  float seed;
-  uint32_t frame;  // rotation: bits 2j..2j+1 = row of column j's nonzero, bit 6+j = column j negated
-  int32_t entry;
-  uint32_t axiom;
-  uint32_t kind;   // PgaShape
-  uint64_t path;
+// Entry points of one build of the kernels (host stubs), for the host code.
+struct FrameKernels {
+  const void* persistent[4];  // k_derive_persistent<LEAF, AFF>, index LEAF + 2 AFF
+  const void* seed;           // k_seed (plain form)
+  const void* expand;         // k_expand_level (plain form)
 };
-
-constexpr uint32_t kIdentityFrame = 0u | (1u << 2) | (2u << 4);
-
-__device__ __forceinline__ uint32_t frame_row(uint32_t f, uint32_t col) { return (f >> (2 * col)) & 3u; }
-__device__ __forceinline__ uint32_t frame_neg(uint32_t f, uint32_t col) { return (f >> (6 + col)) & 1u; }
-// Column `col` of the result is column `src` of f, negated when `flip`.
-__device__ __forceinline__ uint32_t frame_set(uint32_t g, uint32_t col, uint32_t f, uint32_t src, uint32_t flip) {
-  g &= ~((3u << (2 * col)) | (1u << (6 + col)));
-  return g | (frame_row(f, src) << (2 * col)) | ((frame_neg(f, src) ^ flip) << (6 + col));
-}
-// R[row][col] of a frame: 0, 1 or -1.
-__device__ __forceinline__ float frame_entry(uint32_t f, uint32_t row, uint32_t col) {
-  return frame_row(f, col) == row ? (frame_neg(f, col) ? -1.0f : 1.0f) : 0.0f;
-}
 
 __device__ __forceinline__ void raise_error(DevState* st, int code, int detail) {
   if (atomicCAS(&st->status, 0, code) == 0) atomicExch(&st->detail, detail);
@@ -194,11 +191,156 @@ __device__ __forceinline__ void put3(float v[3], uint32_t k, float x) {
   v[2] = (k == 2) ? x : v[2];
 }
 
+// ------------------------------------------------------------ shape state
+
+inline namespace PGA_FRAMES_NS {
+
+struct Shape {
+  float t[3];      // translation (model column 3)
+  float s[3];      // size
+  float seed;
+#if PGA_GENERAL_FRAMES
+  float R[9];      // rotation (model columns 0..2), row-major
+#else
+  uint32_t frame;  // rotation: bits 2j..2j+1 = row of column j's nonzero, bit 6+j = column j negated
+#endif
+  int32_t entry;
+  uint32_t axiom;
+  uint32_t kind;   // PgaShape
+  uint64_t path;
+};
+
+#if PGA_GENERAL_FRAMES
+
+__device__ __forceinline__ void frame_identity(Shape& x) {
+#pragma unroll
+  for (int k = 0; k < 9; k++) x.R[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+}
+// R[row][col] for run-time row and col, without local memory.
+__device__ __forceinline__ float frame_at(const Shape& x, uint32_t row, uint32_t col) {
+  const float r0 = pick3(&x.R[0], col), r1 = pick3(&x.R[3], col), r2 = pick3(&x.R[6], col);
+  return row == 0 ? r0 : (row == 1 ? r1 : r2);
+}
+// The model axis a translation runs along.
+struct AxisRef {
+  uint32_t col;
+};
+__device__ __forceinline__ AxisRef axis_ref(const Shape&, uint32_t ax) { return AxisRef{ax}; }
+// model * translate(o e_col): column 3 of the 4x4 product is, per row,
+// ((R[i][0] T03 + R[i][1] T13) + R[i][2] T23) + t_i with one nonzero T, so
+// t_i' = fl(fl(R[i][col] * o) + t_i) (the other products are exact zeros).
+__device__ __forceinline__ void translate_ref(Shape& y, const Shape& x, AxisRef r, float o) {
+  const float t0 = __fadd_rn(__fmul_rn(pick3(&x.R[0], r.col), o), x.t[0]);
+  const float t1 = __fadd_rn(__fmul_rn(pick3(&x.R[3], r.col), o), x.t[1]);
+  const float t2 = __fadd_rn(__fmul_rn(pick3(&x.R[6], r.col), o), x.t[2]);
+  y.t[0] = t0;
+  y.t[1] = t1;
+  y.t[2] = t2;
+}
+// y's rotation = x's with columns ca and cb replaced by x's columns sa and sb,
+// negated when fa / fb (the products with the fixed face and extrude matrices,
+// whose entries are 0 and +-1).  The column arguments are constants at every
+// call site, so the entries stay in registers.
+__device__ __forceinline__ void frame_set2(Shape& y, const Shape& x, uint32_t ca, uint32_t sa, uint32_t fa,
+                                           uint32_t cb, uint32_t sb, uint32_t fb) {
+  float nr[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) nr[k] = x.R[k];
+#pragma unroll
+  for (uint32_t i = 0; i < 3; i++) {
+    nr[i * 3 + ca] = fa ? -x.R[i * 3 + sa] : x.R[i * 3 + sa];
+    nr[i * 3 + cb] = fb ? -x.R[i * 3 + sb] : x.R[i * 3 + sb];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) y.R[k] = nr[k];
+}
+// R[i][j] * s_j: column j of model4 * scale(size).
+__device__ __forceinline__ void frame_scaled(const Shape& x, float m[3][3]) {
+#pragma unroll
+  for (uint32_t i = 0; i < 3; i++)
+#pragma unroll
+    for (uint32_t j = 0; j < 3; j++) m[i][j] = __fmul_rn(x.R[i * 3 + j], x.s[j]);
+}
+// model4 * rotateXYZ(q) (Rotate.cuh:37, matrix.h:776-782): R'[i][j] =
+// ((R[i][0] q[0][j] + R[i][1] q[1][j]) + R[i][2] q[2][j]) + t_i * 0; the
+// translation is unchanged.
+__device__ __forceinline__ void frame_rotate(Shape& x, const float* q) {
+  float qq[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) qq[k] = q[k];
+  float nr[9];
+#pragma unroll
+  for (uint32_t i = 0; i < 3; i++)
+#pragma unroll
+    for (uint32_t j = 0; j < 3; j++)
+      nr[i * 3 + j] = __fadd_rn(__fadd_rn(__fmul_rn(x.R[i * 3 + 0], qq[0 * 3 + j]), __fmul_rn(x.R[i * 3 + 1], qq[1 * 3 + j])),
+                                __fmul_rn(x.R[i * 3 + 2], qq[2 * 3 + j]));
+#pragma unroll
+  for (int k = 0; k < 9; k++) x.R[k] = nr[k];
+}
+
+#else  // signed-permutation frames
+
+constexpr uint32_t kIdentityFrame = 0u | (1u << 2) | (2u << 4);
+
+__device__ __forceinline__ uint32_t frame_row(uint32_t f, uint32_t col) { return (f >> (2 * col)) & 3u; }
+__device__ __forceinline__ uint32_t frame_neg(uint32_t f, uint32_t col) { return (f >> (6 + col)) & 1u; }
+// Column `col` of the result is column `src` of f, negated when `flip`.
+__device__ __forceinline__ uint32_t frame_set(uint32_t g, uint32_t col, uint32_t f, uint32_t src, uint32_t flip) {
+  g &= ~((3u << (2 * col)) | (1u << (6 + col)));
+  return g | (frame_row(f, src) << (2 * col)) | ((frame_neg(f, src) ^ flip) << (6 + col));
+}
+// R[row][col] of a frame: 0, 1 or -1.
+__device__ __forceinline__ float frame_entry(uint32_t f, uint32_t row, uint32_t col) {
+  return frame_row(f, col) == row ? (frame_neg(f, col) ? -1.0f : 1.0f) : 0.0f;
+}
+
+__device__ __forceinline__ void frame_identity(Shape& x) { x.frame = kIdentityFrame; }
+__device__ __forceinline__ float frame_at(const Shape& x, uint32_t row, uint32_t col) {
+  return frame_entry(x.frame, row, col);
+}
+// The model axis a translation runs along: its row in the frame and its sign.
+struct AxisRef {
+  uint32_t row;
+  float sign;
+};
+__device__ __forceinline__ AxisRef axis_ref(const Shape& x, uint32_t ax) {
+  return AxisRef{frame_row(x.frame, ax), frame_neg(x.frame, ax) ? -1.0f : 1.0f};
+}
+// Translation by o along a model axis: t' = fl(fl(R[:,ax] * o) + t), which
+// for a signed-permutation R is one rounded add in row perm_ax.
+__device__ __forceinline__ void translate_ref(Shape& y, const Shape& x, AxisRef r, float o) {
+  const float v = __fmul_rn(r.sign, o);  // exact: sign is +-1
+#pragma unroll
+  for (uint32_t i = 0; i < 3; i++) y.t[i] = (i == r.row) ? __fadd_rn(v, x.t[i]) : x.t[i];
+}
+__device__ __forceinline__ void frame_set2(Shape& y, const Shape& x, uint32_t ca, uint32_t sa, uint32_t fa,
+                                           uint32_t cb, uint32_t sb, uint32_t fb) {
+  const uint32_t f = x.frame;
+  y.frame = frame_set(frame_set(f, ca, f, sa, fa), cb, f, sb, fb);
+}
+// R[i][j] * s_j is exactly +-s_j in row perm_j and zero elsewhere.
+__device__ __forceinline__ void frame_scaled(const Shape& x, float m[3][3]) {
+#pragma unroll
+  for (uint32_t j = 0; j < 3; j++) {
+    const uint32_t row = frame_row(x.frame, j);
+    const float v = frame_neg(x.frame, j) ? -x.s[j] : x.s[j];
+#pragma unroll
+    for (uint32_t i = 0; i < 3; i++) m[i][j] = (i == row) ? v : 0.0f;
+  }
+}
+
+#endif
+
+__device__ __forceinline__ void translate_axis(Shape& y, const Shape& x, uint32_t ax, float o) {
+  translate_ref(y, x, axis_ref(x, ax), o);
+}
+
 // Shape::at (include/pga/core/Shape.cuh:120-171).
 __device__ __forceinline__ float shape_attr(const Shape& x, uint32_t i, float custom) {
   if (i < 12) {
     uint32_t row = i >> 2, col = i & 3;
-    return col == 3 ? pick3(x.t, row) : frame_entry(x.frame, row, col);
+    return col == 3 ? pick3(x.t, row) : frame_at(x, row, col);
   }
   if (i < 15) return pick3(x.s, i - 12);
   if (i == 15) return x.seed;
@@ -250,4 +392,5 @@ __device__ inline float eval_exp(const float* b, const Shape& x, float custom, D
   return stack[top - 1];
 }
 
+}  // inline namespace PGA_FRAMES_NS
 }  // namespace pga

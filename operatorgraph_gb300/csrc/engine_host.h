@@ -32,6 +32,7 @@ struct PgaEngine {
   // Work storage (allocated once in pga_engine_create).
   pga::DevState* dState = nullptr;
   pga::Node* dNodes = nullptr;
+  float4* dNodeRot = nullptr;  // general frames: 2 float4 of rotation entries per work item
   uint2* dTermLinks = nullptr;
   unsigned long long* dLevelStart = nullptr;
   unsigned long long* dLevelClock = nullptr;
@@ -64,7 +65,9 @@ struct PgaEngine {
   PgaTerminal* lastOut = nullptr;
   unsigned long long lastCap = 0;
   bool leafKernel = false;  // launch the instantiation that expands leaf children in place
-  bool affineKernel = false;  // the table has Translate / Scale / RandomRule rules
+  bool affineKernel = false;  // the table has Translate / Scale / RandomRule / Rotate rules
+  bool generalFrames = false;  // the table has Rotate rules: general-frame kernels (derive_gen.cu)
+  pga::FrameKernels kernels{};  // the kernels of the engine's frame build
   bool lastWasBatched = false;
   int adjointBlocks = 0;  // grid of the cooperative adjoint launch (set on first use)
   // pga_derive_to_host staging (allocated on first use, grown as needed)

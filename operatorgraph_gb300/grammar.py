@@ -24,9 +24,9 @@ PT_BLOCK = 16
 # PgaOperator
 OP_SUBDIVIDE, OP_SUBDIVIDE_STATIC, OP_REPEAT, OP_COMPONENT_SPLIT = 0, 1, 2, 3
 OP_EXTRUDE, OP_IF_SIZE_LESS, OP_GENERATE, OP_DISCARD = 4, 5, 6, 7
-OP_TRANSLATE, OP_SCALE, OP_RANDOM_RULE = 8, 9, 10
+OP_TRANSLATE, OP_SCALE, OP_RANDOM_RULE, OP_ROTATE, OP_REPLICATE = 8, 9, 10, 11, 12
 OP_NAMES = ["Subdivide", "SubdivideStatic", "Repeat", "ComponentSplit", "Extrude", "IfSizeLess", "Generate", "Discard",
-            "Translate", "Scale", "RandomRule"]
+            "Translate", "Scale", "RandomRule", "Rotate", "Replicate"]
 
 SHAPE_BOX, SHAPE_QUAD = 0, 1
 
@@ -44,6 +44,8 @@ BOX_DISCARD, QUAD_DISCARD = 12, 13
 BOX_TRANSLATE, QUAD_TRANSLATE = 14, 15
 BOX_SCALE, QUAD_SCALE = 16, 17
 BOX_RANDOM_RULE, QUAD_RANDOM_RULE = 18, 19
+BOX_ROTATE, QUAD_ROTATE = 20, 21
+BOX_REPLICATE, QUAD_REPLICATE = 22, 23
 
 PARAM_DT = np.dtype([("type", "<i4"), ("value", "<f4", (MAX_VALUES,))])
 SUCC_DT = np.dtype([("entryIndex", "<i4"), ("phaseIndex", "<i4")])
@@ -71,6 +73,8 @@ DEFAULT_PROCS = np.array([
     (OP_TRANSLATE, SHAPE_BOX, 0, 1), (OP_TRANSLATE, SHAPE_QUAD, 0, 1),
     (OP_SCALE, SHAPE_BOX, 0, 1), (OP_SCALE, SHAPE_QUAD, 0, 1),
     (OP_RANDOM_RULE, SHAPE_BOX, 0, 1), (OP_RANDOM_RULE, SHAPE_QUAD, 0, 1),
+    (OP_ROTATE, SHAPE_BOX, 0, 1), (OP_ROTATE, SHAPE_QUAD, 0, 1),
+    (OP_REPLICATE, SHAPE_BOX, 0, 1), (OP_REPLICATE, SHAPE_QUAD, 0, 1),
 ], dtype=PROC_DT)
 
 

@@ -103,6 +103,23 @@ inline M4<F> scale(F x, F y, F z) {
   return make<F>(x, F(0), F(0), F(0), F(0), y, F(0), F(0), F(0), F(0), z, F(0));
 }
 
+// math::float4x4::rotateXYZ (matrix.h:876-888) after Rotate's degree to radian
+// conversion (Rotate.cuh:34-36), all in float: sines and cosines of the three
+// angles, products left to right.
+template <typename F>
+inline M4<F> rotate_xyz(float x, float y, float z) {
+  const float k = 3.1415926535897932384626434f / 180.0f;
+  x *= k;
+  y *= k;
+  z *= k;
+  const float sa = std::sin(x), sb = std::sin(y), sg = std::sin(z);
+  const float ca = std::cos(x), cb = std::cos(y), cg = std::cos(z);
+  const float r00 = cb * cg, r01 = cg * sa * sb - ca * sg, r02 = ca * cg * sb + sa * sg;
+  const float r10 = cb * sg, r11 = ca * cg + sa * sb * sg, r12 = -cg * sa + ca * sb * sg;
+  const float r20 = -sb, r21 = cb * sa, r22 = ca * cb;
+  return make<F>(F(r00), F(r01), F(r02), F(0), F(r10), F(r11), F(r12), F(0), F(r20), F(r21), F(r22), F(0));
+}
+
 // Shapes::Shape + Symbol<ShapeT> (Shape.cuh:16-22, Symbol.cuh:9-15): model
 // (3x4, kept as 4x4 with the constant last row), size, seed, custom attribute,
 // entry index; plus the shape kind, the axiom index and the path hash.
@@ -587,6 +604,33 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
           dispatch(c, o, s);
           return;
         }
+      }
+      return;
+    }
+    case PGA_OP_ROTATE: {
+      // Rotate<X, Y, Z, Next>::execute (Rotate.cuh:24-41): the angles in
+      // degrees, times pi / 180 in float, setModel(model * rotateXYZ(angles))
+      // (matrix.h:876-888), then the successor on the same symbol.
+      if (!param_ok<F>(c, e, 2, s.entry)) return;
+      float x = float(dyn_eval(c, blk, s, e.parameters[0])), y = float(dyn_eval(c, blk, s, e.parameters[1])),
+            z = float(dyn_eval(c, blk, s, e.parameters[2]));
+      int32_t nxt;
+      if (!successor<F>(c, e, 0, s.entry, nxt)) return;
+      s.model = mul(s.model, rotate_xyz<F>(x, y, z));
+      s.entry = nxt;
+      dispatch(c, o, s);
+      return;
+    }
+    case PGA_OP_REPLICATE: {
+      // Replicate<DynParams>::execute (Replicate.cuh:95-110): the symbol, with
+      // only its entry changed, dispatched once per successor.
+      for (uint32_t i = 0; i < e.numSuccessors; i++) {
+        int32_t nxt;
+        if (!successor<F>(c, e, i, s.entry, nxt)) return;
+        Sym<F> child = s;
+        child.entry = nxt;
+        child.path = child_path(s.path, i, nxt);
+        dispatch(c, o, child);
       }
       return;
     }

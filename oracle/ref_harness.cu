@@ -30,6 +30,8 @@
 #include <pga/core/Proc.cuh>
 #include <pga/core/RandomRule.cuh>
 #include <pga/core/Repeat.cuh>
+#include <pga/core/Replicate.cuh>
+#include <pga/core/Rotate.cuh>
 #include <pga/core/Scale.cuh>
 #include <pga/core/ShapeGenerator.cuh>
 #include <pga/core/Subdivide.cuh>
@@ -92,7 +94,7 @@ template <> struct GenerationFunction<HarnessFilter, 1> {
 };
 }  // namespace PGA
 
-// Operator codes 0..19 (see pga_default_procs() in include/pga_gb300.h).
+// Operator codes 0..23 (see pga_default_procs() in include/pga_gb300.h).
 struct HarnessProcs : T::List<
   /* 0 */ Proc<Box, Subdivide<DynParams>, 1>,
   /* 1 */ Proc<Quad, Subdivide<DynParams>, 1>,
@@ -113,7 +115,11 @@ struct HarnessProcs : T::List<
   /* 16 */ Proc<Box, Scale<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
   /* 17 */ Proc<Quad, Scale<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
   /* 18 */ Proc<Box, RandomRule<DynParams>, 1>,
-  /* 19 */ Proc<Quad, RandomRule<DynParams>, 1>
+  /* 19 */ Proc<Quad, RandomRule<DynParams>, 1>,
+  /* 20 */ Proc<Box, Rotate<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 21 */ Proc<Quad, Rotate<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 22 */ Proc<Box, Replicate<DynParams>, 1>,
+  /* 23 */ Proc<Quad, Replicate<DynParams>, 1>
 > {};
 
 #pragma pack(push, 1)

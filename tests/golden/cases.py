@@ -107,7 +107,47 @@ def affine_mix():
     return _single(tab, ax, "affine_mix")
 
 
-def rich_random(seed, depth=5, n_axioms=4, affine=False):
+def rotate_mix():
+    """Rotate (Rotate.cuh:24-41, rotateXYZ in matrix.h:876-888) and
+    Replicate<DynParams> (Replicate.cuh:95-110): a box replicated into an
+    unrotated copy, a copy turned 90 degrees about y then split, and a copy
+    turned by arbitrary angles about all three axes then split into faces; a
+    face rotated again, translated along its rotated axes, scaled and
+    extruded; a quad replicated into three turned copies; chained rotations
+    whose matrices are general (not signed permutations)."""
+    tab = DispatchTable([
+        Entry(G.BOX_REPLICATE, [], [(1, 0), (2, 0), (4, 0)]),                                        # 0
+        Entry(G.BOX_GENERATE, [scalar(0)], []),                                                      # 1
+        Entry(G.BOX_ROTATE, [scalar(0), scalar(90), scalar(0)], [(3, 0)]),                           # 2
+        Entry(G.BOX_SUBDIVIDE, [scalar(0), scalar(-1), scalar(-2)], [(1, 0), (5, 0)]),               # 3
+        Entry(G.BOX_ROTATE, [scalar(30), scalar(-47.5), scalar(12.25)], [(6, 0)]),                   # 4
+        Entry(G.BOX_ROTATE, [scalar(0), scalar(0), scalar(-37)], [(1, 0)]),                          # 5
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(7, 0), (11, 0), (12, 0)]),                                # 6
+        Entry(G.QUAD_ROTATE, [scalar(0), scalar(0), scalar(45)], [(8, 0)]),                          # 7
+        Entry(G.QUAD_TRANSLATE, [scalar(0.5), G.exp(("a", 13), ("s", 0.5), ("op", G.OPT_MULTI)), scalar(-0.25)],
+              [(9, 0)]),                                                                              # 8
+        Entry(G.QUAD_SCALE, [scalar(-0.5), scalar(2), scalar(1)], [(10, 0)]),                        # 9
+        Entry(G.QUAD_EXTRUDE, [scalar(0), scalar(0.75)], [(13, 0)]),                                 # 10
+        Entry(G.QUAD_DISCARD, [], []),                                                               # 11
+        Entry(G.QUAD_REPLICATE, [], [(14, 0), (15, 0), (16, 0)]),                                    # 12
+        Entry(G.BOX_REPEAT, [scalar(1), scalar(-0.3), scalar(2)], [(5, 0)]),                         # 13
+        Entry(G.QUAD_GENERATE, [scalar(1)], []),                                                     # 14
+        Entry(G.QUAD_ROTATE, [scalar(90), scalar(90), scalar(0)], [(14, 0)]),                        # 15
+        Entry(G.QUAD_ROTATE, [scalar(-132.63), scalar(18.95), scalar(180)], [(17, 0)]),              # 16
+        Entry(G.QUAD_IF_SIZE_LESS, [scalar(0), scalar(1.5)], [(14, 0), (18, 0)]),                    # 17
+        Entry(G.QUAD_SUBDIVIDE, [scalar(0), scalar(-1), scalar(-1)], [(19, 0), (19, 0)]),            # 18
+        Entry(G.QUAD_ROTATE, [scalar(0), scalar(-94.74), scalar(0)], [(20, 0)]),                     # 19
+        Entry(G.QUAD_GENERATE, [scalar(2)], []),                                                     # 20
+    ]).to_array()
+    ax = G.make_axioms(5)
+    ax["size"] = [(2.0, 3.0, 1.5), (1.0, 1.0, 1.0), (4.0, 2.0, 0.5), (0.7, 5.0, 2.2), (3.3, 1.9, 2.8)]
+    ax["position"] = [(0, 0, 0), (5, -1, 2), (-7.25, 5, 0.5), (-3, 2, 1), (100, -40, 7)]
+    ax["seed"] = [0.25, 0.75, 1.5, 0.999, 2.5]
+    ax["custom"] = [0.1, 0.5, 0.9, 0.333, 0.666]
+    return _single(tab, ax, "rotate_mix")
+
+
+def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False):
     """A random grammar over all eight operators and both shapes: a DAG of
     rules `depth` levels deep (rules of a level reused with some probability),
     with scalar, random-range, shape-attribute and expression parameters,
@@ -116,7 +156,8 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False):
     attribute, IfSizeLess on scalars and expressions, constant and random
     terminal indices.  Seeds >= 1 and custom attributes vary per axiom.
     With affine=True the grammar also draws Translate, Scale and RandomRule
-    rules (the default draws exactly the grammars it always drew)."""
+    rules, with rotate=True also Rotate and Replicate rules (the defaults draw
+    exactly the grammars they always drew)."""
     rng = np.random.default_rng(seed)
     BOX, QUAD = G.SHAPE_BOX, G.SHAPE_QUAD
     GEN = {BOX: G.BOX_GENERATE, QUAD: G.QUAD_GENERATE}
@@ -128,6 +169,8 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False):
     TRA = {BOX: G.BOX_TRANSLATE, QUAD: G.QUAD_TRANSLATE}
     SCA = {BOX: G.BOX_SCALE, QUAD: G.QUAD_SCALE}
     RRU = {BOX: G.BOX_RANDOM_RULE, QUAD: G.QUAD_RANDOM_RULE}
+    ROT = {BOX: G.BOX_ROTATE, QUAD: G.QUAD_ROTATE}
+    REPL = {BOX: G.BOX_REPLICATE, QUAD: G.QUAD_REPLICATE}
     entries = []
     made = {}
 
@@ -161,6 +204,8 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False):
         ops = ["sub", "sub3", "rep", "ifl"] + (["cs"] if kind == BOX else ["ext"])
         if affine:
             ops += ["tr", "sc", "rr"]
+        if rotate:
+            ops += ["rot", "repl"]
         op = ops[int(rng.integers(0, len(ops)))]
         if op == "sub":
             k = int(rng.integers(2, 5))
@@ -205,6 +250,13 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False):
             if rng.random() < 0.2:
                 weights[int(rng.integers(0, k))] = scalar(0.0)
             e = add(Entry(RRU[kind], [chance] + weights, [(make(kind, level + 1), 0) for _ in range(k)]))
+        elif op == "rot":
+            ang = [scalar(float(rng.choice([0.0, 90.0, -90.0, 180.0]))) if rng.random() < 0.4 else
+                   scalar(round(float(rng.uniform(-180.0, 180.0)), 2)) for _ in range(3)]
+            e = add(Entry(ROT[kind], ang, [(make(kind, level + 1), 0)]))
+        elif op == "repl":
+            k = int(rng.integers(2, 4))
+            e = add(Entry(REPL[kind], [], [(make(kind, level + 1), 0) for _ in range(k)]))
         else:  # ext
             u = rng.random()
             extent = scalar(float(rng.uniform(0.2, 2.0))) if u < 0.5 else (shape_attr(16) if u < 0.8 else rand(0.3, 1.5))
@@ -224,7 +276,8 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False):
     ax["position"] = rng.uniform(-10.0, 10.0, (n_axioms, 3)).astype(np.float32)
     ax["seed"] = rng.uniform(0.0, 3.0, n_axioms).astype(np.float32)
     ax["custom"] = rng.uniform(0.5, 3.0, n_axioms).astype(np.float32)
-    return _single(tab, ax, f"rich_affine_{seed}" if affine else f"rich_random_{seed}")
+    name = "rich_rotate" if rotate else ("rich_affine" if affine else "rich_random")
+    return _single(tab, ax, f"{name}_{seed}")
 
 
 # Seeds of rich_random() with golden fixtures: seeds among the first sixty
@@ -236,6 +289,11 @@ RICH_SEEDS = (3, 5, 6, 8, 20, 26, 29, 32, 36, 38, 53, 58)
 # Seeds of rich_random(affine=True) with golden fixtures: together they use
 # Translate, Scale and RandomRule on both shapes, with every chance kind.
 AFFINE_SEEDS = (2, 3, 5, 12, 13, 19, 27, 29, 49, 58)
+
+# Seeds of rich_random(affine=True, rotate=True) with golden fixtures: together
+# they use Rotate (right angles and arbitrary ones) and Replicate on both
+# shapes, mixed with every other operator.
+ROTATE_SEEDS = (3, 6, 8, 13, 24, 47, 58, 71, 73, 75)
 
 
 def cases():
@@ -262,6 +320,10 @@ def cases():
     out.append(("affine_mix", affine_mix()))
     for seed in AFFINE_SEEDS:
         b = rich_random(seed, affine=True)
+        out.append((b["name"], b))
+    out.append(("rotate_mix", rotate_mix()))
+    for seed in ROTATE_SEEDS:
+        b = rich_random(seed, affine=True, rotate=True)
         out.append((b["name"], b))
     return out
 

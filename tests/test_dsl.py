@@ -90,7 +90,7 @@ def test_a_rule_used_on_both_shapes_is_lowered_per_shape():
 
 
 @pytest.mark.parametrize("text, words", [
-    ("axiom Box A; A = Rotate(0, 90, 0) B; B = Discard();", ["Rotate", "'A'"]),
+    ("axiom Box A; A = SwapSize(Y, X, Z) B; B = Discard();", ["SwapSize", "'A'"]),
     ("axiom Box A; terminal T (1, 0); A = Scale(-1, 2) T;", ["Scale", "three"]),
     ("axiom Box A; terminal T (1, 0); A = RandomRule() { 0.5: T | 0.5: T };", ["RandomRule", "chance"]),
     ("axiom Box A; A = SubDiv(X) { -1: Nowhere };", ["unknown symbol", "Nowhere"]),
@@ -155,16 +155,41 @@ def test_translate_scale_random_rule_from_pga_match_the_data_table():
     assert len(kinds) == 3  # blocks (box), roofs and panels (quads) all chosen somewhere
 
 
-def test_skyscraper_from_its_file_matches_the_reference_evaluator(tmp_path):
-    """The reference's mc_skyscraper grammar (RandomRule, Scale, Translate,
-    SubDiv, Repeat, CompSplit, Extrude, Discard) lowered from its .pga file and
-    derived by the oracle gives the reference evaluator's terminals on the same
-    table, for axioms whose seeds and custom attributes reach every choice.
-    Lot sizes follow the reference's skyscraper scene
-    (src/test_runner/MC_Skyscrapers.cuh:88-101): side (round(2 seed) + 2) * 5,
-    height (round(3 seed) + 2) * 15; the grammar's absolute splits do not fit
-    arbitrary lots (the reference evaluator throws on those)."""
-    path = os.path.join(oracle.REFERENCE_ROOT, "src", "interpreter", "grammars", "mc_skyscraper", "grammar.pga")
+def _scene_lots(name, n, rng):
+    """(sizes, positions, seeds) of n lots as the reference's test-runner scene
+    for the grammar builds them (src/test_runner/*.cuh AxiomTraits): the
+    grammars' absolute splits and extents are written for those sizes, and the
+    reference evaluator throws on lots they do not fit."""
+    seed = rng.uniform(0.0, 1.0, n).astype(np.float32)
+    if name == "mc_skyscraper":  # MC_Skyscrapers.cuh:88-101
+        side = (np.round(2 * seed) + 2) * 5
+        size = np.stack([side, (np.round(3 * seed) + 2) * 15, side], 1)
+    elif name.startswith("3d_tree"):  # 3DTree_*.cuh: 16 x 16 x 16
+        size = np.full((n, 3), 16.0)
+    elif name == "mc_spaceship":  # MC_Spaceship.cuh
+        size = np.tile([5.0, 4.5, 8.0], (n, 1))
+    elif name == "commercial":  # Commercial.cuh
+        size = np.tile([30.0, 45.0, 30.0], (n, 1))
+    else:  # MengerSponge.cuh: unit cubes
+        size = np.ones((n, 3))
+    pos = rng.uniform(-200, 200, (n, 3)).astype(np.float32)
+    return size.astype(np.float32), pos, seed
+
+
+# The reference grammars this engine derives (every operator they use is one of
+# its operators) and the smallest terminal count expected for 12 lots.
+FROM_FILE = {"menger_sponge_3": 96_000, "mc_skyscraper": 1000, "3d_tree_4_3": 1000, "3d_tree_8_3": 100_000,
+             "3d_tree_12_2": 50_000, "mc_spaceship": 100, "commercial": 1000}
+
+
+@pytest.mark.parametrize("name", sorted(FROM_FILE))
+def test_reference_grammar_from_its_file_matches_the_reference_evaluator(name, tmp_path):
+    """A grammar the reference's interpreter ships, lowered from its .pga file
+    and derived by the oracle, gives the reference evaluator's terminals on the
+    same table bit for bit, for 12 lots whose seeds and custom attributes reach
+    the grammar's random choices.  Run where the reference sources are present;
+    no grammar file is copied into this repository."""
+    path = os.path.join(oracle.REFERENCE_ROOT, "src", "interpreter", "grammars", name, "grammar.pga")
     if not os.path.isfile(path) or not os.path.isfile(oracle.REF_HARNESS):
         pytest.skip("reference sources or the reference evaluator not present")
     import sys
@@ -172,23 +197,22 @@ def test_skyscraper_from_its_file_matches_the_reference_evaluator(tmp_path):
     sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
     import cases as C
 
-    b = dsl.load(open(path).read(), n_axioms=24)
+    b = dsl.load(open(path).read(), n_axioms=12)
     rng = np.random.default_rng(11)
-    seed = rng.uniform(0.0, 1.0, 24).astype(np.float32)
-    side = (np.round(2 * seed) + 2) * 5
-    height = (np.round(3 * seed) + 2) * 15
-    b["axioms"]["size"] = np.stack([side, height, side], 1)
-    b["axioms"]["position"] = rng.uniform(-200, 200, (24, 3)).astype(np.float32)
+    size, pos, seed = _scene_lots(name, 12, rng)
+    b["axioms"]["size"] = size
+    b["axioms"]["position"] = pos
     b["axioms"]["seed"] = seed
-    b["axioms"]["custom"] = rng.uniform(0.0, 1.0, 24).astype(np.float32)
+    b["axioms"]["custom"] = rng.uniform(0.0, 1.0, 12).astype(np.float32)
     bf, tf = str(tmp_path / "b.bin"), str(tmp_path / "t.bin")
     G.write_batch_file(bf, b["entries"], b["axioms"])
     oracle.run_reference(bf, tf)
     ref = G.read_terminal_file(tf)
     got = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
-    assert len(got) == len(ref) > 1000
+    assert len(got) == len(ref) >= FROM_FILE[name]
     assert C.digest(C.canonical(got)) == C.digest(C.canonical(ref))
-    assert len(set((got["rule"] >> 24).tolist())) >= 8  # the terminal kinds of columns, walls, windows, roofs
+    if name == "mc_skyscraper":
+        assert len(set((got["rule"] >> 24).tolist())) >= 8  # columns, walls, windows, roofs
 
 
 def test_reference_grammar_files_parse():
@@ -212,14 +236,13 @@ def test_reference_grammar_files_parse():
             continue
         ax = G.make_axioms(1)
         ax["shape"], ax["entry"] = roots[0]
-        # the skyscraper's absolute splits need a lot of the reference scene's size
-        ax["size"] = (10.0, 30.0, 10.0) if name.startswith("mc_skyscraper") else 1.0
+        ax["size"] = _scene_lots(name, 1, np.random.default_rng(0))[0]
         n = len(oracle.derive(G.DEFAULT_PROCS, entries, ax))
         assert n > 0
         if name.startswith("menger_sponge"):
             assert n == 8000  # the depth-3 sponge of a unit cube
         lowered += 1
-    assert lowered >= 2
+    assert lowered >= len(FROM_FILE)
 
 
 @pytest.mark.gpu

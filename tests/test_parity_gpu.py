@@ -345,11 +345,13 @@ def test_derive_to_host_reports_overflow():
     eng.release()
 
 
-@pytest.mark.parametrize("affine", [False, True], ids=["split_ops", "with_affine_ops"])
-def test_rich_random_grammars_fuzz(affine):
+@pytest.mark.parametrize("affine,rotate", [(False, False), (True, False), (True, True)],
+                         ids=["split_ops", "with_affine_ops", "with_rotate_ops"])
+def test_rich_random_grammars_fuzz(affine, rotate):
     """120 more seeds of the rich random grammar generator (all operators, both
     shapes, every parameter kind; with_affine_ops adds Translate, Scale and
-    RandomRule), each derived by the batched engine with leaf
+    RandomRule, with_rotate_ops also Rotate and Replicate, which run the
+    general-frame kernels), each derived by the batched engine with leaf
     children in place, with every child queued, and in the plain form, and
     compared bit for bit with the oracle.  Seeds the oracle rejects (grammars
     the reference would throw on) are skipped; statuses must then agree."""
@@ -362,7 +364,7 @@ def test_rich_random_grammars_fuzz(affine):
 
     checked = 0
     for seed in range(1000, 1120):
-        b = cases.rich_random(seed, affine=affine)
+        b = cases.rich_random(seed, affine=affine, rotate=rotate)
         try:
             ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
         except oracle.OracleError as err:
