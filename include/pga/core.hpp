@@ -7,9 +7,12 @@
  *   - PGA::Proc<ShapeT, OperatorT, NumThreadsT>           (include/pga/core/Proc.cuh:19-27)
  *   - PGA::Shapes::Box, Quad                              (include/pga/core/Shapes.cuh)
  *   - PGA::Operators::Subdivide, Repeat, ComponentSplit, Extrude, IfSizeLess,
- *     Generate, Discard                                    (Subdivide.cuh:22,170; Repeat.cuh:35-64;
+ *     Generate, Discard, Translate, Rotate, Scale, RandomRule, Replicate
+ *                                                          (Subdivide.cuh:22,170; Repeat.cuh:35-64;
  *                                                          ComponentSplit.cuh:234-270; Extrude.cuh:24;
- *                                                          If.cuh:60; Generate.cuh:23-49; Discard.cuh:15)
+ *                                                          If.cuh:60; Generate.cuh:23-49; Discard.cuh:15;
+ *                                                          Translate.cuh:24; Rotate.cuh:21; Scale.cuh:23;
+ *                                                          RandomRule.cuh:20,121; Replicate.cuh:19,92)
  *   - PGA::Operators::DCall, PSCall, FSCall                (Call.cuh:23-346)
  *   - PGA::Parameters::DynParam, DynParams, Scalar, AxisParam, RepeatModeParam,
  *     ShapeAttr, ShapePos, ShapeRotation, ShapeNormal, ShapeSize, ShapeSeed,
@@ -306,6 +309,16 @@ template <bool ParallelT, unsigned int GenFuncIdxT = 0, typename TerminalIdxT = 
           typename Attr5T = Parameters::Scalar<0>>
 class Generate {};
 class Discard {};
+template <typename XT, typename YT, typename ZT, typename NextOperatorT>
+class Translate {};
+template <typename XT, typename YT, typename ZT, typename NextOperatorT>
+class Rotate {};
+template <typename XT, typename YT, typename ZT, typename NextOperatorT>
+class Scale {};
+template <typename ChanceT, typename... Params1T>
+class RandomRule {};
+template <typename... Params1T>
+class Replicate {};
 
 }  // namespace Operators
 
@@ -510,6 +523,59 @@ template <typename ShapeT>
 struct LowerOp<Operators::Discard, ShapeT> {
   static void run(Builder& b, const PgaEntry&, uint32_t i) {
     set_entry(b, i, b.proc(PGA_OP_DISCARD, ShapeT::kind, 0), {}, {});
+  }
+};
+// Translate / Rotate / Scale<X, Y, Z, Next>: three parameters and the successor
+// on the same shape (Translate.cuh:24-43, Rotate.cuh:24-41, Scale.cuh:23-45).
+// Rotate's angles must be scalars when the engine is created.
+template <uint32_t Op, typename XT, typename YT, typename ZT, typename NextT, typename ShapeT>
+struct LowerXYZ {
+  static void run(Builder& b, const PgaEntry& src, uint32_t i) {
+    std::vector<PgaParameter> params{LowerParam<XT>::run(src), LowerParam<YT>::run(src), LowerParam<ZT>::run(src)};
+    std::vector<PgaSuccessor> succs{LowerSucc<NextT, ShapeT>::run(b, src)};
+    set_entry(b, i, b.proc(Op, ShapeT::kind, 0), params, succs);
+  }
+};
+template <typename XT, typename YT, typename ZT, typename NextT, typename ShapeT>
+struct LowerOp<Operators::Translate<XT, YT, ZT, NextT>, ShapeT> : LowerXYZ<PGA_OP_TRANSLATE, XT, YT, ZT, NextT, ShapeT> {};
+template <typename XT, typename YT, typename ZT, typename NextT, typename ShapeT>
+struct LowerOp<Operators::Rotate<XT, YT, ZT, NextT>, ShapeT> : LowerXYZ<PGA_OP_ROTATE, XT, YT, ZT, NextT, ShapeT> {};
+template <typename XT, typename YT, typename ZT, typename NextT, typename ShapeT>
+struct LowerOp<Operators::Scale<XT, YT, ZT, NextT>, ShapeT> : LowerXYZ<PGA_OP_SCALE, XT, YT, ZT, NextT, ShapeT> {};
+// RandomRule<DynParams>: chance and weights from the entry, successor j for weight j + 1 (RandomRule.cuh:121-150).
+template <typename... RestT, typename ShapeT>
+struct LowerOp<Operators::RandomRule<Parameters::DynParams, RestT...>, ShapeT> {
+  static void run(Builder& b, const PgaEntry& src, uint32_t i) {
+    std::vector<PgaParameter> params(src.parameters, src.parameters + src.numParameters);
+    std::vector<PgaSuccessor> succs(src.successors, src.successors + src.numSuccessors);
+    set_entry(b, i, b.proc(PGA_OP_RANDOM_RULE, ShapeT::kind, 0), params, succs);
+  }
+};
+// RandomRule<Chance, Pair<weight, successor>...>: the static form, with its own
+// selection rule (RandomRule.cuh:33-99): PGA_OP_RANDOM_RULE_STATIC.
+template <typename ChanceT, typename... PairsT, typename ShapeT>
+struct LowerOp<Operators::RandomRule<ChanceT, PairsT...>, ShapeT> {
+  static void run(Builder& b, const PgaEntry& src, uint32_t i) {
+    std::vector<PgaParameter> params{LowerParam<ChanceT>::run(src)};
+    std::vector<PgaSuccessor> succs;
+    StaticPairs<PairsT...>::template run<ShapeT>(b, src, params, succs);
+    set_entry(b, i, b.proc(PGA_OP_RANDOM_RULE_STATIC, ShapeT::kind, 0), params, succs);
+  }
+};
+// Replicate<DynParams>: every successor of the entry (Replicate.cuh:95-110).
+template <typename... RestT, typename ShapeT>
+struct LowerOp<Operators::Replicate<Parameters::DynParams, RestT...>, ShapeT> {
+  static void run(Builder& b, const PgaEntry& src, uint32_t i) {
+    std::vector<PgaSuccessor> succs(src.successors, src.successors + src.numSuccessors);
+    set_entry(b, i, b.proc(PGA_OP_REPLICATE, ShapeT::kind, 0), {}, succs);
+  }
+};
+// Replicate<Next...>: the shape once per listed operator (Replicate.cuh:21-79).
+template <typename... NextT, typename ShapeT>
+struct LowerOp<Operators::Replicate<NextT...>, ShapeT> {
+  static void run(Builder& b, const PgaEntry& src, uint32_t i) {
+    std::vector<PgaSuccessor> succs{LowerSucc<NextT, ShapeT>::run(b, src)...};
+    set_entry(b, i, b.proc(PGA_OP_REPLICATE, ShapeT::kind, 0), {}, succs);
   }
 };
 

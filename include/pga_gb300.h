@@ -84,7 +84,10 @@ typedef enum PgaOperator {
   PGA_OP_RANDOM_RULE = 10,     /* RandomRule<DynParams>: p0 chance (fractional part), p1.. weights, successor per weight */
   PGA_OP_ROTATE = 11,          /* Rotate<DynParam<0..2> degrees about x y z, DCall<0>>: model * rotateXYZ, in place;
                                   the angles must be scalars (the rotation is built once, at engine creation) */
-  PGA_OP_REPLICATE = 12        /* Replicate<DynParams>: the shape, unchanged, once per successor */
+  PGA_OP_REPLICATE = 12,       /* Replicate<DynParams>: the shape, unchanged, once per successor */
+  PGA_OP_RANDOM_RULE_STATIC = 13 /* RandomRule<Chance, Pair<weight, successor>...> (the static form): p0 chance,
+                                    p1.. weights; a zero weight is never picked and the last pair is taken when
+                                    no other is (RandomRule.cuh:33-99) */
 } PgaOperator;
 
 typedef enum PgaShape { PGA_SHAPE_BOX = 0, PGA_SHAPE_QUAD = 1 } PgaShape;
@@ -207,7 +210,10 @@ const char* pga_last_error(void);
  *  16 Box  Scale                        17 Quad Scale
  *  18 Box  RandomRule<DynParams>        19 Quad RandomRule<DynParams>
  *  20 Box  Rotate                       21 Quad Rotate
- *  22 Box  Replicate<DynParams>         23 Quad Replicate<DynParams> */
+ *  22 Box  Replicate<DynParams>         23 Quad Replicate<DynParams>
+ *  24 Box  RandomRule, 2 static pairs   25 Quad RandomRule, 2 static pairs
+ *  26 Box  RandomRule, 3 static pairs   27 Quad RandomRule, 3 static pairs
+ *  28 Box  RandomRule, 4 static pairs   29 Quad RandomRule, 4 static pairs */
 const PgaProc* pga_default_procs(uint32_t* numProcs);
 
 /* Replaces SinglePhaseEvaluator::initialize(DispatchTableEntry*, n)

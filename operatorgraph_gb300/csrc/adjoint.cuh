@@ -356,7 +356,7 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
       x.entry = succ_at(a, r.succBase + branch);
       continue;
     }
-    if (r.op == PGA_OP_RANDOM_RULE) {
+    if (r.op == PGA_OP_RANDOM_RULE || r.op == PGA_OP_RANDOM_RULE_STATIC) {
       const int pick = random_pick(a, r, x);
       if (pick < 0) return false;
       const int32_t nxt = succ_at(a, r.succBase + (uint32_t)pick);

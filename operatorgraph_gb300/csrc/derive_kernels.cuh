@@ -169,17 +169,28 @@ __device__ __forceinline__ void apply_scale(const DeriveArgs& a, const DevRule& 
 }
 
 // RandomRule<DynParams>::execute (RandomRule.cuh:121-150): chance = frac(p0);
-// the first successor whose running share of the weights p1.. reaches it, or
-// -1 when rounding leaves none (the shape is dropped).
+// the weights p1.. summed left to right; the first successor whose running
+// share reaches the chance, or -1 when rounding leaves none (the shape is
+// dropped).  The static form RandomRule<Chance, Pair<weight, next>...>
+// (RandomRule.cuh:33-99, PGA_OP_RANDOM_RULE_STATIC) sums the weights right to
+// left (p1 + (p2 + ...)), never picks a zero share and takes the last pair
+// when no other is picked.
 __device__ __forceinline__ int random_pick(const DeriveArgs& a, const DevRule& r, const Shape& x) {
   const float c0 = param(a, r, 0, x);
   const float chance = __fsub_rn(c0, floorf(c0));
+  const bool dyn = r.op == PGA_OP_RANDOM_RULE;
   float sum = 0.0f;
-  for (uint32_t i = 1; i < r.nParams; i++) sum = __fadd_rn(sum, param(a, r, i, x));
+  if (dyn) {
+    for (uint32_t i = 1; i < r.nParams; i++) sum = __fadd_rn(sum, param(a, r, i, x));
+  } else {
+    sum = param(a, r, r.nParams - 1u, x);
+    for (uint32_t i = r.nParams - 1u; i > 1; i--) sum = __fadd_rn(param(a, r, i - 1u, x), sum);
+  }
   float acc = 0.0f;
   for (uint32_t i = 1; i < r.nParams; i++) {
-    acc = __fadd_rn(acc, __fdiv_rn(param(a, r, i, x), sum));
-    if (chance <= acc) return (int)i - 1;
+    const float share = __fdiv_rn(param(a, r, i, x), sum);
+    acc = __fadd_rn(acc, share);
+    if (dyn ? (chance <= acc) : (i + 1 == r.nParams || (share != 0.0f && chance <= acc))) return (int)i - 1;
   }
   return -1;
 }
@@ -252,7 +263,8 @@ __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& 
         x.entry = succ_at(a, r.succBase);
         continue;
       }
-      case PGA_OP_RANDOM_RULE: {
+      case PGA_OP_RANDOM_RULE:
+      case PGA_OP_RANDOM_RULE_STATIC: {
         if (!AFF || r.nParams < 2 || r.nSucc + 1 < r.nParams) {
           raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
           return kNone;

@@ -24,9 +24,9 @@ PT_BLOCK = 16
 # PgaOperator
 OP_SUBDIVIDE, OP_SUBDIVIDE_STATIC, OP_REPEAT, OP_COMPONENT_SPLIT = 0, 1, 2, 3
 OP_EXTRUDE, OP_IF_SIZE_LESS, OP_GENERATE, OP_DISCARD = 4, 5, 6, 7
-OP_TRANSLATE, OP_SCALE, OP_RANDOM_RULE, OP_ROTATE, OP_REPLICATE = 8, 9, 10, 11, 12
+OP_TRANSLATE, OP_SCALE, OP_RANDOM_RULE, OP_ROTATE, OP_REPLICATE, OP_RANDOM_RULE_STATIC = 8, 9, 10, 11, 12, 13
 OP_NAMES = ["Subdivide", "SubdivideStatic", "Repeat", "ComponentSplit", "Extrude", "IfSizeLess", "Generate", "Discard",
-            "Translate", "Scale", "RandomRule", "Rotate", "Replicate"]
+            "Translate", "Scale", "RandomRule", "Rotate", "Replicate", "RandomRuleStatic"]
 
 SHAPE_BOX, SHAPE_QUAD = 0, 1
 
@@ -46,6 +46,8 @@ BOX_SCALE, QUAD_SCALE = 16, 17
 BOX_RANDOM_RULE, QUAD_RANDOM_RULE = 18, 19
 BOX_ROTATE, QUAD_ROTATE = 20, 21
 BOX_REPLICATE, QUAD_REPLICATE = 22, 23
+# RandomRule<DynParam<0>, Pair<DynParam<k>, DCall<k-1>>...> with 2, 3 and 4 pairs (the static form)
+BOX_RANDOM_RULE2, QUAD_RANDOM_RULE2, BOX_RANDOM_RULE3, QUAD_RANDOM_RULE3, BOX_RANDOM_RULE4, QUAD_RANDOM_RULE4 = range(24, 30)
 
 PARAM_DT = np.dtype([("type", "<i4"), ("value", "<f4", (MAX_VALUES,))])
 SUCC_DT = np.dtype([("entryIndex", "<i4"), ("phaseIndex", "<i4")])
@@ -75,6 +77,9 @@ DEFAULT_PROCS = np.array([
     (OP_RANDOM_RULE, SHAPE_BOX, 0, 1), (OP_RANDOM_RULE, SHAPE_QUAD, 0, 1),
     (OP_ROTATE, SHAPE_BOX, 0, 1), (OP_ROTATE, SHAPE_QUAD, 0, 1),
     (OP_REPLICATE, SHAPE_BOX, 0, 1), (OP_REPLICATE, SHAPE_QUAD, 0, 1),
+    (OP_RANDOM_RULE_STATIC, SHAPE_BOX, 2, 1), (OP_RANDOM_RULE_STATIC, SHAPE_QUAD, 2, 1),
+    (OP_RANDOM_RULE_STATIC, SHAPE_BOX, 3, 1), (OP_RANDOM_RULE_STATIC, SHAPE_QUAD, 3, 1),
+    (OP_RANDOM_RULE_STATIC, SHAPE_BOX, 4, 1), (OP_RANDOM_RULE_STATIC, SHAPE_QUAD, 4, 1),
 ], dtype=PROC_DT)
 
 

@@ -607,6 +607,33 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
       }
       return;
     }
+    case PGA_OP_RANDOM_RULE_STATIC: {
+      // RandomRule<Chance, Pair<P, Next>...>::execute (RandomRule.cuh:33-99):
+      // getProbabilitiesSum recurses as p1 + (p2 + (... + pn)); each pair's
+      // normalised share is added to the running sum and the pair is taken
+      // when the share is nonzero and the chance is within the sum; the last
+      // pair is taken unconditionally.
+      if (e.numParameters < 2) { fail(c, PGA_ERR_BAD_PARAM, s.entry); return; }
+      float c0 = float(dyn_eval(c, blk, s, e.parameters[0]));
+      float chance = c0 - std::floor(c0);
+      const uint32_t n = e.numParameters - 1;
+      F sum = dyn_eval(c, blk, s, e.parameters[n]);
+      for (uint32_t i = n - 1; i >= 1; i--) sum = dyn_eval(c, blk, s, e.parameters[i]) + sum;
+      F acc = F(0);
+      for (uint32_t i = 1; i <= n; i++) {
+        F share = dyn_eval(c, blk, s, e.parameters[i]) / sum;
+        acc += share;
+        if (i == n || (share != F(0) && F(chance) <= acc)) {
+          int32_t nxt;
+          if (!successor<F>(c, e, i - 1, s.entry, nxt)) return;
+          s.entry = nxt;
+          s.path = child_path(s.path, i - 1, nxt);
+          dispatch(c, o, s);
+          return;
+        }
+      }
+      return;
+    }
     case PGA_OP_ROTATE: {
       // Rotate<X, Y, Z, Next>::execute (Rotate.cuh:24-41): the angles in
       // degrees, times pi / 180 in float, setModel(model * rotateXYZ(angles))

@@ -94,7 +94,7 @@ template <> struct GenerationFunction<HarnessFilter, 1> {
 };
 }  // namespace PGA
 
-// Operator codes 0..23 (see pga_default_procs() in include/pga_gb300.h).
+// Operator codes 0..29 (see pga_default_procs() in include/pga_gb300.h).
 struct HarnessProcs : T::List<
   /* 0 */ Proc<Box, Subdivide<DynParams>, 1>,
   /* 1 */ Proc<Quad, Subdivide<DynParams>, 1>,
@@ -119,7 +119,17 @@ struct HarnessProcs : T::List<
   /* 20 */ Proc<Box, Rotate<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
   /* 21 */ Proc<Quad, Rotate<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
   /* 22 */ Proc<Box, Replicate<DynParams>, 1>,
-  /* 23 */ Proc<Quad, Replicate<DynParams>, 1>
+  /* 23 */ Proc<Quad, Replicate<DynParams>, 1>,
+  /* 24 */ Proc<Box, RandomRule<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>>, 1>,
+  /* 25 */ Proc<Quad, RandomRule<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>>, 1>,
+  /* 26 */ Proc<Box, RandomRule<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>,
+                                T::Pair<DynParam<3>, DCall<2>>>, 1>,
+  /* 27 */ Proc<Quad, RandomRule<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>,
+                                 T::Pair<DynParam<3>, DCall<2>>>, 1>,
+  /* 28 */ Proc<Box, RandomRule<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>,
+                                T::Pair<DynParam<3>, DCall<2>>, T::Pair<DynParam<4>, DCall<3>>>, 1>,
+  /* 29 */ Proc<Quad, RandomRule<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>,
+                                 T::Pair<DynParam<3>, DCall<2>>, T::Pair<DynParam<4>, DCall<3>>>, 1>
 > {};
 
 #pragma pack(push, 1)

@@ -126,6 +126,74 @@ struct ProcedureList
               Proc<Box, Generate<false, 1, DynParam<0>>, 1>> {};
 }  // namespace calls
 
+namespace random_static_dyn {
+// The static RandomRule with DynParam weights and DCall successors (2, 3 and 4
+// pairs, both shapes) plus ComponentSplit / Generate / Discard: the same
+// grammar as tests/golden/cases.py random_static_mix, procedure for procedure.
+template <typename ShapeT, typename... PairsT>
+using RR = Proc<ShapeT, RandomRule<DynParam<0>, PairsT...>, 1>;
+using P1 = T::Pair<DynParam<1>, DCall<0>>;
+using P2 = T::Pair<DynParam<2>, DCall<1>>;
+using P3 = T::Pair<DynParam<3>, DCall<2>>;
+using P4 = T::Pair<DynParam<4>, DCall<3>>;
+struct ProcedureList
+    : T::List<RR<Box, P1, P2, P3>,                                            // 0
+              Proc<Box, Generate<false, 1, DynParam<0>>, 1>,                  // 1
+              Proc<Box, ComponentSplit<false, DCall<0>, DCall<1>, DCall<2>>, 1>,  // 2
+              RR<Box, P1, P2, P3, P4>,                                        // 3
+              RR<Quad, P1, P2>,                                               // 4
+              Proc<Quad, Discard, 1>,                                         // 5
+              RR<Quad, P1, P2, P3>,                                           // 6
+              Proc<Quad, Generate<false, 1, DynParam<0>>, 1>,                 // 7
+              RR<Quad, P1, P2, P3, P4>> {};                                   // 8
+
+DispatchTable table() {
+  using P = DispatchTable::Parameter;
+  auto s = [](double v) { return P{PT_SCALAR, {v}}; };
+  const P seed{PT_SHAPE_ATTR, {15}}, custom{PT_SHAPE_ATTR, {16}}, rnd{PT_RAND, {0.0, 1.0}};
+  return DispatchTable{
+      {0, {seed, s(0.333), s(0.333), s(0.333)}, {{1, 0}, {2, 0}, {3, 0}}},
+      {1, {s(0)}, {}},
+      {2, {}, {{4, 0}, {5, 0}, {6, 0}}},
+      {3, {custom, s(0.1), s(0.2), s(0.3), s(0.15)}, {{1, 0}, {7, 0}, {8, 0}, {9, 0}}},
+      {4, {seed, s(0.0), s(1.0)}, {{10, 0}, {11, 0}}},
+      {5, {}, {}},
+      {6, {rnd, s(2.0), s(0.0), s(1.0)}, {{10, 0}, {11, 0}, {12, 0}}},
+      {1, {s(1)}, {}},
+      {1, {s(2)}, {}},
+      {1, {s(3)}, {}},
+      {7, {s(4)}, {}},
+      {7, {s(5)}, {}},
+      {8, {custom, s(0.25), s(0.25), s(0.25), s(0.25)}, {{10, 0}, {11, 0}, {13, 0}, {11, 0}}},
+      {7, {s(6)}, {}},
+  };
+}
+}  // namespace random_static_dyn
+
+namespace rotate_static {
+// One procedure, statically chained: a box replicated into an unrotated
+// copy, a copy turned 90 degrees about y then split along x (the second piece
+// turned -37 degrees about z), and a copy turned (30, -47.5, 12.25) degrees
+// then split into faces; the top face turned 45 degrees, translated by
+// (0.5, size_y / 2, -0.25), scaled to (x / 2, 2, 1) and extruded to 0.75; the
+// sides replicated into the face itself and a copy turned (90, 90, 0).
+using Gen0 = Generate<false, 1, Scalar<0>>;
+using QGen1 = Generate<false, 1, Scalar<1>>;
+using Turned = Rotate<Scalar<0>, Scalar<0>, Scalar<-37>, Gen0>;
+using Top = Rotate<Scalar<0>, Scalar<0>, Scalar<45>,
+                   Translate<Scalar<5, 1>, Exp<ShapeSize<Y>, Scalar<5, 1>, Multi>, Scalar<-25, 2>,
+                             Scale<Scalar<-5, 1>, Scalar<2>, Scalar<1>, Extrude<AxisParam<X>, Scalar<75, 2>, Gen0>>>>;
+using Sides = Replicate<QGen1, Rotate<Scalar<90>, Scalar<90>, Scalar<0>, QGen1>>;
+struct ProcedureList
+    : T::List<Proc<Box,
+                   Replicate<Gen0,
+                             Rotate<Scalar<0>, Scalar<90>, Scalar<0>,
+                                    Subdivide<AxisParam<X>, T::Pair<Scalar<-1>, Gen0>, T::Pair<Scalar<-2>, Turned>>>,
+                             Rotate<Scalar<30>, Scalar<-475, 1>, Scalar<1225, 2>,
+                                    ComponentSplit<false, Top, Discard, Sides>>>,
+                   1>> {};
+}  // namespace rotate_static
+
 namespace bad {
 // Triangle-mesh generation (GenFuncIdx 0) is outside the engine.
 struct ProcedureList : T::List<Proc<Box, Generate<false, 0, Scalar<0>>, 1>> {};
@@ -176,6 +244,8 @@ int main(int argc, char** argv) {
   scene<building_static::ProcedureList<ADJUST_TO_FILL>>(f, "building_static_m2", building_static::table());
   scene<building_exp::ProcedureList>(f, "building_exp", building_static::table());
   scene<calls::ProcedureList>(f, "menger_calls", menger::table());
+  scene<random_static_dyn::ProcedureList>(f, "random_static_dyn", random_static_dyn::table());
+  scene<rotate_static::ProcedureList>(f, "rotate_static", building_static::table());
   scene<bad::ProcedureList>(f, "triangle_mesh", DispatchTable{{0, {}, {}}});
   scene<menger::ProcedureList>(f, "bad_dynparam", DispatchTable{{2, {}, {{1, 0}, {2, 0}}}});
   std::fclose(f);

@@ -147,6 +147,47 @@ def rotate_mix():
     return _single(tab, ax, "rotate_mix")
 
 
+def random_static_mix():
+    """The static RandomRule<Chance, Pair<weight, next>...> (RandomRule.cuh:33-99):
+    two, three and four pairs on both shapes; weights summed right to left;
+    shares that do not reach one (the last pair is then taken anyway); a zero
+    first weight (never taken, unlike the DynParams form, which takes it at
+    chance 0); chances from the seed, the custom attribute and a random range;
+    64 axioms whose seeds include 0, values just below 1 and values >= 1."""
+    tab = DispatchTable([
+        Entry(G.BOX_RANDOM_RULE3, [shape_attr(15), scalar(0.333), scalar(0.333), scalar(0.333)],
+              [(1, 0), (2, 0), (3, 0)]),                                                                   # 0
+        Entry(G.BOX_GENERATE, [scalar(0)], []),                                                           # 1
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(4, 0), (5, 0), (6, 0)]),                                       # 2
+        Entry(G.BOX_RANDOM_RULE4, [shape_attr(16), scalar(0.1), scalar(0.2), scalar(0.3), scalar(0.15)],
+              [(1, 0), (7, 0), (8, 0), (9, 0)]),                                                          # 3
+        Entry(G.QUAD_RANDOM_RULE2, [shape_attr(15), scalar(0.0), scalar(1.0)], [(10, 0), (11, 0)]),      # 4
+        Entry(G.QUAD_DISCARD, [], []),                                                                    # 5
+        Entry(G.QUAD_RANDOM_RULE3, [rand(0.0, 1.0), scalar(2.0), scalar(0.0), scalar(1.0)],
+              [(10, 0), (11, 0), (12, 0)]),                                                               # 6
+        Entry(G.BOX_GENERATE, [scalar(1)], []),                                                           # 7
+        Entry(G.BOX_GENERATE, [scalar(2)], []),                                                           # 8
+        Entry(G.BOX_GENERATE, [scalar(3)], []),                                                           # 9
+        Entry(G.QUAD_GENERATE, [scalar(4)], []),                                                          # 10
+        Entry(G.QUAD_GENERATE, [scalar(5)], []),                                                          # 11
+        Entry(G.QUAD_RANDOM_RULE4, [shape_attr(16), scalar(0.25), scalar(0.25), scalar(0.25), scalar(0.25)],
+              [(10, 0), (11, 0), (13, 0), (11, 0)]),                                                      # 12
+        Entry(G.QUAD_GENERATE, [scalar(6)], []),                                                          # 13
+    ]).to_array()
+    rng = np.random.default_rng(17)
+    n = 64
+    ax = G.make_axioms(n)
+    ax["size"] = rng.uniform(0.5, 3.0, (n, 3)).astype(np.float32)
+    ax["position"] = rng.uniform(-20, 20, (n, 3)).astype(np.float32)
+    seeds = rng.uniform(0.0, 3.0, n).astype(np.float32)
+    seeds[:8] = [0.0, 1.0, 0.333, 0.666, 0.999, np.nextafter(np.float32(1), np.float32(0)), 2.0, 0.3329999]
+    ax["seed"] = seeds
+    custom = rng.uniform(0.0, 1.0, n).astype(np.float32)
+    custom[:6] = [0.0, 0.1, 0.3, 0.6, 0.75, np.nextafter(np.float32(1), np.float32(0))]
+    ax["custom"] = custom
+    return _single(tab, ax, "random_static_mix")
+
+
 def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False):
     """A random grammar over all eight operators and both shapes: a DAG of
     rules `depth` levels deep (rules of a level reused with some probability),
@@ -322,6 +363,7 @@ def cases():
         b = rich_random(seed, affine=True)
         out.append((b["name"], b))
     out.append(("rotate_mix", rotate_mix()))
+    out.append(("random_static_mix", random_static_mix()))
     for seed in ROTATE_SEEDS:
         b = rich_random(seed, affine=True, rotate=True)
         out.append((b["name"], b))

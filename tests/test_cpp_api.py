@@ -136,6 +136,61 @@ def test_static_calls_follow_the_table(lowered):
     _same_bits(_derive(procs, entries, b["axioms"]), _derive(G.DEFAULT_PROCS, scenes.menger_table(0.05), b["axioms"]))
 
 
+def test_static_random_rule_with_dynamic_pairs_is_bit_exact(lowered):
+    """RandomRule<DynParam<0>, Pair<DynParam<k>, DCall<k-1>>...> lowers to the
+    static-form operator with the entry's chance, weights and successors: the
+    same table as the golden random_static_mix case (whose fixture came from
+    the reference's evaluator), so the terminals match bit for bit."""
+    import sys
+
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    import cases as C
+
+    procs, entries, nuser = lowered["random_static_dyn"]
+    b = C.random_static_mix()
+    assert nuser == len(entries) == len(b["entries"])
+    assert {int(p["op"]) for p in procs} >= {G.OP_RANDOM_RULE_STATIC, G.OP_COMPONENT_SPLIT}
+    _same_bits(_derive(procs, entries, b["axioms"]), _derive(G.DEFAULT_PROCS, b["entries"], b["axioms"]))
+
+
+def _rotate_static_table():
+    """tests/cpp/lower_scenes.cpp rotate_static built as data."""
+    from operatorgraph_gb300.grammar import DispatchTable, Entry, scalar
+
+    return DispatchTable([
+        Entry(G.BOX_REPLICATE, [], [(1, 0), (2, 0), (5, 0)]),                                      # 0
+        Entry(G.BOX_GENERATE, [scalar(0)], []),                                                    # 1
+        Entry(G.BOX_ROTATE, [scalar(0), scalar(90), scalar(0)], [(3, 0)]),                         # 2
+        Entry(G.BOX_SUBDIVIDE, [scalar(0), scalar(-1), scalar(-2)], [(1, 0), (4, 0)]),             # 3
+        Entry(G.BOX_ROTATE, [scalar(0), scalar(0), scalar(-37)], [(1, 0)]),                        # 4
+        Entry(G.BOX_ROTATE, [scalar(30), scalar(-47.5), scalar(12.25)], [(6, 0)]),                 # 5
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(7, 0), (12, 0), (13, 0)]),                              # 6
+        Entry(G.QUAD_ROTATE, [scalar(0), scalar(0), scalar(45)], [(8, 0)]),                        # 7
+        Entry(G.QUAD_TRANSLATE, [scalar(0.5), G.exp(("a", 13), ("s", 0.5), ("op", G.OPT_MULTI)), scalar(-0.25)],
+              [(9, 0)]),                                                                            # 8
+        Entry(G.QUAD_SCALE, [scalar(-0.5), scalar(2), scalar(1)], [(10, 0)]),                      # 9
+        Entry(G.QUAD_EXTRUDE, [scalar(0), scalar(0.75)], [(11, 0)]),                               # 10
+        Entry(G.BOX_GENERATE, [scalar(0)], []),                                                    # 11
+        Entry(G.QUAD_DISCARD, [], []),                                                             # 12
+        Entry(G.QUAD_REPLICATE, [], [(14, 0), (15, 0)]),                                           # 13
+        Entry(G.QUAD_GENERATE, [scalar(1)], []),                                                   # 14
+        Entry(G.QUAD_ROTATE, [scalar(90), scalar(90), scalar(0)], [(14, 0)]),                      # 15
+    ]).to_array()
+
+
+def test_static_rotate_replicate_chain_matches(lowered):
+    procs, entries, nuser = lowered["rotate_static"]
+    assert nuser == 1 and len(entries) > 10
+    ax = G.make_axioms(6)
+    rng = np.random.default_rng(5)
+    ax["size"] = rng.uniform(1.0, 4.0, (6, 3)).astype(np.float32)
+    ax["position"] = rng.uniform(-10, 10, (6, 3)).astype(np.float32)
+    got = _derive(procs, entries, ax)
+    want = _derive(G.DEFAULT_PROCS, _rotate_static_table(), ax)
+    assert len(got) == len(want) == 6 * 12  # copy, 2 pieces, top, 4 sides x 2
+    assert (_multiset(got) == _multiset(want)).all()
+
+
 def test_unsupported_forms_are_lowering_errors(lowered):
     assert "instanced" in lowered["triangle_mesh"]
     assert "DynParam<0>" in lowered["bad_dynparam"]
