@@ -527,6 +527,32 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["mixed65536_terminals_per_s"] = n_mx / (res["mixed65536_ms"] * 1e-3)
     em.release()
     del mout
+    # Forest: 4096 trees (Rotate with arbitrary angles, Replicate, Translate,
+    # Scale: the general-frame kernels), about 13.4M terminals in one launch.
+    fo = scenes.forest(4096)
+    fcap = 14_000_000
+    eo = Engine(fo["entries"], node_capacity=1 << 23, max_terminals=fcap)
+    d_fo = torch.from_numpy(fo["axioms"].view(np.uint8).copy()).to(dev)
+    fout = torch.empty((fcap, 64), dtype=torch.uint8, device=dev)
+    ts = []
+    for it in range(7):
+        flush.fill_(3)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eo.derive_raw(d_fo.data_ptr(), 4096, None, fout.data_ptr(), fcap, count.data_ptr())
+        b.record(stream)
+        torch.cuda.synchronize()
+        if it >= 2:
+            ts.append(a.elapsed_time(b))
+    rep = eo.report()
+    assert rep["status"] == 0, rep
+    n_fo = int(count.item())
+    res["forest4096_terminals"] = n_fo
+    res["forest4096_ms"] = statistics.median(ts)
+    res["forest4096_terminals_per_s"] = n_fo / (res["forest4096_ms"] * 1e-3)
+    res["forest4096_roofline_frac"] = 64.0 * n_fo / (res["forest4096_ms"] * 1e-3) / 1e9 / peak
+    eo.release()
+    del fout
     return res
 
 

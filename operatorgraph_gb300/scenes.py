@@ -21,6 +21,12 @@ returns a dict with ``entries`` (ENTRY_DT array), ``axioms`` (AXIOM_DT array),
 * random_grammars(): 64-rule random grammars (branching U{2..6}, IfSizeLess
   thresholds U[0.01, 0.2], Discard probability 0.15, depth cap 12).
 * mixed(n): 40 % Menger (depth 1-3), 40 % city buildings, 20 % random grammars.
+* forest(n): n trees on a 64-wide grid (pitch 40 m), boxes 2 x 16 x 2 m
+  turned by a per-tree angle about y; a trunk and a crown that forks into
+  three branches (Replicate) turned 35 degrees out and 0 / 120 / 240 degrees
+  around the stem, each 0.6 of its parent's size, until a branch is shorter
+  than 0.5 m (a leaf).  Rotate with arbitrary angles: the general-frame
+  kernels.
 """
 import math
 
@@ -239,3 +245,43 @@ def mixed(n=65536, seed=99, menger_depths=(1, 2, 3), num_random_grammars=16):
             ax[j]["entry"] = offs[len(menger_tables) + 1 + rand_pick[j]]
             ax[j]["size"] = (1.0, 1.0, 1.0)
     return _batch(entries, ax, name=f"mixed({n})")
+
+
+def forest_table(angles=(0.0, 22.5, 45.0, 67.5)):
+    """Tree grammar with Rotate / Replicate / Translate / Scale / IfSizeLess;
+    entries 0..len(angles)-1 are the roots, one per base angle about y."""
+    k = len(angles)
+    half = G.exp(("a", 13), ("s", 0.5), ("op", G.OPT_MULTI))  # half the branch length
+    # entries after the roots
+    TRUNK, CROWN, BRANCH, LEAF, FORK = k, k + 1, k + 2, k + 3, k + 4
+    entries = [Entry(G.BOX_ROTATE, [scalar(0), scalar(a), scalar(0)], [(k + 5, 0)]) for a in angles]
+    rest = [
+        Entry(G.BOX_SCALE, [scalar(-0.5), scalar(-0.5), scalar(-0.5)], [(k + 9, 0)]),        # TRUNK
+        Entry(G.BOX_TRANSLATE, [scalar(0), half, scalar(0)], [(BRANCH, 0)]),                  # CROWN
+        Entry(G.BOX_IF_SIZE_LESS, [scalar(1), scalar(0.5)], [(LEAF, 0), (FORK, 0)]),         # BRANCH
+        Entry(G.BOX_GENERATE, [scalar(1)], []),                                               # LEAF
+        Entry(G.BOX_REPLICATE, [], [(k + 6, 0), (k + 7, 0), (k + 8, 0), (TRUNK, 0)]),         # FORK
+        Entry(G.BOX_REPLICATE, [], [(TRUNK, 0), (CROWN, 0)]),                                 # k + 5: tree
+    ]
+    for i, yaw in enumerate((0.0, 120.0, 240.0)):
+        # k + 6 + 3 i: turn around the stem, tilt out, shrink, move up by half the new length
+        rest.append(Entry(G.BOX_ROTATE, [scalar(0), scalar(yaw), scalar(35)], [(k + 10 + 2 * i, 0)]))
+    rest.append(Entry(G.BOX_GENERATE, [scalar(0)], []))                                       # k + 9: trunk piece
+    for i in range(3):
+        rest.append(Entry(G.BOX_SCALE, [scalar(-0.6), scalar(-0.6), scalar(-0.6)], [(k + 11 + 2 * i, 0)]))
+        rest.append(Entry(G.BOX_TRANSLATE, [scalar(0), half, scalar(0)], [(BRANCH, 0)]))
+    # fix the three forks' successors (k + 6 .. k + 8 point at k + 10, 12, 14)
+    return DispatchTable(entries + rest).to_array()
+
+
+def forest(n=4096, seed=4321, cols=64, pitch=40.0):
+    angles = (0.0, 22.5, 45.0, 67.5)
+    rng = np.random.default_rng(seed)
+    ax = G.make_axioms(n)
+    i = np.arange(n)
+    ax["position"][:, 0] = (i % cols) * pitch
+    ax["position"][:, 2] = (i // cols) * pitch
+    ax["size"] = (2.0, 16.0, 2.0)
+    ax["entry"] = rng.integers(0, len(angles), n)
+    ax["seed"] = rng.uniform(0.0, 1.0, n).astype(np.float32)
+    return _batch(forest_table(angles), ax, name=f"forest({n})")

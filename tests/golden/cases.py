@@ -364,6 +364,7 @@ def cases():
         out.append((b["name"], b))
     out.append(("rotate_mix", rotate_mix()))
     out.append(("random_static_mix", random_static_mix()))
+    out.append(("forest_4", scenes.forest(4)))
     for seed in ROTATE_SEEDS:
         b = rich_random(seed, affine=True, rotate=True)
         out.append((b["name"], b))

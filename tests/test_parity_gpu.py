@@ -345,6 +345,24 @@ def test_derive_to_host_reports_overflow():
     eng.release()
 
 
+def test_forest_general_frames_bit_exact():
+    """256 trees of the forest scene (Rotate with arbitrary angles, Replicate,
+    Translate, Scale, IfSizeLess: the general-frame kernels, 840k terminals)
+    in the persistent, queued and plain forms against the oracle, bit for bit
+    including path hashes."""
+    from operatorgraph_gb300.engine import terminals_to_numpy
+
+    b = scenes.forest(256)
+    ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    assert len(ref) == 256 * 3281
+    for form in ("persistent", "queued", "plain"):
+        eng = _engine(b["entries"], no_inline=form == "queued")
+        out, n, rep = eng.execute(b["axioms"], capacity=len(ref), plain=form == "plain")
+        assert rep["status"] == 0, (form, rep)
+        _assert_same(terminals_to_numpy(out, n), ref)
+        eng.release()
+
+
 @pytest.mark.parametrize("affine,rotate", [(False, False), (True, False), (True, True)],
                          ids=["split_ops", "with_affine_ops", "with_rotate_ops"])
 def test_rich_random_grammars_fuzz(affine, rotate):
