@@ -7,12 +7,14 @@
  *   - PGA::Proc<ShapeT, OperatorT, NumThreadsT>           (include/pga/core/Proc.cuh:19-27)
  *   - PGA::Shapes::Box, Quad                              (include/pga/core/Shapes.cuh)
  *   - PGA::Operators::Subdivide, Repeat, ComponentSplit, Extrude, IfSizeLess,
- *     Generate, Discard, Translate, Rotate, Scale, RandomRule, Replicate
+ *     Generate, Discard, Translate, Rotate, Scale, RandomRule, Replicate, If,
+ *     SwapSize
  *                                                          (Subdivide.cuh:22,170; Repeat.cuh:35-64;
  *                                                          ComponentSplit.cuh:234-270; Extrude.cuh:24;
  *                                                          If.cuh:60; Generate.cuh:23-49; Discard.cuh:15;
  *                                                          Translate.cuh:24; Rotate.cuh:21; Scale.cuh:23;
- *                                                          RandomRule.cuh:20,121; Replicate.cuh:19,92)
+ *                                                          RandomRule.cuh:20,121; Replicate.cuh:19,92;
+ *                                                          If.cuh:22; SwapSize.cuh:20)
  *   - PGA::Operators::DCall, PSCall, FSCall                (Call.cuh:23-346)
  *   - PGA::Parameters::DynParam, DynParams, Scalar, AxisParam, RepeatModeParam,
  *     ShapeAttr, ShapePos, ShapeRotation, ShapeNormal, ShapeSize, ShapeSeed,
@@ -319,6 +321,10 @@ template <typename ChanceT, typename... Params1T>
 class RandomRule {};
 template <typename... Params1T>
 class Replicate {};
+template <typename ExpressionT, typename NextOperatorIfTrueT, typename NextOperatorIfFalseT>
+class If {};
+template <typename XT, typename YT, typename ZT, typename NextOperatorT>
+class SwapSize {};
 
 }  // namespace Operators
 
@@ -542,6 +548,17 @@ template <typename XT, typename YT, typename ZT, typename NextT, typename ShapeT
 struct LowerOp<Operators::Rotate<XT, YT, ZT, NextT>, ShapeT> : LowerXYZ<PGA_OP_ROTATE, XT, YT, ZT, NextT, ShapeT> {};
 template <typename XT, typename YT, typename ZT, typename NextT, typename ShapeT>
 struct LowerOp<Operators::Scale<XT, YT, ZT, NextT>, ShapeT> : LowerXYZ<PGA_OP_SCALE, XT, YT, ZT, NextT, ShapeT> {};
+template <typename XT, typename YT, typename ZT, typename NextT, typename ShapeT>
+struct LowerOp<Operators::SwapSize<XT, YT, ZT, NextT>, ShapeT> : LowerXYZ<PGA_OP_SWAP_SIZE, XT, YT, ZT, NextT, ShapeT> {};
+// If<Expression, True, False> (If.cuh:22-49).
+template <typename ExprT, typename TrueT, typename FalseT, typename ShapeT>
+struct LowerOp<Operators::If<ExprT, TrueT, FalseT>, ShapeT> {
+  static void run(Builder& b, const PgaEntry& src, uint32_t i) {
+    std::vector<PgaParameter> params{LowerParam<ExprT>::run(src)};
+    std::vector<PgaSuccessor> succs{LowerSucc<TrueT, ShapeT>::run(b, src), LowerSucc<FalseT, ShapeT>::run(b, src)};
+    set_entry(b, i, b.proc(PGA_OP_IF, ShapeT::kind, 0), params, succs);
+  }
+};
 // RandomRule<DynParams>: chance and weights from the entry, successor j for weight j + 1 (RandomRule.cuh:121-150).
 template <typename... RestT, typename ShapeT>
 struct LowerOp<Operators::RandomRule<Parameters::DynParams, RestT...>, ShapeT> {

@@ -87,7 +87,9 @@ typedef enum PgaOperator {
   PGA_OP_REPLICATE = 12,       /* Replicate<DynParams>: the shape, unchanged, once per successor */
   PGA_OP_RANDOM_RULE_STATIC = 13 /* RandomRule<Chance, Pair<weight, successor>...> (the static form): p0 chance,
                                     p1.. weights; a zero weight is never picked and the last pair is taken when
-                                    no other is (RandomRule.cuh:33-99) */
+                                    no other is (RandomRule.cuh:33-99) */,
+  PGA_OP_IF = 14,              /* If<DynParam<0> condition, DCall<0> true, DCall<1> false>: nonzero is true */
+  PGA_OP_SWAP_SIZE = 15        /* SwapSize<DynParam<0..2> axes, DCall<0>>: size = (size[a0], size[a1], size[a2]) */
 } PgaOperator;
 
 typedef enum PgaShape { PGA_SHAPE_BOX = 0, PGA_SHAPE_QUAD = 1 } PgaShape;
@@ -213,7 +215,9 @@ const char* pga_last_error(void);
  *  22 Box  Replicate<DynParams>         23 Quad Replicate<DynParams>
  *  24 Box  RandomRule, 2 static pairs   25 Quad RandomRule, 2 static pairs
  *  26 Box  RandomRule, 3 static pairs   27 Quad RandomRule, 3 static pairs
- *  28 Box  RandomRule, 4 static pairs   29 Quad RandomRule, 4 static pairs */
+ *  28 Box  RandomRule, 4 static pairs   29 Quad RandomRule, 4 static pairs
+ *  30 Box  If                           31 Quad If
+ *  32 Box  SwapSize                     33 Quad SwapSize */
 const PgaProc* pga_default_procs(uint32_t* numProcs);
 
 /* Replaces SinglePhaseEvaluator::initialize(DispatchTableEntry*, n)

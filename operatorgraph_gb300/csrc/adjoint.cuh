@@ -25,7 +25,8 @@
 //  Extrude    size (s0, extent, s1).
 //  Translate  t' = t + R v: t and s pass through, dL/dv_k = R[:, k] . g_t.
 //  Scale      s'_k = -v_k s_k (v_k < 0), v_k (v_k > 0), 0 (v_k = 0).
-//  IfSizeLess, RandomRule  discrete: the gradient passes through unchanged.
+//  SwapSize   s'_k = s[a_k]: dL/ds[a] = sum of g_k over the k with a_k = a.
+//  IfSizeLess, If, RandomRule  discrete: the gradient passes through unchanged.
 //  Generate   M[:, j] = R[:, j] s_j, M[:, 3] = t.
 
 namespace pga {
@@ -312,7 +313,7 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
 // Recomputes the shape created as child `ordinal` of `link` (an item or an
 // axiom) and replays its 1 -> 1 chain until `stopAt` (a terminal: the Generate
 // rule; an item: its branching rule).  The smooth steps (Extrude, Translate,
-// Scale) are recorded so that the reverse pass can undo them; a chain with
+// Scale, SwapSize) are recorded so that the reverse pass can undo them; a chain with
 // more than kChainSteps of them has no adjoint (PGA_ERR_NO_TAPE).
 constexpr int kChainSteps = 8;
 struct Chain {
@@ -364,15 +365,23 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
       x.entry = nxt;
       continue;
     }
-    if (r.op == PGA_OP_TRANSLATE || r.op == PGA_OP_SCALE) {
+    if (r.op == PGA_OP_IF) {
+      const uint32_t branch = (param(a, r, 0, x) != 0.0f) ? 0u : 1u;
+      x.path = child_path(x.path, branch, succ_at(a, r.succBase + branch));
+      x.entry = succ_at(a, r.succBase + branch);
+      continue;
+    }
+    if (r.op == PGA_OP_TRANSLATE || r.op == PGA_OP_SCALE || r.op == PGA_OP_SWAP_SIZE) {
       if (ch.n >= kChainSteps) return false;
       ch.entry[ch.n] = x.entry;
       ch.before[ch.n] = x;
       ch.n++;
       if (r.op == PGA_OP_TRANSLATE)
         apply_translate(a, r, x);
-      else
+      else if (r.op == PGA_OP_SCALE)
         apply_scale(a, r, x);
+      else if (!swap_size(a, r, x))
+        return false;
       x.entry = succ_at(a, r.succBase);
       continue;
     }
@@ -424,6 +433,12 @@ __device__ void push_back_replayed(const DeriveArgs& a, const AdjArgs& j, uint32
         dv[q] = (v[q] < 0.0f) ? -xb.s[q] : (v[q] > 0.0f ? 1.0f : 0.0f);
       }
       for (uint32_t q = 0; q < 3; q++) param_grad(a, j, r, q, xb, g.s[q] * dv[q], &gb);
+    } else if (r.op == PGA_OP_SWAP_SIZE) {
+      // after[k] = before[axis_k]: each component's gradient goes back to the axis it was read from
+      const uint32_t a0 = f2u(param(a, r, 0, xb)), a1 = f2u(param(a, r, 1, xb)), a2 = f2u(param(a, r, 2, xb));
+#pragma unroll
+      for (uint32_t q = 0; q < 3; q++)
+        gb.s[q] = (a0 == q ? g.s[0] : 0.0f) + (a1 == q ? g.s[1] : 0.0f) + (a2 == q ? g.s[2] : 0.0f);
     } else {  // Extrude: after = (s0, extent, s1)
       gb.s[0] = g.s[0];
       gb.s[1] = g.s[2];

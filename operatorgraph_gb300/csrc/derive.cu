@@ -154,7 +154,7 @@ static void rotate_xyz(float x, float y, float z, float q[9]) {
   q[8] = ca * cb;
 }
 
-static const PgaProc kDefaultProcs[30] = {
+static const PgaProc kDefaultProcs[34] = {
     {PGA_OP_SUBDIVIDE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SUBDIVIDE, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_BOX, 3, 1}, {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_QUAD, 3, 1},
     {PGA_OP_REPEAT, PGA_SHAPE_BOX, 0, 1},           {PGA_OP_REPEAT, PGA_SHAPE_QUAD, 0, 1},
@@ -170,6 +170,8 @@ static const PgaProc kDefaultProcs[30] = {
     {PGA_OP_RANDOM_RULE_STATIC, PGA_SHAPE_BOX, 2, 1}, {PGA_OP_RANDOM_RULE_STATIC, PGA_SHAPE_QUAD, 2, 1},
     {PGA_OP_RANDOM_RULE_STATIC, PGA_SHAPE_BOX, 3, 1}, {PGA_OP_RANDOM_RULE_STATIC, PGA_SHAPE_QUAD, 3, 1},
     {PGA_OP_RANDOM_RULE_STATIC, PGA_SHAPE_BOX, 4, 1}, {PGA_OP_RANDOM_RULE_STATIC, PGA_SHAPE_QUAD, 4, 1},
+    {PGA_OP_IF, PGA_SHAPE_BOX, 0, 1},               {PGA_OP_IF, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_SWAP_SIZE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SWAP_SIZE, PGA_SHAPE_QUAD, 0, 1},
 };
 
 extern "C" {
@@ -179,7 +181,7 @@ const char* pga_version(void) { return "pga_gb300 0.1.0 (sm_103a)"; }
 const char* pga_last_error(void) { return g_error.c_str(); }
 
 const PgaProc* pga_default_procs(uint32_t* numProcs) {
-  if (numProcs) *numProcs = 30;
+  if (numProcs) *numProcs = 34;
   return kDefaultProcs;
 }
 
@@ -239,7 +241,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     r.op = 0xFF;
     if (en.operatorCode >= 0 && (uint32_t)en.operatorCode < table->numProcs) {
       const PgaProc& p = table->procs[en.operatorCode];
-      if (p.op <= PGA_OP_RANDOM_RULE_STATIC && p.shape <= PGA_SHAPE_QUAD) {
+      if (p.op <= PGA_OP_SWAP_SIZE && p.shape <= PGA_SHAPE_QUAD) {
         r.op = (uint8_t)p.op;
         r.shape = (uint8_t)p.shape;
         r.nChildren = p.numChildren;
@@ -331,7 +333,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   }
   for (const DevRule& r : e->hRules) {
     if (r.op == PGA_OP_TRANSLATE || r.op == PGA_OP_SCALE || r.op == PGA_OP_RANDOM_RULE || r.op == PGA_OP_ROTATE ||
-        r.op == PGA_OP_REPLICATE || r.op == PGA_OP_RANDOM_RULE_STATIC)
+        r.op == PGA_OP_REPLICATE || r.op == PGA_OP_RANDOM_RULE_STATIC || r.op == PGA_OP_IF || r.op == PGA_OP_SWAP_SIZE)
       e->affineKernel = true;
     if (r.op == PGA_OP_ROTATE) e->generalFrames = true;
   }

@@ -195,6 +195,22 @@ __device__ __forceinline__ int random_pick(const DeriveArgs& a, const DevRule& r
   return -1;
 }
 
+// SwapSize<X, Y, Z, Next>::execute (SwapSize.cuh:20-38): size = (size[x],
+// size[y], size[z]) for the axes the parameters name (truncated toward zero);
+// an axis above 2 is an error (the reference would read past the vector).
+__device__ __forceinline__ bool swap_size(const DeriveArgs& a, const DevRule& r, Shape& x) {
+  const uint32_t ax = f2u(param(a, r, 0, x)), ay = f2u(param(a, r, 1, x)), az = f2u(param(a, r, 2, x));
+  if (ax > 2 || ay > 2 || az > 2) {
+    raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+    return false;
+  }
+  const float sx = pick3(x.s, ax), sy = pick3(x.s, ay), sz = pick3(x.s, az);
+  x.s[0] = sx;
+  x.s[1] = sy;
+  x.s[2] = sz;
+  return true;
+}
+
 // Resolves a freshly created shape through IfSizeLess / Extrude / Translate /
 // Scale / RandomRule rules (If.cuh:65-89, Extrude.cuh:29-56, Translate.cuh:24-43,
 // Scale.cuh:23-45, RandomRule.cuh:121-150) until it reaches a Generate (terminal), a
@@ -274,6 +290,22 @@ __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& 
         const int32_t nxt = succ_at(a, r.succBase + (uint32_t)pick);
         x.path = child_path(x.path, (uint32_t)pick, nxt);
         x.entry = nxt;
+        continue;
+      }
+      case PGA_OP_IF: {
+        // If<Expression, True, False>::execute (If.cuh:22-49): a nonzero value
+        // takes the first successor.
+        if (!AFF || r.nParams < 1 || r.nSucc < 2) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        const uint32_t branch = (param(a, r, 0, x) != 0.0f) ? 0u : 1u;
+        const int32_t nxt = succ_at(a, r.succBase + branch);
+        x.path = child_path(x.path, branch, nxt);
+        x.entry = nxt;
+        continue;
+      }
+      case PGA_OP_SWAP_SIZE: {
+        if (!AFF || r.nParams < 3 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        if (!swap_size(a, r, x)) return kNone;
+        x.entry = succ_at(a, r.succBase);
         continue;
       }
 #if PGA_GENERAL_FRAMES

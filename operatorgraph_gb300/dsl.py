@@ -26,12 +26,12 @@ Lowered operators, with the reference generator's parameter layouts
 (DispatchTableGenerator.cpp:266-440, 541-554): SubDiv (axis, factors...) as
 the dynamic Subdivide, Repeat (axis, extent, mode), CompSplit (successors top,
 bottom, sides), Extrude (axis slot, extent), IfSizeLess (axis, size; true,
-false), Translate (x, y, z), Scale (x, y, z), Rotate (x, y, z degrees),
-RandomRule (chance, weights...; one successor per weight), Replicate
-(successors), Discard, and terminals as Generate (terminal index; only the
-instanced generation function 1).  The others (SwapSize, If, SetAs...) parse
-but are not engine operators: lowering raises DslError naming the operator and
-the rule.  A rule applied to both a Box and a
+false), If (condition; true, false), Translate (x, y, z), Scale (x, y, z),
+Rotate (x, y, z degrees), SwapSize (three axes), RandomRule (chance,
+weights...; one successor per weight), Replicate (successors), Discard, and
+terminals as Generate (terminal index; only the instanced generation function
+1).  The others (the prism SetAs operators, IfCollides...) parse but are not
+engine operators: lowering raises DslError naming the operator and the rule.  A rule applied to both a Box and a
 Quad is lowered once per shape.
 """
 import re
@@ -46,7 +46,7 @@ MODES = {"ANCHOR_TO_START": G.ANCHOR_TO_START, "ANCHOR_TO_END": G.ANCHOR_TO_END,
 SHAPES = {"Box": G.SHAPE_BOX, "Quad": G.SHAPE_QUAD}
 BRANCHING = {"SubDiv", "CompSplit", "IfSizeLess", "If", "Replicate", "RandomRule"}
 SUPPORTED = {"SubDiv", "Repeat", "CompSplit", "Extrude", "IfSizeLess", "Discard", "Translate", "Scale", "RandomRule",
-             "Rotate", "Replicate"}
+             "Rotate", "Replicate", "If", "SwapSize"}
 
 
 class DslError(ValueError):
@@ -390,7 +390,7 @@ class _Lowering:
             extent = _param(args[-1])
             axis = _param(args[0]) if len(args) > 1 else G.scalar(0.0)  # the axis slot is unused
             self.entries[i] = G.Entry(G.QUAD_EXTRUDE, [axis, extent], [(self.chain(rest, G.SHAPE_BOX, rule), 0)])
-        elif name in ("Translate", "Scale", "Rotate"):
+        elif name in ("Translate", "Scale", "Rotate", "SwapSize"):
             if not rest:
                 raise DslError(f"{where}: {name} needs a successor")
             if len(args) < 3:
@@ -399,6 +399,8 @@ class _Lowering:
                 op = G.BOX_TRANSLATE if box else G.QUAD_TRANSLATE
             elif name == "Scale":
                 op = G.BOX_SCALE if box else G.QUAD_SCALE
+            elif name == "SwapSize":
+                op = G.BOX_SWAP_SIZE if box else G.QUAD_SWAP_SIZE
             else:
                 op = G.BOX_ROTATE if box else G.QUAD_ROTATE
             self.entries[i] = G.Entry(op, [_param(a) for a in args[:3]], [(self.chain(rest, shape, rule), 0)])
@@ -415,6 +417,11 @@ class _Lowering:
                 raise DslError(f"{where}: Replicate needs successors ({{ a | b | ... }})")
             succ = [(self.chain(c, shape, rule), 0) for _, c in block]
             self.entries[i] = G.Entry(G.BOX_REPLICATE if box else G.QUAD_REPLICATE, [], succ)
+        elif name == "If":
+            succ = [(self.chain(c, shape, rule), 0) for _, c in block]
+            if len(succ) != 2 or not args:
+                raise DslError(f"{where}: If takes a condition and two successors (true | false)")
+            self.entries[i] = G.Entry(G.BOX_IF if box else G.QUAD_IF, [_param(args[0])], succ)
         elif name == "IfSizeLess":
             succ = [(self.chain(c, shape, rule), 0) for _, c in block]
             if len(succ) != 2:

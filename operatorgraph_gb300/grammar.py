@@ -25,8 +25,9 @@ PT_BLOCK = 16
 OP_SUBDIVIDE, OP_SUBDIVIDE_STATIC, OP_REPEAT, OP_COMPONENT_SPLIT = 0, 1, 2, 3
 OP_EXTRUDE, OP_IF_SIZE_LESS, OP_GENERATE, OP_DISCARD = 4, 5, 6, 7
 OP_TRANSLATE, OP_SCALE, OP_RANDOM_RULE, OP_ROTATE, OP_REPLICATE, OP_RANDOM_RULE_STATIC = 8, 9, 10, 11, 12, 13
+OP_IF, OP_SWAP_SIZE = 14, 15
 OP_NAMES = ["Subdivide", "SubdivideStatic", "Repeat", "ComponentSplit", "Extrude", "IfSizeLess", "Generate", "Discard",
-            "Translate", "Scale", "RandomRule", "Rotate", "Replicate", "RandomRuleStatic"]
+            "Translate", "Scale", "RandomRule", "Rotate", "Replicate", "RandomRuleStatic", "If", "SwapSize"]
 
 SHAPE_BOX, SHAPE_QUAD = 0, 1
 
@@ -48,6 +49,8 @@ BOX_ROTATE, QUAD_ROTATE = 20, 21
 BOX_REPLICATE, QUAD_REPLICATE = 22, 23
 # RandomRule<DynParam<0>, Pair<DynParam<k>, DCall<k-1>>...> with 2, 3 and 4 pairs (the static form)
 BOX_RANDOM_RULE2, QUAD_RANDOM_RULE2, BOX_RANDOM_RULE3, QUAD_RANDOM_RULE3, BOX_RANDOM_RULE4, QUAD_RANDOM_RULE4 = range(24, 30)
+BOX_IF, QUAD_IF = 30, 31
+BOX_SWAP_SIZE, QUAD_SWAP_SIZE = 32, 33
 
 PARAM_DT = np.dtype([("type", "<i4"), ("value", "<f4", (MAX_VALUES,))])
 SUCC_DT = np.dtype([("entryIndex", "<i4"), ("phaseIndex", "<i4")])
@@ -80,6 +83,8 @@ DEFAULT_PROCS = np.array([
     (OP_RANDOM_RULE_STATIC, SHAPE_BOX, 2, 1), (OP_RANDOM_RULE_STATIC, SHAPE_QUAD, 2, 1),
     (OP_RANDOM_RULE_STATIC, SHAPE_BOX, 3, 1), (OP_RANDOM_RULE_STATIC, SHAPE_QUAD, 3, 1),
     (OP_RANDOM_RULE_STATIC, SHAPE_BOX, 4, 1), (OP_RANDOM_RULE_STATIC, SHAPE_QUAD, 4, 1),
+    (OP_IF, SHAPE_BOX, 0, 1), (OP_IF, SHAPE_QUAD, 0, 1),
+    (OP_SWAP_SIZE, SHAPE_BOX, 0, 1), (OP_SWAP_SIZE, SHAPE_QUAD, 0, 1),
 ], dtype=PROC_DT)
 
 

@@ -607,6 +607,36 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
       }
       return;
     }
+    case PGA_OP_IF: {
+      // If<Expression, True, False>::execute (If.cuh:22-49): the first
+      // successor when the value is nonzero, else the second.
+      if (!param_ok<F>(c, e, 0, s.entry)) return;
+      const bool yes = dyn_eval(c, blk, s, e.parameters[0]) != F(0);
+      int32_t nxt;
+      if (!successor<F>(c, e, yes ? 0 : 1, s.entry, nxt)) return;
+      s.path = child_path(s.path, yes ? 0u : 1u, nxt);
+      s.entry = nxt;
+      dispatch(c, o, s);
+      return;
+    }
+    case PGA_OP_SWAP_SIZE: {
+      // SwapSize<X, Y, Z, Next>::execute (SwapSize.cuh:20-38): the size's
+      // components re-read along the three axes (host truncation).
+      if (!param_ok<F>(c, e, 2, s.entry)) return;
+      unsigned ax[3];
+      for (int k = 0; k < 3; k++) {
+        const float v = float(dyn_eval(c, blk, s, e.parameters[k]));
+        ax[k] = v > 0.0f ? static_cast<unsigned>(v) : 0u;
+        if (ax[k] > 2) { fail(c, PGA_ERR_BAD_PARAM, s.entry); return; }
+      }
+      int32_t nxt;
+      if (!successor<F>(c, e, 0, s.entry, nxt)) return;
+      const F sz[3] = {s.size[ax[0]], s.size[ax[1]], s.size[ax[2]]};
+      for (int k = 0; k < 3; k++) s.size[k] = sz[k];
+      s.entry = nxt;
+      dispatch(c, o, s);
+      return;
+    }
     case PGA_OP_RANDOM_RULE_STATIC: {
       // RandomRule<Chance, Pair<P, Next>...>::execute (RandomRule.cuh:33-99):
       // getProbabilitiesSum recurses as p1 + (p2 + (... + pn)); each pair's

@@ -33,6 +33,7 @@
 #include <pga/core/Replicate.cuh>
 #include <pga/core/Rotate.cuh>
 #include <pga/core/Scale.cuh>
+#include <pga/core/SwapSize.cuh>
 #include <pga/core/ShapeGenerator.cuh>
 #include <pga/core/Subdivide.cuh>
 #include <pga/core/TStdLib.h>
@@ -94,7 +95,7 @@ template <> struct GenerationFunction<HarnessFilter, 1> {
 };
 }  // namespace PGA
 
-// Operator codes 0..29 (see pga_default_procs() in include/pga_gb300.h).
+// Operator codes 0..33 (see pga_default_procs() in include/pga_gb300.h).
 struct HarnessProcs : T::List<
   /* 0 */ Proc<Box, Subdivide<DynParams>, 1>,
   /* 1 */ Proc<Quad, Subdivide<DynParams>, 1>,
@@ -129,7 +130,11 @@ struct HarnessProcs : T::List<
   /* 28 */ Proc<Box, RandomRule<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>,
                                 T::Pair<DynParam<3>, DCall<2>>, T::Pair<DynParam<4>, DCall<3>>>, 1>,
   /* 29 */ Proc<Quad, RandomRule<DynParam<0>, T::Pair<DynParam<1>, DCall<0>>, T::Pair<DynParam<2>, DCall<1>>,
-                                 T::Pair<DynParam<3>, DCall<2>>, T::Pair<DynParam<4>, DCall<3>>>, 1>
+                                 T::Pair<DynParam<3>, DCall<2>>, T::Pair<DynParam<4>, DCall<3>>>, 1>,
+  /* 30 */ Proc<Box, If<DynParam<0>, DCall<0>, DCall<1>>, 1>,
+  /* 31 */ Proc<Quad, If<DynParam<0>, DCall<0>, DCall<1>>, 1>,
+  /* 32 */ Proc<Box, SwapSize<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 33 */ Proc<Quad, SwapSize<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>
 > {};
 
 #pragma pack(push, 1)

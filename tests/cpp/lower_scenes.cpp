@@ -194,6 +194,20 @@ struct ProcedureList
                    1>> {};
 }  // namespace rotate_static
 
+namespace if_swap_static {
+// If on an expression (size x > 1.5): the sizes cycled (y, z, x) then a box
+// terminal; otherwise split along x into a terminal and a piece whose sizes
+// are swapped (x, z, y) before it becomes a terminal of index 1.
+using Gen0 = Generate<false, 1, Scalar<0>>;
+using Gen1 = Generate<false, 1, Scalar<1>>;
+struct ProcedureList
+    : T::List<Proc<Box,
+                   If<Exp<ShapeSize<X>, Scalar<15, 1>, Gt>, SwapSize<AxisParam<Y>, AxisParam<Z>, AxisParam<X>, Gen0>,
+                      Subdivide<AxisParam<X>, T::Pair<Scalar<-1>, Gen0>,
+                                T::Pair<Scalar<-1>, SwapSize<AxisParam<X>, AxisParam<Z>, AxisParam<Y>, Gen1>>>>,
+                   1>> {};
+}  // namespace if_swap_static
+
 namespace bad {
 // Triangle-mesh generation (GenFuncIdx 0) is outside the engine.
 struct ProcedureList : T::List<Proc<Box, Generate<false, 0, Scalar<0>>, 1>> {};
@@ -246,6 +260,7 @@ int main(int argc, char** argv) {
   scene<calls::ProcedureList>(f, "menger_calls", menger::table());
   scene<random_static_dyn::ProcedureList>(f, "random_static_dyn", random_static_dyn::table());
   scene<rotate_static::ProcedureList>(f, "rotate_static", building_static::table());
+  scene<if_swap_static::ProcedureList>(f, "if_swap_static", building_static::table());
   scene<bad::ProcedureList>(f, "triangle_mesh", DispatchTable{{0, {}, {}}});
   scene<menger::ProcedureList>(f, "bad_dynparam", DispatchTable{{2, {}, {{1, 0}, {2, 0}}}});
   std::fclose(f);

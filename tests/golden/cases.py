@@ -188,7 +188,41 @@ def random_static_mix():
     return _single(tab, ax, "random_static_mix")
 
 
-def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False):
+def if_swap_mix():
+    """If<Expression, True, False> (If.cuh:22-49) and SwapSize (SwapSize.cuh:20-38):
+    conditions from comparisons of the size and the seed, a logical and, a
+    plain shape attribute (nonzero is true) and scalars; SwapSize as a cyclic
+    permutation, a swap, and with a repeated axis, on both shapes."""
+    gt = G.OPT_GT
+    tab = DispatchTable([
+        Entry(G.BOX_IF, [G.exp(("a", 12), ("s", 1.5), ("op", gt))], [(1, 0), (4, 0)]),                 # 0
+        Entry(G.BOX_SWAP_SIZE, [scalar(1), scalar(2), scalar(0)], [(2, 0)]),                            # 1
+        Entry(G.BOX_SUBDIVIDE, [scalar(0), scalar(-1), scalar(-1)], [(3, 0), (5, 0)]),                  # 2
+        Entry(G.BOX_GENERATE, [scalar(0)], []),                                                         # 3
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(6, 0), (7, 0), (8, 0)]),                                     # 4
+        Entry(G.BOX_IF, [shape_attr(15)], [(9, 0), (3, 0)]),                                            # 5
+        Entry(G.QUAD_SWAP_SIZE, [scalar(1), scalar(0), scalar(2)], [(10, 0)]),                          # 6
+        Entry(G.QUAD_DISCARD, [], []),                                                                  # 7
+        Entry(G.QUAD_IF, [G.exp(("a", 13), ("s", 1.0), ("op", gt), ("a", 15), ("s", 0.5), ("op", gt),
+                                ("op", G.OPT_AND))], [(11, 0), (12, 0)]),                               # 8
+        Entry(G.BOX_SWAP_SIZE, [scalar(2), scalar(2), scalar(1)], [(3, 0)]),                            # 9
+        Entry(G.QUAD_GENERATE, [scalar(1)], []),                                                        # 10
+        Entry(G.QUAD_IF, [scalar(0)], [(7, 0), (13, 0)]),                                               # 11
+        Entry(G.QUAD_EXTRUDE, [scalar(0), scalar(0.5)], [(14, 0)]),                                     # 12
+        Entry(G.QUAD_GENERATE, [scalar(2)], []),                                                        # 13
+        Entry(G.BOX_IF, [scalar(1)], [(9, 0), (3, 0)]),                                                 # 14
+    ]).to_array()
+    rng = np.random.default_rng(23)
+    n = 12
+    ax = G.make_axioms(n)
+    ax["size"] = rng.uniform(0.5, 3.0, (n, 3)).astype(np.float32)
+    ax["position"] = rng.uniform(-20, 20, (n, 3)).astype(np.float32)
+    ax["seed"] = rng.uniform(0.0, 1.0, n).astype(np.float32)
+    ax["seed"][:2] = 0.0
+    return _single(tab, ax, "if_swap_mix")
+
+
+def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False, more=False):
     """A random grammar over all eight operators and both shapes: a DAG of
     rules `depth` levels deep (rules of a level reused with some probability),
     with scalar, random-range, shape-attribute and expression parameters,
@@ -197,8 +231,9 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False):
     attribute, IfSizeLess on scalars and expressions, constant and random
     terminal indices.  Seeds >= 1 and custom attributes vary per axiom.
     With affine=True the grammar also draws Translate, Scale and RandomRule
-    rules, with rotate=True also Rotate and Replicate rules (the defaults draw
-    exactly the grammars they always drew)."""
+    rules, with rotate=True also Rotate and Replicate rules, with more=True also
+    If and SwapSize rules (the defaults draw exactly the grammars they always
+    drew)."""
     rng = np.random.default_rng(seed)
     BOX, QUAD = G.SHAPE_BOX, G.SHAPE_QUAD
     GEN = {BOX: G.BOX_GENERATE, QUAD: G.QUAD_GENERATE}
@@ -212,6 +247,8 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False):
     RRU = {BOX: G.BOX_RANDOM_RULE, QUAD: G.QUAD_RANDOM_RULE}
     ROT = {BOX: G.BOX_ROTATE, QUAD: G.QUAD_ROTATE}
     REPL = {BOX: G.BOX_REPLICATE, QUAD: G.QUAD_REPLICATE}
+    IFX = {BOX: G.BOX_IF, QUAD: G.QUAD_IF}
+    SWP = {BOX: G.BOX_SWAP_SIZE, QUAD: G.QUAD_SWAP_SIZE}
     entries = []
     made = {}
 
@@ -247,6 +284,8 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False):
             ops += ["tr", "sc", "rr"]
         if rotate:
             ops += ["rot", "repl"]
+        if more:
+            ops += ["if", "swap"]
         op = ops[int(rng.integers(0, len(ops)))]
         if op == "sub":
             k = int(rng.integers(2, 5))
@@ -295,6 +334,19 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False):
             ang = [scalar(float(rng.choice([0.0, 90.0, -90.0, 180.0]))) if rng.random() < 0.4 else
                    scalar(round(float(rng.uniform(-180.0, 180.0)), 2)) for _ in range(3)]
             e = add(Entry(ROT[kind], ang, [(make(kind, level + 1), 0)]))
+        elif op == "if":
+            u = rng.random()
+            if u < 0.5:
+                cond = G.exp(("a", 12 + int(rng.integers(0, 2))), ("s", float(rng.uniform(0.3, 1.5))),
+                             ("op", G.OPT_GT if rng.random() < 0.5 else G.OPT_LT))
+            elif u < 0.8:
+                cond = G.exp(("a", 15), ("s", 0.5), ("op", G.OPT_GEQ))
+            else:
+                cond = scalar(float(rng.integers(0, 2)))
+            e = add(Entry(IFX[kind], [cond], [(make(kind, level + 1), 0), (make(kind, level + 1), 0)]))
+        elif op == "swap":
+            axes = [scalar(int(rng.integers(0, 3))) for _ in range(3)]
+            e = add(Entry(SWP[kind], axes, [(make(kind, level + 1), 0)]))
         elif op == "repl":
             k = int(rng.integers(2, 4))
             e = add(Entry(REPL[kind], [], [(make(kind, level + 1), 0) for _ in range(k)]))
@@ -317,7 +369,7 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False):
     ax["position"] = rng.uniform(-10.0, 10.0, (n_axioms, 3)).astype(np.float32)
     ax["seed"] = rng.uniform(0.0, 3.0, n_axioms).astype(np.float32)
     ax["custom"] = rng.uniform(0.5, 3.0, n_axioms).astype(np.float32)
-    name = "rich_rotate" if rotate else ("rich_affine" if affine else "rich_random")
+    name = "rich_more" if more else ("rich_rotate" if rotate else ("rich_affine" if affine else "rich_random"))
     return _single(tab, ax, f"{name}_{seed}")
 
 
@@ -335,6 +387,11 @@ AFFINE_SEEDS = (2, 3, 5, 12, 13, 19, 27, 29, 49, 58)
 # they use Rotate (right angles and arbitrary ones) and Replicate on both
 # shapes, mixed with every other operator.
 ROTATE_SEEDS = (3, 6, 8, 13, 24, 47, 58, 71, 73, 75)
+
+# Seeds of rich_random(affine=True, more=True) with golden fixtures: together
+# they use If (expression, attribute and scalar conditions) and SwapSize on
+# both shapes.
+MORE_SEEDS = (0, 3, 4, 18, 19, 20, 34, 47, 49, 50)
 
 
 def cases():
@@ -365,6 +422,10 @@ def cases():
     out.append(("rotate_mix", rotate_mix()))
     out.append(("random_static_mix", random_static_mix()))
     out.append(("forest_4", scenes.forest(4)))
+    out.append(("if_swap_mix", if_swap_mix()))
+    for seed in MORE_SEEDS:
+        b = rich_random(seed, affine=True, more=True)
+        out.append((b["name"], b))
     for seed in ROTATE_SEEDS:
         b = rich_random(seed, affine=True, rotate=True)
         out.append((b["name"], b))

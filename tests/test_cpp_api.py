@@ -191,6 +191,27 @@ def test_static_rotate_replicate_chain_matches(lowered):
     assert (_multiset(got) == _multiset(want)).all()
 
 
+def test_static_if_swap_size_chain_matches(lowered):
+    from operatorgraph_gb300.grammar import DispatchTable, Entry, scalar
+
+    procs, entries, _ = lowered["if_swap_static"]
+    tab = DispatchTable([
+        Entry(G.BOX_IF, [G.exp(("a", 12), ("s", 1.5), ("op", G.OPT_GT))], [(1, 0), (3, 0)]),
+        Entry(G.BOX_SWAP_SIZE, [scalar(1), scalar(2), scalar(0)], [(2, 0)]),
+        Entry(G.BOX_GENERATE, [scalar(0)], []),
+        Entry(G.BOX_SUBDIVIDE, [scalar(0), scalar(-1), scalar(-1)], [(2, 0), (4, 0)]),
+        Entry(G.BOX_SWAP_SIZE, [scalar(0), scalar(2), scalar(1)], [(5, 0)]),
+        Entry(G.BOX_GENERATE, [scalar(1)], []),
+    ]).to_array()
+    ax = G.make_axioms(8)
+    rng = np.random.default_rng(9)
+    ax["size"] = rng.uniform(0.5, 3.0, (8, 3)).astype(np.float32)
+    got = _derive(procs, entries, ax)
+    want = _derive(G.DEFAULT_PROCS, tab, ax)
+    assert len(got) == len(want) > 8
+    assert (_multiset(got) == _multiset(want)).all()
+
+
 def test_unsupported_forms_are_lowering_errors(lowered):
     assert "instanced" in lowered["triangle_mesh"]
     assert "DynParam<0>" in lowered["bad_dynparam"]

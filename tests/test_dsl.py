@@ -90,7 +90,8 @@ def test_a_rule_used_on_both_shapes_is_lowered_per_shape():
 
 
 @pytest.mark.parametrize("text, words", [
-    ("axiom Box A; A = SwapSize(Y, X, Z) B; B = Discard();", ["SwapSize", "'A'"]),
+    ("axiom Box A; A = SetAsDynamicConvexRightPrism((0, 0.5), (-0.5, -0.5), (0.5, -0.5)) B; B = Discard();",
+     ["SetAsDynamicConvexRightPrism", "'A'"]),
     ("axiom Box A; terminal T (1, 0); A = Scale(-1, 2) T;", ["Scale", "three"]),
     ("axiom Box A; terminal T (1, 0); A = RandomRule() { 0.5: T | 0.5: T };", ["RandomRule", "chance"]),
     ("axiom Box A; A = SubDiv(X) { -1: Nowhere };", ["unknown symbol", "Nowhere"]),

@@ -363,13 +363,15 @@ def test_forest_general_frames_bit_exact():
         eng.release()
 
 
-@pytest.mark.parametrize("affine,rotate", [(False, False), (True, False), (True, True)],
-                         ids=["split_ops", "with_affine_ops", "with_rotate_ops"])
-def test_rich_random_grammars_fuzz(affine, rotate):
+@pytest.mark.parametrize("affine,rotate,more", [(False, False, False), (True, False, False), (True, True, False),
+                                               (True, False, True)],
+                         ids=["split_ops", "with_affine_ops", "with_rotate_ops", "with_if_swap_ops"])
+def test_rich_random_grammars_fuzz(affine, rotate, more):
     """120 more seeds of the rich random grammar generator (all operators, both
     shapes, every parameter kind; with_affine_ops adds Translate, Scale and
     RandomRule, with_rotate_ops also Rotate and Replicate, which run the
-    general-frame kernels), each derived by the batched engine with leaf
+    general-frame kernels, with_if_swap_ops If and SwapSize), each derived by
+    the batched engine with leaf
     children in place, with every child queued, and in the plain form, and
     compared bit for bit with the oracle.  Seeds the oracle rejects (grammars
     the reference would throw on) are skipped; statuses must then agree."""
@@ -382,7 +384,7 @@ def test_rich_random_grammars_fuzz(affine, rotate):
 
     checked = 0
     for seed in range(1000, 1120):
-        b = cases.rich_random(seed, affine=affine, rotate=rotate)
+        b = cases.rich_random(seed, affine=affine, rotate=rotate, more=more)
         try:
             ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
         except oracle.OracleError as err:
