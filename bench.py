@@ -553,6 +553,43 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["forest4096_roofline_frac"] = 64.0 * n_fo / (res["forest4096_ms"] * 1e-3) / 1e9 / peak
     eo.release()
     del fout
+    # Triangle meshes of the city (walls, windows and roofs as triangle-mesh
+    # terminals: 5.86M quads): pga_generate_meshes alone, from derived records.
+    cm = scenes.city(4096, meshes=True)
+    ec = Engine(cm["entries"], node_capacity=1 << 22, max_terminals=6_000_000)
+    d_cm = torch.from_numpy(cm["axioms"].view(np.uint8).copy()).to(dev)
+    cout = torch.empty((6_000_000, 64), dtype=torch.uint8, device=dev)
+    ec.derive_raw(d_cm.data_ptr(), 4096, None, cout.data_ptr(), 6_000_000, count.data_ptr())
+    torch.cuda.synchronize()
+    n_cm = int(count.item())
+    caps = [(4 * n_cm, 6 * n_cm)] * 3
+    vbufs = [torch.empty((mv, 48), dtype=torch.uint8, device=dev) for mv, _ in caps]
+    ibufs = [torch.empty((mi,), dtype=torch.int32, device=dev) for _, mi in caps]
+    table = np.array([(0, 0, mv, mi, v.data_ptr(), i.data_ptr()) for (mv, mi), v, i in zip(caps, vbufs, ibufs)],
+                     dtype=G.MESH_DT)
+    d_table = torch.from_numpy(table.view(np.uint8).copy()).to(dev)
+    ts = []
+    for it in range(8):
+        d_table.view(-1, 32)[:, :8].zero_()  # numVertices, numIndices
+        flush.fill_(4)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ec.generate_meshes_raw(cout.data_ptr(), n_cm, d_table.data_ptr(), 3, stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if it >= 3:
+            ts.append(a.elapsed_time(b))
+    rep = ec.report()
+    assert rep["status"] == 0, rep
+    nv = int(d_table.cpu().numpy().view(G.MESH_DT)["numVertices"].sum())
+    assert nv == 4 * n_cm, (nv, n_cm)
+    mesh_bytes = 64.0 * n_cm + 48.0 * nv + 4.0 * 1.5 * nv
+    res["city_meshes_quads"] = n_cm
+    res["city_meshes_ms"] = statistics.median(ts)
+    res["city_meshes_gbs"] = mesh_bytes / (res["city_meshes_ms"] * 1e-3) / 1e9
+    res["city_meshes_roofline_frac"] = res["city_meshes_gbs"] / peak
+    ec.release()
+    del cout, vbufs, ibufs
     return res
 
 

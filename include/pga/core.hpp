@@ -41,12 +41,14 @@
  * Entry i of the dispatch table stays entry i of the rule table, so axioms
  * keep their root entries.
  *
- * Not lowered (an exception names them): triangle-mesh generation
- * (Generate<..., 0, ...>), the Vec2/Vec4 parameter types, FSCall without an
- * entry index, and the operators outside this engine (Rotate, Scale, Translate,
- * SwapSize, Replicate, RandomRule, IfCollides, If).  Generate's Attr1..Attr5
- * arguments are accepted and unused: the instanced generation function writes
- * the shape's custom attribute (GenerationFunctions.cuh:158-188).
+ * Generate<..., 1, ...> is an instanced terminal, Generate<..., 0, ...> a
+ * triangle-mesh terminal (PGA_OP_GENERATE_MESH, expanded by
+ * pga_generate_meshes).  Not lowered (an exception names them): other
+ * generation functions, the Vec2/Vec4 parameter types, FSCall without an entry
+ * index, and the operators outside this engine (IfCollides, the SetAs prism and
+ * polygon operators).  Generate's Attr1..Attr5 arguments are accepted and
+ * unused: the instanced generation function writes the shape's custom
+ * attribute (GenerationFunctions.cuh:158-188).
  */
 #ifndef PGA_GB300_CORE_HPP
 #define PGA_GB300_CORE_HPP
@@ -521,8 +523,11 @@ template <bool ParallelT, unsigned int GenFuncIdxT, typename TerminalIdxT, typen
           typename A4, typename A5, typename ShapeT>
 struct LowerOp<Operators::Generate<ParallelT, GenFuncIdxT, TerminalIdxT, A1, A2, A3, A4, A5>, ShapeT> {
   static void run(Builder& b, const PgaEntry& src, uint32_t i) {
-    if (GenFuncIdxT != 1) throw LoweringError("only the instanced generation function (GenFuncIdx 1) is supported");
-    set_entry(b, i, b.proc(PGA_OP_GENERATE, ShapeT::kind, 0), {LowerParam<TerminalIdxT>::run(src)}, {});
+    if (GenFuncIdxT > 1)
+      throw LoweringError("generation function " + std::to_string(GenFuncIdxT) +
+                          ": only 0 (triangle mesh) and 1 (instanced) are supported");
+    set_entry(b, i, b.proc(GenFuncIdxT == 0 ? PGA_OP_GENERATE_MESH : PGA_OP_GENERATE, ShapeT::kind, 0),
+              {LowerParam<TerminalIdxT>::run(src)}, {});
   }
 };
 template <typename ShapeT>

@@ -89,7 +89,9 @@ typedef enum PgaOperator {
                                     p1.. weights; a zero weight is never picked and the last pair is taken when
                                     no other is (RandomRule.cuh:33-99) */,
   PGA_OP_IF = 14,              /* If<DynParam<0> condition, DCall<0> true, DCall<1> false>: nonzero is true */
-  PGA_OP_SWAP_SIZE = 15        /* SwapSize<DynParam<0..2> axes, DCall<0>>: size = (size[a0], size[a1], size[a2]) */
+  PGA_OP_SWAP_SIZE = 15,       /* SwapSize<DynParam<0..2> axes, DCall<0>>: size = (size[a0], size[a1], size[a2]) */
+  PGA_OP_GENERATE_MESH = 16    /* Generate<false, 0, DynParam<0> mesh index>: a triangle-mesh terminal; its record
+                                  is written like an instanced one and pga_generate_meshes expands it */
 } PgaOperator;
 
 typedef enum PgaShape { PGA_SHAPE_BOX = 0, PGA_SHAPE_QUAD = 1 } PgaShape;
@@ -217,7 +219,8 @@ const char* pga_last_error(void);
  *  26 Box  RandomRule, 3 static pairs   27 Quad RandomRule, 3 static pairs
  *  28 Box  RandomRule, 4 static pairs   29 Quad RandomRule, 4 static pairs
  *  30 Box  If                           31 Quad If
- *  32 Box  SwapSize                     33 Quad SwapSize */
+ *  32 Box  SwapSize                     33 Quad SwapSize
+ *  34 Box  Generate (triangle mesh)     35 Quad Generate (triangle mesh) */
 const PgaProc* pga_default_procs(uint32_t* numProcs);
 
 /* Replaces SinglePhaseEvaluator::initialize(DispatchTableEntry*, n)
@@ -308,6 +311,44 @@ PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const
  * reference counterpart. */
 PgaStatus pga_adjoint(PgaEngine* engine, const float* dGradTerminals, float* dGradParams,
                       uint32_t numBlocks, float* dGradAxiomSizes, void* stream);
+
+/* One vertex of a generated triangle mesh: the layout of
+ * PGA::Rendering::TriangleMeshData::VertexAttributes (16-byte aligned
+ * position, normal and uv; include/pga/rendering/TriangleMeshData.h:10-18). */
+typedef struct PgaVertex {
+  float position[4];
+  float normal[3];
+  float uv[2];
+  float pad[3];
+} PgaVertex;
+
+/* A triangle mesh being filled: the layout of PGA::Rendering::TriangleMeshData
+ * (TriangleMeshData.h:19-27).  numVertices / numIndices are advanced
+ * atomically by pga_generate_meshes and keep counting past the maxima. */
+typedef struct PgaTriangleMesh {
+  uint32_t numVertices, numIndices;
+  uint32_t maxNumVertices, maxNumIndices;
+  PgaVertex* vertices; /* device, maxNumVertices */
+  uint32_t* indices;   /* device, maxNumIndices */
+} PgaTriangleMesh;
+
+/* Triangle-mesh generation, GenerationFunction<GenFuncFilter, 0> over
+ * ShapeGenerator<Box> / <Quad> (include/pga/rendering/GenerationFunctions.cuh:41-153,
+ * include/pga/core/ShapeGenerator.cuh:377-512, 671-708): for every record of
+ * dTerminals whose rule is a triangle-mesh Generate (PGA_OP_GENERATE_MESH) of
+ * this engine's table, appends to mesh dMeshes[mesh index] its vertices (24
+ * for a Box: 6 faces x 4, 4 for a Quad) with the reference's positions,
+ * normals and uvs (counter-clockwise), and its indices (two triangles per
+ * face, absolute vertex numbers).  dMeshes is a DEVICE array of numMeshes
+ * meshes (the reference's Device::TriangleMeshes).  Space is taken with one
+ * atomic per mesh per warp, so the order of terminals in a mesh is not fixed
+ * (the reference's atomics give no order either); a terminal's vertices and
+ * indices are contiguous.  A mesh index >= numMeshes is PGA_ERR_BAD_PARAM; a
+ * terminal that does not fit is not written (PGA_ERR_OUTPUT_OVERFLOW, the
+ * counters keep counting; the reference wraps around instead).  Statuses
+ * through pga_engine_sync_report.  One launch on `stream`, asynchronous. */
+PgaStatus pga_generate_meshes(PgaEngine* engine, const PgaTerminal* dTerminals, uint64_t numTerminals,
+                              PgaTriangleMesh* dMeshes, uint32_t numMeshes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -154,7 +154,7 @@ static void rotate_xyz(float x, float y, float z, float q[9]) {
   q[8] = ca * cb;
 }
 
-static const PgaProc kDefaultProcs[34] = {
+static const PgaProc kDefaultProcs[36] = {
     {PGA_OP_SUBDIVIDE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SUBDIVIDE, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_BOX, 3, 1}, {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_QUAD, 3, 1},
     {PGA_OP_REPEAT, PGA_SHAPE_BOX, 0, 1},           {PGA_OP_REPEAT, PGA_SHAPE_QUAD, 0, 1},
@@ -172,6 +172,7 @@ static const PgaProc kDefaultProcs[34] = {
     {PGA_OP_RANDOM_RULE_STATIC, PGA_SHAPE_BOX, 4, 1}, {PGA_OP_RANDOM_RULE_STATIC, PGA_SHAPE_QUAD, 4, 1},
     {PGA_OP_IF, PGA_SHAPE_BOX, 0, 1},               {PGA_OP_IF, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_SWAP_SIZE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SWAP_SIZE, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_GENERATE_MESH, PGA_SHAPE_BOX, 0, 1},    {PGA_OP_GENERATE_MESH, PGA_SHAPE_QUAD, 0, 1},
 };
 
 extern "C" {
@@ -181,7 +182,7 @@ const char* pga_version(void) { return "pga_gb300 0.1.0 (sm_103a)"; }
 const char* pga_last_error(void) { return g_error.c_str(); }
 
 const PgaProc* pga_default_procs(uint32_t* numProcs) {
-  if (numProcs) *numProcs = 34;
+  if (numProcs) *numProcs = 36;
   return kDefaultProcs;
 }
 
@@ -241,8 +242,11 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     r.op = 0xFF;
     if (en.operatorCode >= 0 && (uint32_t)en.operatorCode < table->numProcs) {
       const PgaProc& p = table->procs[en.operatorCode];
-      if (p.op <= PGA_OP_SWAP_SIZE && p.shape <= PGA_SHAPE_QUAD) {
-        r.op = (uint8_t)p.op;
+      if (p.op <= PGA_OP_GENERATE_MESH && p.shape <= PGA_SHAPE_QUAD) {
+        // A triangle-mesh Generate derives exactly like an instanced one; the
+        // flag marks its records for pga_generate_meshes.
+        r.op = (uint8_t)(p.op == PGA_OP_GENERATE_MESH ? PGA_OP_GENERATE : p.op);
+        if (p.op == PGA_OP_GENERATE_MESH) r.flags = kRuleMesh;
         r.shape = (uint8_t)p.shape;
         r.nChildren = p.numChildren;
       }
@@ -268,7 +272,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
       if (p.type == PGA_PT_RAND || p.type == PGA_PT_EXP) e->useSeeds = true;
       if (p.type == PGA_PT_SHAPE_ATTR && p.value[0] >= 15.0f && p.value[0] < 16.0f) e->useSeeds = true;
     }
-    r.flags = pure ? kRulePure : 0;
+    r.flags = (uint16_t)((r.flags & kRuleMesh) | (pure ? kRulePure : 0));
     // A scalar terminal index is decided here once (the device truncates it
     // toward zero like __float2uint_rz; only 0..127 are valid mesh indices).
     if (r.op == PGA_OP_GENERATE && en.numParameters >= 1 && en.parameters[0].type == PGA_PT_SCALAR &&

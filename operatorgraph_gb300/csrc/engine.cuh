@@ -67,6 +67,7 @@ struct __align__(16) DevRule {
 constexpr uint16_t kRulePure = 1;
 constexpr uint16_t kRuleConstTerminal = 2;  // Generate with a scalar terminal index, kept in nChildren
 constexpr uint16_t kRuleLeaf = 4;           // Subdivide whose children all end at once (expanded in place)
+constexpr uint16_t kRuleMesh = 8;           // a triangle-mesh Generate (lowered to op GENERATE for the derivation)
 
 struct DevTables {
   const DevRule* rules;

@@ -29,9 +29,10 @@ bottom, sides), Extrude (axis slot, extent), IfSizeLess (axis, size; true,
 false), If (condition; true, false), Translate (x, y, z), Scale (x, y, z),
 Rotate (x, y, z degrees), SwapSize (three axes), RandomRule (chance,
 weights...; one successor per weight), Replicate (successors), Discard, and
-terminals as Generate (terminal index; only the instanced generation function
-1).  The others (the prism SetAs operators, IfCollides...) parse but are not
-engine operators: lowering raises DslError naming the operator and the rule.  A rule applied to both a Box and a
+terminals as Generate (terminal index; generation function 1 is the instanced
+one, 0 the triangle mesh that pga_generate_meshes expands).  The others (the
+prism SetAs operators, IfCollides...) parse but are not engine operators:
+lowering raises DslError naming the operator and the rule.  A rule applied to both a Box and a
 Quad is lowered once per shape.
 """
 import re
@@ -322,13 +323,17 @@ class _Lowering:
     def rule(self, name, shape, line):
         if name in self.g["terminals"]:
             fn, *rest = self.g["terminals"][name]
-            if int(fn) != 1:
-                raise DslError(f"terminal {name!r}: only the instanced generation function (1) is supported")
+            if int(fn) not in (0, 1):
+                raise DslError(f"terminal {name!r}: generation function {int(fn)}; only 0 (triangle mesh) and 1 "
+                               "(instanced) are supported")
             key = ("terminal", name, shape)
             if key not in self.memo:
                 i = self.new()
                 self.memo[key] = i
-                gen = G.BOX_GENERATE if shape == G.SHAPE_BOX else G.QUAD_GENERATE
+                if int(fn) == 1:
+                    gen = G.BOX_GENERATE if shape == G.SHAPE_BOX else G.QUAD_GENERATE
+                else:
+                    gen = G.BOX_GENERATE_MESH if shape == G.SHAPE_BOX else G.QUAD_GENERATE_MESH
                 self.entries[i] = G.Entry(gen, [G.scalar(rest[0] if rest else 0.0)], [])
             return self.memo[key]
         if name not in self.g["rules"]:

@@ -26,7 +26,7 @@ STATUS = {
 # Every symbol include/pga_gb300.h declares.
 EXPORTS = ["pga_version", "pga_last_error", "pga_default_procs", "pga_engine_create", "pga_engine_destroy",
            "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_engine_levels", "pga_lbvh_build",
-           "pga_lbvh_build_static", "pga_adjoint", "pga_derive_to_host"]
+           "pga_lbvh_build_static", "pga_adjoint", "pga_derive_to_host", "pga_generate_meshes"]
 
 
 class PgaError(RuntimeError):
@@ -97,6 +97,7 @@ def load_library(path=LIB_PATH):
     L.pga_engine_levels.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(u32)]
     L.pga_lbvh_build_static.argtypes = [vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
     L.pga_derive_to_host.argtypes = [vp, vp, u32, vp, vp, u64, ctypes.POINTER(u64), vp]
+    L.pga_generate_meshes.argtypes = [vp, vp, u64, vp, u32, vp]
     for name in EXPORTS[3:]:
         getattr(L, name).restype = ctypes.c_int
     _lib = L
@@ -232,6 +233,38 @@ class Engine:
         _check(L.pga_lbvh_build(self.handle, terminals.data_ptr(), n, ctypes.byref(pb), ctypes.byref(out),
                                 _stream_handle(stream)), "pga_lbvh_build")
         return res
+
+    def generate_meshes_raw(self, d_terminals, n, d_meshes, num_meshes, stream=None):
+        _check(load_library().pga_generate_meshes(self.handle, d_terminals, n, d_meshes, num_meshes,
+                                                  _stream_handle(stream)), "pga_generate_meshes")
+
+    def generate_meshes(self, terminals, n, capacities, stream=None):
+        """Triangle meshes of the triangle-mesh terminals among terminals[:n]
+        (a device tensor of records).  capacities: (maxNumVertices,
+        maxNumIndices) per mesh.  Returns, per mesh, (vertices [numVertices, 12]
+        float32 tensor in PgaVertex layout, indices uint32-as-int32 tensor,
+        numVertices, numIndices) after a synchronize; statuses raise."""
+        import torch
+
+        bufs, rows = [], []
+        for mv, mi in capacities:
+            v = torch.zeros((max(mv, 1), 12), dtype=torch.float32, device="cuda")
+            i = torch.zeros(max(mi, 1), dtype=torch.int32, device="cuda")
+            bufs.append((v, i))
+            rows.append((0, 0, mv, mi, v.data_ptr(), i.data_ptr()))
+        table = np.array(rows, dtype=G.MESH_DT)
+        d_table = torch.from_numpy(table.view(np.uint8).copy()).to("cuda")
+        self.generate_meshes_raw(terminals.data_ptr(), n, d_table.data_ptr(), len(rows), stream)
+        torch.cuda.synchronize()
+        rep = self.report(stream)
+        if rep["status"] != 0:
+            raise PgaError(rep["status"], f"pga_generate_meshes: {STATUS.get(rep['status'])} (detail {rep['detail']})")
+        counts = d_table.cpu().numpy().view(G.MESH_DT)
+        out = []
+        for (v, i), c in zip(bufs, counts):
+            nv, ni = int(c["numVertices"]), int(c["numIndices"])
+            out.append((v[:nv], i[:ni], nv, ni))
+        return out
 
     def adjoint_raw(self, d_grad_terminals, d_grad_params, num_blocks, d_grad_sizes, stream=None):
         L = load_library()

@@ -25,9 +25,10 @@ PT_BLOCK = 16
 OP_SUBDIVIDE, OP_SUBDIVIDE_STATIC, OP_REPEAT, OP_COMPONENT_SPLIT = 0, 1, 2, 3
 OP_EXTRUDE, OP_IF_SIZE_LESS, OP_GENERATE, OP_DISCARD = 4, 5, 6, 7
 OP_TRANSLATE, OP_SCALE, OP_RANDOM_RULE, OP_ROTATE, OP_REPLICATE, OP_RANDOM_RULE_STATIC = 8, 9, 10, 11, 12, 13
-OP_IF, OP_SWAP_SIZE = 14, 15
+OP_IF, OP_SWAP_SIZE, OP_GENERATE_MESH = 14, 15, 16
 OP_NAMES = ["Subdivide", "SubdivideStatic", "Repeat", "ComponentSplit", "Extrude", "IfSizeLess", "Generate", "Discard",
-            "Translate", "Scale", "RandomRule", "Rotate", "Replicate", "RandomRuleStatic", "If", "SwapSize"]
+            "Translate", "Scale", "RandomRule", "Rotate", "Replicate", "RandomRuleStatic", "If", "SwapSize",
+            "GenerateMesh"]
 
 SHAPE_BOX, SHAPE_QUAD = 0, 1
 
@@ -51,6 +52,7 @@ BOX_REPLICATE, QUAD_REPLICATE = 22, 23
 BOX_RANDOM_RULE2, QUAD_RANDOM_RULE2, BOX_RANDOM_RULE3, QUAD_RANDOM_RULE3, BOX_RANDOM_RULE4, QUAD_RANDOM_RULE4 = range(24, 30)
 BOX_IF, QUAD_IF = 30, 31
 BOX_SWAP_SIZE, QUAD_SWAP_SIZE = 32, 33
+BOX_GENERATE_MESH, QUAD_GENERATE_MESH = 34, 35  # Generate<false, 0, DynParam<0>>: triangle-mesh terminals
 
 PARAM_DT = np.dtype([("type", "<i4"), ("value", "<f4", (MAX_VALUES,))])
 SUCC_DT = np.dtype([("entryIndex", "<i4"), ("phaseIndex", "<i4")])
@@ -64,7 +66,12 @@ AXIOM_DT = np.dtype([
     ("entry", "<u4"), ("shape", "<u4"), ("block", "<u4"), ("flags", "<u4"),
 ])
 TERMINAL_DT = np.dtype([("m", "<f4", (12,)), ("rule", "<u4"), ("custom", "<f4"), ("path", "<u8")])
+# PgaVertex / PgaTriangleMesh (the reference's TriangleMeshData layouts).
+VERTEX_DT = np.dtype([("position", "<f4", (4,)), ("normal", "<f4", (3,)), ("uv", "<f4", (2,)), ("pad", "<f4", (3,))])
+MESH_DT = np.dtype([("numVertices", "<u4"), ("numIndices", "<u4"), ("maxNumVertices", "<u4"), ("maxNumIndices", "<u4"),
+                    ("vertices", "<u8"), ("indices", "<u8")])
 assert ENTRY_DT.itemsize == 1332 and AXIOM_DT.itemsize == 48 and TERMINAL_DT.itemsize == 64
+assert VERTEX_DT.itemsize == 48 and MESH_DT.itemsize == 32
 
 # The generic procedure list: (operator, shape, numChildren) per operator code.
 DEFAULT_PROCS = np.array([
@@ -85,6 +92,7 @@ DEFAULT_PROCS = np.array([
     (OP_RANDOM_RULE_STATIC, SHAPE_BOX, 4, 1), (OP_RANDOM_RULE_STATIC, SHAPE_QUAD, 4, 1),
     (OP_IF, SHAPE_BOX, 0, 1), (OP_IF, SHAPE_QUAD, 0, 1),
     (OP_SWAP_SIZE, SHAPE_BOX, 0, 1), (OP_SWAP_SIZE, SHAPE_QUAD, 0, 1),
+    (OP_GENERATE_MESH, SHAPE_BOX, 0, 1), (OP_GENERATE_MESH, SHAPE_QUAD, 0, 1),
 ], dtype=PROC_DT)
 
 
@@ -259,3 +267,36 @@ def sort_terminals(t, by_path=False):
     m = t["m"].view(np.uint32)
     keys = [t["custom"].view(np.uint32), t["rule"]] + [m[:, i] for i in range(11, -1, -1)]
     return t[np.lexsort(keys)]
+
+
+def mesh_faces(vertices, indices):
+    """Faces of a generated triangle mesh as an order-free array: for each run
+    of 6 indices (v, v+1, v+2, v, v+2, v+3) the 4 vertices' 12 floats (PgaVertex
+    without padding; -0 -> +0), checked against that pattern; sorted by bytes.
+    vertices: [nv, 12] float32 (PgaVertex layout), indices: [ni] integers."""
+    v = np.asarray(vertices, np.float32).reshape(-1, 12)[:, :9] + np.float32(0)
+    v = np.where(np.isnan(v), np.float32(np.nan), v).astype(np.float32)  # one NaN pattern (degenerate faces)
+    idx = np.asarray(indices).astype(np.int64).reshape(-1, 6)
+    base = idx[:, 0]
+    want = base[:, None] + np.array([0, 1, 2, 0, 2, 3])
+    assert (idx == want).all(), "index pattern of a face"
+    assert base.size == 0 or (base.min() >= 0 and base.max() + 3 < len(v)), "face vertex out of range"
+    faces = v[base[:, None] + np.arange(4)].reshape(len(base), 36)
+    key = np.ascontiguousarray(faces).view(np.dtype((np.void, 36 * 4))).ravel()
+    return faces[np.argsort(key, kind="stable")]
+
+
+def read_mesh_file(path):
+    """Meshes written by the reference harness: per mesh (vertices [nv, 12]
+    float32, indices [ni] uint32)."""
+    out = []
+    with open(path, "rb") as f:
+        head = f.read(8)
+        assert head[:4] == b"PGAM", head
+        n = int(np.frombuffer(head[4:], "<u4")[0])
+        for _ in range(n):
+            nv, ni = np.frombuffer(f.read(8), "<u4")
+            v = np.frombuffer(f.read(int(nv) * 48), np.float32).reshape(-1, 12)
+            i = np.frombuffer(f.read(int(ni) * 4), "<u4")
+            out.append((v, i))
+    return out

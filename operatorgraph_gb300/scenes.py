@@ -71,8 +71,11 @@ def menger(threshold=0.05, n=1, seed=0.5):
     return _batch(menger_table(threshold), ax, name=f"menger(threshold={threshold})")
 
 
-def building_table(mode=G.ANCHOR_TO_START):
-    """One city building: Extrude -> ComponentSplit -> Repeat Y -> Repeat X -> IfSizeLess -> Subdivide."""
+def building_table(mode=G.ANCHOR_TO_START, meshes=False):
+    """One city building: Extrude -> ComponentSplit -> Repeat Y -> Repeat X -> IfSizeLess -> Subdivide.
+    meshes=True makes the walls, windows and roofs triangle-mesh terminals
+    (meshes 0, 1, 2) instead of instanced ones."""
+    gen = G.QUAD_GENERATE_MESH if meshes else G.QUAD_GENERATE
     return DispatchTable([
         Entry(G.QUAD_EXTRUDE, [scalar(1), shape_attr(16)], [(1, 0)]),                      # 0 extrude to height
         Entry(G.BOX_COMPONENT_SPLIT, [], [(9, 0), (7, 0), (2, 0)]),                       # 1 top, bottom, sides
@@ -81,10 +84,10 @@ def building_table(mode=G.ANCHOR_TO_START):
         Entry(G.QUAD_IF_SIZE_LESS, [scalar(0), scalar(1.2)], [(7, 0), (5, 0)]),           # 4 narrow tile?
         Entry(G.QUAD_SUBDIVIDE, [scalar(0), scalar(0.2), scalar(-1), scalar(0.2)],
               [(8, 0), (6, 0), (8, 0)]),                                                  # 5 window
-        Entry(G.QUAD_GENERATE, [scalar(1)], []),                                          # 6 window terminal
+        Entry(gen, [scalar(1)], []),                                                      # 6 window terminal
         Entry(G.QUAD_DISCARD, [], []),                                                    # 7
-        Entry(G.QUAD_GENERATE, [scalar(0)], []),                                          # 8 wall terminal
-        Entry(G.QUAD_GENERATE, [scalar(2)], []),                                          # 9 roof terminal
+        Entry(gen, [scalar(0)], []),                                                      # 8 wall terminal
+        Entry(gen, [scalar(2)], []),                                                      # 9 roof terminal
     ]).to_array()
 
 
@@ -116,8 +119,8 @@ def city_axioms(n=4096, seed=1234, cols=64, pitch=50.0):
     return ax
 
 
-def city(n=4096, seed=1234, mode=G.ANCHOR_TO_START):
-    return _batch(building_table(mode), city_axioms(n, seed), name=f"city({n})")
+def city(n=4096, seed=1234, mode=G.ANCHOR_TO_START, meshes=False):
+    return _batch(building_table(mode, meshes), city_axioms(n, seed), name=f"city({n})")
 
 
 FACADE_STRIDE = 16

@@ -52,6 +52,9 @@ def lib():
         L.oracle_derive_f64.restype = ctypes.c_int
         L.oracle_lbvh.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp]
         L.oracle_lbvh.restype = ctypes.c_int
+        L.oracle_mesh_count.restype = u32
+        L.oracle_mesh_sizes.argtypes = [u32, vp, vp]
+        L.oracle_mesh_copy.argtypes = [u32, vp, vp]
         _lib = L
     return _lib
 
@@ -90,6 +93,22 @@ def derive(procs, entries, axioms, blocks=None, block_stride=0, capacity=None):
     if st != 0:
         raise OracleError(st, int(det[0]))
     return out[: int(cnt[0])]
+
+
+def derive_meshes(procs, entries, axioms, blocks=None, block_stride=0):
+    """Terminals and the triangle meshes of the triangle-mesh terminals:
+    (terminals, [(vertices [nv, 12] float32, indices [ni] uint32) per mesh])."""
+    terms = derive(procs, entries, axioms, blocks, block_stride)
+    L = lib()
+    out = []
+    nv, ni = np.zeros(1, np.uint32), np.zeros(1, np.uint32)
+    for m in range(L.oracle_mesh_count()):
+        L.oracle_mesh_sizes(m, _ptr(nv), _ptr(ni))
+        v = np.zeros((int(nv[0]), 12), np.float32)
+        i = np.zeros(int(ni[0]), np.uint32)
+        L.oracle_mesh_copy(m, _ptr(v), _ptr(i))
+        out.append((v, i))
+    return terms, out
 
 
 def derive_f64(procs, entries, axioms, blocks64=None, block_stride=0, axiom_sizes64=None, capacity=None):

@@ -7,9 +7,10 @@ What it does
 ------------
 1. When the reference checkout is present (first argument, default
    /root/reference), copy the header-only operator library it ships
-   (``include/pga/core``), the vendored math headers (``deps/math/include``)
-   and the Whippletree headers that ``CPUEvaluator.h`` pulls in
-   (``deps/whippletree/include``) into ``oracle/_ref/shadow``.  Nothing is
+   (``include/pga/core``), the vendored math headers (``deps/math/include``),
+   the Whippletree headers that ``CPUEvaluator.h`` pulls in
+   (``deps/whippletree/include``) and the mesh vertex counts
+   (``include/pga/rendering/ShapeMeshAttributes.cuh``) into ``oracle/_ref/shadow``.  Nothing is
    copied into the tracked tree: ``oracle/_ref`` is git-ignored.
 2. Apply the mechanical MSVC-portability edits listed in ``EDITS`` to the
    shadow copy.  None of them touches operator math: they replace
@@ -63,6 +64,10 @@ def make_shadow(ref_root):
     shutil.copytree(os.path.join(ref_root, "include", "pga", "core"), os.path.join(SHADOW, "pga", "core"))
     shutil.copytree(os.path.join(ref_root, "deps", "math", "include", "math"), os.path.join(SHADOW, "math"))
     shutil.copytree(os.path.join(ref_root, "deps", "whippletree", "include"), os.path.join(SHADOW, "whippletree"))
+    # the vertex and index counts of the triangle-mesh generation function
+    os.makedirs(os.path.join(SHADOW, "pga", "rendering"))
+    shutil.copy(os.path.join(ref_root, "include", "pga", "rendering", "ShapeMeshAttributes.cuh"),
+                os.path.join(SHADOW, "pga", "rendering", "ShapeMeshAttributes.cuh"))
     stubs = os.path.join(SHADOW, "stubs")
     os.makedirs(stubs)
     # HighResClock.h and ClockCycleCounter.cuh include Windows headers but use

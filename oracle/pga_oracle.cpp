@@ -257,7 +257,58 @@ struct Out {
   uint64_t* termPath;
   uint64_t cap;
   uint64_t count;
+  std::vector<struct OracleMesh>* meshes = nullptr;  // triangle meshes (float derivation only)
 };
+
+// One triangle mesh as GenerationFunction<GenFuncFilter, 0> fills
+// TriangleMeshData: 12 floats per vertex (position 4, normal 3, uv 2, 3 unused)
+// and the triangles' vertex numbers, both in the order they were written.
+struct OracleMesh {
+  std::vector<float> vertices;
+  std::vector<uint32_t> indices;
+};
+
+// ShapeGenerator<Box / Quad, false>::run (ShapeGenerator.cuh:377-512, 671-708),
+// counter-clockwise build: each face's four corners model4 * (+-hx, +-hy, +-hz, 1)
+// with hx = size * 0.5 (Shape.cuh:70-73), the face normal
+// normalize(cross(v0 - v1, v2 - v1)) (vector.h:505-575: dot left to right,
+// length = sqrt, normalize = v * (1 / length)), uvs (1,1) (0,1) (0,0) (1,0),
+// triangles (v, v+1, v+2) and (v, v+2, v+3) per face.
+inline void shape_mesh(const M4<float>& model, const float size[3], bool quad, OracleMesh& mesh) {
+  static const int box[6][4][3] = {
+      {{-1, 1, -1}, {1, 1, -1}, {1, 1, 1}, {-1, 1, 1}},      // top
+      {{-1, -1, 1}, {1, -1, 1}, {1, -1, -1}, {-1, -1, -1}},  // bottom
+      {{-1, 1, -1}, {-1, 1, 1}, {-1, -1, 1}, {-1, -1, -1}},  // left
+      {{1, 1, 1}, {1, 1, -1}, {1, -1, -1}, {1, -1, 1}},      // right
+      {{-1, 1, 1}, {1, 1, 1}, {1, -1, 1}, {-1, -1, 1}},      // front
+      {{1, 1, -1}, {-1, 1, -1}, {-1, -1, -1}, {1, -1, -1}},  // back
+  };
+  static const int quadCorners[4][3] = {{-1, 1, 0}, {1, 1, 0}, {1, -1, 0}, {-1, -1, 0}};
+  const float h[3] = {size[0] * 0.5f, size[1] * 0.5f, size[2] * 0.5f};
+  const float uv[4][2] = {{1.0f, 1.0f}, {0.0f, 1.0f}, {0.0f, 0.0f}, {1.0f, 0.0f}};
+  const int faces = quad ? 1 : 6;
+  for (int f = 0; f < faces; f++) {
+    float v[4][4];
+    for (int c = 0; c < 4; c++) {
+      const int* sg = quad ? quadCorners[c] : box[f][c];
+      const float p[4] = {sg[0] * h[0], sg[1] * h[1], quad ? 0.0f : sg[2] * h[2], 1.0f};
+      for (int i = 0; i < 4; i++)
+        v[c][i] = model.a[i][0] * p[0] + model.a[i][1] * p[1] + model.a[i][2] * p[2] + model.a[i][3] * p[3];
+    }
+    const float a[3] = {v[0][0] - v[1][0], v[0][1] - v[1][1], v[0][2] - v[1][2]};
+    const float b[3] = {v[2][0] - v[1][0], v[2][1] - v[1][1], v[2][2] - v[1][2]};
+    const float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    const float inv = 1.0f / std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const uint32_t base = (uint32_t)(mesh.vertices.size() / 12);
+    for (int c = 0; c < 4; c++) {
+      const float vert[12] = {v[c][0], v[c][1], v[c][2], v[c][3], n[0] * inv, n[1] * inv, n[2] * inv,
+                              uv[c][0], uv[c][1], 0.0f, 0.0f, 0.0f};
+      mesh.vertices.insert(mesh.vertices.end(), vert, vert + 12);
+    }
+    const uint32_t tri[6] = {base, base + 1, base + 2, base, base + 2, base + 3};
+    mesh.indices.insert(mesh.indices.end(), tri, tri + 6);
+  }
+}
 
 // BaseSymbolManager::dispatchNonTerminal (CPUEvaluator.h:230-239): the symbol
 // goes to the queue of its entry's procedure; a shape of the wrong type is
@@ -534,6 +585,7 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
       dispatch(c, o, s);
       return;
     }
+    case PGA_OP_GENERATE_MESH:
     case PGA_OP_GENERATE: {
       // Generate<false, 1, TerminalIdx>::execute (Generate.cuh:30-34) ->
       // GenerationFunction<.., 1>::perShape (GenerationFunctions.cuh:158-188).
@@ -555,6 +607,16 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
           for (int r = 0; r < 3; r++)
             for (int q = 0; q < 4; q++) o.termM[k * 12 + r * 4 + q] = double(M.a[r][q]);
         if (o.termPath) o.termPath[k] = s.path;
+      }
+      if (proc.op == PGA_OP_GENERATE_MESH && o.meshes) {
+        // Generate<false, 0, TerminalIdx>: the terminal's triangle mesh (float derivation only).
+        if (tidx >= o.meshes->size()) o.meshes->resize(tidx + 1);
+        M4<float> model;
+        float size[3];
+        for (int r = 0; r < 4; r++)
+          for (int q = 0; q < 4; q++) model.a[r][q] = float(s.model.a[r][q]);
+        for (int k2 = 0; k2 < 3; k2++) size[k2] = float(s.size[k2]);
+        shape_mesh(model, size, s.shape == PGA_SHAPE_QUAD, (*o.meshes)[tidx]);
       }
       return;
     }
@@ -758,12 +820,30 @@ inline int clz32(uint32_t x) { return x ? __builtin_clz(x) : 32; }
 
 extern "C" {
 
+// Triangle meshes of the last oracle_derive call (its triangle-mesh terminals).
+static std::vector<OracleMesh> g_meshes;
+
+uint32_t oracle_mesh_count(void) { return (uint32_t)g_meshes.size(); }
+
+void oracle_mesh_sizes(uint32_t mesh, uint32_t* numVertices, uint32_t* numIndices) {
+  *numVertices = mesh < g_meshes.size() ? (uint32_t)(g_meshes[mesh].vertices.size() / 12) : 0u;
+  *numIndices = mesh < g_meshes.size() ? (uint32_t)g_meshes[mesh].indices.size() : 0u;
+}
+
+void oracle_mesh_copy(uint32_t mesh, float* vertices, uint32_t* indices) {
+  if (mesh >= g_meshes.size()) return;
+  std::copy(g_meshes[mesh].vertices.begin(), g_meshes[mesh].vertices.end(), vertices);
+  std::copy(g_meshes[mesh].indices.begin(), g_meshes[mesh].indices.end(), indices);
+}
+
 int oracle_derive(const PgaProc* procs, uint32_t nProcs, const PgaEntry* entries, uint32_t nEntries,
                   const PgaAxiom* axioms, uint32_t nAxioms, const float* blocks, uint32_t blockStride,
                   PgaTerminal* out, uint64_t cap, uint64_t* count, int32_t* detail) {
   Ctx c = {procs, nProcs, entries, nEntries, axioms, blockStride, PGA_OK, 0};
   Blocks<float> blk = {blocks, nullptr};
   Out<float> o;
+  g_meshes.clear();
+  o.meshes = &g_meshes;
   o.term = out;
   o.termM = nullptr;
   o.termPath = nullptr;

@@ -12,6 +12,10 @@
 //                   include/pga_gb300.h, path hash left 0 because the reference
 //                   has no derivation-path hash)
 // argv[3] (optional): number of timed repetitions of execute().
+// When the grammar has triangle-mesh terminals (Generate<false, 0, ...>), their
+// meshes go to argv[2] + ".mesh": "PGAM", mesh count, then per mesh the vertex
+// and index counts, the vertices (48 B each, TriangleMeshData::VertexAttributes
+// layout) and the indices, in the order the reference wrote them.
 //
 // The procedure list is the generic "interpreter style" list: one procedure per
 // (operator, shape) with every argument a DynParam and every successor a DCall,
@@ -38,6 +42,7 @@
 #include <pga/core/Subdivide.cuh>
 #include <pga/core/TStdLib.h>
 #include <pga/core/Translate.cuh>
+#include <pga/rendering/ShapeMeshAttributes.cuh>
 
 #include <algorithm>
 #include <chrono>
@@ -45,6 +50,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 using namespace PGA;
@@ -93,9 +99,59 @@ template <> struct GenerationFunction<HarnessFilter, 1> {
   template <typename ShapeT, typename... ArgsT> static unsigned int allocateIndices(ShapeT&, unsigned int, ArgsT...) { return 0; }
   template <typename... ArgsT> static void perTriangle(unsigned int, unsigned int, unsigned int, unsigned int, unsigned int, ArgsT...) {}
 };
+
+// Triangle meshes, mirroring GenerationFunction<GenFuncFilter, 0>
+// (GenerationFunctions.cuh:41-153) on the host side: vertex and index space
+// taken in order, the vertex attributes and triangles the reference's
+// ShapeGenerator computes stored as given.  perShape also records the
+// terminal, so that the derivation itself is compared for these rules too.
+struct HarnessMesh {
+  std::vector<float> vertices;  // 12 floats per vertex
+  std::vector<uint32_t> indices;
+};
+static std::vector<HarnessMesh> g_meshes;
+
+template <> struct GenerationFunction<HarnessFilter, 0> {
+  static HarnessMesh& mesh(unsigned int terminalIndex) {
+    if (terminalIndex >= g_meshes.size()) g_meshes.resize(terminalIndex + 1);
+    return g_meshes[terminalIndex];
+  }
+  template <typename ShapeT, typename... ArgsT>
+  static void perShape(ShapeT& shape, unsigned int terminalIndex, float attr1, ArgsT... args) {
+    GenerationFunction<HarnessFilter, 1>::perShape(shape, terminalIndex, attr1, args...);
+  }
+  template <typename ShapeT, typename... ArgsT>
+  static unsigned int allocateVertices(ShapeT& shape, unsigned int terminalIndex, ArgsT...) {
+    HarnessMesh& m = mesh(terminalIndex);
+    const unsigned int i = (unsigned int)(m.vertices.size() / 12);
+    m.vertices.resize(m.vertices.size() + 12 * Rendering::ShapeMeshAttributes<ShapeT>::getNumVertices(shape), 0.0f);
+    return i;
+  }
+  template <typename... ArgsT>
+  static void perVertex(unsigned int vertexIndex, const math::float4& vertex, const math::float3& normal,
+                        const math::float2& uv, unsigned int terminalIndex, ArgsT...) {
+    float* v = &mesh(terminalIndex).vertices[(size_t)vertexIndex * 12];
+    v[0] = vertex.x; v[1] = vertex.y; v[2] = vertex.z; v[3] = vertex.w;
+    v[4] = normal.x; v[5] = normal.y; v[6] = normal.z;
+    v[7] = uv.x; v[8] = uv.y;
+  }
+  template <typename ShapeT, typename... ArgsT>
+  static unsigned int allocateIndices(ShapeT& shape, unsigned int terminalIndex, ArgsT...) {
+    HarnessMesh& m = mesh(terminalIndex);
+    const unsigned int i = (unsigned int)m.indices.size();
+    m.indices.resize(m.indices.size() + Rendering::ShapeMeshAttributes<ShapeT>::getNumIndices(shape), 0u);
+    return i;
+  }
+  template <typename... ArgsT>
+  static void perTriangle(unsigned int index, unsigned int v0, unsigned int v1, unsigned int v2,
+                          unsigned int terminalIndex, ArgsT...) {
+    uint32_t* d = &mesh(terminalIndex).indices[index];
+    d[0] = v0; d[1] = v1; d[2] = v2;
+  }
+};
 }  // namespace PGA
 
-// Operator codes 0..33 (see pga_default_procs() in include/pga_gb300.h).
+// Operator codes 0..35 (see pga_default_procs() in include/pga_gb300.h).
 struct HarnessProcs : T::List<
   /* 0 */ Proc<Box, Subdivide<DynParams>, 1>,
   /* 1 */ Proc<Quad, Subdivide<DynParams>, 1>,
@@ -134,7 +190,9 @@ struct HarnessProcs : T::List<
   /* 30 */ Proc<Box, If<DynParam<0>, DCall<0>, DCall<1>>, 1>,
   /* 31 */ Proc<Quad, If<DynParam<0>, DCall<0>, DCall<1>>, 1>,
   /* 32 */ Proc<Box, SwapSize<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
-  /* 33 */ Proc<Quad, SwapSize<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>
+  /* 33 */ Proc<Quad, SwapSize<DynParam<0>, DynParam<1>, DynParam<2>, DCall<0>>, 1>,
+  /* 34 */ Proc<Box, Generate<false, 0, DynParam<0>>, 1>,
+  /* 35 */ Proc<Quad, Generate<false, 0, DynParam<0>>, 1>
 > {};
 
 #pragma pack(push, 1)
@@ -217,6 +275,7 @@ int main(int argc, char** argv) {
   for (int r = 0; r < repeats; r++) {
     g_terminals.clear();
     g_terminals.reserve(1 << 20);
+    g_meshes.clear();
     CPU::SinglePhaseEvaluator<HarnessProcs, HarnessAxioms, HarnessFilter> ev;
     ev.initialize(table.data(), table.size());
     try {
@@ -240,6 +299,22 @@ int main(int argc, char** argv) {
   fwrite(&n, 8, 1, o);
   fwrite(g_terminals.data(), sizeof(HarnessTerminal), n, o);
   fclose(o);
+  if (!g_meshes.empty()) {
+    std::string mp = std::string(argv[2]) + ".mesh";
+    FILE* mf = fopen(mp.c_str(), "wb");
+    if (!mf) { perror("open mesh output"); return 2; }
+    fwrite("PGAM", 1, 4, mf);
+    uint32_t nm = (uint32_t)g_meshes.size();
+    fwrite(&nm, 4, 1, mf);
+    for (const HarnessMesh& m : g_meshes) {
+      uint32_t nv = (uint32_t)(m.vertices.size() / 12), ni = (uint32_t)m.indices.size();
+      fwrite(&nv, 4, 1, mf);
+      fwrite(&ni, 4, 1, mf);
+      fwrite(m.vertices.data(), sizeof(float), m.vertices.size(), mf);
+      fwrite(m.indices.data(), sizeof(uint32_t), m.indices.size(), mf);
+    }
+    fclose(mf);
+  }
   std::sort(times.begin(), times.end());
   double med = times.empty() ? 0.0 : times[times.size() / 2];
   printf("{\"terminals\": %llu, \"seconds\": %.9g, \"repeats\": %d, \"status\": %d}\n",

@@ -209,9 +209,20 @@ struct ProcedureList
 }  // namespace if_swap_static
 
 namespace bad {
-// Triangle-mesh generation (GenFuncIdx 0) is outside the engine.
-struct ProcedureList : T::List<Proc<Box, Generate<false, 0, Scalar<0>>, 1>> {};
+// A generation function other than 0 (triangle mesh) and 1 (instanced).
+struct ProcedureList : T::List<Proc<Box, Generate<false, 2, Scalar<0>>, 1>> {};
 }  // namespace bad
+
+namespace mesh_terminals {
+// Triangle-mesh terminals (GenFuncIdx 0) beside instanced ones: a box split
+// into faces; the top is a mesh quad, the sides instanced, the box itself a
+// mesh box.
+struct ProcedureList
+    : T::List<Proc<Box,
+                   Replicate<Generate<false, 0, Scalar<0>>,
+                             ComponentSplit<false, Generate<false, 0, Scalar<1>>, Discard, Generate<false, 1, Scalar<2>>>>,
+                   1>> {};
+}  // namespace mesh_terminals
 
 static void write_scene(FILE* f, const std::string& name, const LoweredTable& t) {
   const uint32_t n = (uint32_t)name.size();
@@ -261,7 +272,8 @@ int main(int argc, char** argv) {
   scene<random_static_dyn::ProcedureList>(f, "random_static_dyn", random_static_dyn::table());
   scene<rotate_static::ProcedureList>(f, "rotate_static", building_static::table());
   scene<if_swap_static::ProcedureList>(f, "if_swap_static", building_static::table());
-  scene<bad::ProcedureList>(f, "triangle_mesh", DispatchTable{{0, {}, {}}});
+  scene<bad::ProcedureList>(f, "bad_generation_function", DispatchTable{{0, {}, {}}});
+  scene<mesh_terminals::ProcedureList>(f, "mesh_terminals", DispatchTable{{0, {}, {}}});
   scene<menger::ProcedureList>(f, "bad_dynparam", DispatchTable{{2, {}, {{1, 0}, {2, 0}}}});
   std::fclose(f);
   return 0;

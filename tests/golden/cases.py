@@ -222,7 +222,34 @@ def if_swap_mix():
     return _single(tab, ax, "if_swap_mix")
 
 
-def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False, more=False):
+def mesh_mix():
+    """Triangle-mesh terminals (Generate<false, 0, mesh>, GenerationFunctions.cuh:41-153,
+    ShapeGenerator.cuh:377-512, 671-708): boxes and quads into three meshes,
+    beside instanced terminals; unrotated, right-angle and arbitrary rotations
+    (the general-frame kernels); a face extruded to a box; a degenerate quad of
+    zero width (its normal is NaN in the reference too)."""
+    tab = DispatchTable([
+        Entry(G.BOX_REPLICATE, [], [(1, 0), (2, 0), (4, 0), (9, 0)]),                                 # 0
+        Entry(G.BOX_GENERATE_MESH, [scalar(0)], []),                                                  # 1
+        Entry(G.BOX_ROTATE, [scalar(0), scalar(90), scalar(0)], [(3, 0)]),                            # 2
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(5, 0), (6, 0), (7, 0)]),                                   # 3
+        Entry(G.BOX_ROTATE, [scalar(17.5), scalar(-33), scalar(61.25)], [(8, 0)]),                    # 4
+        Entry(G.QUAD_GENERATE_MESH, [scalar(1)], []),                                                 # 5
+        Entry(G.QUAD_GENERATE, [scalar(2)], []),                                                      # 6
+        Entry(G.QUAD_EXTRUDE, [scalar(0), scalar(0.4)], [(1, 0)]),                                    # 7
+        Entry(G.BOX_SUBDIVIDE, [scalar(1), scalar(-1), scalar(-2)], [(1, 0), (3, 0)]),                # 8
+        Entry(G.BOX_SCALE, [scalar(0), scalar(-1), scalar(-1)], [(10, 0)]),                           # 9
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(11, 0), (11, 0), (11, 0)]),                                # 10
+        Entry(G.QUAD_GENERATE_MESH, [scalar(2)], []),                                                 # 11
+    ]).to_array()
+    ax = G.make_axioms(3)
+    ax["size"] = [(1.0, 2.0, 3.0), (0.5, 0.25, 4.0), (3.3, 1.7, 2.9)]
+    ax["position"] = [(0, 0, 0), (10, 5, -3), (-7.5, 2.25, 100)]
+    ax["seed"] = [0.1, 0.5, 0.9]
+    return _single(tab, ax, "mesh_mix")
+
+
+def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False, more=False, meshes=False):
     """A random grammar over all eight operators and both shapes: a DAG of
     rules `depth` levels deep (rules of a level reused with some probability),
     with scalar, random-range, shape-attribute and expression parameters,
@@ -232,11 +259,13 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False, more=Fals
     terminal indices.  Seeds >= 1 and custom attributes vary per axiom.
     With affine=True the grammar also draws Translate, Scale and RandomRule
     rules, with rotate=True also Rotate and Replicate rules, with more=True also
-    If and SwapSize rules (the defaults draw exactly the grammars they always
+    If and SwapSize rules, with meshes=True half of the terminal rules are
+    triangle-mesh Generates (the defaults draw exactly the grammars they always
     drew)."""
     rng = np.random.default_rng(seed)
     BOX, QUAD = G.SHAPE_BOX, G.SHAPE_QUAD
     GEN = {BOX: G.BOX_GENERATE, QUAD: G.QUAD_GENERATE}
+    GEN_MESH = {BOX: G.BOX_GENERATE_MESH, QUAD: G.QUAD_GENERATE_MESH}
     DIS = {BOX: G.BOX_DISCARD, QUAD: G.QUAD_DISCARD}
     SUB = {BOX: G.BOX_SUBDIVIDE, QUAD: G.QUAD_SUBDIVIDE}
     SUB3 = {BOX: G.BOX_SUBDIVIDE3, QUAD: G.QUAD_SUBDIVIDE3}
@@ -276,7 +305,8 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False, more=Fals
                 e = add(Entry(DIS[kind], [], []))
             else:
                 tidx = scalar(int(rng.integers(0, 4))) if rng.random() < 0.8 else rand(0.0, 3.9)
-                e = add(Entry(GEN[kind], [tidx], []))
+                gen = GEN_MESH[kind] if meshes and rng.random() < 0.5 else GEN[kind]
+                e = add(Entry(gen, [tidx], []))
             made.setdefault(key, []).append(e)
             return e
         ops = ["sub", "sub3", "rep", "ifl"] + (["cs"] if kind == BOX else ["ext"])
@@ -369,7 +399,8 @@ def rich_random(seed, depth=5, n_axioms=4, affine=False, rotate=False, more=Fals
     ax["position"] = rng.uniform(-10.0, 10.0, (n_axioms, 3)).astype(np.float32)
     ax["seed"] = rng.uniform(0.0, 3.0, n_axioms).astype(np.float32)
     ax["custom"] = rng.uniform(0.5, 3.0, n_axioms).astype(np.float32)
-    name = "rich_more" if more else ("rich_rotate" if rotate else ("rich_affine" if affine else "rich_random"))
+    name = "rich_mesh" if meshes else (
+        "rich_more" if more else ("rich_rotate" if rotate else ("rich_affine" if affine else "rich_random")))
     return _single(tab, ax, f"{name}_{seed}")
 
 
@@ -392,6 +423,11 @@ ROTATE_SEEDS = (3, 6, 8, 13, 24, 47, 58, 71, 73, 75)
 # they use If (expression, attribute and scalar conditions) and SwapSize on
 # both shapes.
 MORE_SEEDS = (0, 3, 4, 18, 19, 20, 34, 47, 49, 50)
+
+# Seeds of rich_random(affine=True, rotate=True, more=True, meshes=True) with
+# golden fixtures, meshes included: boxes and quads into up to four meshes,
+# rotated and not.
+MESH_SEEDS = (3, 8, 13, 15, 24, 26, 29, 34, 36, 39)
 
 
 def cases():
@@ -426,10 +462,21 @@ def cases():
     for seed in MORE_SEEDS:
         b = rich_random(seed, affine=True, more=True)
         out.append((b["name"], b))
+    out.append(("mesh_mix", mesh_mix()))
+    for seed in MESH_SEEDS:
+        b = rich_random(seed, affine=True, rotate=True, more=True, meshes=True)
+        out.append((b["name"], b))
     for seed in ROTATE_SEEDS:
         b = rich_random(seed, affine=True, rotate=True)
         out.append((b["name"], b))
     return out
+
+
+def mesh_digest(vertices, indices):
+    """Digest of a generated mesh's faces, order-free (grammar.mesh_faces)."""
+    import hashlib
+
+    return hashlib.sha256(np.ascontiguousarray(G.mesh_faces(vertices, indices)).tobytes()).hexdigest()
 
 
 def canonical(terminals, num_entries=None):

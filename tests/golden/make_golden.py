@@ -5,7 +5,9 @@ Runs oracle/_ref/ref_harness (the reference's SinglePhaseEvaluator, built by
 oracle/make_ref.py from the reference sources) on every case of cases.py and
 stores: the grammar batch, the terminal count, a SHA-256 digest and checksum
 of the canonical (sorted, path-free) terminal records, and -- for cases of at
-most 2,000 terminals -- the canonical records themselves.
+most 2,000 terminals -- the canonical records themselves.  For grammars with
+triangle-mesh terminals it also stores each mesh's vertex and index counts and
+the digest of its order-free faces (cases.mesh_digest).
 
 Usage: python tests/golden/make_golden.py [case-name-prefix ...]   (needs oracle/_ref built)
 With prefixes, only the matching cases are (re)written.
@@ -40,9 +42,12 @@ def main():
             entries, axioms = G.expand_blocks(entries, axioms, b["blocks"], b["block_stride"])
             n_base = len(b["entries"])
         bf, tf = os.path.join(tmp, "b.bin"), os.path.join(tmp, "t.bin")
+        if os.path.exists(tf + ".mesh"):
+            os.remove(tf + ".mesh")
         G.write_batch_file(bf, entries, axioms)
         info = oracle.run_reference(bf, tf)
         ref = G.read_terminal_file(tf)
+        meshes = G.read_mesh_file(tf + ".mesh") if os.path.exists(tf + ".mesh") else []
         canon = C.canonical(ref, n_base)
         m = canon["m"].astype(np.float64)
         checksum = float((m[:, 3] + 2 * m[:, 7] + 3 * m[:, 11] + m[:, 0]).sum())
@@ -53,6 +58,9 @@ def main():
             payload["block_stride"] = np.int64(b["block_stride"])
         if len(ref) <= FULL_LIMIT:
             payload["terminals"] = canon.view(np.uint8)
+        if meshes:
+            payload["mesh_counts"] = np.array([(len(v), len(i)) for v, i in meshes], np.int64)
+            payload["mesh_digests"] = np.array([C.mesh_digest(v, i) for v, i in meshes])
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **payload)
         print(f"{name}: {len(ref)} terminals, checksum {checksum:.6f}, reference {info['seconds']:.6f} s")
 

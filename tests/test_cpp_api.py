@@ -212,8 +212,33 @@ def test_static_if_swap_size_chain_matches(lowered):
     assert (_multiset(got) == _multiset(want)).all()
 
 
+def test_mesh_generates_lower_to_the_mesh_operator(lowered):
+    """Generate<false, 0, ...> lowers to PGA_OP_GENERATE_MESH; the oracle's
+    meshes of the lowered table equal those of the same grammar built as data."""
+    from operatorgraph_gb300.grammar import DispatchTable, Entry, scalar
+
+    procs, entries, _ = lowered["mesh_terminals"]
+    assert G.OP_GENERATE_MESH in {int(p["op"]) for p in procs}
+    tab = DispatchTable([
+        Entry(G.BOX_REPLICATE, [], [(1, 0), (2, 0)]),
+        Entry(G.BOX_GENERATE_MESH, [scalar(0)], []),
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(3, 0), (4, 0), (5, 0)]),
+        Entry(G.QUAD_GENERATE_MESH, [scalar(1)], []),
+        Entry(G.QUAD_DISCARD, [], []),
+        Entry(G.QUAD_GENERATE, [scalar(2)], []),
+    ]).to_array()
+    ax = G.make_axioms(3)
+    ax["size"] = [(1.0, 2.0, 3.0), (2.5, 0.5, 1.5), (4.0, 4.0, 0.25)]
+    t_got, m_got = oracle.derive_meshes(procs, entries, ax)
+    t_want, m_want = oracle.derive_meshes(G.DEFAULT_PROCS, tab, ax)
+    assert (_multiset(t_got) == _multiset(t_want)).all()
+    assert len(m_got) == len(m_want) == 2
+    for (v, i), (w, j) in zip(m_got, m_want):
+        assert np.array_equal(G.mesh_faces(v, i).view(np.uint32), G.mesh_faces(w, j).view(np.uint32))
+
+
 def test_unsupported_forms_are_lowering_errors(lowered):
-    assert "instanced" in lowered["triangle_mesh"]
+    assert "generation function 2" in lowered["bad_generation_function"]
     assert "DynParam<0>" in lowered["bad_dynparam"]
 
 

@@ -96,7 +96,7 @@ def test_a_rule_used_on_both_shapes_is_lowered_per_shape():
     ("axiom Box A; terminal T (1, 0); A = RandomRule() { 0.5: T | 0.5: T };", ["RandomRule", "chance"]),
     ("axiom Box A; A = SubDiv(X) { -1: Nowhere };", ["unknown symbol", "Nowhere"]),
     ("axiom Box A;\nA = SubDiv(X) { -1 Discard() };", ["line 2", "':'"]),
-    ("axiom Box A; terminal T (0, 3); A = T;", ["instanced"]),
+    ("axiom Box A; terminal T (2, 3); A = T;", ["generation function 2"]),
 ])
 def test_errors_name_the_problem(text, words):
     with pytest.raises(dsl.DslError) as e:

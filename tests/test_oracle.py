@@ -50,6 +50,26 @@ def test_oracle_matches_reference_golden(path):
     assert digest(canon) == str(z["digest"])
 
 
+@pytest.mark.parametrize("path", [p for p in GOLDEN if "mesh_counts" in np.load(p)],
+                         ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_meshes_match_reference_golden(path):
+    """Triangle meshes: the restatement's vertices (positions, normals, uvs)
+    and triangles against the reference's GenerationFunction<.., 0> output, as
+    order-free faces, mesh by mesh."""
+    import sys
+
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import cases
+
+    b, z = load_case(path)
+    _, meshes = oracle.derive_meshes(G.DEFAULT_PROCS, b["entries"], b["axioms"], b["blocks"], b["block_stride"])
+    counts = z["mesh_counts"]
+    assert len(meshes) == len(counts)
+    for m, ((v, i), (nv, ni), dg) in enumerate(zip(meshes, counts, z["mesh_digests"])):
+        assert (len(v), len(i)) == (nv, ni), m
+        assert cases.mesh_digest(v, i) == str(dg), m
+
+
 def test_golden_fixtures_present():
     assert len(GOLDEN) >= 15
 

@@ -97,6 +97,13 @@ def test_golden_case(path, form):
     assert cases.digest(canon) == str(z["digest"]), "differs from the reference's own output"
     ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"], b["blocks"], b["block_stride"])
     _assert_same(got, ref)
+    if "mesh_counts" in z:
+        # triangle meshes from the derived records (pga_generate_meshes)
+        counts = z["mesh_counts"]
+        meshes = eng.generate_meshes(out, len(got), [(int(nv), int(ni)) for nv, ni in counts])
+        for m, ((v, i, nv, ni), (rv, ri), dg) in enumerate(zip(meshes, counts, z["mesh_digests"])):
+            assert (nv, ni) == (rv, ri), m
+            assert cases.mesh_digest(v.cpu().numpy(), i.cpu().numpy().view(np.uint32)) == str(dg), m
     eng.release()
 
 
@@ -342,6 +349,35 @@ def test_derive_to_host_reports_overflow():
     assert st == 2 and n > 1000
     with pytest.raises(PgaError):
         eng.derive_to_host(h_ax.data_ptr(), len(b["axioms"]), h_out.data_ptr(), 1000)
+    eng.release()
+
+
+def test_city_meshes_match_the_oracle():
+    """pga_generate_meshes on 64 city buildings with triangle-mesh terminals
+    (walls, windows, roofs: about 90k quads in three meshes) against the
+    oracle's meshes, face for face, bit for bit; then with too little space
+    (PGA_ERR_OUTPUT_OVERFLOW) and too few meshes (PGA_ERR_BAD_PARAM)."""
+    from operatorgraph_gb300.engine import PgaError
+
+    b = scenes.city(64, meshes=True)
+    _, meshes_ref = oracle.derive_meshes(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    eng, out, got, rep = _run(b)
+    assert rep["status"] == 0
+    caps = [(len(v), len(i)) for v, i in meshes_ref]
+    meshes = eng.generate_meshes(out, len(got), caps)
+    for (v, i, nv, ni), (rv, ri) in zip(meshes, meshes_ref):
+        assert (nv, ni) == (len(rv), len(ri))
+        a = G.mesh_faces(v.cpu().numpy(), i.cpu().numpy().view(np.uint32))
+        c = G.mesh_faces(rv, ri)
+        assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
+    with pytest.raises(PgaError) as e:
+        eng.generate_meshes(out, len(got), [(nv // 2, ni // 2) for nv, ni in caps])
+    assert e.value.status == 2
+    eng.release()
+    eng, out, got, rep = _run(b)
+    with pytest.raises(PgaError) as e:
+        eng.generate_meshes(out, len(got), caps[:2])
+    assert e.value.status == 5
     eng.release()
 
 
