@@ -120,7 +120,7 @@ __device__ __forceinline__ int record_mesh(const PgaTerminal* terms, unsigned lo
 constexpr int kMeshBatches = 8;
 constexpr uint32_t kMaxMeshes = 128;  // terminal indices are 7 bits
 
-__global__ void __launch_bounds__(kMeshThreads) k_meshes(const PgaTerminal* __restrict__ terms, unsigned long long n,
+__global__ void __launch_bounds__(kMeshThreads, 6) k_meshes(const PgaTerminal* __restrict__ terms, unsigned long long n,
                                                           const DevRule* __restrict__ rules, uint32_t numEntries,
                                                           PgaTriangleMesh* meshes, uint32_t numMeshes, DevState* st) {
   __shared__ uint32_t sFaces[kMaxMeshes];   // faces of each mesh in this tile
@@ -263,7 +263,7 @@ extern "C" PgaStatus pga_generate_meshes(PgaEngine* e, const PgaTerminal* dTermi
   cudaStream_t s = (cudaStream_t)stream;
   const unsigned long long tiles = (numTerminals + (unsigned long long)kMeshThreads * kMeshBatches - 1) /
                                    ((unsigned long long)kMeshThreads * kMeshBatches);
-  const unsigned long long maxBlocks = (unsigned long long)e->numSMs * 4ull;  // resident at 124 registers
+  const unsigned long long maxBlocks = (unsigned long long)e->numSMs * 6ull;  // resident at 80 registers
   const unsigned blocks = (unsigned)(tiles < maxBlocks ? tiles : maxBlocks);
   k_meshes<<<blocks, kMeshThreads, 0, s>>>(dTerminals, numTerminals, e->dRules, e->numEntries, dMeshes, numMeshes,
                                           e->dState);
