@@ -53,6 +53,7 @@ def lib():
         L.oracle_lbvh.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp]
         L.oracle_lbvh.restype = ctypes.c_int
         L.oracle_mesh_count.restype = u32
+        L.oracle_collide.argtypes = [vp, u64, vp]
         L.oracle_mesh_sizes.argtypes = [u32, vp, vp]
         L.oracle_mesh_copy.argtypes = [u32, vp, vp]
         _lib = L
@@ -109,6 +110,29 @@ def derive_meshes(procs, entries, axioms, blocks=None, block_stride=0):
         L.oracle_mesh_copy(m, _ptr(v), _ptr(i))
         out.append((v, i))
     return terms, out
+
+
+PAIR_DT = np.dtype([("kind", "<u4", (2,)), ("ma", "<f4", (12,)), ("sa", "<f4", (3,)), ("mb", "<f4", (12,)),
+                    ("sb", "<f4", (3,))])
+
+
+def collide(pairs):
+    """The restated collision predicate on PAIR_DT records (bool array)."""
+    pairs = np.ascontiguousarray(pairs, dtype=PAIR_DT)
+    out = np.zeros(len(pairs), np.uint8)
+    lib().oracle_collide(_ptr(pairs), len(pairs), _ptr(out))
+    return out.astype(bool)
+
+
+def collide_reference(pairs, tmpdir):
+    """The reference's Collision::check on the same records (oracle/_ref)."""
+    pairs = np.ascontiguousarray(pairs, dtype=PAIR_DT)
+    pf, of = os.path.join(tmpdir, "pairs.bin"), os.path.join(tmpdir, "hits.bin")
+    pairs.tofile(pf)
+    r = subprocess.run([REF_HARNESS, "--collide", pf, of], capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        raise RuntimeError(f"ref_harness --collide failed ({r.returncode}): {r.stderr.strip()}")
+    return np.fromfile(of, np.uint8).astype(bool)
 
 
 def derive_f64(procs, entries, axioms, blocks64=None, block_stride=0, axiom_sizes64=None, capacity=None):

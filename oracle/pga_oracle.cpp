@@ -120,6 +120,66 @@ inline M4<F> rotate_xyz(float x, float y, float z) {
   return make<F>(F(r00), F(r01), F(r02), F(0), F(r10), F(r11), F(r12), F(0), F(r20), F(r21), F(r22), F(0));
 }
 
+// Oriented-box overlap, the separating-axis test of Gottschalk, Lin and
+// Manocha (OBBTree, 1996; the form in Ericson, Real-Time Collision Detection,
+// 4.4.1) as Collision::check states it for Box/Box, Box/Quad and Quad/Quad
+// (Collision.cuh:35-262, 263-490, 506-738): A's 3 face axes, B's 3, the 9 edge
+// cross products, separated when |T . L| > ra + rb.  A quad has no thickness in
+// the projected sums (its half-extent z there is 0, which drops the same terms
+// the reference drops) but keeps size.z / 2 where an axis test reads its own
+// half-extent (ra = a[i], rb = b[k]).  Float, left-to-right sums, as written.
+struct Obb {
+  float c[3];     // centre: model column 3
+  float u[3][3];  // u[j]: model column j
+  float e[3];     // size / 2
+  float es[3];    // size / 2 in the projected sums (a quad: z = 0)
+};
+
+inline float dot3(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+inline Obb make_obb(const float m[12], const float size[3], bool quad) {
+  Obb o;
+  for (int r = 0; r < 3; r++) {
+    o.c[r] = m[r * 4 + 3];
+    for (int j = 0; j < 3; j++) o.u[j][r] = m[r * 4 + j];
+  }
+  for (int k = 0; k < 3; k++) o.e[k] = o.es[k] = size[k] * 0.5f;
+  if (quad) o.es[2] = 0.0f;
+  return o;
+}
+
+inline bool obb_overlap(const Obb& A, const Obb& B) {
+  const float v[3] = {B.c[0] - A.c[0], B.c[1] - A.c[1], B.c[2] - A.c[2]};
+  float T[3], R[3][3], AR[3][3];
+  for (int i = 0; i < 3; i++) T[i] = dot3(v, A.u[i]);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      R[i][j] = dot3(A.u[i], B.u[j]);
+      AR[i][j] = std::fabs(R[i][j]);
+    }
+  const float* a = A.es;
+  const float* b = B.es;
+  for (int i = 0; i < 3; i++)
+    if (std::fabs(T[i]) > A.e[i] + (b[0] * AR[i][0] + b[1] * AR[i][1] + b[2] * AR[i][2])) return false;
+  for (int k = 0; k < 3; k++)
+    if (std::fabs(T[0] * R[0][k] + T[1] * R[1][k] + T[2] * R[2][k]) >
+        (a[0] * AR[0][k] + a[1] * AR[1][k] + a[2] * AR[2][k]) + B.e[k])
+      return false;
+  // L = A_i x B_j: with (p, q) the other two axes of A and (r, s) those of B,
+  // ra = a_p |R_qj| + a_q |R_pj|, rb = b_r |R_is| + b_s |R_ir|,
+  // t = |T_q R_pj - T_p R_qj| in the order the reference lists them.
+  static const int P[3][2] = {{1, 2}, {0, 2}, {0, 1}};
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      const int p = P[i][0], q = P[i][1], r = P[j][0], s2 = P[j][1];
+      const float ra = a[p] * AR[q][j] + a[q] * AR[p][j];
+      const float rb = b[r] * AR[i][s2] + b[s2] * AR[i][r];
+      const float t = i == 1 ? std::fabs(T[p] * R[q][j] - T[q] * R[p][j]) : std::fabs(T[q] * R[p][j] - T[p] * R[q][j]);
+      if (t > ra + rb) return false;
+    }
+  return true;
+}
+
 // Shapes::Shape + Symbol<ShapeT> (Shape.cuh:16-22, Symbol.cuh:9-15): model
 // (3x4, kept as 4x4 with the constant last row), size, seed, custom attribute,
 // entry index; plus the shape kind, the axiom index and the path hash.
@@ -824,6 +884,22 @@ extern "C" {
 static std::vector<OracleMesh> g_meshes;
 
 uint32_t oracle_mesh_count(void) { return (uint32_t)g_meshes.size(); }
+
+// obb_overlap on n pairs laid out as the reference harness reads them: kinds
+// (uint32 0 box / 1 quad) of A and B, then A's row-major 3x4 model and size,
+// then B's (128 bytes a pair); one result byte per pair.
+void oracle_collide(const void* pairs, uint64_t n, uint8_t* out) {
+  const uint8_t* p = static_cast<const uint8_t*>(pairs);
+  for (uint64_t k = 0; k < n; k++, p += 128) {
+    uint32_t kind[2];
+    float f[30];
+    std::memcpy(kind, p, 8);
+    std::memcpy(f, p + 8, 120);
+    const Obb a = make_obb(f, f + 12, kind[0] == 1), b = make_obb(f + 15, f + 27, kind[1] == 1);
+    // Collision::check(Quad, Box) is check(Box, Quad) (Collision.cuh:734-737)
+    out[k] = (kind[0] == 1 && kind[1] == 0) ? obb_overlap(b, a) : obb_overlap(a, b);
+  }
+}
 
 void oracle_mesh_sizes(uint32_t mesh, uint32_t* numVertices, uint32_t* numIndices) {
   *numVertices = mesh < g_meshes.size() ? (uint32_t)(g_meshes[mesh].vertices.size() / 12) : 0u;

@@ -12,6 +12,11 @@
 //                   include/pga_gb300.h, path hash left 0 because the reference
 //                   has no derivation-path hash)
 // argv[3] (optional): number of timed repetitions of execute().
+//
+// ref_harness --collide <pairs.bin> <out.bin> runs the reference's collision
+// predicate PGA::ContextSensitivity::Collision::check (Collision.cuh) on shape
+// pairs instead: per pair two uint32 kinds (0 box, 1 quad), then for A and B a
+// row-major 3x4 model and a size (15 floats each); out: one byte per pair.
 // When the grammar has triangle-mesh terminals (Generate<false, 0, ...>), their
 // meshes go to argv[2] + ".mesh": "PGAM", mesh count, then per mesh the vertex
 // and index counts, the vertices (48 B each, TriangleMeshData::VertexAttributes
@@ -42,6 +47,7 @@
 #include <pga/core/Subdivide.cuh>
 #include <pga/core/TStdLib.h>
 #include <pga/core/Translate.cuh>
+#include <pga/core/Collision.cuh>
 #include <pga/rendering/ShapeMeshAttributes.cuh>
 
 #include <algorithm>
@@ -230,7 +236,40 @@ struct HarnessAxioms {
   }
 };
 
+template <typename ShapeT>
+static ShapeT make_shape(const float* m, const float* size) {
+  ShapeT s;
+  s.setModel(math::float3x4(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10], m[11]));
+  s.setSize(math::float3(size[0], size[1], size[2]));
+  return s;
+}
+
+static int collide_main(const char* in, const char* outPath) {
+  FILE* f = fopen(in, "rb");
+  if (!f) { perror("open pairs"); return 2; }
+  std::vector<uint8_t> results;
+  struct Pair { uint32_t ka, kb; float ma[12], sa[3], mb[12], sb[3]; } p;
+  static_assert(sizeof(Pair) == 128, "pair record");
+  while (fread(&p, sizeof p, 1, f) == 1) {
+    bool hit;
+    using ContextSensitivity::Collision;
+    if (p.ka == 0 && p.kb == 0) hit = Collision::check(make_shape<Box>(p.ma, p.sa), make_shape<Box>(p.mb, p.sb));
+    else if (p.ka == 0) hit = Collision::check(make_shape<Box>(p.ma, p.sa), make_shape<Quad>(p.mb, p.sb));
+    else if (p.kb == 0) hit = Collision::check(make_shape<Quad>(p.ma, p.sa), make_shape<Box>(p.mb, p.sb));
+    else hit = Collision::check(make_shape<Quad>(p.ma, p.sa), make_shape<Quad>(p.mb, p.sb));
+    results.push_back(hit ? 1 : 0);
+  }
+  fclose(f);
+  FILE* o = fopen(outPath, "wb");
+  if (!o) { perror("open output"); return 2; }
+  fwrite(results.data(), 1, results.size(), o);
+  fclose(o);
+  printf("{\"pairs\": %zu}\n", results.size());
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 4 && strcmp(argv[1], "--collide") == 0) return collide_main(argv[2], argv[3]);
   if (argc < 3) {
     fprintf(stderr, "usage: ref_harness <batch.bin> <terminals.bin> [repeats]\n");
     return 2;
