@@ -90,8 +90,11 @@ typedef enum PgaOperator {
                                     no other is (RandomRule.cuh:33-99) */,
   PGA_OP_IF = 14,              /* If<DynParam<0> condition, DCall<0> true, DCall<1> false>: nonzero is true */
   PGA_OP_SWAP_SIZE = 15,       /* SwapSize<DynParam<0..2> axes, DCall<0>>: size = (size[a0], size[a1], size[a2]) */
-  PGA_OP_GENERATE_MESH = 16    /* Generate<false, 0, DynParam<0> mesh index>: a triangle-mesh terminal; its record
+  PGA_OP_GENERATE_MESH = 16,   /* Generate<false, 0, DynParam<0> mesh index>: a triangle-mesh terminal; its record
                                   is written like an instanced one and pga_generate_meshes expands it */
+  PGA_OP_COLLIDER = 17,        /* Collider<DynParam<0> tag, DCall<0>>: a tag > 0 stores the shape for IfCollides */
+  PGA_OP_IF_COLLIDES = 18      /* IfCollides<DynParam<0> tag, DCall<0> true, DCall<1> false>: does a shape stored
+                                  with the tag in an earlier phase overlap this one */
 } PgaOperator;
 
 typedef enum PgaShape { PGA_SHAPE_BOX = 0, PGA_SHAPE_QUAD = 1 } PgaShape;
@@ -220,7 +223,9 @@ const char* pga_last_error(void);
  *  28 Box  RandomRule, 4 static pairs   29 Quad RandomRule, 4 static pairs
  *  30 Box  If                           31 Quad If
  *  32 Box  SwapSize                     33 Quad SwapSize
- *  34 Box  Generate (triangle mesh)     35 Quad Generate (triangle mesh) */
+ *  34 Box  Generate (triangle mesh)     35 Quad Generate (triangle mesh)
+ *  36 Box  Collider                     37 Quad Collider
+ *  38 Box  IfCollides                   39 Quad IfCollides */
 const PgaProc* pga_default_procs(uint32_t* numProcs);
 
 /* Replaces SinglePhaseEvaluator::initialize(DispatchTableEntry*, n)

@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -92,6 +93,21 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.numParams = (uint32_t)e->hParams.size();
   a.numSucc = (uint32_t)e->hSucc.size();
   a.st = e->dState;
+  a.phase = 0;
+  a.deferIn = nullptr;
+  a.deferRotIn = nullptr;
+  a.numDeferIn = 0;
+  a.deferOut = e->dDefer[0];
+  a.deferRotOut = e->dDeferRot[0];
+  a.deferCap = e->phased ? e->cfg.nodeCapacity : 0;
+  a.phaseCounters = e->dPhaseCounters;
+  a.colRec = e->dColRec;
+  a.colShape = e->dColShape;
+  a.colCap = e->colCap;
+  a.colNodes = e->dColNodes;
+  a.colAabbs = e->dColAabbs;
+  a.colLeaf = e->dColLeaf;
+  a.numColliders = 0;
   return a;
 }
 
@@ -106,6 +122,7 @@ FrameKernels general_frame_kernels();  // derive_gen.cu
 // The instantiation of the persistent kernel for an engine: its frame build,
 // leaf children in place or not, with or without the 1 -> 1 affine steps.
 static const void* persistent_kernel(const PgaEngine* e) {
+  if (e->phased) return e->kernels.phased;
   return e->kernels.persistent[(e->leafKernel ? 1 : 0) + (e->affineKernel ? 2 : 0)];
 }
 
@@ -114,8 +131,9 @@ static const void* persistent_kernel(const PgaEngine* e) {
 // so any of them can run co-resident.
 static cudaError_t set_kernel_smem(const FrameKernels& k, size_t bytes) {
   cudaError_t err = cudaSuccess;
-  for (int i = 0; i < 4 && err == cudaSuccess; i++)
-    err = cudaFuncSetAttribute(k.persistent[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  for (int i = 0; i < 5 && err == cudaSuccess; i++)
+    err = cudaFuncSetAttribute(i < 4 ? k.persistent[i] : k.phased, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)bytes);
   if (err == cudaSuccess) err = cudaFuncSetAttribute(k.seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (err == cudaSuccess) err = cudaFuncSetAttribute(k.expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   return err;
@@ -123,9 +141,9 @@ static cudaError_t set_kernel_smem(const FrameKernels& k, size_t bytes) {
 static cudaError_t persistent_occupancy(const FrameKernels& k, int* perSM, int threads, size_t smem) {
   int best = 1 << 30;
   cudaError_t err = cudaSuccess;
-  for (int i = 0; i < 4 && err == cudaSuccess; i++) {
+  for (int i = 0; i < 5 && err == cudaSuccess; i++) {
     int n = 0;
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.persistent[i], threads, smem);
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, i < 4 ? k.persistent[i] : k.phased, threads, smem);
     best = std::min(best, n);
   }
   *perSM = best;
@@ -154,7 +172,7 @@ static void rotate_xyz(float x, float y, float z, float q[9]) {
   q[8] = ca * cb;
 }
 
-static const PgaProc kDefaultProcs[36] = {
+static const PgaProc kDefaultProcs[40] = {
     {PGA_OP_SUBDIVIDE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SUBDIVIDE, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_BOX, 3, 1}, {PGA_OP_SUBDIVIDE_STATIC, PGA_SHAPE_QUAD, 3, 1},
     {PGA_OP_REPEAT, PGA_SHAPE_BOX, 0, 1},           {PGA_OP_REPEAT, PGA_SHAPE_QUAD, 0, 1},
@@ -173,6 +191,8 @@ static const PgaProc kDefaultProcs[36] = {
     {PGA_OP_IF, PGA_SHAPE_BOX, 0, 1},               {PGA_OP_IF, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_SWAP_SIZE, PGA_SHAPE_BOX, 0, 1},        {PGA_OP_SWAP_SIZE, PGA_SHAPE_QUAD, 0, 1},
     {PGA_OP_GENERATE_MESH, PGA_SHAPE_BOX, 0, 1},    {PGA_OP_GENERATE_MESH, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_COLLIDER, PGA_SHAPE_BOX, 0, 1},         {PGA_OP_COLLIDER, PGA_SHAPE_QUAD, 0, 1},
+    {PGA_OP_IF_COLLIDES, PGA_SHAPE_BOX, 0, 1},      {PGA_OP_IF_COLLIDES, PGA_SHAPE_QUAD, 0, 1},
 };
 
 extern "C" {
@@ -182,11 +202,15 @@ const char* pga_version(void) { return "pga_gb300 0.1.0 (sm_103a)"; }
 const char* pga_last_error(void) { return g_error.c_str(); }
 
 const PgaProc* pga_default_procs(uint32_t* numProcs) {
-  if (numProcs) *numProcs = 36;
+  if (numProcs) *numProcs = 40;
   return kDefaultProcs;
 }
 
 static void free_engine(PgaEngine* e) {
+  void* phasePtrs[] = {e->dDefer[0], e->dDefer[1], e->dDeferRot[0], e->dDeferRot[1], e->dColRec, e->dColShape,
+                       e->dColNodes, e->dColParents, e->dColAabbs, e->dColLeaf, e->dColKeys, e->dPhaseCounters};
+  for (void* p : phasePtrs)
+    if (p) cudaFree(p);
   void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dNodeRot, e->dLevelClock,
                   e->dTail, e->dTailLinks, e->dScratch,
                   e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA,
@@ -242,7 +266,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     r.op = 0xFF;
     if (en.operatorCode >= 0 && (uint32_t)en.operatorCode < table->numProcs) {
       const PgaProc& p = table->procs[en.operatorCode];
-      if (p.op <= PGA_OP_GENERATE_MESH && p.shape <= PGA_SHAPE_QUAD) {
+      if (p.op <= PGA_OP_IF_COLLIDES && p.shape <= PGA_SHAPE_QUAD) {
         // A triangle-mesh Generate derives exactly like an instanced one; the
         // flag marks its records for pga_generate_meshes.
         r.op = (uint8_t)(p.op == PGA_OP_GENERATE_MESH ? PGA_OP_GENERATE : p.op);
@@ -335,14 +359,50 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     // replays one work item per branching shape) or when disabled.
     if (leaf && !c.recordTape && !(c.flags & PGA_FLAG_NO_INLINE)) e->leafKernel = true;
   }
+  // Phases: the phase of a rule is the phaseIndex of the successor edges that
+  // lead to it (the reference queues a symbol in the phase its edge names,
+  // CPUEvaluator.h:155-190); edges into one rule must agree.  A shape reaching
+  // a rule of a later phase is deferred to that phase's launch.
+  {
+    std::vector<int> phaseOf(e->hRules.size(), -1);
+    for (uint32_t i = 0; i < table->numEntries; i++) {
+      const PgaEntry& en = table->entries[i];
+      for (uint32_t k = 0; k < en.numSuccessors && k < PGA_MAX_NUM_SUCCESSORS; k++) {
+        const int32_t t = en.successors[k].entryIndex;
+        if (t < 0 || (uint32_t)t >= table->numEntries) continue;
+        const int ph = en.successors[k].phaseIndex < 0 ? 0 : en.successors[k].phaseIndex;
+        if (ph >= (int)kMaxPhases || (phaseOf[t] >= 0 && phaseOf[t] != ph)) {
+          set_error("pga_engine_create: entry " + std::to_string(t) +
+                    ": successor edges name different phases (or a phase >= 16)");
+          delete e;
+          return PGA_ERR_BAD_PARAM;
+        }
+        phaseOf[t] = ph;
+      }
+    }
+    for (size_t t = 0; t < e->hRules.size(); t++) {
+      if (phaseOf[t] > 0) {
+        e->hRules[t].flags = (uint16_t)(e->hRules[t].flags | (phaseOf[t] << kRulePhaseShift));
+        e->phased = true;
+      }
+    }
+  }
   for (const DevRule& r : e->hRules) {
+    if (r.op == PGA_OP_COLLIDER || r.op == PGA_OP_IF_COLLIDES) e->phased = true;
     if (r.op == PGA_OP_TRANSLATE || r.op == PGA_OP_SCALE || r.op == PGA_OP_RANDOM_RULE || r.op == PGA_OP_ROTATE ||
         r.op == PGA_OP_REPLICATE || r.op == PGA_OP_RANDOM_RULE_STATIC || r.op == PGA_OP_IF || r.op == PGA_OP_SWAP_SIZE)
       e->affineKernel = true;
     if (r.op == PGA_OP_ROTATE) e->generalFrames = true;
   }
-  if (e->generalFrames && c.recordTape) {
-    set_error("pga_engine_create: the adjoint (recordTape) does not cover Rotate");
+  if (e->phased) {
+    // phase checks, Collider and IfCollides live in the AFF instantiations;
+    // leaf children in place would skip the phase check of their Generates
+    e->affineKernel = true;
+    e->leafKernel = false;
+    for (DevRule& r : e->hRules) r.flags = (uint16_t)(r.flags & ~kRuleLeaf);
+  }
+  if ((e->generalFrames || e->phased) && c.recordTape) {
+    set_error("pga_engine_create: the adjoint (recordTape) covers neither Rotate nor phases and colliders");
     delete e;
     return PGA_ERR_BAD_PARAM;
   }
@@ -368,6 +428,23 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   ALLOC(e->dState, sizeof(DevState));
   ALLOC(e->dNodes, c.nodeCapacity * sizeof(Node));
   if (e->generalFrames) ALLOC(e->dNodeRot, c.nodeCapacity * 2 * sizeof(float4));
+  if (e->phased) {
+    // deferred shapes (two buffers: the phase's input and its output),
+    // colliders (records, oriented boxes) and the colliders' LBVH
+    for (int k = 0; k < 2; k++) {
+      ALLOC(e->dDefer[k], c.nodeCapacity * sizeof(Node));
+      if (e->generalFrames) ALLOC(e->dDeferRot[k], c.nodeCapacity * 2 * sizeof(float4));
+    }
+    e->colCap = std::min<uint64_t>(c.nodeCapacity, c.maxTerminals);
+    ALLOC(e->dColRec, e->colCap * sizeof(PgaTerminal));
+    ALLOC(e->dColShape, e->colCap * 5 * sizeof(float4));
+    ALLOC(e->dColNodes, std::max<uint64_t>(e->colCap, 2) * 3 * sizeof(int32_t));
+    ALLOC(e->dColParents, e->colCap * sizeof(uint32_t));
+    ALLOC(e->dColAabbs, std::max<uint64_t>(e->colCap, 2) * 6 * sizeof(float));
+    ALLOC(e->dColLeaf, e->colCap * sizeof(uint32_t));
+    ALLOC(e->dColKeys, e->colCap * sizeof(uint64_t));
+    ALLOC(e->dPhaseCounters, 4 * sizeof(unsigned long long));
+  }
   ALLOC(e->dLevelStart, (c.maxLevels + 2) * sizeof(unsigned long long));
   ALLOC(e->dLevelClock, (c.maxLevels + 2) * sizeof(unsigned long long));
   ALLOC(e->dScratchCount, sizeof(unsigned long long));
@@ -478,6 +555,116 @@ static PgaStatus launch_persistent(PgaEngine* e, const PgaAxiom* dAxioms, uint32
   return PGA_OK;
 }
 
+// Bounds of the colliders' centres (one block), for the Morton codes of their LBVH.
+__global__ void k_collider_bounds(const PgaTerminal* rec, unsigned long long n, float* out) {
+  __shared__ float sh[6][256];
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (unsigned long long i = threadIdx.x; i < n; i += blockDim.x)
+    for (int k = 0; k < 3; k++) {
+      const float c = rec[i].m[k * 4 + 3];
+      lo[k] = fminf(lo[k], c);
+      hi[k] = fmaxf(hi[k], c);
+    }
+  for (int k = 0; k < 3; k++) {
+    sh[k][threadIdx.x] = lo[k];
+    sh[3 + k][threadIdx.x] = hi[k];
+  }
+  __syncthreads();
+  for (unsigned w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < 3; k++) {
+        sh[k][threadIdx.x] = fminf(sh[k][threadIdx.x], sh[k][threadIdx.x + w]);
+        sh[3 + k][threadIdx.x] = fmaxf(sh[3 + k][threadIdx.x], sh[3 + k][threadIdx.x + w]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) out[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// Multi-phase derivation (MultiPhaseEvaluator::execute, CPUEvaluator.h:330-352,
+// with the GPU evaluator's BVH construction between phases): phase 0 from the
+// axioms; every later phase from the shapes the previous launch deferred, with
+// the colliders stored so far in an LBVH for IfCollides.  Each phase is one
+// persistent launch appending to the output; the host reads the counts back
+// between phases.
+static PgaStatus derive_phases(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dBlocks,
+                               PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount, cudaStream_t s) {
+  PGA_CUDA_TRY(cudaMemsetAsync(e->dPhaseCounters, 0, 4 * sizeof(unsigned long long), s));
+  uint64_t total = 0, numDefer = 0;
+  uint32_t visible = 0;
+  e->phasesRun = 0;
+  for (uint32_t phase = 0; phase < kMaxPhases; phase++) {
+    PGA_CUDA_TRY(cudaMemsetAsync(e->dState, 0, sizeof(DevState), s));
+    PGA_CUDA_TRY(cudaMemsetAsync(e->dPhaseCounters + 1, 0, 2 * sizeof(unsigned long long), s));
+    const uint64_t off = std::min(total, capacity);
+    DeriveArgs a = make_args(e, dAxioms, numAxioms, dBlocks, dOut ? dOut + off : nullptr, capacity - off,
+                             e->dPhaseCounters + 2);
+    a.phase = phase;
+    if (phase > 0) {
+      a.deferIn = e->dDefer[(phase + 1) & 1];
+      a.deferRotIn = e->dDeferRot[(phase + 1) & 1];
+      a.numDeferIn = numDefer;
+    }
+    a.deferOut = e->dDefer[phase & 1];
+    a.deferRotOut = e->dDeferRot[phase & 1];
+    a.numColliders = visible;
+    void* args[] = {&a};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)e->persistentBlocks);
+    cfg.blockDim = dim3((unsigned)e->threads);
+    cfg.dynamicSmemBytes = e->smemBytes;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, persistent_kernel(e), args));
+    DevState snap;
+    unsigned long long counters[2];
+    PGA_CUDA_TRY(cudaMemcpyAsync(&snap, e->dState, sizeof snap, cudaMemcpyDeviceToHost, s));
+    PGA_CUDA_TRY(cudaMemcpyAsync(counters, e->dPhaseCounters, sizeof counters, cudaMemcpyDeviceToHost, s));
+    PGA_CUDA_TRY(cudaStreamSynchronize(s));
+    e->phasesRun = phase + 1;
+    total += snap.termCount;
+    numDefer = counters[1];
+    if (snap.status != 0 || numDefer == 0) break;
+    // The colliders stored so far, for the next phase's IfCollides.
+    visible = (uint32_t)std::min<unsigned long long>(counters[0], e->colCap);
+    if (visible == 1) {
+      PGA_CUDA_TRY(cudaMemsetAsync(e->dColLeaf, 0, sizeof(uint32_t), s));
+    } else if (visible >= 2) {
+      float* dB = reinterpret_cast<float*>(e->dColAabbs);  // scratch until the LBVH writes it
+      k_collider_bounds<<<1, 256, 0, s>>>(e->dColRec, visible, dB);
+      PGA_CUDA_TRY(cudaGetLastError());
+      float hb[6];
+      PGA_CUDA_TRY(cudaMemcpyAsync(hb, dB, sizeof hb, cudaMemcpyDeviceToHost, s));
+      PGA_CUDA_TRY(cudaStreamSynchronize(s));
+      PgaBounds b;
+      for (int k = 0; k < 3; k++) {
+        b.min[k] = hb[k] - 1.0f;
+        b.max[k] = hb[3 + k] + 1.0f;
+      }
+      PgaLbvh out = {e->dColNodes, e->dColParents, e->dColAabbs, e->dColLeaf, e->dColKeys};
+      const PgaStatus st = pga_lbvh_build(e, e->dColRec, visible, &b, &out, s);
+      if (st != PGA_OK) return st;
+    }
+  }
+  e->phaseTerminals = total;
+  if (dCount) {
+    e->phaseTerminalsHost = total;
+    PGA_CUDA_TRY(cudaMemcpyAsync(dCount, &e->phaseTerminalsHost, sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    PGA_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  e->lastAxioms = dAxioms;
+  e->lastNumAxioms = numAxioms;
+  e->lastBlocks = dBlocks;
+  e->lastOut = dOut;
+  e->lastCap = capacity;
+  e->lastWasBatched = true;
+  return PGA_OK;
+}
+
 extern "C" {
 
 PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dParamBlocks,
@@ -486,6 +673,7 @@ PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, 
     set_error("pga_derive: null engine or buffers");
     return PGA_ERR_INVALID_ARGUMENT;
   }
+  if (e->phased) return derive_phases(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, dCount, (cudaStream_t)stream);
   return launch_persistent(e, dAxioms, 0, numAxioms, dParamBlocks, dOut, capacity, dCount, (cudaStream_t)stream);
 }
 
@@ -504,6 +692,10 @@ PgaStatus pga_derive_to_host(PgaEngine* e, const PgaAxiom* hAxioms, uint32_t num
                              PgaTerminal* hOut, uint64_t capacity, uint64_t* hCount, void* stream) {
   if (!e || (!hAxioms && numAxioms) || (!hOut && capacity) || !hCount) {
     set_error("pga_derive_to_host: null engine, buffers or count");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  if (e->phased) {
+    set_error("pga_derive_to_host: a multi-phase table (phases, Collider, IfCollides) needs pga_derive");
     return PGA_ERR_INVALID_ARGUMENT;
   }
   cudaStream_t s = (cudaStream_t)stream;
@@ -565,6 +757,10 @@ PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAx
     set_error("pga_derive_plain: null engine or buffers");
     return PGA_ERR_INVALID_ARGUMENT;
   }
+  if (e->phased) {
+    set_error("pga_derive_plain: a multi-phase table (phases, Collider, IfCollides) needs pga_derive");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   PGA_CUDA_TRY(cudaMemsetAsync(e->dState, 0, sizeof(DevState), s));
   DeriveArgs a = make_args(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
@@ -618,6 +814,7 @@ PgaStatus pga_engine_sync_report(PgaEngine* e, void* stream, PgaDeriveReport* re
   PGA_CUDA_TRY(cudaMemcpyAsync(&snap, e->dState, sizeof(DevState), cudaMemcpyDeviceToHost, s));
   PGA_CUDA_TRY(cudaStreamSynchronize(s));
   memset(report, 0, sizeof *report);
+  if (e->phased) snap.termCount = e->phaseTerminals;  // over all phases
   // Terminals past the caller's capacity were dropped (never wrapped around):
   // that is an output overflow, reported with the full count.
   if (snap.status == 0 && snap.termCount > e->lastCap) snap.status = PGA_ERR_OUTPUT_OVERFLOW;

@@ -211,6 +211,202 @@ __device__ __forceinline__ bool swap_size(const DeriveArgs& a, const DevRule& r,
   return true;
 }
 
+// ------------------------------------------------------ phases and colliders
+
+// A shape reaching a rule of a later phase waits there: it is written to the
+// deferred buffer, which seeds the next phase's launch (the reference puts it
+// in that phase's queue, CPUEvaluator.h:155-190).
+__device__ __noinline__ void defer_shape(const DeriveArgs& a, const Shape& x) {
+  const unsigned long long i = atomicAdd(a.phaseCounters + 1, 1ull);
+  if (i >= a.deferCap) {
+    raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, x.entry);
+    return;
+  }
+#if PGA_GENERAL_FRAMES
+  const float w = x.R[8];
+  a.deferRotOut[2 * i] = make_float4(x.R[0], x.R[1], x.R[2], x.R[3]);
+  a.deferRotOut[2 * i + 1] = make_float4(x.R[4], x.R[5], x.R[6], x.R[7]);
+#else
+  const float w = __uint_as_float(x.frame);
+#endif
+  float4* p = reinterpret_cast<float4*>(a.deferOut + i);
+  p[0] = make_float4(x.t[0], x.t[1], x.t[2], x.s[0]);
+  p[1] = make_float4(x.s[1], x.s[2], x.seed, w);
+  reinterpret_cast<uint4*>(p)[2] = make_uint4((uint32_t)x.entry, x.axiom, (uint32_t)x.path, (uint32_t)(x.path >> 32));
+  reinterpret_cast<uint4*>(p)[3] = make_uint4(0u, 0u, kAxiomLink | x.axiom, 0u);
+}
+
+// Collider<Tag, Next> (Collider.cuh:20-45) stores the shape with its tag
+// (IntermediateSymbolsBufferAdapter.cuh:200-215): here as a record for the
+// LBVH (model * scale, tag, shape bit, path) and as an oriented box of 5
+// float4: rotation columns u0 u1 u2 (9) and centre (3), half extents (3), tag.
+__device__ __noinline__ void store_collider(const DeriveArgs& a, const Shape& x, uint32_t tag) {
+  const unsigned long long i = atomicAdd(a.phaseCounters, 1ull);
+  if (i >= a.colCap) {
+    raise_error(a.st, PGA_ERR_QUEUE_OVERFLOW, x.entry);
+    return;
+  }
+  float m[3][3];
+  frame_scaled(x, m);
+  float4* rec = reinterpret_cast<float4*>(a.colRec + i);
+  rec[0] = make_float4(m[0][0], m[0][1], m[0][2], x.t[0]);
+  rec[1] = make_float4(m[1][0], m[1][1], m[1][2], x.t[1]);
+  rec[2] = make_float4(m[2][0], m[2][1], m[2][2], x.t[2]);
+  const uint32_t quad = x.kind == PGA_SHAPE_QUAD ? 0x80000000u : 0u;
+  reinterpret_cast<uint4*>(rec)[3] = make_uint4((tag & 0xFFFFFFu) | quad, 0u, (uint32_t)x.path, (uint32_t)(x.path >> 32));
+  float u[3][3];
+#pragma unroll
+  for (uint32_t j = 0; j < 3; j++)
+#pragma unroll
+    for (uint32_t r = 0; r < 3; r++) u[j][r] = frame_at(x, r, j);
+  float4* sh = a.colShape + 5 * i;
+  sh[0] = make_float4(u[0][0], u[0][1], u[0][2], u[1][0]);
+  sh[1] = make_float4(u[1][1], u[1][2], u[2][0], u[2][1]);
+  sh[2] = make_float4(u[2][2], x.t[0], x.t[1], x.t[2]);
+  sh[3] = make_float4(__fmul_rn(x.s[0], 0.5f), __fmul_rn(x.s[1], 0.5f), __fmul_rn(x.s[2], 0.5f),
+                      __uint_as_float(quad ? 1u : 0u));
+  sh[4] = make_float4(__int_as_float((int)tag), 0.0f, 0.0f, 0.0f);
+}
+
+// An oriented box for the separating-axis test: centre, axes (model columns),
+// half extents, and the half extents in the projected sums (a quad: z = 0).
+struct Obb {
+  float c[3], u[3][3], e[3], es[3];
+};
+
+__device__ __forceinline__ float dot3(const float* p, const float* q) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(p[0], q[0]), __fmul_rn(p[1], q[1])), __fmul_rn(p[2], q[2]));
+}
+
+// Collision::check for Box/Box, Box/Quad and Quad/Quad (Collision.cuh:35-738):
+// the separating-axis test of Gottschalk, Lin and Manocha (OBBTree, 1996) over
+// A's 3 face axes, B's 3 and the 9 edge cross products, separated when
+// |T . L| > ra + rb, every sum left to right as the reference writes it.
+__device__ __forceinline__ bool obb_overlap(const Obb& A, const Obb& B) {
+  const float v[3] = {__fsub_rn(B.c[0], A.c[0]), __fsub_rn(B.c[1], A.c[1]), __fsub_rn(B.c[2], A.c[2])};
+  float T[3], R[3][3], AR[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) T[i] = dot3(v, A.u[i]);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R[i][j] = dot3(A.u[i], B.u[j]);
+      AR[i][j] = fabsf(R[i][j]);
+    }
+  const float* a = A.es;
+  const float* b = B.es;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float rb = __fadd_rn(__fadd_rn(__fmul_rn(b[0], AR[i][0]), __fmul_rn(b[1], AR[i][1])), __fmul_rn(b[2], AR[i][2]));
+    if (fabsf(T[i]) > __fadd_rn(A.e[i], rb)) return false;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float ra = __fadd_rn(__fadd_rn(__fmul_rn(a[0], AR[0][k]), __fmul_rn(a[1], AR[1][k])), __fmul_rn(a[2], AR[2][k]));
+    const float t =
+        fabsf(__fadd_rn(__fadd_rn(__fmul_rn(T[0], R[0][k]), __fmul_rn(T[1], R[1][k])), __fmul_rn(T[2], R[2][k])));
+    if (t > __fadd_rn(ra, B.e[k])) return false;
+  }
+  // L = A_i x B_j: (p, q) the other axes of A, (r, s) those of B.
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const int p = i == 0 ? 1 : 0, q = i == 2 ? 1 : 2;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int r = j == 0 ? 1 : 0, s = j == 2 ? 1 : 2;
+      const float ra = __fadd_rn(__fmul_rn(a[p], AR[q][j]), __fmul_rn(a[q], AR[p][j]));
+      const float rb = __fadd_rn(__fmul_rn(b[r], AR[i][s]), __fmul_rn(b[s], AR[i][r]));
+      const float t = i == 1 ? fabsf(__fsub_rn(__fmul_rn(T[p], R[q][j]), __fmul_rn(T[q], R[p][j])))
+                             : fabsf(__fsub_rn(__fmul_rn(T[q], R[p][j]), __fmul_rn(T[p], R[q][j])));
+      if (t > __fadd_rn(ra, rb)) return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ Obb collider_obb(const float4* sh, bool& quad, int& tag) {
+  const float4 s0 = __ldg(sh), s1 = __ldg(sh + 1), s2 = __ldg(sh + 2), s3 = __ldg(sh + 3), s4 = __ldg(sh + 4);
+  Obb o;
+  o.u[0][0] = s0.x; o.u[0][1] = s0.y; o.u[0][2] = s0.z;
+  o.u[1][0] = s0.w; o.u[1][1] = s1.x; o.u[1][2] = s1.y;
+  o.u[2][0] = s1.z; o.u[2][1] = s1.w; o.u[2][2] = s2.x;
+  o.c[0] = s2.y; o.c[1] = s2.z; o.c[2] = s2.w;
+  o.e[0] = o.es[0] = s3.x;
+  o.e[1] = o.es[1] = s3.y;
+  o.e[2] = s3.z;
+  quad = __float_as_uint(s3.w) != 0u;
+  o.es[2] = quad ? 0.0f : s3.z;
+  tag = __float_as_int(s4.x);
+  return o;
+}
+
+// IfCollides<Tag, ...> (IfCollides.cuh:18-36, BVHTraversal.cuh:16-120): does a
+// collider stored with the tag in an earlier phase overlap x?  The colliders'
+// LBVH is traversed with a conservative box test (x's world box, widened by a
+// relative 1e-5, against a node's box), so that no collider the exact test
+// would report is pruned: the answer is "any collider with the tag overlaps",
+// with Collision::check(stored, x) deciding at the leaves.
+__device__ __noinline__ bool collides(const DeriveArgs& a, const Shape& x, uint32_t tag) {
+  const uint32_t n = a.numColliders;
+  if (n == 0) return false;
+  Obb me;
+  const bool quad = x.kind == PGA_SHAPE_QUAD;
+#pragma unroll
+  for (uint32_t j = 0; j < 3; j++)
+#pragma unroll
+    for (uint32_t r = 0; r < 3; r++) me.u[j][r] = frame_at(x, r, j);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    me.c[k] = x.t[k];
+    me.e[k] = me.es[k] = __fmul_rn(x.s[k], 0.5f);
+  }
+  if (quad) me.es[2] = 0.0f;
+  float lo[3], hi[3];
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    float h = fabsf(me.u[0][r]) * me.e[0] + fabsf(me.u[1][r]) * me.e[1] + fabsf(me.u[2][r]) * me.e[2];
+    h = h * 1.00001f + 1e-5f * (fabsf(me.c[r]) + 1.0f);
+    lo[r] = me.c[r] - h;
+    hi[r] = me.c[r] + h;
+  }
+  auto leaf_hits = [&](uint32_t leaf) -> bool {
+    const uint32_t rec = __ldg(a.colLeaf + leaf);
+    bool cq;
+    int ctag;
+    const Obb other = collider_obb(a.colShape + 5ull * rec, cq, ctag);
+    if (ctag != (int)tag) return false;
+    // Collision::check(Quad, Box) is check(Box, Quad) (Collision.cuh:734-737)
+    return (cq && !quad) ? obb_overlap(me, other) : obb_overlap(other, me);
+  };
+  if (n == 1) return leaf_hits(0);
+  int stack[64];
+  int top = 0;
+  stack[top++] = 0;
+  while (top > 0) {
+    const int node = stack[--top];
+#pragma unroll
+    for (int side = 1; side <= 2; side++) {
+      const int child = __ldg(a.colNodes + 3 * node + side);
+      if (child >= 0) {
+        if (leaf_hits((uint32_t)child)) return true;
+      } else {
+        const float* bx = a.colAabbs + 6ll * (-child);
+        const bool overlap = __ldg(bx) <= hi[0] && __ldg(bx + 3) >= lo[0] && __ldg(bx + 1) <= hi[1] &&
+                             __ldg(bx + 4) >= lo[1] && __ldg(bx + 2) <= hi[2] && __ldg(bx + 5) >= lo[2];
+        if (overlap) {
+          if (top >= 64) {
+            raise_error(a.st, PGA_ERR_DEPTH, x.entry);
+            return false;
+          }
+          stack[top++] = -child;
+        }
+      }
+    }
+  }
+  return false;
+}
+
 // Resolves a freshly created shape through IfSizeLess / Extrude / Translate /
 // Scale / RandomRule rules (If.cuh:65-89, Extrude.cuh:29-56, Translate.cuh:24-43,
 // Scale.cuh:23-45, RandomRule.cuh:121-150) until it reaches a Generate (terminal), a
@@ -218,7 +414,7 @@ __device__ __forceinline__ bool swap_size(const DeriveArgs& a, const DevRule& r,
 // steps are compiled in with AFF only: the persistent kernel has an
 // instantiation without them for grammars that use none, which keeps their
 // registers out of its expansion loops.
-template <bool AFF>
+template <int AFF>
 __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& tidx) {
   for (int step = 0; step < kMaxChain; step++) {
     if (x.entry < 0 || (uint32_t)x.entry >= a.tab.numEntries) {
@@ -229,6 +425,28 @@ __device__ __forceinline__ int resolve(const DeriveArgs& a, Shape& x, uint32_t& 
     if (r.op == 0xFF || r.shape != x.kind) {
       raise_error(a.st, PGA_ERR_BAD_OPCODE, x.entry);
       return kNone;
+    }
+    if (AFF >= 2) {
+      // phases and colliders: compiled in the instantiation for multi-phase tables only
+      if ((uint32_t)(r.flags >> kRulePhaseShift) > a.phase) {
+        defer_shape(a, x);
+        return kNone;
+      }
+      if (r.op == PGA_OP_COLLIDER) {
+        if (r.nParams < 1 || r.nSucc < 1) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        const uint32_t tag = f2u(param(a, r, 0, x));
+        if (tag > 0) store_collider(a, x, tag);
+        x.entry = succ_at(a, r.succBase);
+        continue;
+      }
+      if (r.op == PGA_OP_IF_COLLIDES) {
+        if (r.nParams < 1 || r.nSucc < 2) { raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry); return kNone; }
+        const uint32_t branch = collides(a, x, f2u(param(a, r, 0, x)) & 0xFFu) ? 0u : 1u;
+        const int32_t nxt = succ_at(a, r.succBase + branch);
+        x.path = child_path(x.path, branch, nxt);
+        x.entry = nxt;
+        continue;
+      }
     }
     switch (r.op) {
       case PGA_OP_IF_SIZE_LESS: {
@@ -442,7 +660,7 @@ __device__ __forceinline__ uint32_t subdivide_setup(const DeriveArgs& a, const D
 
 // Operator set-up; returns the number of child slots (0 on error).  Replicate
 // is compiled in with AFF only (see resolve).
-template <bool AFF = true>
+template <int AFF = 1>
 __device__ __forceinline__ uint32_t expander_init(const DeriveArgs& a, Expander& E) {
   const Shape& x = E.base;
   const DevRule& r = E.r;
@@ -532,7 +750,7 @@ __device__ __forceinline__ void expander_skip(const DeriveArgs& a, Expander& E, 
 
 // Produces child slot c (slots are produced in increasing order).  Returns
 // false when the slot yields no child (a zero factor of a static Subdivide).
-template <bool AFF = true>
+template <int AFF = 1>
 __device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Shape& y,
                                                uint32_t& ordinal) {
   const Shape& x = E.base;
@@ -939,7 +1157,7 @@ __device__ __forceinline__ void axiom_shape(const DeriveArgs& a, uint32_t i, Sha
 }
 
 // Expands the work items first + 32 k + lane (k < K, item < hi) of one warp.
-template <bool PAGED, bool LEAF, bool AFF>
+template <bool PAGED, bool LEAF, int AFF>
 __device__ __forceinline__ void warp_items(const DeriveArgs& a, WarpOut& w, unsigned long long first,
                                            unsigned long long hi, uint32_t K) {
   const unsigned lane = threadIdx.x & 31u;
@@ -981,7 +1199,7 @@ __device__ __forceinline__ void warp_items(const DeriveArgs& a, WarpOut& w, unsi
 }
 
 // Seeds the axioms [first, first + count) with a warp-uniform grid-stride loop.
-template <bool PAGED, bool LEAF, bool AFF>
+template <bool PAGED, bool LEAF, int AFF>
 __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uint32_t count) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
@@ -1000,9 +1218,46 @@ __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uin
   }
 }
 
+// Seeds the shapes deferred to this phase (multi-phase derivation): each is
+// loaded as it was stored and resolved from the rule it was waiting at.
+template <bool PAGED, bool LEAF, int AFF>
+__device__ void seed_deferred(const DeriveArgs& a, WarpOut& w) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
+  const unsigned long long end = a.numDeferIn;
+  for (unsigned long long b = warpId * 32ull; b < end; b += numWarps * 32ull) {
+    const unsigned long long i = b + lane;
+    int kind = kNone;
+    Shape y;
+    uint32_t tidx = 0;
+    if (i < end) {
+      const float4* p = reinterpret_cast<const float4*>(a.deferIn + i);
+      const float4 p0 = __ldcg(p), p1 = __ldcg(p + 1);
+      const uint4 m = __ldcg(reinterpret_cast<const uint4*>(p + 2));
+      y.t[0] = p0.x; y.t[1] = p0.y; y.t[2] = p0.z; y.s[0] = p0.w;
+      y.s[1] = p1.x; y.s[2] = p1.y; y.seed = p1.z;
+#if PGA_GENERAL_FRAMES
+      const float4 r0 = __ldcg(a.deferRotIn + 2 * i), r1 = __ldcg(a.deferRotIn + 2 * i + 1);
+      y.R[0] = r0.x; y.R[1] = r0.y; y.R[2] = r0.z; y.R[3] = r0.w;
+      y.R[4] = r1.x; y.R[5] = r1.y; y.R[6] = r1.z; y.R[7] = r1.w;
+      y.R[8] = p1.w;
+#else
+      y.frame = __float_as_uint(p1.w);
+#endif
+      y.entry = (int32_t)m.x;
+      y.axiom = m.y;
+      y.path = ((uint64_t)m.w << 32) | m.z;
+      y.kind = ((uint32_t)y.entry < a.tab.numEntries) ? rule_at(a, (uint32_t)y.entry).shape : 0u;
+      kind = resolve<AFF>(a, y, tidx);
+    }
+    emit_new<PAGED, LEAF>(a, w, kind, y, tidx, kAxiomLink | y.axiom, 0u);
+  }
+}
+
 // All items of one level [lo, hi): warp chunks of 32 K items in a static
 // grid-stride order (no shared work counter).
-template <bool PAGED, bool LEAF, bool AFF>
+template <bool PAGED, bool LEAF, int AFF>
 __device__ __forceinline__ void expand_level(const DeriveArgs& a, WarpOut& w, unsigned long long lo,
                                              unsigned long long hi, uint32_t K) {
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
@@ -1273,15 +1528,20 @@ __device__ __forceinline__ unsigned long long global_ns() {
 #define PGA_PERSISTENT_MIN_BLOCKS 2
 #endif
 
-template <bool LEAF, bool AFF>
+template <bool LEAF, int AFF>
 __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   if (blockIdx.x == 0 && threadIdx.x == 0) a.st->clockStart = global_ns();
   setup_block(a, sm);
   WarpOut w;
   warpout_init(a, w);
-  warpout_level(a, w, a.numAxioms - a.axiomBase);
-  seed_axioms<true, LEAF, AFF>(a, w, a.axiomBase, a.numAxioms - a.axiomBase);
+  if (AFF >= 2 && a.deferIn != nullptr) {
+    warpout_level(a, w, a.numDeferIn);
+    seed_deferred<true, LEAF, AFF>(a, w);
+  } else {
+    warpout_level(a, w, a.numAxioms - a.axiomBase);
+    seed_axioms<true, LEAF, AFF>(a, w, a.axiomBase, a.numAxioms - a.axiomBase);
+  }
   close_node_page(a, w);
   if (!grid_barrier(a, [&] {
         volatile DevState* vs = a.st;
@@ -1310,7 +1570,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_seed(DeriveArgs a, uint32_t fir
   setup_block(a, sm);
   WarpOut w;
   warpout_init(a, w);
-  seed_axioms<false, false, true>(a, w, first, count);
+  seed_axioms<false, false, 1>(a, w, first, count);
 }
 
 __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsigned long long lo,
@@ -1319,24 +1579,27 @@ __global__ void __launch_bounds__(kThreads, 2) k_expand_level(DeriveArgs a, unsi
   setup_block(a, sm);
   WarpOut w;
   warpout_init(a, w);
-  expand_level<false, false, true>(a, w, lo, hi, 1);
+  expand_level<false, false, 1>(a, w, lo, hi, 1);
 }
 
 __global__ void k_write_count(const DevState* st, unsigned long long* out) { *out = st->termCount; }
 
-// This build's kernels, for the host code.  The general-frame build only has
-// the instantiations with the Translate / Scale / RandomRule / Rotate steps.
+// This build's kernels, for the host code.  AFF: 0 the split operators only,
+// 1 also the 1 -> 1 affine and selection steps, 2 also phases, Collider and
+// IfCollides (no leaf children in place there).  The general-frame build only
+// has the AFF >= 1 instantiations.
 inline FrameKernels frame_kernels() {
   FrameKernels k;
 #if PGA_GENERAL_FRAMES
-  k.persistent[0] = k.persistent[2] = (const void*)k_derive_persistent<false, true>;
-  k.persistent[1] = k.persistent[3] = (const void*)k_derive_persistent<true, true>;
+  k.persistent[0] = k.persistent[2] = (const void*)k_derive_persistent<false, 1>;
+  k.persistent[1] = k.persistent[3] = (const void*)k_derive_persistent<true, 1>;
 #else
-  k.persistent[0] = (const void*)k_derive_persistent<false, false>;
-  k.persistent[1] = (const void*)k_derive_persistent<true, false>;
-  k.persistent[2] = (const void*)k_derive_persistent<false, true>;
-  k.persistent[3] = (const void*)k_derive_persistent<true, true>;
+  k.persistent[0] = (const void*)k_derive_persistent<false, 0>;
+  k.persistent[1] = (const void*)k_derive_persistent<true, 0>;
+  k.persistent[2] = (const void*)k_derive_persistent<false, 1>;
+  k.persistent[3] = (const void*)k_derive_persistent<true, 1>;
 #endif
+  k.phased = (const void*)k_derive_persistent<false, 2>;
   k.seed = (const void*)k_seed;
   k.expand = (const void*)k_expand_level;
   return k;

@@ -68,6 +68,8 @@ constexpr uint16_t kRulePure = 1;
 constexpr uint16_t kRuleConstTerminal = 2;  // Generate with a scalar terminal index, kept in nChildren
 constexpr uint16_t kRuleLeaf = 4;           // Subdivide whose children all end at once (expanded in place)
 constexpr uint16_t kRuleMesh = 8;           // a triangle-mesh Generate (lowered to op GENERATE for the derivation)
+constexpr uint32_t kRulePhaseShift = 8;     // flags bits 8..11: the phase of the edges into the rule (multi-phase)
+constexpr uint32_t kMaxPhases = 16;
 
 struct DevTables {
   const DevRule* rules;
@@ -134,11 +136,28 @@ struct DeriveArgs {
   uint32_t tableInSmem; // 1: rule table copied to shared memory at launch
   uint32_t numParams, numSucc;
   DevState* st;
+  // Multi-phase derivation (tables whose successors name phases > 0).
+  uint32_t phase;                      // the phase being derived
+  const Node* deferIn;                 // shapes deferred to this phase (seeded instead of the axioms when set)
+  const float4* deferRotIn;            // their rotations (general frames)
+  unsigned long long numDeferIn;
+  Node* deferOut;                      // shapes reaching a rule of a later phase
+  float4* deferRotOut;
+  unsigned long long deferCap;
+  unsigned long long* phaseCounters;   // [0] colliders stored, [1] shapes deferred by this launch
+  PgaTerminal* colRec;                 // Collider shapes as records (model * scale, tag, path): the LBVH input
+  float4* colShape;                    // and as oriented boxes: 5 float4 per collider (see store_collider)
+  unsigned long long colCap;
+  const int32_t* colNodes;             // LBVH over the colliders of earlier phases
+  const float* colAabbs;
+  const uint32_t* colLeaf;
+  uint32_t numColliders;
 };
 
 // Entry points of one build of the kernels (host stubs), for the host code.
 struct FrameKernels {
-  const void* persistent[4];  // k_derive_persistent<LEAF, AFF>, index LEAF + 2 AFF
+  const void* persistent[4];  // k_derive_persistent<LEAF, AFF = 0 / 1>, index LEAF + 2 AFF
+  const void* phased;         // k_derive_persistent<false, 2>: multi-phase tables
   const void* seed;           // k_seed (plain form)
   const void* expand;         // k_expand_level (plain form)
 };

@@ -33,6 +33,22 @@ struct PgaEngine {
   pga::DevState* dState = nullptr;
   pga::Node* dNodes = nullptr;
   float4* dNodeRot = nullptr;  // general frames: 2 float4 of rotation entries per work item
+  // Multi-phase derivation (successor edges into later phases, Collider, IfCollides).
+  bool phased = false;
+  pga::Node* dDefer[2] = {nullptr, nullptr};   // shapes deferred to the next phase (input / output)
+  float4* dDeferRot[2] = {nullptr, nullptr};
+  PgaTerminal* dColRec = nullptr;              // colliders as records (LBVH input)
+  float4* dColShape = nullptr;                 // colliders as oriented boxes (5 float4 each)
+  int32_t* dColNodes = nullptr;                // the colliders' LBVH
+  uint32_t* dColParents = nullptr;
+  float* dColAabbs = nullptr;
+  uint32_t* dColLeaf = nullptr;
+  uint64_t* dColKeys = nullptr;
+  unsigned long long* dPhaseCounters = nullptr;  // [0] colliders, [1] deferred, [2] terminals of a launch
+  uint64_t colCap = 0;
+  uint64_t phaseTerminals = 0;                 // terminals of the last multi-phase derivation
+  uint64_t phaseTerminalsHost = 0;             // its copy for the device count
+  uint32_t phasesRun = 0;
   uint2* dTermLinks = nullptr;
   unsigned long long* dLevelStart = nullptr;
   unsigned long long* dLevelClock = nullptr;

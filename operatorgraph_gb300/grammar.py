@@ -25,10 +25,10 @@ PT_BLOCK = 16
 OP_SUBDIVIDE, OP_SUBDIVIDE_STATIC, OP_REPEAT, OP_COMPONENT_SPLIT = 0, 1, 2, 3
 OP_EXTRUDE, OP_IF_SIZE_LESS, OP_GENERATE, OP_DISCARD = 4, 5, 6, 7
 OP_TRANSLATE, OP_SCALE, OP_RANDOM_RULE, OP_ROTATE, OP_REPLICATE, OP_RANDOM_RULE_STATIC = 8, 9, 10, 11, 12, 13
-OP_IF, OP_SWAP_SIZE, OP_GENERATE_MESH = 14, 15, 16
+OP_IF, OP_SWAP_SIZE, OP_GENERATE_MESH, OP_COLLIDER, OP_IF_COLLIDES = 14, 15, 16, 17, 18
 OP_NAMES = ["Subdivide", "SubdivideStatic", "Repeat", "ComponentSplit", "Extrude", "IfSizeLess", "Generate", "Discard",
             "Translate", "Scale", "RandomRule", "Rotate", "Replicate", "RandomRuleStatic", "If", "SwapSize",
-            "GenerateMesh"]
+            "GenerateMesh", "Collider", "IfCollides"]
 
 SHAPE_BOX, SHAPE_QUAD = 0, 1
 
@@ -53,6 +53,9 @@ BOX_RANDOM_RULE2, QUAD_RANDOM_RULE2, BOX_RANDOM_RULE3, QUAD_RANDOM_RULE3, BOX_RA
 BOX_IF, QUAD_IF = 30, 31
 BOX_SWAP_SIZE, QUAD_SWAP_SIZE = 32, 33
 BOX_GENERATE_MESH, QUAD_GENERATE_MESH = 34, 35  # Generate<false, 0, DynParam<0>>: triangle-mesh terminals
+# Collider<DynParam<0> tag, DCall<0>> and IfCollides<DynParam<0> tag, DCall<0>, DCall<1>> (multi-phase tables;
+# the reference evaluates them on the GPU only, so the reference harness has no procedures for them)
+BOX_COLLIDER, QUAD_COLLIDER, BOX_IF_COLLIDES, QUAD_IF_COLLIDES = 36, 37, 38, 39
 
 PARAM_DT = np.dtype([("type", "<i4"), ("value", "<f4", (MAX_VALUES,))])
 SUCC_DT = np.dtype([("entryIndex", "<i4"), ("phaseIndex", "<i4")])
@@ -93,6 +96,8 @@ DEFAULT_PROCS = np.array([
     (OP_IF, SHAPE_BOX, 0, 1), (OP_IF, SHAPE_QUAD, 0, 1),
     (OP_SWAP_SIZE, SHAPE_BOX, 0, 1), (OP_SWAP_SIZE, SHAPE_QUAD, 0, 1),
     (OP_GENERATE_MESH, SHAPE_BOX, 0, 1), (OP_GENERATE_MESH, SHAPE_QUAD, 0, 1),
+    (OP_COLLIDER, SHAPE_BOX, 0, 1), (OP_COLLIDER, SHAPE_QUAD, 0, 1),
+    (OP_IF_COLLIDES, SHAPE_BOX, 0, 1), (OP_IF_COLLIDES, SHAPE_QUAD, 0, 1),
 ], dtype=PROC_DT)
 
 

@@ -21,6 +21,11 @@ returns a dict with ``entries`` (ENTRY_DT array), ``axioms`` (AXIOM_DT array),
 * random_grammars(): 64-rule random grammars (branching U{2..6}, IfSizeLess
   thresholds U[0.01, 0.2], Discard probability 0.15, depth cap 12).
 * mixed(n): 40 % Menger (depth 1-3), 40 % city buildings, 20 % random grammars.
+* collisions(...): a two-phase scene for Collider / IfCollides: in phase 0
+  buildings (boxes, tag 1) and billboards (quads, tag 2) store themselves and
+  emit terminals; trees (boxes, optionally turned) wait for phase 1, where a
+  tree that overlaps a building is discarded, one that overlaps a billboard
+  becomes terminal 2 and a free one terminal 3.
 * forest(n): n trees on a 64-wide grid (pitch 40 m), boxes 2 x 16 x 2 m
   turned by a per-tree angle about y; a trunk and a crown that forks into
   three branches (Replicate) turned 35 degrees out and 0 / 120 / 240 degrees
@@ -288,3 +293,58 @@ def forest(n=4096, seed=4321, cols=64, pitch=40.0):
     ax["entry"] = rng.integers(0, len(angles), n)
     ax["seed"] = rng.uniform(0.0, 1.0, n).astype(np.float32)
     return _batch(forest_table(angles), ax, name=f"forest({n})")
+
+
+TREE_TURNS = ((0.0, 30.0, 0.0), (10.0, -47.5, 12.25), (0.0, 45.0, 90.0), (-20.0, 0.0, 33.0))
+
+
+def collision_table(rotate=True):
+    """The two-phase grammar of collisions(); successors (entry, phase).
+    Trees enter at entry 6 (rotate=False: a size swap instead of a turn) or,
+    with rotate=True, at 12..15, turned by TREE_TURNS."""
+    tree_yaw = 30.0 if rotate else 90.0
+    turns = [Entry(G.BOX_ROTATE, [scalar(x), scalar(y), scalar(z)], [(7, 1)]) for x, y, z in TREE_TURNS]
+    return DispatchTable([
+        Entry(G.BOX_COLLIDER, [scalar(1)], [(1, 0)]),                                    # 0 building
+        Entry(G.BOX_COMPONENT_SPLIT, [], [(2, 0), (3, 0), (2, 0)]),                      # 1
+        Entry(G.QUAD_GENERATE, [scalar(0)], []),                                         # 2 roof / wall
+        Entry(G.QUAD_DISCARD, [], []),                                                   # 3
+        Entry(G.QUAD_COLLIDER, [scalar(2)], [(5, 0)]),                                   # 4 billboard
+        Entry(G.QUAD_GENERATE, [scalar(1)], []),                                         # 5
+        Entry(G.BOX_ROTATE if rotate else G.BOX_SWAP_SIZE,
+              [scalar(0), scalar(tree_yaw), scalar(0)] if rotate else [scalar(0), scalar(1), scalar(2)],
+              [(7, 1)]),                                                                 # 6 tree: waits for phase 1
+        Entry(G.BOX_IF_COLLIDES, [scalar(1)], [(8, 1), (9, 1)]),                         # 7 building?
+        Entry(G.BOX_DISCARD, [], []),                                                    # 8
+        Entry(G.BOX_IF_COLLIDES, [scalar(2)], [(10, 1), (11, 1)]),                       # 9 billboard?
+        Entry(G.BOX_GENERATE, [scalar(2)], []),                                          # 10
+        Entry(G.BOX_GENERATE, [scalar(3)], []),                                          # 11
+    ] + (turns if rotate else [])).to_array()
+
+
+def collisions(n_buildings=64, n_trees=512, n_boards=96, seed=77, rotate=True):
+    rng = np.random.default_rng(seed)
+    n = n_buildings + n_boards + n_trees
+    ax = G.make_axioms(n)
+    area = 40.0 * math.sqrt(n_buildings)
+    b = slice(0, n_buildings)
+    ax["entry"][b] = 0
+    ax["shape"][b] = G.SHAPE_BOX
+    ax["size"][b] = np.stack([rng.uniform(5, 15, n_buildings), rng.uniform(8, 40, n_buildings),
+                              rng.uniform(5, 15, n_buildings)], 1)
+    ax["position"][b] = np.stack([rng.uniform(0, area, n_buildings), ax["size"][b][:, 1] * 0.5,
+                                  rng.uniform(0, area, n_buildings)], 1)
+    q = slice(n_buildings, n_buildings + n_boards)
+    ax["entry"][q] = 4
+    ax["shape"][q] = G.SHAPE_QUAD
+    ax["size"][q] = np.stack([rng.uniform(4, 12, n_boards), rng.uniform(2, 6, n_boards), np.ones(n_boards)], 1)
+    ax["position"][q] = np.stack([rng.uniform(0, area, n_boards), rng.uniform(1, 4, n_boards),
+                                  rng.uniform(0, area, n_boards)], 1)
+    t = slice(n_buildings + n_boards, n)
+    ax["entry"][t] = rng.integers(12, 16, n_trees) if rotate else 6
+    ax["shape"][t] = G.SHAPE_BOX
+    ax["size"][t] = np.stack([rng.uniform(1, 4, n_trees), rng.uniform(3, 9, n_trees), rng.uniform(1, 4, n_trees)], 1)
+    ax["position"][t] = np.stack([rng.uniform(0, area, n_trees), ax["size"][t][:, 1] * 0.5,
+                                  rng.uniform(0, area, n_trees)], 1)
+    ax["seed"] = rng.uniform(0, 1, n).astype(np.float32)
+    return _batch(collision_table(rotate), ax, name=f"collisions({n_buildings}, {n_trees}, {n_boards})")

@@ -180,6 +180,14 @@ inline bool obb_overlap(const Obb& A, const Obb& B) {
   return true;
 }
 
+// IntermediateSymbol<Box / Quad> as Collider stores it (IntermediateSymbol.cuh,
+// IntermediateSymbolsBufferAdapter.cuh:200-215): the shape and its int tag.
+struct StoredCollider {
+  Obb obb;
+  bool quad;
+  int tag;
+};
+
 // Shapes::Shape + Symbol<ShapeT> (Shape.cuh:16-22, Symbol.cuh:9-15): model
 // (3x4, kept as 4x4 with the constant last row), size, seed, custom attribute,
 // entry index; plus the shape kind, the axiom index and the path hash.
@@ -195,6 +203,8 @@ struct Sym {
   uint64_t path;
 };
 
+struct StoredCollider;
+
 struct Ctx {
   const PgaProc* procs;
   uint32_t nProcs;
@@ -204,6 +214,12 @@ struct Ctx {
   uint32_t blockStride;
   int status;
   int detail;
+  // Phases (multi-phase derivation): the phase being run, the phase of the
+  // edges into each entry, and the colliders of the phases before this one.
+  uint32_t phase = 0;
+  std::vector<uint32_t> entryPhase;
+  std::vector<StoredCollider>* colliders = nullptr;
+  size_t visibleColliders = 0;
 };
 
 template <typename F>
@@ -318,6 +334,7 @@ struct Out {
   uint64_t cap;
   uint64_t count;
   std::vector<struct OracleMesh>* meshes = nullptr;  // triangle meshes (float derivation only)
+  std::vector<std::vector<Sym<F>>> deferred;          // symbols waiting for a later phase, per phase
 };
 
 // One triangle mesh as GenerationFunction<GenFuncFilter, 0> fills
@@ -378,6 +395,14 @@ void dispatch(Ctx& c, Out<F>& o, const Sym<F>& s) {
   if (s.entry < 0 || (uint32_t)s.entry >= c.nEntries) { fail(c, PGA_ERR_BAD_OPCODE, s.entry); return; }
   int32_t code = c.entries[s.entry].operatorCode;
   if (code < 0 || (uint32_t)code >= c.nProcs || c.procs[code].shape != s.shape) { fail(c, PGA_ERR_BAD_OPCODE, s.entry); return; }
+  // enqueue(symbol, phaseIdx) (CPUEvaluator.h:155-190): a symbol whose edge
+  // names a later phase waits for that phase's queues.
+  const uint32_t ph = c.entryPhase.empty() ? 0u : c.entryPhase[(size_t)s.entry];
+  if (ph > c.phase) {
+    if (o.deferred.size() <= ph) o.deferred.resize(ph + 1);
+    o.deferred[ph].push_back(s);
+    return;
+  }
   o.work.push_back(s);
 }
 
@@ -759,6 +784,54 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
       dispatch(c, o, s);
       return;
     }
+    case PGA_OP_COLLIDER: {
+      // Collider<Tag, Next>::execute (Collider.cuh:20-45): a positive tag stores
+      // the shape with it (visible to IfCollides from the next phase on).
+      if (!param_ok<F>(c, e, 0, s.entry)) return;
+      const unsigned tag = f2u(float(dyn_eval(c, blk, s, e.parameters[0])));
+      int32_t nxt;
+      if (!successor<F>(c, e, 0, s.entry, nxt)) return;
+      if (tag > 0 && c.colliders) {
+        float m[12], size[3];
+        for (int r = 0; r < 3; r++)
+          for (int q = 0; q < 4; q++) m[r * 4 + q] = float(s.model.a[r][q]);
+        for (int k2 = 0; k2 < 3; k2++) size[k2] = float(s.size[k2]);
+        c.colliders->push_back(StoredCollider{make_obb(m, size, s.shape == PGA_SHAPE_QUAD), s.shape == PGA_SHAPE_QUAD,
+                                              (int)tag});
+      }
+      s.entry = nxt;
+      dispatch(c, o, s);
+      return;
+    }
+    case PGA_OP_IF_COLLIDES: {
+      // IfCollides<Tag, True, False>::execute (IfCollides.cuh:18-36): true when
+      // a stored shape with the tag (compared as the unsigned char rule tag,
+      // BVHTraversal.cuh:16) overlaps this one (Collision::check(stored,
+      // shape)).  The reference prunes with a BVH; the answer is the same
+      // "any" over the stored shapes, which is what this loop computes.
+      if (!param_ok<F>(c, e, 0, s.entry)) return;
+      const unsigned char tag = (unsigned char)f2u(float(dyn_eval(c, blk, s, e.parameters[0])));
+      float m[12], size[3];
+      for (int r = 0; r < 3; r++)
+        for (int q = 0; q < 4; q++) m[r * 4 + q] = float(s.model.a[r][q]);
+      for (int k2 = 0; k2 < 3; k2++) size[k2] = float(s.size[k2]);
+      const bool quad = s.shape == PGA_SHAPE_QUAD;
+      const Obb me = make_obb(m, size, quad);
+      bool hit = false;
+      for (size_t k = 0; c.colliders && k < c.visibleColliders && !hit; k++) {
+        const StoredCollider& sc = (*c.colliders)[k];
+        if (sc.tag != (int)tag) continue;
+        // Collision::check(Quad, Box) is check(Box, Quad) (Collision.cuh:734-737)
+        hit = (sc.quad && !quad) ? obb_overlap(me, sc.obb) : obb_overlap(sc.obb, me);
+      }
+      const uint32_t branch = hit ? 0u : 1u;
+      int32_t nxt;
+      if (!successor<F>(c, e, branch, s.entry, nxt)) return;
+      s.path = child_path(s.path, branch, nxt);
+      s.entry = nxt;
+      dispatch(c, o, s);
+      return;
+    }
     case PGA_OP_RANDOM_RULE_STATIC: {
       // RandomRule<Chance, Pair<P, Next>...>::execute (RandomRule.cuh:33-99):
       // getProbabilitiesSum recurses as p1 + (p2 + (... + pn)); each pair's
@@ -821,8 +894,36 @@ void execute(Ctx& c, const Blocks<F>& blk, Out<F>& o, Sym<F> s) {
   }
 }
 
+// The phase of every entry: the phaseIndex of the successor edges that lead to
+// it (the engine requires them to agree; axioms start in phase 0).  Returns
+// false, with BAD_PARAM, when two edges into one entry name different phases.
+inline bool entry_phases(Ctx& c) {
+  c.entryPhase.assign(c.nEntries, 0u);
+  std::vector<int> seen(c.nEntries, -1);
+  for (uint32_t i = 0; i < c.nEntries; i++) {
+    const PgaEntry& e = c.entries[i];
+    for (uint32_t k = 0; k < e.numSuccessors && k < PGA_MAX_NUM_SUCCESSORS; k++) {
+      const int32_t t = e.successors[k].entryIndex;
+      if (t < 0 || (uint32_t)t >= c.nEntries) continue;
+      const int ph = e.successors[k].phaseIndex < 0 ? 0 : e.successors[k].phaseIndex;
+      if (seen[t] >= 0 && seen[t] != ph) {
+        fail(c, PGA_ERR_BAD_PARAM, (int)i);
+        return false;
+      }
+      seen[t] = ph;
+      c.entryPhase[t] = (uint32_t)ph;
+    }
+  }
+  return true;
+}
+
 template <typename F>
 int derive(Ctx& c, const Blocks<F>& blk, const double* axiomSizes, Out<F>& o, uint32_t nAxioms) {
+  std::vector<StoredCollider> colliders;
+  c.colliders = &colliders;
+  c.phase = 0;
+  c.visibleColliders = 0;
+  if (!entry_phases(c)) return c.status;
   for (uint32_t id = 0; id < nAxioms && c.status == PGA_OK; id++) {
     // Axiom generation as Grid::...::generateAxiom (Grid.cuh:199-204) then
     // dispatchAxiom (CPUEvaluator.h:255-266).
@@ -844,6 +945,23 @@ int derive(Ctx& c, const Blocks<F>& blk, const double* axiomSizes, Out<F>& o, ui
       execute(c, blk, o, cur);
     }
   }
+  // Later phases: MultiPhaseEvaluator::execute (CPUEvaluator.h:330-352) runs
+  // the phases in order; the colliders stored so far are what IfCollides sees.
+  for (uint32_t ph = 1; ph < o.deferred.size() && c.status == PGA_OK; ph++) {
+    c.phase = ph;
+    c.visibleColliders = colliders.size();
+    std::vector<Sym<F>> start;
+    start.swap(o.deferred[ph]);
+    for (size_t k = 0; k < start.size() && c.status == PGA_OK; k++) {
+      o.work.push_back(start[k]);
+      while (!o.work.empty() && c.status == PGA_OK) {
+        Sym<F> cur = o.work.back();
+        o.work.pop_back();
+        execute(c, blk, o, cur);
+      }
+    }
+  }
+  c.colliders = nullptr;
   return c.status;
 }
 

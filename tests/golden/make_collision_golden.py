@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Writes tests/golden/collision_pairs.npz: box / quad pairs and the results of
+"""Writes tests/golden/collision/pairs.npz: box / quad pairs and the results of
 the reference's own collision predicate on them (Collision::check,
 include/pga/core/Collision.cuh, through oracle/_ref/ref_harness --collide).
 
@@ -68,7 +68,7 @@ def pairs(seed, n):
 def main():
     P = pairs(2024, 24000)
     hits = oracle.collide_reference(P, tempfile.mkdtemp())
-    np.savez_compressed(os.path.join(HERE, "collision_pairs.npz"), pairs=P.view(np.uint8).reshape(len(P), -1),
+    np.savez_compressed(os.path.join(HERE, "collision", "pairs.npz"), pairs=P.view(np.uint8).reshape(len(P), -1),
                         hits=hits.astype(np.uint8))
     print(f"{len(P)} pairs, {int(hits.sum())} overlapping")
 

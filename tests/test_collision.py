@@ -2,7 +2,7 @@
 (oracle.collide) against the reference's own Collision::check
 (include/pga/core/Collision.cuh, run by oracle/_ref/ref_harness --collide) on
 random box / quad pairs and on pairs that touch exactly, and against the
-committed fixture tests/golden/collision_pairs.npz (written by
+committed fixture tests/golden/collision/pairs.npz (written by
 tests/golden/make_collision_golden.py from the reference), which the GPU test
 uses too."""
 import os
@@ -20,7 +20,7 @@ import make_collision_golden as MC  # noqa: E402
 
 
 def test_restated_predicate_matches_the_committed_reference_results():
-    z = np.load(os.path.join(HERE, "golden", "collision_pairs.npz"))
+    z = np.load(os.path.join(HERE, "golden", "collision", "pairs.npz"))
     pairs = z["pairs"].view(oracle.PAIR_DT).reshape(-1)
     ref = z["hits"].astype(bool)
     got = oracle.collide(pairs)

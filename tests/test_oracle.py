@@ -174,3 +174,33 @@ def test_oracle_lbvh_invariants(scene):
         for ch in nodes[i, 1:]:
             if ch < 0:
                 assert np.all(aabb[-ch, :3] >= aabb[i, :3]) and np.all(aabb[-ch, 3:] <= aabb[i, 3:])
+
+
+def test_phases_defer_and_collide():
+    """Multi-phase semantics of the restatement: a shape reaching a rule of a
+    later phase waits for it; IfCollides in phase 1 sees the colliders stored
+    in phase 0 (and none stored in its own phase); edges into one entry that
+    name different phases are rejected."""
+    from operatorgraph_gb300.grammar import DispatchTable, Entry, scalar
+
+    tab = DispatchTable([
+        Entry(G.BOX_COLLIDER, [scalar(5)], [(1, 0)]),                  # 0: store with tag 5
+        Entry(G.BOX_GENERATE, [scalar(0)], []),                        # 1
+        Entry(G.BOX_IF_COLLIDES, [scalar(5)], [(3, 1), (4, 1)]),       # 2: phase-0 test (sees nothing yet)
+        Entry(G.BOX_GENERATE, [scalar(1)], []),                        # 3 hit
+        Entry(G.BOX_REPLICATE, [], [(5, 1)]),                          # 4 miss: retry in phase 1
+        Entry(G.BOX_IF_COLLIDES, [scalar(5)], [(6, 1), (7, 1)]),       # 5
+        Entry(G.BOX_GENERATE, [scalar(2)], []),                        # 6 hit in phase 1
+        Entry(G.BOX_GENERATE, [scalar(3)], []),                        # 7
+    ]).to_array()
+    ax = G.make_axioms(3)
+    ax["entry"] = [0, 2, 2]
+    ax["size"] = 1.0
+    ax["position"] = [(0, 0, 0), (0.5, 0, 0), (5, 0, 0)]  # axiom 1 overlaps the collider, axiom 2 does not
+    t = oracle.derive(G.DEFAULT_PROCS, tab, ax)
+    tidx = sorted(((t["rule"] >> 24) & 0x7F).tolist())
+    assert tidx == [0, 2, 3]
+    bad = DispatchTable([Entry(G.BOX_REPLICATE, [], [(1, 0), (1, 1)]), Entry(G.BOX_GENERATE, [scalar(0)], [])]).to_array()
+    with pytest.raises(oracle.OracleError) as e:
+        oracle.derive(G.DEFAULT_PROCS, bad, G.make_axioms(1))
+    assert e.value.status == 5
