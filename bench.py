@@ -590,6 +590,29 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["city_meshes_roofline_frac"] = res["city_meshes_gbs"] / peak
     ec.release()
     del cout, vbufs, ibufs
+    # Two-phase derivation with colliders (scenes.collisions: 4096 buildings and
+    # 4096 billboards stored in phase 0, 65,536 turned trees tested against
+    # them in phase 1): the whole pga_derive, host round trip and collider
+    # LBVH between the phases included.
+    co = scenes.collisions(4096, 65536, 4096, rotate=True)
+    ek = Engine(co["entries"], node_capacity=1 << 20, max_terminals=1 << 20)
+    d_co = torch.from_numpy(co["axioms"].view(np.uint8).copy()).to(dev)
+    kout = torch.empty((1 << 20, 64), dtype=torch.uint8, device=dev)
+    ts = []
+    for it in range(6):
+        t0 = time.perf_counter()
+        ek.derive_raw(d_co.data_ptr(), len(co["axioms"]), None, kout.data_ptr(), 1 << 20, count.data_ptr())
+        torch.cuda.synchronize()
+        if it >= 2:
+            ts.append((time.perf_counter() - t0) * 1e3)
+    rep = ek.report()
+    assert rep["status"] == 0, rep
+    res["collisions_trees"] = 65536
+    res["collisions_terminals"] = int(count.item())
+    res["collisions_ms"] = statistics.median(ts)
+    res["collisions_trees_per_s"] = 65536 / (res["collisions_ms"] * 1e-3)
+    ek.release()
+    del kout
     return res
 
 

@@ -8,7 +8,7 @@
  *   - PGA::Shapes::Box, Quad                              (include/pga/core/Shapes.cuh)
  *   - PGA::Operators::Subdivide, Repeat, ComponentSplit, Extrude, IfSizeLess,
  *     Generate, Discard, Translate, Rotate, Scale, RandomRule, Replicate, If,
- *     SwapSize
+ *     SwapSize, Collider, IfCollides
  *                                                          (Subdivide.cuh:22,170; Repeat.cuh:35-64;
  *                                                          ComponentSplit.cuh:234-270; Extrude.cuh:24;
  *                                                          If.cuh:60; Generate.cuh:23-49; Discard.cuh:15;
@@ -45,8 +45,8 @@
  * triangle-mesh terminal (PGA_OP_GENERATE_MESH, expanded by
  * pga_generate_meshes).  Not lowered (an exception names them): other
  * generation functions, the Vec2/Vec4 parameter types, FSCall without an entry
- * index, and the operators outside this engine (IfCollides, the SetAs prism and
- * polygon operators).  Generate's Attr1..Attr5 arguments are accepted and
+ * index, and the operators outside this engine (the SetAs prism and polygon
+ * operators).  Generate's Attr1..Attr5 arguments are accepted and
  * unused: the instanced generation function writes the shape's custom
  * attribute (GenerationFunctions.cuh:158-188).
  */
@@ -327,6 +327,10 @@ template <typename ExpressionT, typename NextOperatorIfTrueT, typename NextOpera
 class If {};
 template <typename XT, typename YT, typename ZT, typename NextOperatorT>
 class SwapSize {};
+template <typename ColliderTagT, typename NextOperatorT>
+class Collider {};
+template <typename ColliderTagT, typename NextOperatorIfTrueT, typename NextOperatorIfFalseT>
+class IfCollides {};
 
 }  // namespace Operators
 
@@ -555,6 +559,25 @@ template <typename XT, typename YT, typename ZT, typename NextT, typename ShapeT
 struct LowerOp<Operators::Scale<XT, YT, ZT, NextT>, ShapeT> : LowerXYZ<PGA_OP_SCALE, XT, YT, ZT, NextT, ShapeT> {};
 template <typename XT, typename YT, typename ZT, typename NextT, typename ShapeT>
 struct LowerOp<Operators::SwapSize<XT, YT, ZT, NextT>, ShapeT> : LowerXYZ<PGA_OP_SWAP_SIZE, XT, YT, ZT, NextT, ShapeT> {};
+// Collider<Tag, Next> (Collider.cuh:20-45) and IfCollides<Tag, True, False>
+// (IfCollides.cuh:18-36); the phases of their successors come from the
+// dispatch table's successor entries (PSCall / DCall keep the phase index).
+template <typename TagT, typename NextT, typename ShapeT>
+struct LowerOp<Operators::Collider<TagT, NextT>, ShapeT> {
+  static void run(Builder& b, const PgaEntry& src, uint32_t i) {
+    std::vector<PgaParameter> params{LowerParam<TagT>::run(src)};
+    std::vector<PgaSuccessor> succs{LowerSucc<NextT, ShapeT>::run(b, src)};
+    set_entry(b, i, b.proc(PGA_OP_COLLIDER, ShapeT::kind, 0), params, succs);
+  }
+};
+template <typename TagT, typename TrueT, typename FalseT, typename ShapeT>
+struct LowerOp<Operators::IfCollides<TagT, TrueT, FalseT>, ShapeT> {
+  static void run(Builder& b, const PgaEntry& src, uint32_t i) {
+    std::vector<PgaParameter> params{LowerParam<TagT>::run(src)};
+    std::vector<PgaSuccessor> succs{LowerSucc<TrueT, ShapeT>::run(b, src), LowerSucc<FalseT, ShapeT>::run(b, src)};
+    set_entry(b, i, b.proc(PGA_OP_IF_COLLIDES, ShapeT::kind, 0), params, succs);
+  }
+};
 // If<Expression, True, False> (If.cuh:22-49).
 template <typename ExprT, typename TrueT, typename FalseT, typename ShapeT>
 struct LowerOp<Operators::If<ExprT, TrueT, FalseT>, ShapeT> {
