@@ -77,3 +77,16 @@ def test_inconsistent_phases_are_rejected():
     with pytest.raises(PgaError) as e:
         Engine(tab)
     assert e.value.status == 5
+
+
+def test_collider_and_deferral_overflow_are_statuses():
+    """More colliders or deferred shapes than the engine holds (both bounded by
+    nodeCapacity) end the derivation with PGA_ERR_QUEUE_OVERFLOW, not a fault."""
+    from operatorgraph_gb300.engine import Engine, PgaError
+
+    b = scenes.collisions(64, 512, 96, rotate=False)
+    eng = Engine(b["entries"], node_capacity=128, max_terminals=1 << 16)
+    with pytest.raises(PgaError) as e:
+        eng.execute(b["axioms"], capacity=1 << 16)
+    assert e.value.status == 1
+    eng.release()
