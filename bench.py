@@ -531,7 +531,15 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     # Scale: the general-frame kernels), about 13.4M terminals in one launch.
     fo = scenes.forest(4096)
     fcap = 14_000_000
-    eo = Engine(fo["entries"], node_capacity=1 << 23, max_terminals=fcap)
+    # The forest's forks have four children and its first levels are narrow:
+    # a short autotune over the split knobs (the city's sweep, reduced).
+    from operatorgraph_gb300 import autotune
+
+    fbest, _, _ = autotune.tune(fo, fcap, node_capacity=1 << 23, runs=3,
+                                space={"sub_item": (1, 2, 4, 8), "narrow_sub_item": (0, 1), "items_per_lane": (1,),
+                                       "blocks_per_sm": (0,)})
+    res["forest4096_schedule"] = fbest
+    eo = Engine(fo["entries"], node_capacity=1 << 23, max_terminals=fcap, **fbest)
     d_fo = torch.from_numpy(fo["axioms"].view(np.uint8).copy()).to(dev)
     fout = torch.empty((fcap, 64), dtype=torch.uint8, device=dev)
     ts = []
