@@ -285,18 +285,16 @@ __device__ __forceinline__ void frame_scaled(const Shape& x, float m[3][3]) {
 // ((R[i][0] q[0][j] + R[i][1] q[1][j]) + R[i][2] q[2][j]) + t_i * 0; the
 // translation is unchanged.
 __device__ __forceinline__ void frame_rotate(Shape& x, const float* q) {
-  float qq[9];
+  // row by row: a row of R' needs only that row of R, so the update is in
+  // place and q is read as it is used (fewer live registers than a copy)
 #pragma unroll
-  for (int k = 0; k < 9; k++) qq[k] = q[k];
-  float nr[9];
-#pragma unroll
-  for (uint32_t i = 0; i < 3; i++)
+  for (uint32_t i = 0; i < 3; i++) {
+    const float r0 = x.R[i * 3 + 0], r1 = x.R[i * 3 + 1], r2 = x.R[i * 3 + 2];
 #pragma unroll
     for (uint32_t j = 0; j < 3; j++)
-      nr[i * 3 + j] = __fadd_rn(__fadd_rn(__fmul_rn(x.R[i * 3 + 0], qq[0 * 3 + j]), __fmul_rn(x.R[i * 3 + 1], qq[1 * 3 + j])),
-                                __fmul_rn(x.R[i * 3 + 2], qq[2 * 3 + j]));
-#pragma unroll
-  for (int k = 0; k < 9; k++) x.R[k] = nr[k];
+      x.R[i * 3 + j] = __fadd_rn(__fadd_rn(__fmul_rn(r0, q[j]), __fmul_rn(r1, q[3 + j])),
+                                 __fmul_rn(r2, q[6 + j]));
+  }
 }
 
 #else  // signed-permutation frames
