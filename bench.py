@@ -404,6 +404,114 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
+def mixed_step(mx, mout, count, dev, n_expected):
+    """The mixed batch as one differentiable step captured in one CUDA graph:
+    derivation with the tape recorded, LBVH over all its terminals (the leaf
+    count read on the device, pga_lbvh_build_counted), dL/dM = M for the loss
+    L = |M|^2 / 2 (a torch copy over the output's capacity), and the adjoint
+    to the 65,536 axiom sizes (the batch's grammars take constant parameters,
+    so the sizes are its continuous inputs).  The four parts are also timed
+    one by one, eagerly."""
+    import torch
+
+    from operatorgraph_gb300.engine import Engine
+
+    res = {}
+    n_ax = len(mx["axioms"])
+    mcap = mout.shape[0]
+    et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True)
+    d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
+    g_term = torch.empty((mcap, 12), dtype=torch.float32, device=dev)
+    g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
+    m_rows = mout.view(torch.float32).view(mcap, 16)
+    # LBVH bounds: the box of the terminal centres of a first derivation, one
+    # metre wider on every side.
+    et.derive_raw(d_mx.data_ptr(), n_ax, None, mout.data_ptr(), mcap, count.data_ptr())
+    torch.cuda.synchronize()
+    rep = et.report()
+    assert rep["status"] == 0, rep
+    n = int(count.item())
+    assert n == n_expected, (n, n_expected)
+    c = m_rows[:n][:, [3, 7, 11]]
+    lo, hi = c.amin(dim=0).double().cpu().numpy() - 1.0, c.amax(dim=0).double().cpu().numpy() + 1.0
+    del c
+    bounds = tuple(float(v) for v in lo) + tuple(float(v) for v in hi)
+    n_items = int(rep["nodes"])
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+
+    def step(st, marks=None):
+        def mark(k):
+            if marks is not None:
+                marks[k].record(st)
+
+        mark(0)
+        et.derive_raw(d_mx.data_ptr(), n_ax, None, mout.data_ptr(), mcap, count.data_ptr(), stream=st)
+        mark(1)
+        bv = et.lbvh(mout, mcap, bounds, stream=st, count=count)
+        mark(2)
+        g_term.copy_(m_rows[:, :12])
+        mark(3)
+        et.adjoint_raw(g_term.data_ptr(), None, 0, g_sz.data_ptr(), stream=st)
+        mark(4)
+        return bv
+
+    seg = []
+    with torch.cuda.stream(s):
+        for it in range(5):
+            marks = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+            bv = step(s, marks)
+            s.synchronize()
+            if it >= 2:
+                seg.append([marks[k].elapsed_time(marks[k + 1]) for k in range(4)])
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    rep = et.report()
+    assert rep["status"] == 0, rep
+    assert int(count.item()) == n
+    keys = bv["keys"][:n] ^ (-(1 << 63))  # sign bit flipped: signed order = the keys' unsigned order
+    assert bool((keys[1:] >= keys[:-1]).all()), "LBVH keys not sorted"
+    del bv, keys
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        bv = step(torch.cuda.current_stream())
+    ts = []
+    for it in range(6):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        g.replay()
+        b.record()
+        torch.cuda.synchronize()
+        if it >= 2:
+            ts.append(a.elapsed_time(b))
+    rep = et.report()
+    assert rep["status"] == 0, rep
+    assert int(count.item()) == n
+    assert bool(torch.isfinite(g_sz).all()) and float(g_sz.abs().max()) > 0
+    names = ("derive_tape", "lbvh", "loss_grad", "adjoint")
+    med = [statistics.median(x[k] for x in seg) for k in range(4)]
+    # Algorithmic bytes: derivation 64 B per terminal, its 8-B tape link and
+    # 48 B per axiom; LBVH 236 B per leaf (the 64-B record read, 52 B of tree
+    # written, five radix passes over 12-B key/value pairs read and written);
+    # the loss gradient 48 B read and 48 B written per output slot; adjoint as
+    # for the facades (per terminal 48 + 8 B, per item 2 x 64 + 2 x 24 B, 12 B
+    # per axiom size).
+    parts = [72.0 * n + 48.0 * n_ax, 236.0 * n, 96.0 * mcap, 56.0 * n + 176.0 * n_items + 12.0 * n_ax]
+    peak, _ = read_peaks()
+    step_ms = statistics.median(ts)
+    res["mixed65536_step_graph_ms"] = step_ms
+    res["mixed65536_step_items"] = n_items
+    res["mixed65536_step_segments_ms"] = {k: v for k, v in zip(names, med)}
+    res["mixed65536_step_segments_gbs"] = {k: b / (v * 1e-3) / 1e9 for k, b, v in zip(names, parts, med)}
+    res["mixed65536_step_bytes"] = sum(parts)
+    res["mixed65536_step_gbs"] = sum(parts) / (step_ms * 1e-3) / 1e9
+    res["mixed65536_step_roofline_frac"] = res["mixed65536_step_gbs"] / peak
+    res["mixed65536_step_lbvh_bounds"] = [round(v, 3) for v in bounds]
+    del g, bv
+    et.release()
+    return res
+
+
 def extras(eng, batch, out, n_term, dev, stream, flush):
     """Plain GPU form, Menger depth 5 and LBVH timings (reported beside the headline)."""
     import torch
@@ -526,6 +634,7 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["mixed65536_ms"] = statistics.median(ts)
     res["mixed65536_terminals_per_s"] = n_mx / (res["mixed65536_ms"] * 1e-3)
     em.release()
+    res.update(mixed_step(mx, mout, count, dev, n_mx))
     del mout
     # Forest: 4096 trees (Rotate with arbitrary angles, Replicate, Translate,
     # Scale: the general-frame kernels), about 13.4M terminals in one launch.

@@ -293,6 +293,18 @@ PgaStatus pga_engine_levels(PgaEngine* engine, void* stream, uint64_t* starts, u
 PgaStatus pga_lbvh_build(PgaEngine* engine, const PgaTerminal* dTerminals, uint64_t n,
                          const PgaBounds* bounds, const PgaLbvh* out, void* stream);
 
+/* pga_lbvh_build (same construct(), GPUBVHConstructor.cuh:265-331) over the
+ * first min(*dCount, capacity) terminals, with the count read on the device:
+ * dCount is a device pointer, typically the one pga_derive wrote, so a
+ * derivation, its LBVH and its adjoint can be captured in one CUDA graph with
+ * no host read-back between them.  `capacity` (2 <= capacity <= maxTerminals,
+ * below 2^31) sizes the launches and the radix sort, which orders `capacity`
+ * keys: out->keys[count, capacity) holds padding (all ones) after the real
+ * keys.  The tree and leaf arrays are those of pga_lbvh_build for `count`
+ * leaves, bit for bit; a count below 2 builds no tree. */
+PgaStatus pga_lbvh_build_counted(PgaEngine* engine, const PgaTerminal* dTerminals, const uint64_t* dCount,
+                                 uint64_t capacity, const PgaBounds* bounds, const PgaLbvh* out, void* stream);
+
 /* Same LBVH as pga_lbvh_build, for callers that cannot allocate device memory
  * (their budget is fixed up front, or the allocator belongs to a host
  * application): it needs no engine and calls no allocator.  Its scratch is a

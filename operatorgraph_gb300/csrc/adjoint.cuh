@@ -46,7 +46,11 @@ struct AdjArgs {
   uint32_t numBlocks;
   float* gradSizes;            // 3 per axiom
   float* nodeGrad;             // 6 per item: d/dt, d/ds
-  unsigned long long numTerminals;
+  uint32_t* childKey;          // per item: slot of the child with ordinal o = childKey + o
+  uint32_t* pageNext;          // per item: next page of the same child, or kNoRecord
+  uint32_t* slots;             // per child slot: its record (see kItemTag)
+  unsigned long long* blockSums;
+  unsigned long long slotCap;
 };
 
 // Dual-number evaluation of an expression program (eval_exp's postfix VM):
@@ -134,11 +138,39 @@ __device__ __forceinline__ float axis_dot(const Shape& x, uint32_t ax, const flo
   return frame_neg(x.frame, ax) ? -v : v;
 }
 
-// VJP of child c of the item held in E (state before producing children,
+// Per-child terms of a Subdivide's VJP, gathered over the children of one
+// work item (child_vjp) and swept back through the recurrence once
+// (subdivide_sweep).
+constexpr uint32_t kMaxN = PGA_MAX_NUM_PARAMETERS;
+struct SubAcc {
+  int last;          // highest child slot gathered; -1: none
+  float gN[kMaxN];   // dL/dN_i, child i's size along the split axis
+  float goI[kMaxN];  // dL/do_i, child i's offset along the split axis
+};
+
+// A Subdivide child's terms through the recurrence: dL/dN and dL/do of slot idx.
+struct SubTerm {
+  int idx;  // -1: none
+  float gN, goI;
+};
+
+__device__ __forceinline__ void sub_add(SubAcc& acc, int idx, float gN, float goI) {
+  if (idx < 0 || idx >= (int)kMaxN) return;
+  while (acc.last < idx) {
+    acc.last++;
+    acc.gN[acc.last] = 0.0f;
+    acc.goI[acc.last] = 0.0f;
+  }
+  acc.gN[idx] += gN;
+  acc.goI[idx] += goI;
+}
+
+// VJP of child c of the item held in E0 (state before producing children,
 // i.e. right after expander_init).  gc is the gradient of the child's state;
-// the parent's gradient is accumulated into gp.
+// the parent's gradient is accumulated into gp, except a Subdivide's terms
+// through its recurrence, which are returned in st for subdivide_sweep.
 __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander& E0, uint32_t c, const Grad& gc,
-                          Grad& gp) {
+                          Grad& gp, SubTerm& st) {
   const Shape& x = E0.base;
   const DevRule& r = E0.r;
 #pragma unroll
@@ -149,93 +181,11 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
       const bool dyn = r.op == PGA_OP_SUBDIVIDE;
       const uint32_t n = dyn ? r.nParams - 1u : r.nChildren;
       const uint32_t ax = E0.axis;
-      const float go = axis_dot(x, ax, gc.t);
       for (uint32_t k = 0; k < 3; k++)
         if (k != ax) gp.s[k] += gc.s[k];
-      // Reverse pass over the recurrence that produced child c:
-      //   offset_0 = -S/2;  N_i = size(f_i, scale);  o_i = offset_i + N_i/2;
-      //   offset_{i+1} = offset_i + N_i;  child c: size N_c, translation t + R_a o_c.
-      // Factor f_i is read on the base shape (static form, i = 0, or a rule
-      // whose factors do not read the shape) or, for a dynamic Subdivide, on the
-      // symbol as child i - 1 left it in place: size N_{i-1} along a and
-      // translation t + R_a o_{i-1}; its gradient then flows to N_{i-1},
-      // o_{i-1} and the base's other sizes and translation.  The scale uses
-      // the factors read from the base shape.
-      constexpr uint32_t kMaxN = PGA_MAX_NUM_PARAMETERS;
-      float fv[kMaxN], Nv[kMaxN], ov[kMaxN], gN[kMaxN], goI[kMaxN];
-      const uint32_t last = min(c, n - 1u);
-      Expander W = E0;
-      for (uint32_t i = 0; i <= last && i < kMaxN; i++) {
-        const float f = dyn ? dyn_factor(a, W, i) : param(a, r, i + 1, x);
-        const float sz = subdivide_size(f, W.scale);
-        fv[i] = f;
-        Nv[i] = sz;
-        ov[i] = __fadd_rn(W.offset, __fmul_rn(sz, 0.5f));
-        W.prevOff = ov[i];
-        W.prevSize = sz;
-        W.offset = __fadd_rn(W.offset, sz);
-        gN[i] = 0.0f;
-        goI[i] = 0.0f;
-      }
-      if (last >= kMaxN) return;
-      gN[last] += pick3(gc.s, ax);
-      goI[last] += go;
-      const bool readsUpdated = dyn && !(r.flags & kRulePure);
-      float gS = 0.0f, gscale = 0.0f, gOffNext = 0.0f;
-      for (int i = (int)last; i >= 0; i--) {
-        // o_i = offset_i + N_i/2 and offset_{i+1} = offset_i + N_i
-        const float gOff = gOffNext + goI[i];
-        gN[i] += gOffNext + 0.5f * goI[i];
-        gOffNext = gOff;
-        const float f = fv[i];
-        if (!dyn && f == 0.0f) continue;  // a skipped static slot
-        float gf = 0.0f;
-        if (f > 0.0f) {
-          gf = gN[i];
-        } else if (f < 0.0f) {
-          gf = gN[i] * (-E0.scale);
-          gscale += gN[i] * (-f);
-        }
-        if (gf == 0.0f) continue;
-        if (!readsUpdated || i == 0) {
-          param_grad(a, j, r, i + 1, x, gf, &gp);
-        } else {
-          Shape cur = x;
-          put3(cur.s, ax, Nv[i - 1]);
-          translate_ref(cur, x, E0.axisRef, ov[i - 1]);
-          cur.seed = seed_of(a, x.seed, (uint32_t)i - 1u);
-          Grad gst;
-          grad_zero(gst);
-          param_grad(a, j, r, i + 1, cur, gf, &gst);
-          gN[i - 1] += pick3(gst.s, ax);
-          for (uint32_t k = 0; k < 3; k++)
-            if (k != ax) gp.s[k] += gst.s[k];
-#pragma unroll
-          for (int q = 0; q < 3; q++) gp.t[q] += gst.t[q];
-          goI[i - 1] += axis_dot(x, ax, gst.t);
-        }
-      }
-      gS += -0.5f * gOffNext;  // offset_0 = -S/2
-      if (gscale != 0.0f) {
-        float relSum = 0.0f;
-        for (uint32_t i = 0; i < n; i++) {
-          const float f = param(a, r, i + 1, x);
-          if (f < 0.0f) relSum += -f;
-        }
-        if (relSum != 0.0f) {
-          // scale = (S - sum_{f>0} f) / sum_{f<0} -f
-          gS += gscale / relSum;
-          const float gA = -gscale / relSum, gR = gscale * E0.scale / relSum;
-          for (uint32_t i = 0; i < n; i++) {
-            const float f = param(a, r, i + 1, x);
-            if (f > 0.0f) param_grad(a, j, r, i + 1, x, gA, &gp);
-            if (f < 0.0f) param_grad(a, j, r, i + 1, x, gR, &gp);
-          }
-        }
-      }
-      gp.s[0] += (ax == 0) ? gS : 0.0f;
-      gp.s[1] += (ax == 1) ? gS : 0.0f;
-      gp.s[2] += (ax == 2) ? gS : 0.0f;
+      st.idx = (int)min(c, n - 1u);
+      st.gN = pick3(gc.s, ax);
+      st.goI = axis_dot(x, ax, gc.t);
       return;
     }
     case PGA_OP_REPEAT: {
@@ -310,11 +260,100 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
   }
 }
 
-// Recomputes the shape created as child `ordinal` of `link` (an item or an
-// axiom) and replays its 1 -> 1 chain until `stopAt` (a terminal: the Generate
-// rule; an item: its branching rule).  The smooth steps (Extrude, Translate,
-// Scale, SwapSize) are recorded so that the reverse pass can undo them; a chain with
-// more than kChainSteps of them has no adjoint (PGA_ERR_NO_TAPE).
+// The reverse pass of a Subdivide over the terms gathered in acc, into gp.
+__device__ void subdivide_sweep(const DeriveArgs& a, const AdjArgs& j, const Expander& E0, SubAcc& acc, Grad& gp) {
+  if (acc.last < 0) return;
+  const Shape& x = E0.base;
+  const DevRule& r = E0.r;
+  const bool dyn = r.op == PGA_OP_SUBDIVIDE;
+  const uint32_t n = dyn ? r.nParams - 1u : r.nChildren;
+  const uint32_t ax = E0.axis;
+  // Reverse pass over the recurrence that produced the children:
+  //   offset_0 = -S/2;  N_i = size(f_i, scale);  o_i = offset_i + N_i/2;
+  //   offset_{i+1} = offset_i + N_i;  child c: size N_c, translation t + R_a o_c.
+  // Factor f_i is read on the base shape (static form, i = 0, or a rule
+  // whose factors do not read the shape) or, for a dynamic Subdivide, on the
+  // symbol as child i - 1 left it in place: size N_{i-1} along a and
+  // translation t + R_a o_{i-1}; its gradient then flows to N_{i-1},
+  // o_{i-1} and the base's other sizes and translation.  The scale uses
+  // the factors read from the base shape.
+  float fv[kMaxN], Nv[kMaxN], ov[kMaxN];
+  const uint32_t last = (uint32_t)acc.last;
+  Expander W = E0;
+  for (uint32_t i = 0; i <= last && i < kMaxN; i++) {
+    const float f = dyn ? dyn_factor(a, W, i) : param(a, r, i + 1, x);
+    const float sz = subdivide_size(f, W.scale);
+    fv[i] = f;
+    Nv[i] = sz;
+    ov[i] = __fadd_rn(W.offset, __fmul_rn(sz, 0.5f));
+    W.prevOff = ov[i];
+    W.prevSize = sz;
+    W.offset = __fadd_rn(W.offset, sz);
+  }
+  const bool readsUpdated = dyn && !(r.flags & kRulePure);
+  float gS = 0.0f, gscale = 0.0f, gOffNext = 0.0f;
+  for (int i = (int)last; i >= 0; i--) {
+    // o_i = offset_i + N_i/2 and offset_{i+1} = offset_i + N_i
+    const float gOff = gOffNext + acc.goI[i];
+    acc.gN[i] += gOffNext + 0.5f * acc.goI[i];
+    gOffNext = gOff;
+    const float f = fv[i];
+    if (!dyn && f == 0.0f) continue;  // a skipped static slot
+    float gf = 0.0f;
+    if (f > 0.0f) {
+      gf = acc.gN[i];
+    } else if (f < 0.0f) {
+      gf = acc.gN[i] * (-E0.scale);
+      gscale += acc.gN[i] * (-f);
+    }
+    if (gf == 0.0f) continue;
+    if (!readsUpdated || i == 0) {
+      param_grad(a, j, r, i + 1, x, gf, &gp);
+    } else {
+      Shape cur = x;
+      put3(cur.s, ax, Nv[i - 1]);
+      translate_ref(cur, x, E0.axisRef, ov[i - 1]);
+      cur.seed = seed_of(a, x.seed, (uint32_t)i - 1u);
+      Grad gst;
+      grad_zero(gst);
+      param_grad(a, j, r, i + 1, cur, gf, &gst);
+      acc.gN[i - 1] += pick3(gst.s, ax);
+      for (uint32_t k = 0; k < 3; k++)
+        if (k != ax) gp.s[k] += gst.s[k];
+#pragma unroll
+      for (int q = 0; q < 3; q++) gp.t[q] += gst.t[q];
+      acc.goI[i - 1] += axis_dot(x, ax, gst.t);
+    }
+  }
+  gS += -0.5f * gOffNext;  // offset_0 = -S/2
+  if (gscale != 0.0f) {
+    float relSum = 0.0f;
+    for (uint32_t i = 0; i < n; i++) {
+      const float f = param(a, r, i + 1, x);
+      if (f < 0.0f) relSum += -f;
+    }
+    if (relSum != 0.0f) {
+      // scale = (S - sum_{f>0} f) / sum_{f<0} -f
+      gS += gscale / relSum;
+      const float gA = -gscale / relSum, gR = gscale * E0.scale / relSum;
+      for (uint32_t i = 0; i < n; i++) {
+        const float f = param(a, r, i + 1, x);
+        if (f > 0.0f) param_grad(a, j, r, i + 1, x, gA, &gp);
+        if (f < 0.0f) param_grad(a, j, r, i + 1, x, gR, &gp);
+      }
+    }
+  }
+  gp.s[0] += (ax == 0) ? gS : 0.0f;
+  gp.s[1] += (ax == 1) ? gS : 0.0f;
+  gp.s[2] += (ax == 2) ? gS : 0.0f;
+}
+
+// The 1 -> 1 chain a created shape runs through before it becomes a record
+// (a terminal, a queued work item, or nothing): IfSizeLess, If and RandomRule
+// pick a branch and pass the gradient through unchanged; the smooth steps
+// (Extrude, Translate, Scale, SwapSize) are recorded so that the reverse pass
+// can undo them.  A chain with more than kChainSteps of them has no adjoint
+// (PGA_ERR_NO_TAPE).
 constexpr int kChainSteps = 8;
 struct Chain {
   uint32_t n;                   // smooth steps
@@ -322,35 +361,18 @@ struct Chain {
   Shape before[kChainSteps];    // state entering each step
 };
 
-__device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, bool toTerminal, Expander& E,
-                       bool& fromAxiom, uint32_t& c, Shape& y0, Chain& ch, Shape& yEnd) {
-  fromAxiom = (link & kAxiomLink) != 0;
-  if (fromAxiom) {
-    axiom_shape(a, link & ~kAxiomLink, y0);
-    c = 0;
-  } else {
-    uint4 ext;
-    load_node(a, link, E.base, ext);
-    const int32_t e = E.base.entry;
-    if (e < 0 || (uint32_t)e >= a.tab.numEntries) return false;
-    E.r = rule_at(a, (uint32_t)e);
-    E.base.kind = E.r.shape;
-    const uint32_t all = expander_init(a, E);
-    c = (E.r.op == PGA_OP_REPEAT) ? ordinal - 1u : ordinal;
-    if (c >= all) return false;
-    Expander W = E;
-    expander_skip(a, W, c);
-    uint32_t ord;
-    if (!expander_child(a, W, c, y0, ord)) return false;
-  }
+enum ChainEnd : int { kEndFail = -1, kEndTerminal = 0, kEndItem = 1, kEndDiscard = 2 };
+
+// Replays the chain from x, the shape as its creator produced it, to its end
+// state yEnd (the record's state); returns how it ends.
+__device__ int replay_chain(const DeriveArgs& a, Shape x, Chain& ch, Shape& yEnd) {
   ch.n = 0;
-  Shape x = y0;
   for (int step = 0; step < kMaxChain; step++) {
-    if (x.entry < 0 || (uint32_t)x.entry >= a.tab.numEntries) return false;
+    if (x.entry < 0 || (uint32_t)x.entry >= a.tab.numEntries) return kEndFail;
     const DevRule r = rule_at(a, (uint32_t)x.entry);
     if (r.op == PGA_OP_IF_SIZE_LESS) {
       uint32_t axis;
-      if (!axis_param(a, r, x, axis)) return false;
+      if (!axis_param(a, r, x, axis)) return kEndFail;
       const float size = param(a, r, 1, x);
       const uint32_t branch = (pick3(x.s, axis) < size) ? 0u : 1u;
       x.path = child_path(x.path, branch, succ_at(a, r.succBase + branch));
@@ -359,7 +381,7 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
     }
     if (r.op == PGA_OP_RANDOM_RULE || r.op == PGA_OP_RANDOM_RULE_STATIC) {
       const int pick = random_pick(a, r, x);
-      if (pick < 0) return false;
+      if (pick < 0) return kEndFail;
       const int32_t nxt = succ_at(a, r.succBase + (uint32_t)pick);
       x.path = child_path(x.path, (uint32_t)pick, nxt);
       x.entry = nxt;
@@ -372,7 +394,7 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
       continue;
     }
     if (r.op == PGA_OP_TRANSLATE || r.op == PGA_OP_SCALE || r.op == PGA_OP_SWAP_SIZE) {
-      if (ch.n >= kChainSteps) return false;
+      if (ch.n >= kChainSteps) return kEndFail;
       ch.entry[ch.n] = x.entry;
       ch.before[ch.n] = x;
       ch.n++;
@@ -381,12 +403,12 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
       else if (r.op == PGA_OP_SCALE)
         apply_scale(a, r, x);
       else if (!swap_size(a, r, x))
-        return false;
+        return kEndFail;
       x.entry = succ_at(a, r.succBase);
       continue;
     }
     if (r.op == PGA_OP_EXTRUDE) {
-      if (ch.n >= kChainSteps) return false;
+      if (ch.n >= kChainSteps) return kEndFail;
       ch.entry[ch.n] = x.entry;
       ch.before[ch.n] = x;
       ch.n++;
@@ -402,18 +424,17 @@ __device__ bool replay(const DeriveArgs& a, uint32_t link, uint32_t ordinal, boo
       x.entry = nxt;
       continue;
     }
-    const bool isTerm = r.op == PGA_OP_GENERATE;
     yEnd = x;
-    return isTerm == toTerminal;
+    if (r.op == PGA_OP_GENERATE) return kEndTerminal;
+    return r.op == PGA_OP_DISCARD ? kEndDiscard : kEndItem;
   }
-  return false;
+  return kEndFail;
 }
 
-// Pushes the gradient g of a record, whose creation has been replayed into
-// (E, fromAxiom, c, ch), back to its parent.
-__device__ void push_back_replayed(const DeriveArgs& a, const AdjArgs& j, uint32_t link, const Expander& E,
-                                   bool fromAxiom, uint32_t c, const Chain& ch, Grad g) {
-  // Undo the smooth steps, last first.
+// Undoes the smooth steps of ch, last first: g, the gradient of the chain's
+// end state, becomes that of the state it started from.  Parameter gradients
+// go to j.gradParams.
+__device__ void chain_vjp(const DeriveArgs& a, const AdjArgs& j, const Chain& ch, Grad& g) {
   for (int k = (int)ch.n - 1; k >= 0; k--) {
     const Shape& xb = ch.before[k];
     const DevRule r = rule_at(a, (uint32_t)ch.entry[k]);
@@ -447,91 +468,208 @@ __device__ void push_back_replayed(const DeriveArgs& a, const AdjArgs& j, uint32
     }
     g = gb;
   }
-  if (fromAxiom) {
-    const uint32_t ax = link & ~kAxiomLink;
-    if (j.gradSizes != nullptr)
-      for (int q = 0; q < 3; q++)
-        if (g.s[q] != 0.0f) atomicAdd(&j.gradSizes[(size_t)ax * 3 + q], g.s[q]);
+}
+
+// dL/d(state) of a Generate rule's shape y from dL/dM of its terminal t:
+// M[:, k] = R[:, k] s_k and M[:, 3] = t.
+__device__ __forceinline__ Grad terminal_grad(const AdjArgs& j, unsigned long long t, const Shape& y) {
+  const float* gm = j.gradTerminals + t * 12;
+  Grad g;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    g.t[q] = __ldg(gm + q * 4 + 3);
+    const uint32_t row = frame_row(y.frame, q);
+    const float v = __ldg(gm + row * 4 + q);
+    g.s[q] = frame_neg(y.frame, q) ? -v : v;
+  }
+  return g;
+}
+
+// A record created from axiom ax's root shape (a terminal t, or a work item
+// whose gradient is g): back through the root's chain into the axiom's size
+// gradient.  An axiom has few such records (one terminal, or the pages of
+// one item), so they add atomically.
+__device__ void push_to_axiom(const DeriveArgs& a, const AdjArgs& j, uint32_t ax, bool terminal,
+                              unsigned long long t, Grad g) {
+  Shape y0, yEnd;
+  axiom_shape(a, ax, y0);
+  Chain ch;
+  if (replay_chain(a, y0, ch, yEnd) != (terminal ? kEndTerminal : kEndItem)) {
+    raise_error(a.st, PGA_ERR_NO_TAPE, (int)ax);
     return;
+  }
+  if (terminal) g = terminal_grad(j, t, yEnd);
+  chain_vjp(a, j, ch, g);
+  if (j.gradSizes != nullptr)
+    for (int q = 0; q < 3; q++)
+      if (g.s[q] != 0.0f) atomicAdd(&j.gradSizes[(size_t)ax * 3 + q], g.s[q]);
+}
+
+// The slot map.  Work item i (one page of a queued shape: its children
+// [c0, c1)) owns the slots [base_i, base_i + c1 - c0), base_i an exclusive
+// scan of the pages' child counts; childKey_i = base_i - c0 - (1 for Repeat,
+// whose child c has ordinal c + 1), so the child with tape link
+// (i, ordinal) sits at childKey_i + ordinal.  A slot holds the terminal the
+// child became, or the first of the pages it was queued as (kItemTag | page,
+// the others linked through pageNext), or kNoRecord (discarded).
+constexpr uint32_t kNoRecord = 0xFFFFFFFFu;
+constexpr uint32_t kItemTag = 0x80000000u;
+
+__device__ __forceinline__ uint32_t page_children(const uint4& ext) {
+  return ext.x == kEmptyItem ? 0u : ext.y - ext.x;
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Slots read ahead per work item (a work item has max(subItem, narrowSubItem)
+// children at most, 8 by default).
+constexpr uint32_t kPrefetch = 8;
+
+// Gradient of a child queued as the pages in the list starting at v: the sum
+// of their gradients (each page's covers its own children).
+__device__ __forceinline__ Grad pages_grad(const AdjArgs& j, uint32_t v, unsigned long long nodes) {
+  Grad g;
+  grad_zero(g);
+  uint32_t k = v & ~kItemTag;
+  for (unsigned long long guard = 0; k != kNoRecord && k < nodes && guard < nodes; guard++) {
+    const float* src = j.nodeGrad + (size_t)k * 6;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      g.t[q] += __ldcg(src + q);
+      g.s[q] += __ldcg(src + 3 + q);
+    }
+    k = __ldcg(j.pageNext + k);
+  }
+  return g;
+}
+
+// Reverse step of work item i: its children in order -- each one's gradient
+// read through the slot map (a terminal's dL/dM, or the sum over the pages it
+// was queued as) and pushed back through its chain and the operator that
+// created it -- summed into the item's gradient, which is stored (or, for an
+// axiom's root item, pushed into the axiom's sizes).
+__device__ void adj_page(const DeriveArgs& a, const AdjArgs& j, unsigned long long i, unsigned long long nodes) {
+  Expander E;
+  uint4 ext;
+  load_node(a, i, E.base, ext);
+  if (ext.x == kEmptyItem) return;
+  const int32_t e = E.base.entry;
+  if (e < 0 || (uint32_t)e >= a.tab.numEntries) {
+    raise_error(a.st, PGA_ERR_NO_TAPE, (int)i);
+    return;
+  }
+  E.r = rule_at(a, (uint32_t)e);
+  E.base.kind = E.r.shape;
+  const uint32_t all = expander_init(a, E);
+  const uint32_t c0 = ext.x, c1 = min(ext.y, all);
+  const uint32_t key = __ldcg(j.childKey + i);
+  {
+    // Start the loads of the children's slots and of the gradients they
+    // point to, so that their latencies overlap instead of adding up child
+    // after child below (a child's slot is key + c + 1 for Repeat, else key + c).
+    const uint32_t rep = E.r.op == PGA_OP_REPEAT ? 1u : 0u;
+    uint32_t sv[kPrefetch];
+#pragma unroll
+    for (uint32_t q = 0; q < kPrefetch; q++)
+      sv[q] = (c0 + q < c1) ? __ldcg(j.slots + (uint32_t)(key + c0 + q + rep)) : kNoRecord;
+#pragma unroll
+    for (uint32_t q = 0; q < kPrefetch; q++) {
+      if (sv[q] == kNoRecord) continue;
+      if (sv[q] & kItemTag) {
+        prefetch_l2(j.nodeGrad + (size_t)(sv[q] & ~kItemTag) * 6);
+      } else {
+        const float* gm = j.gradTerminals + (size_t)sv[q] * 12;
+        prefetch_l2(gm);
+        prefetch_l2(gm + 11);
+      }
+    }
   }
   Grad gp;
   grad_zero(gp);
-  child_vjp(a, j, E, c, g, gp);
-  float* dst = j.nodeGrad + (size_t)link * 6;
-#pragma unroll
-  for (int q = 0; q < 3; q++) {
-    if (gp.t[q] != 0.0f) atomicAdd(dst + q, gp.t[q]);
-    if (gp.s[q] != 0.0f) atomicAdd(dst + 3 + q, gp.s[q]);
+  SubAcc acc;
+  acc.last = -1;
+  Expander W = E;
+  if (c0 < c1) expander_skip(a, W, c0);
+  for (uint32_t c = c0; c < c1; c++) {
+    Shape y0, yEnd;
+    uint32_t ord;
+    if (!expander_child(a, W, c, y0, ord)) continue;
+    const uint32_t v = __ldcg(j.slots + (uint32_t)(key + ord));
+    if (v == kNoRecord) continue;  // discarded
+    Chain ch;
+    const int end = replay_chain(a, y0, ch, yEnd);
+    Grad g;
+    if (end == kEndTerminal && !(v & kItemTag)) {
+      g = terminal_grad(j, v, yEnd);
+    } else if (end == kEndItem && (v & kItemTag)) {
+      g = pages_grad(j, v, nodes);
+    } else {
+      raise_error(a.st, PGA_ERR_NO_TAPE, (int)i);
+      return;
+    }
+    chain_vjp(a, j, ch, g);
+    SubTerm st;
+    st.idx = -1;
+    child_vjp(a, j, E, c, g, gp, st);
+    sub_add(acc, st.idx, st.gN, st.goI);
   }
-}
-
-// Pushes the gradient g of the recorded record back to its parent.
-__device__ void push_back(const DeriveArgs& a, const AdjArgs& j, uint32_t link, uint32_t ordinal, bool toTerminal,
-                          Grad g) {
-  Expander E;
-  bool fromAxiom;
-  uint32_t c;
-  Shape y0, yEnd;
-  Chain ch;
-  if (!replay(a, link, ordinal, toTerminal, E, fromAxiom, c, y0, ch, yEnd)) {
-    raise_error(a.st, PGA_ERR_NO_TAPE, (int)link);
+  subdivide_sweep(a, j, E, acc, gp);
+  if (ext.z & kAxiomLink) {
+    push_to_axiom(a, j, ext.z & ~kAxiomLink, false, 0, gp);
     return;
   }
-  push_back_replayed(a, j, link, E, fromAxiom, c, ch, g);
-}
-
-// Reverse step of terminal t: dL/dM (12 floats) to the gradient of the
-// Generate rule's shape, then back to its parent.
-__device__ __forceinline__ void adj_terminal(const DeriveArgs& a, const AdjArgs& j, unsigned long long t) {
-  const float* gm = j.gradTerminals + t * 12;
-  const uint2 link = a.termLinks[t];
-  Grad g;
-  float G[12];
-#pragma unroll
-  for (int q = 0; q < 12; q++) G[q] = __ldg(gm + q);
-  // Generate: M[:, k] = R[:, k] s_k and M[:, 3] = t, with R from the replayed state.
-  Expander E;
-  bool fromAxiom;
-  uint32_t c;
-  Shape y0, yEnd;
-  Chain ch;
-  if (!replay(a, link.x, link.y, true, E, fromAxiom, c, y0, ch, yEnd)) {
-    raise_error(a.st, PGA_ERR_NO_TAPE, (int)t);
-    return;
-  }
+  float* dst = j.nodeGrad + (size_t)i * 6;
 #pragma unroll
   for (int q = 0; q < 3; q++) {
-    g.t[q] = G[q * 4 + 3];
-    const uint32_t row = frame_row(yEnd.frame, q);
-    const float v = G[row * 4 + q];
-    g.s[q] = frame_neg(yEnd.frame, q) ? -v : v;
+    __stcg(dst + q, gp.t[q]);
+    __stcg(dst + 3 + q, gp.s[q]);
   }
-  push_back_replayed(a, j, link.x, E, fromAxiom, c, ch, g);
 }
 
-// Reverse step of work item i: its accumulated gradient back to its parent.
-__device__ __forceinline__ void adj_item(const DeriveArgs& a, const AdjArgs& j, unsigned long long i) {
-  const uint4 ext = __ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3);
-  if (ext.x == kEmptyItem) return;
-  Grad g;
-  const float* src = j.nodeGrad + i * 6;
-  bool any = false;
+// Block-wide exclusive scan of one value per thread; total receives the sum.
+__device__ __forceinline__ unsigned long long block_excl_scan(uint32_t v, unsigned long long& total) {
+  __shared__ unsigned long long warpSum[kWarps];
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t wt;
+  const uint32_t pre = warp_excl_scan(v, wt);
+  if (lane == 0) warpSum[warp] = wt;
+  __syncthreads();
+  unsigned long long before = 0, all = 0;
+  for (int w = 0; w < kWarps; w++) {
+    const unsigned long long x = warpSum[w];
+    before += (w < (int)warp) ? x : 0ull;
+    all += x;
+  }
+  __syncthreads();
+  total = all;
+  return before + pre;
+}
+
+__device__ __forceinline__ unsigned long long block_sum(unsigned long long v) {
+  __shared__ unsigned long long part[kWarps];
 #pragma unroll
-  for (int q = 0; q < 3; q++) {
-    g.t[q] = __ldcg(src + q);
-    g.s[q] = __ldcg(src + 3 + q);
-    any |= (g.t[q] != 0.0f) || (g.s[q] != 0.0f);
-  }
-  if (any) push_back(a, j, ext.z, ext.w, false, g);
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+  if ((threadIdx.x & 31u) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned long long s = 0;
+  for (int w = 0; w < kWarps; w++) s += part[w];
+  __syncthreads();
+  return s;
 }
 
-// The whole reverse sweep in one cooperative launch: zero the accumulators and
-// outputs, visit every terminal, then the levels from the deepest up, with a
-// bounded grid barrier after each phase.  The level bounds, the item and the
-// terminal counts are the forward launch's final state, read on the device,
-// so no host round trip is needed.  A failed or overflowed forward pass leaves
-// the gradients zero (the engine report keeps the forward's status; a tape
-// too short for the terminals raises PGA_ERR_NO_TAPE).
+// The whole reverse sweep in one cooperative launch, with a bounded grid
+// barrier after each phase:
+//   1. zero the outputs; each block sums the child counts of its contiguous
+//      chunk of work items;
+//   2. each block scans its chunk into child keys and marks its slots empty;
+//   3. every terminal and work item enters its slot (a terminal of an axiom's
+//      root goes straight to the axiom's sizes);
+//   4. the levels from the deepest up, one adj_page per work item.
+// The level bounds, the item and the terminal counts are the forward launch's
+// final state, read on the device, so no host round trip is needed.  A failed
+// or overflowed forward pass leaves the gradients zero (the engine report
+// keeps the forward's status; a tape too short for the terminals or a slot
+// map larger than its buffer raises PGA_ERR_NO_TAPE).
 __global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, unsigned long long numParamFloats,
                                                       uint32_t numAxioms) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
@@ -541,24 +679,85 @@ __global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, u
   const unsigned long long nodes = min((unsigned long long)vs->nodeNext, a.nodeCap);
   const unsigned long long nTerm = vs->termCount;
   const uint32_t levels = vs->levels;
-  const bool ok = vs->status == 0 && nTerm <= a.cap && nTerm <= a.termLinkCap;
+  const bool ok = vs->status == 0 && nTerm <= a.cap && nTerm <= a.termLinkCap && nTerm < kItemTag;
   const unsigned long long tid = (unsigned long long)blockIdx.x * kThreads + threadIdx.x;
   const unsigned long long stride = (unsigned long long)gridDim.x * kThreads;
-  for (unsigned long long k = tid; k < nodes * 6; k += stride) j.nodeGrad[k] = 0.0f;
   if (j.gradParams)
     for (unsigned long long k = tid; k < numParamFloats; k += stride) j.gradParams[k] = 0.0f;
   if (j.gradSizes)
     for (unsigned long long k = tid; k < (unsigned long long)numAxioms * 3; k += stride) j.gradSizes[k] = 0.0f;
+  const unsigned long long chunk = (nodes + gridDim.x - 1) / gridDim.x;
+  const unsigned long long lo = min((unsigned long long)blockIdx.x * chunk, nodes), hi = min(lo + chunk, nodes);
+  unsigned long long mine = 0;
+  for (unsigned long long i = lo + threadIdx.x; i < hi; i += kThreads)
+    mine += page_children(__ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3));
+  mine = block_sum(mine);
+  if (threadIdx.x == 0) j.blockSums[blockIdx.x] = mine;
   if (!grid_barrier(a, [] {})) return;
   if (!ok) {
     if (tid == 0 && vs->status == 0) raise_error(a.st, PGA_ERR_NO_TAPE, -1);
     return;
   }
-  for (unsigned long long t = tid; t < nTerm; t += stride) adj_terminal(a, j, t);
+  unsigned long long base = 0, total = 0;
+  for (uint32_t b = threadIdx.x; b < gridDim.x; b += kThreads) {
+    const unsigned long long x = __ldcg(j.blockSums + b);
+    base += (b < blockIdx.x) ? x : 0ull;
+    total += x;
+  }
+  base = block_sum(base);
+  total = block_sum(total);
+  if (total > j.slotCap) {  // every block sees the same total and returns here
+    if (tid == 0) raise_error(a.st, PGA_ERR_NO_TAPE, -2);
+    return;
+  }
+  for (unsigned long long t0 = lo; t0 < hi; t0 += kThreads) {
+    const unsigned long long i = t0 + threadIdx.x;
+    uint32_t cnt = 0, key = 0;
+    if (i < hi) {
+      const uint4* rec = reinterpret_cast<const uint4*>(a.nodes + i);
+      const uint4 ext = __ldcg(rec + 3);
+      cnt = page_children(ext);
+      if (cnt) {
+        const int32_t e = (int32_t)__ldcg(rec + 2).x;
+        const bool rep = e >= 0 && (uint32_t)e < a.tab.numEntries && rule_at(a, (uint32_t)e).op == PGA_OP_REPEAT;
+        key = (uint32_t)0u - ext.x - (rep ? 1u : 0u);
+      }
+    }
+    unsigned long long tileTotal;
+    const unsigned long long first = base + block_excl_scan(cnt, tileTotal);
+    if (i < hi) {
+      j.childKey[i] = (uint32_t)first + key;
+      for (uint32_t q = 0; q < cnt; q++) j.slots[first + q] = kNoRecord;
+    }
+    base += tileTotal;
+  }
+  if (!grid_barrier(a, [] {})) return;
+  for (unsigned long long t = tid; t < nTerm; t += stride) {
+    const uint2 link = __ldg(a.termLinks + t);
+    if (link.x & kAxiomLink) {
+      Grad none;
+      grad_zero(none);
+      push_to_axiom(a, j, link.x & ~kAxiomLink, true, t, none);
+    } else if (link.x < nodes) {
+      j.slots[(uint32_t)(__ldcg(j.childKey + link.x) + link.y)] = (uint32_t)t;
+    }
+  }
+  for (unsigned long long i = tid; i < nodes; i += stride) {
+    const uint4 ext = __ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3);
+    if (ext.x == kEmptyItem || (ext.z & kAxiomLink) || ext.z >= nodes) continue;
+    const uint32_t head = atomicExch(j.slots + (uint32_t)(__ldcg(j.childKey + ext.z) + ext.w), kItemTag | (uint32_t)i);
+    j.pageNext[i] = head == kNoRecord ? kNoRecord : (head & ~kItemTag);
+  }
   if (!grid_barrier(a, [] {})) return;
   for (int L = (int)levels; L >= 0; L--) {
-    const unsigned long long lo = a.levelStart[L], hi = min(a.levelStart[L + 1], nodes);
-    for (unsigned long long i = lo + tid; i < hi; i += stride) adj_item(a, j, i);
+    const unsigned long long lv = a.levelStart[L], hv = min(a.levelStart[L + 1], nodes);
+    for (unsigned long long i = lv + tid; i < hv; i += stride) {
+      if (i + stride < hv) {  // the next item's record and key, ahead of its turn
+        prefetch_l2(a.nodes + i + stride);
+        prefetch_l2(j.childKey + i + stride);
+      }
+      adj_page(a, j, i, nodes);
+    }
     if (!grid_barrier(a, [] {})) return;
   }
 }
@@ -586,7 +785,7 @@ extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, floa
       set_error("pga_adjoint: the adjoint kernel does not fit on an SM");
       return PGA_ERR_CUDA;
     }
-    e->adjointBlocks = perSM * e->numSMs;
+    e->adjointBlocks = (int)std::min<uint32_t>((uint32_t)(perSM * e->numSMs), kMaxAdjointBlocks);
   }
   DeriveArgs a = make_args(e, e->lastAxioms, e->lastNumAxioms, e->lastBlocks, e->lastOut, e->lastCap, nullptr);
   AdjArgs j;
@@ -595,7 +794,11 @@ extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, floa
   j.numBlocks = numBlocks;
   j.gradSizes = dGradAxiomSizes;
   j.nodeGrad = e->dNodeGrad;
-  j.numTerminals = 0;  // read on the device
+  j.childKey = e->dChildKey;
+  j.pageNext = e->dPageNext;
+  j.slots = e->dSlots;
+  j.blockSums = e->dBlockSums;
+  j.slotCap = e->slotCap;
   unsigned long long numParamFloats = (unsigned long long)numBlocks * e->cfg.blockStride;
   uint32_t numAxioms = e->lastNumAxioms;
   void* args[] = {&a, &j, &numParamFloats, &numAxioms};

@@ -214,7 +214,8 @@ static void free_engine(PgaEngine* e) {
   void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dNodeRot, e->dLevelClock,
                   e->dTail, e->dTailLinks, e->dScratch,
                   e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA,
-                  e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dLeafAabbSorted, e->dNodeRange, e->dNodeGrad, e->dAxiomGrad};
+                  e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dLeafAabbSorted, e->dNodeRange, e->dNodeGrad, e->dChildKey, e->dPageNext,
+                  e->dSlots, e->dBlockSums};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (e->dStageAxioms) cudaFree(e->dStageAxioms);
@@ -449,8 +450,20 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   ALLOC(e->dLevelClock, (c.maxLevels + 2) * sizeof(unsigned long long));
   ALLOC(e->dScratchCount, sizeof(unsigned long long));
   if (c.recordTape) {
+    // The reverse pass tags work-item indices with bit 31 and counts child
+    // slots in 32 bits; a work item has at most max(subItem, narrowSubItem)
+    // children, which bounds the slots.
+    if (c.nodeCapacity >= 0x7FFFFFFFull) {
+      set_error("pga_engine_create: recordTape needs nodeCapacity < 2^31 - 1");
+      return fail(PGA_ERR_INVALID_ARGUMENT);
+    }
+    e->slotCap = std::min<unsigned long long>(c.nodeCapacity * std::max(c.subItem, c.narrowSubItem), 0xFFFFFFF0ull);
     ALLOC(e->dTermLinks, c.maxTerminals * sizeof(uint2));
     ALLOC(e->dNodeGrad, c.nodeCapacity * 6 * sizeof(float));
+    ALLOC(e->dChildKey, c.nodeCapacity * sizeof(uint32_t));
+    ALLOC(e->dPageNext, c.nodeCapacity * sizeof(uint32_t));
+    ALLOC(e->dSlots, e->slotCap * sizeof(uint32_t));
+    ALLOC(e->dBlockSums, kMaxAdjointBlocks * sizeof(unsigned long long));
   }
   // LBVH scratch for up to maxTerminals leaves.
   e->sortTempBytes = pga_lbvh_temp_bytes(c.maxTerminals);

@@ -15,6 +15,7 @@ inline namespace PGA_FRAMES_NS {
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+constexpr uint32_t kMaxAdjointBlocks = 8192;  // blocks of the reverse launch (slot-map scan)
 enum Kind { kNone = 0, kTerm = 1, kNode = 2 };
 
 struct __align__(16) Smem {

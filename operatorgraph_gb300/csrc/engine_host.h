@@ -70,9 +70,15 @@ struct PgaEngine {
   float* dLeafAabbSorted = nullptr;  // the same in sorted (leaf) order
   int2* dNodeRange = nullptr;        // LBVH internal node leaf ranges [lo, hi]
 
-  // Adjoint scratch: per-node gradient of (translation, size).
+  // Adjoint scratch: per work item the gradient of (translation, size), its
+  // child key and the next page of the same child; the child slots (slotCap
+  // of them); per block of the reverse launch its chunk's child count.
   float* dNodeGrad = nullptr;
-  float* dAxiomGrad = nullptr;
+  uint32_t* dChildKey = nullptr;
+  uint32_t* dPageNext = nullptr;
+  uint32_t* dSlots = nullptr;
+  unsigned long long* dBlockSums = nullptr;
+  unsigned long long slotCap = 0;
 
   // Last pga_derive, for pga_adjoint.
   const PgaAxiom* lastAxioms = nullptr;

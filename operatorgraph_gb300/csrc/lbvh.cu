@@ -61,11 +61,27 @@ __device__ __forceinline__ void leaf_aabb(const float4 r[3], bool quad, float mn
 // generateMortonCodes (GPUBVHConstructor.cuh:66-86) on terminal centres.
 // Also writes each terminal's AABB (6 floats, terminal order) while its record
 // is in registers.
-__global__ void __launch_bounds__(kLbvhThreads) k_morton(const PgaTerminal* __restrict__ t, unsigned long long n,
-                                                         Bounds b, unsigned long long* __restrict__ keys,
+// Leaf count of a build: the host value `n`, or, when the count lives on the
+// device (dN != nullptr), min(*dN, n) with `n` the capacity the launches and
+// the sort were sized for.
+__device__ __forceinline__ unsigned long long leaf_count(const unsigned long long* dN, unsigned long long n) {
+  return dN ? min(*dN, n) : n;
+}
+
+// With a device count, the keys in [count, capacity) are padding: all ones,
+// after every real key in the stable radix sort (a real key can equal it only
+// in the sorted top bits, and it comes first there by input order).
+__global__ void __launch_bounds__(kLbvhThreads) k_morton(const PgaTerminal* __restrict__ t, unsigned long long cap,
+                                                         const unsigned long long* __restrict__ dN, Bounds b,
+                                                         unsigned long long* __restrict__ keys,
                                                          uint32_t* __restrict__ vals, float* __restrict__ leafBox) {
   unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= cap) return;
+  if (i >= leaf_count(dN, cap)) {
+    keys[i] = ~0ull;
+    vals[i] = (uint32_t)i;
+    return;
+  }
   const float4* p = reinterpret_cast<const float4*>(t + i);
   float4 r[3] = {__ldg(p + 0), __ldg(p + 1), __ldg(p + 2)};
   uint4 meta = __ldg(reinterpret_cast<const uint4*>(p + 3));
@@ -102,7 +118,9 @@ __device__ __forceinline__ uint64_t term_path(const PgaTerminal* t, uint32_t i) 
 constexpr int kSortLowBit = 24;  // 5 radix passes of 8 bits instead of 8
 
 __global__ void k_fix_ties(unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
-                           const PgaTerminal* __restrict__ t, unsigned long long n) {
+                           const PgaTerminal* __restrict__ t, unsigned long long cap,
+                           const unsigned long long* __restrict__ dN) {
+  const unsigned long long n = leaf_count(dN, cap);
   unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i + 1 >= n) return;
   const unsigned long long k = keys[i] >> kSortLowBit;
@@ -133,12 +151,17 @@ __device__ __forceinline__ unsigned long long karras_code(const unsigned long lo
 // buildRadixTree (GPUBVHConstructor.cuh:88-213), one thread per internal node,
 // with bounds checks on every probe.
 // Also gathers the leaf boxes into sorted order (one independent load per
-// leaf here instead of a dependent one inside the refit's climb).
-__global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long long* __restrict__ keys, long long n,
+// leaf here instead of a dependent one inside the refit's climb) and clears
+// the refit's arrival counters.  Fewer than two leaves make no tree.
+__global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long long* __restrict__ keys, long long cap,
+                                                         const unsigned long long* __restrict__ dN,
                                                          int32_t* __restrict__ nodes, uint32_t* __restrict__ leafParents,
                                                          uint32_t* __restrict__ sortedVals, const uint32_t* __restrict__ vals,
                                                          const float* __restrict__ leafBox,
-                                                         float* __restrict__ sortedBox, int2* __restrict__ nodeRange) {
+                                                         float* __restrict__ sortedBox, int2* __restrict__ nodeRange,
+                                                         uint32_t* __restrict__ arrival) {
+  const long long n = (long long)leaf_count(dN, (unsigned long long)cap);
+  if (n < 2) return;
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     const uint32_t v = vals[i];
@@ -151,6 +174,7 @@ __global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long lon
     dst[2] = c;
   }
   if (i >= n - 1) return;
+  arrival[i] = 0u;
   const unsigned long long ci = karras_code(keys, i);
   auto delta = [&](long long j) -> int { return __clzll(ci ^ karras_code(keys, j)); };
   long long d, len;
@@ -242,13 +266,16 @@ __device__ __forceinline__ void load_box(const float* p, float mn[3], float mx[3
 // global counters at GPU scope (`arrive`).  Every node's box is also stored
 // to aabbs, the output.  A node's links, its range and a leaf sibling's box
 // are fixed before this kernel, so they are read ahead of the arrival.
-__global__ void __launch_bounds__(kLbvhThreads) k_refit(const float* __restrict__ sortedBox, long long n,
+__global__ void __launch_bounds__(kLbvhThreads) k_refit(const float* __restrict__ sortedBox, long long cap,
+                                                        const unsigned long long* __restrict__ dN,
                                                         const int32_t* __restrict__ nodes,
                                                         const int2* __restrict__ nodeRange,
                                                         const uint32_t* __restrict__ leafParents,
                                                         uint32_t* __restrict__ arrival, float* __restrict__ aabbs) {
   __shared__ uint32_t blockArrive[kLbvhThreads];
   __shared__ float blockBox[kLbvhThreads * 6];
+  const long long n = (long long)leaf_count(dN, (unsigned long long)cap);
+  if (n < 2) return;
   blockArrive[threadIdx.x] = 0u;
   __syncthreads();
   const long long B = (long long)blockIdx.x * kLbvhThreads;
@@ -311,10 +338,63 @@ extern "C" size_t pga_lbvh_temp_bytes(uint64_t n) {
   return bytes ? bytes : 16;
 }
 
+namespace pga {
+
+// Scratch of one build: keys, two value arrays, arrival counters, leaf boxes
+// (terminal and sorted order), node ranges and the radix sort's temp storage.
+struct LbvhScratch {
+  unsigned long long* keysA;
+  uint32_t* valsA;
+  uint32_t* valsB;
+  uint32_t* arrival;
+  float* leafBox;
+  float* sortedBox;
+  int2* nodeRange;
+  void* sortTemp;
+  size_t sortTempBytes;
+};
+
+// The five launches of a build over `cap` leaves, or over min(*dN, cap) when
+// dN is a device count (then `cap` sizes the grids and the sort).
+static PgaStatus launch_lbvh(const PgaTerminal* t, unsigned long long cap, const unsigned long long* dN,
+                             const PgaBounds* bounds, const PgaLbvh* out, const LbvhScratch& w, cudaStream_t s) {
+  Bounds b;
+  for (int k = 0; k < 3; k++) {
+    b.mn[k] = bounds->min[k];
+    b.sz[k] = bounds->max[k] - bounds->min[k];
+  }
+  const unsigned blocks = (unsigned)((cap + kLbvhThreads - 1) / kLbvhThreads);
+  unsigned long long* keys = (unsigned long long*)out->keys;
+  k_morton<<<blocks, kLbvhThreads, 0, s>>>(t, cap, dN, b, w.keysA, w.valsA, w.leafBox);
+  PGA_CUDA_TRY(cudaGetLastError());
+  size_t temp = w.sortTempBytes;
+  PGA_CUDA_TRY(cub::DeviceRadixSort::SortPairs(w.sortTemp, temp, w.keysA, keys, w.valsA, w.valsB, (int64_t)cap,
+                                               kSortLowBit, 64, s));
+  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>(keys, w.valsB, t, cap, dN);
+  PGA_CUDA_TRY(cudaGetLastError());
+  k_karras<<<blocks, kLbvhThreads, 0, s>>>(keys, (long long)cap, dN, out->nodes, out->leafParents, out->leafTerminal,
+                                           w.valsB, w.leafBox, w.sortedBox, w.nodeRange, w.arrival);
+  PGA_CUDA_TRY(cudaGetLastError());
+  k_refit<<<blocks, kLbvhThreads, 0, s>>>(w.sortedBox, (long long)cap, dN, out->nodes, w.nodeRange, out->leafParents,
+                                          w.arrival, out->aabbs);
+  PGA_CUDA_TRY(cudaGetLastError());
+  return PGA_OK;
+}
+
+static LbvhScratch engine_scratch(PgaEngine* e) {
+  return LbvhScratch{e->dKeysA,     e->dValsA,    e->dValsB,    e->dArrival,     e->dLeafAabb,
+                     e->dLeafAabbSorted, e->dNodeRange, e->dSortTemp, e->sortTempBytes};
+}
+
+static bool lbvh_out_ok(const PgaLbvh* out) {
+  return out && out->nodes && out->leafParents && out->aabbs && out->leafTerminal && out->keys;
+}
+
+}  // namespace pga
+
 extern "C" PgaStatus pga_lbvh_build(PgaEngine* e, const PgaTerminal* dTerminals, uint64_t n, const PgaBounds* bounds,
                                     const PgaLbvh* out, void* stream) {
-  if (!e || !dTerminals || !bounds || !out || !out->nodes || !out->leafParents || !out->aabbs || !out->leafTerminal ||
-      !out->keys) {
+  if (!e || !dTerminals || !bounds || !lbvh_out_ok(out)) {
     set_error("pga_lbvh_build: null argument");
     return PGA_ERR_INVALID_ARGUMENT;
   }
@@ -322,29 +402,22 @@ extern "C" PgaStatus pga_lbvh_build(PgaEngine* e, const PgaTerminal* dTerminals,
     set_error("pga_lbvh_build: need 2 <= n <= maxTerminals (and < 2^31)");
     return PGA_ERR_INVALID_ARGUMENT;
   }
-  cudaStream_t s = (cudaStream_t)stream;
-  Bounds b;
-  for (int k = 0; k < 3; k++) {
-    b.mn[k] = bounds->min[k];
-    b.sz[k] = bounds->max[k] - bounds->min[k];
+  return launch_lbvh(dTerminals, n, nullptr, bounds, out, engine_scratch(e), (cudaStream_t)stream);
+}
+
+extern "C" PgaStatus pga_lbvh_build_counted(PgaEngine* e, const PgaTerminal* dTerminals, const uint64_t* dCount,
+                                            uint64_t capacity, const PgaBounds* bounds, const PgaLbvh* out,
+                                            void* stream) {
+  if (!e || !dTerminals || !dCount || !bounds || !lbvh_out_ok(out)) {
+    set_error("pga_lbvh_build_counted: null argument");
+    return PGA_ERR_INVALID_ARGUMENT;
   }
-  unsigned blocks = (unsigned)((n + kLbvhThreads - 1) / kLbvhThreads);
-  k_morton<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, n, b, e->dKeysA, e->dValsA, e->dLeafAabb);
-  PGA_CUDA_TRY(cudaGetLastError());
-  size_t temp = e->sortTempBytes;
-  PGA_CUDA_TRY(cub::DeviceRadixSort::SortPairs(e->dSortTemp, temp, e->dKeysA, (unsigned long long*)out->keys,
-                                               e->dValsA, e->dValsB, (int64_t)n, kSortLowBit, 64, s));
-  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>((unsigned long long*)out->keys, e->dValsB, dTerminals, n);
-  PGA_CUDA_TRY(cudaGetLastError());
-  k_karras<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, (long long)n, out->nodes,
-                                           out->leafParents, out->leafTerminal, e->dValsB, e->dLeafAabb,
-                                           e->dLeafAabbSorted, e->dNodeRange);
-  PGA_CUDA_TRY(cudaGetLastError());
-  PGA_CUDA_TRY(cudaMemsetAsync(e->dArrival, 0, (n - 1) * sizeof(uint32_t), s));
-  k_refit<<<blocks, kLbvhThreads, 0, s>>>(e->dLeafAabbSorted, (long long)n, out->nodes, e->dNodeRange,
-                                          out->leafParents, e->dArrival, out->aabbs);
-  PGA_CUDA_TRY(cudaGetLastError());
-  return PGA_OK;
+  if (capacity < 2 || capacity > e->cfg.maxTerminals || capacity > 0x7FFFFFFFull) {
+    set_error("pga_lbvh_build_counted: need 2 <= capacity <= maxTerminals (and < 2^31)");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  return launch_lbvh(dTerminals, capacity, (const unsigned long long*)dCount, bounds, out, engine_scratch(e),
+                     (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -381,8 +454,7 @@ static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const PgaBounds* bounds,
                                            const PgaLbvh* out, void* stream) {
-  if (!dTerminals || !bounds || !out || !out->nodes || !out->leafParents || !out->aabbs || !out->leafTerminal ||
-      !out->keys) {
+  if (!dTerminals || !bounds || !lbvh_out_ok(out)) {
     set_error("pga_lbvh_build_static: null argument");
     return PGA_ERR_INVALID_ARGUMENT;
   }
@@ -432,25 +504,6 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
     set_error("pga_lbvh_build_static: fixed scratch too small for the radix sort of " + std::to_string(n) + " keys");
     return PGA_ERR_INVALID_ARGUMENT;
   }
-  cudaStream_t s = (cudaStream_t)stream;
-  Bounds b;
-  for (int k = 0; k < 3; k++) {
-    b.mn[k] = bounds->min[k];
-    b.sz[k] = bounds->max[k] - bounds->min[k];
-  }
-  const unsigned blocks = (unsigned)((n + kLbvhThreads - 1) / kLbvhThreads);
-  k_morton<<<blocks, kLbvhThreads, 0, s>>>(dTerminals, n, b, keysA, valsA, leafBox);
-  PGA_CUDA_TRY(cudaGetLastError());
-  PGA_CUDA_TRY(cub::DeviceRadixSort::SortPairs(sortTemp, temp, keysA, (unsigned long long*)out->keys, valsA, valsB,
-                                               (int64_t)n, kSortLowBit, 64, s));
-  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>((unsigned long long*)out->keys, valsB, dTerminals, n);
-  PGA_CUDA_TRY(cudaGetLastError());
-  k_karras<<<blocks, kLbvhThreads, 0, s>>>((const unsigned long long*)out->keys, (long long)n, out->nodes,
-                                           out->leafParents, out->leafTerminal, valsB, leafBox, sortedBox, nodeRange);
-  PGA_CUDA_TRY(cudaGetLastError());
-  PGA_CUDA_TRY(cudaMemsetAsync(arrival, 0, (n - 1) * sizeof(uint32_t), s));
-  k_refit<<<blocks, kLbvhThreads, 0, s>>>(sortedBox, (long long)n, out->nodes, nodeRange, out->leafParents, arrival,
-                                          out->aabbs);
-  PGA_CUDA_TRY(cudaGetLastError());
-  return PGA_OK;
+  const LbvhScratch w{keysA, valsA, valsB, arrival, leafBox, sortedBox, nodeRange, sortTemp, temp};
+  return launch_lbvh(dTerminals, n, nullptr, bounds, out, w, (cudaStream_t)stream);
 }

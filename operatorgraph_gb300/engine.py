@@ -26,7 +26,7 @@ STATUS = {
 # Every symbol include/pga_gb300.h declares.
 EXPORTS = ["pga_version", "pga_last_error", "pga_default_procs", "pga_engine_create", "pga_engine_destroy",
            "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_engine_levels", "pga_lbvh_build",
-           "pga_lbvh_build_static", "pga_adjoint", "pga_derive_to_host", "pga_generate_meshes"]
+           "pga_lbvh_build_counted", "pga_lbvh_build_static", "pga_adjoint", "pga_derive_to_host", "pga_generate_meshes"]
 
 
 class PgaError(RuntimeError):
@@ -93,6 +93,7 @@ def load_library(path=LIB_PATH):
         getattr(L, name).argtypes = [vp, vp, u32, vp, vp, u64, vp, vp]
     L.pga_engine_sync_report.argtypes = [vp, vp, ctypes.POINTER(PgaDeriveReport)]
     L.pga_lbvh_build.argtypes = [vp, vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
+    L.pga_lbvh_build_counted.argtypes = [vp, vp, vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
     L.pga_adjoint.argtypes = [vp, vp, vp, u32, vp, vp]
     L.pga_engine_levels.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(u32)]
     L.pga_lbvh_build_static.argtypes = [vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
@@ -213,8 +214,14 @@ class Engine:
             raise PgaError(2, f"{n} terminals > capacity {capacity}")
         return out, n, rep
 
-    def lbvh(self, terminals, n, bounds, stream=None):
-        """Builds the LBVH over terminals[:n]; returns a dict of device tensors."""
+    def lbvh(self, terminals, n, bounds, stream=None, count=None):
+        """Builds the LBVH over terminals[:n]; returns a dict of device tensors.
+
+        With `count` (a device int64 tensor holding the leaf count, such as the
+        one derive wrote), n is the capacity: the tree covers the first
+        min(count, n) terminals and nothing is read back to the host
+        (pga_lbvh_build_counted), so the call can be captured in a CUDA graph.
+        """
         import torch
 
         L = load_library()
@@ -230,8 +237,12 @@ class Engine:
         pb = PgaBounds((ctypes.c_float * 3)(*b[:3]), (ctypes.c_float * 3)(*b[3:]))
         out = PgaLbvh(res["nodes"].data_ptr(), res["leafParents"].data_ptr(), res["aabbs"].data_ptr(),
                       res["leafTerminal"].data_ptr(), res["keys"].data_ptr())
-        _check(L.pga_lbvh_build(self.handle, terminals.data_ptr(), n, ctypes.byref(pb), ctypes.byref(out),
-                                _stream_handle(stream)), "pga_lbvh_build")
+        if count is None:
+            _check(L.pga_lbvh_build(self.handle, terminals.data_ptr(), n, ctypes.byref(pb), ctypes.byref(out),
+                                    _stream_handle(stream)), "pga_lbvh_build")
+        else:
+            _check(L.pga_lbvh_build_counted(self.handle, terminals.data_ptr(), count.data_ptr(), n, ctypes.byref(pb),
+                                            ctypes.byref(out), _stream_handle(stream)), "pga_lbvh_build_counted")
         return res
 
     def generate_meshes_raw(self, d_terminals, n, d_meshes, num_meshes, stream=None):
