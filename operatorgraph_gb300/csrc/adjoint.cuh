@@ -183,9 +183,37 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
       const uint32_t ax = E0.axis;
       for (uint32_t k = 0; k < 3; k++)
         if (k != ax) gp.s[k] += gc.s[k];
-      st.idx = (int)min(c, n - 1u);
-      st.gN = pick3(gc.s, ax);
-      st.goI = axis_dot(x, ax, gc.t);
+      const uint32_t i = min(c, n - 1u);
+      const float gN = pick3(gc.s, ax), go = axis_dot(x, ax, gc.t);
+      if (r.flags & kRuleScalar) {
+        // Constant factors: N_k = f_k (f_k > 0) or scale * -f_k (f_k < 0) with
+        // scale = (S - sum of the positive f) / relSum, relSum = sum of -f over
+        // the negative f, and o_c = -S/2 + sum_{k<c} N_k + N_c/2.  So
+        // dN_k/dS = -f_k / relSum (f_k < 0, else 0) and
+        // do_c/dS = -1/2 + sum_{k<c} dN_k/dS + dN_c/dS / 2: child c's whole
+        // share of dL/dS, with nothing left for subdivide_sweep.
+        float relSum = 0.0f, below = 0.0f, fc = 0.0f;
+        for (uint32_t k = 0; k < n; k++) {
+          const float f = param_at(a, r.paramBase + k + 1).v0;
+          if (f < 0.0f) {
+            relSum += -f;
+            if (k < i) below += -f;
+          }
+          if (k == i) fc = f;
+        }
+        float gS = -0.5f * go;
+        if (relSum != 0.0f) {
+          const float dN = fc < 0.0f ? -fc / relSum : 0.0f;
+          gS += gN * dN + go * (below / relSum + 0.5f * dN);
+        }
+        gp.s[0] += (ax == 0) ? gS : 0.0f;
+        gp.s[1] += (ax == 1) ? gS : 0.0f;
+        gp.s[2] += (ax == 2) ? gS : 0.0f;
+        return;
+      }
+      st.idx = (int)i;
+      st.gN = gN;
+      st.goI = go;
       return;
     }
     case PGA_OP_REPEAT: {
@@ -364,7 +392,8 @@ struct Chain {
 enum ChainEnd : int { kEndFail = -1, kEndTerminal = 0, kEndItem = 1, kEndDiscard = 2 };
 
 // Replays the chain from x, the shape as its creator produced it, to its end
-// state yEnd (the record's state); returns how it ends.
+// state yEnd (the record's state; its path hash is not kept up to date, the
+// reverse pass has no use for it); returns how it ends.
 __device__ int replay_chain(const DeriveArgs& a, Shape x, Chain& ch, Shape& yEnd) {
   ch.n = 0;
   for (int step = 0; step < kMaxChain; step++) {
@@ -375,7 +404,6 @@ __device__ int replay_chain(const DeriveArgs& a, Shape x, Chain& ch, Shape& yEnd
       if (!axis_param(a, r, x, axis)) return kEndFail;
       const float size = param(a, r, 1, x);
       const uint32_t branch = (pick3(x.s, axis) < size) ? 0u : 1u;
-      x.path = child_path(x.path, branch, succ_at(a, r.succBase + branch));
       x.entry = succ_at(a, r.succBase + branch);
       continue;
     }
@@ -383,13 +411,11 @@ __device__ int replay_chain(const DeriveArgs& a, Shape x, Chain& ch, Shape& yEnd
       const int pick = random_pick(a, r, x);
       if (pick < 0) return kEndFail;
       const int32_t nxt = succ_at(a, r.succBase + (uint32_t)pick);
-      x.path = child_path(x.path, (uint32_t)pick, nxt);
       x.entry = nxt;
       continue;
     }
     if (r.op == PGA_OP_IF) {
       const uint32_t branch = (param(a, r, 0, x) != 0.0f) ? 0u : 1u;
-      x.path = child_path(x.path, branch, succ_at(a, r.succBase + branch));
       x.entry = succ_at(a, r.succBase + branch);
       continue;
     }
@@ -420,7 +446,6 @@ __device__ int replay_chain(const DeriveArgs& a, Shape x, Chain& ch, Shape& yEnd
       x.seed = seed_of(a, x.seed, 0u);
       x.kind = PGA_SHAPE_BOX;
       const int32_t nxt = succ_at(a, r.succBase);
-      x.path = child_path(x.path, 0u, nxt);
       x.entry = nxt;
       continue;
     }
@@ -488,9 +513,9 @@ __device__ __forceinline__ Grad terminal_grad(const AdjArgs& j, unsigned long lo
 // A record created from axiom ax's root shape (a terminal t, or a work item
 // whose gradient is g): back through the root's chain into the axiom's size
 // gradient.  An axiom has few such records (one terminal, or the pages of
-// one item), so they add atomically.
-__device__ void push_to_axiom(const DeriveArgs& a, const AdjArgs& j, uint32_t ax, bool terminal,
-                              unsigned long long t, Grad g) {
+// one item), so they add atomically; out of line, as the rare path it is.
+__device__ __noinline__ void push_to_axiom(const DeriveArgs& a, const AdjArgs& j, uint32_t ax, bool terminal,
+                                           unsigned long long t, Grad g) {
   Shape y0, yEnd;
   axiom_shape(a, ax, y0);
   Chain ch;
@@ -686,13 +711,25 @@ __global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, u
     for (unsigned long long k = tid; k < numParamFloats; k += stride) j.gradParams[k] = 0.0f;
   if (j.gradSizes)
     for (unsigned long long k = tid; k < (unsigned long long)numAxioms * 3; k += stride) j.gradSizes[k] = 0.0f;
+  // Each block owns a contiguous chunk of the work items, each thread a
+  // contiguous run of its block's chunk; loads go kUnroll at a time.
+  constexpr int kUnroll = 4;
   const unsigned long long chunk = (nodes + gridDim.x - 1) / gridDim.x;
   const unsigned long long lo = min((unsigned long long)blockIdx.x * chunk, nodes), hi = min(lo + chunk, nodes);
-  unsigned long long mine = 0;
-  for (unsigned long long i = lo + threadIdx.x; i < hi; i += kThreads)
-    mine += page_children(__ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3));
-  mine = block_sum(mine);
-  if (threadIdx.x == 0) j.blockSums[blockIdx.x] = mine;
+  const unsigned long long run = (hi - lo + kThreads - 1) / kThreads;
+  const unsigned long long tlo = min(lo + threadIdx.x * run, hi), thi = min(tlo + run, hi);
+  uint32_t mine = 0;  // a work item has at most 64 children
+  for (unsigned long long i = tlo; i < thi; i += kUnroll) {
+    uint4 ext[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++)
+      ext[u] = i + u < thi ? __ldcg(reinterpret_cast<const uint4*>(a.nodes + i + u) + 3)
+                           : make_uint4(kEmptyItem, 0u, 0u, 0u);
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) mine += page_children(ext[u]);
+  }
+  const unsigned long long blockTotal = block_sum(mine);
+  if (threadIdx.x == 0) j.blockSums[blockIdx.x] = blockTotal;
   if (!grid_barrier(a, [] {})) return;
   if (!ok) {
     if (tid == 0 && vs->status == 0) raise_error(a.st, PGA_ERR_NO_TAPE, -1);
@@ -710,43 +747,79 @@ __global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, u
     if (tid == 0) raise_error(a.st, PGA_ERR_NO_TAPE, -2);
     return;
   }
-  for (unsigned long long t0 = lo; t0 < hi; t0 += kThreads) {
-    const unsigned long long i = t0 + threadIdx.x;
-    uint32_t cnt = 0, key = 0;
-    if (i < hi) {
-      const uint4* rec = reinterpret_cast<const uint4*>(a.nodes + i);
-      const uint4 ext = __ldcg(rec + 3);
-      cnt = page_children(ext);
-      if (cnt) {
-        const int32_t e = (int32_t)__ldcg(rec + 2).x;
-        const bool rep = e >= 0 && (uint32_t)e < a.tab.numEntries && rule_at(a, (uint32_t)e).op == PGA_OP_REPEAT;
-        key = (uint32_t)0u - ext.x - (rep ? 1u : 0u);
+  for (unsigned long long k = tid; k < total; k += stride) j.slots[k] = kNoRecord;
+  {
+    unsigned long long ignored;
+    unsigned long long first = base + block_excl_scan(mine, ignored);
+    for (unsigned long long i = tlo; i < thi; i += kUnroll) {
+      uint4 m[kUnroll], ext[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) {
+        const uint4* rec = reinterpret_cast<const uint4*>(a.nodes + min(i + u, thi - 1));
+        m[u] = __ldcg(rec + 2);
+        ext[u] = __ldcg(rec + 3);
+      }
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) {
+        if (i + u >= thi) break;
+        const uint32_t cnt = page_children(ext[u]);
+        uint32_t key = 0;
+        if (cnt) {
+          const int32_t e = (int32_t)m[u].x;
+          const bool rep = e >= 0 && (uint32_t)e < a.tab.numEntries && rule_at(a, (uint32_t)e).op == PGA_OP_REPEAT;
+          key = (uint32_t)0u - ext[u].x - (rep ? 1u : 0u);
+        }
+        j.childKey[i + u] = (uint32_t)first + key;
+        first += cnt;
       }
     }
-    unsigned long long tileTotal;
-    const unsigned long long first = base + block_excl_scan(cnt, tileTotal);
-    if (i < hi) {
-      j.childKey[i] = (uint32_t)first + key;
-      for (uint32_t q = 0; q < cnt; q++) j.slots[first + q] = kNoRecord;
-    }
-    base += tileTotal;
   }
   if (!grid_barrier(a, [] {})) return;
-  for (unsigned long long t = tid; t < nTerm; t += stride) {
-    const uint2 link = __ldg(a.termLinks + t);
-    if (link.x & kAxiomLink) {
-      Grad none;
-      grad_zero(none);
-      push_to_axiom(a, j, link.x & ~kAxiomLink, true, t, none);
-    } else if (link.x < nodes) {
-      j.slots[(uint32_t)(__ldcg(j.childKey + link.x) + link.y)] = (uint32_t)t;
+  for (unsigned long long t0 = tid; t0 < nTerm; t0 += stride * kUnroll) {
+    uint2 link[kUnroll];
+    uint32_t key[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      const unsigned long long t = t0 + u * stride;
+      link[u] = t < nTerm ? __ldg(a.termLinks + t) : make_uint2(kAxiomLink, 0u);
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++)
+      key[u] = (!(link[u].x & kAxiomLink) && link[u].x < nodes) ? __ldcg(j.childKey + link[u].x) : 0u;
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      const unsigned long long t = t0 + u * stride;
+      if (t >= nTerm) break;
+      if (link[u].x & kAxiomLink) {
+        Grad none;
+        grad_zero(none);
+        push_to_axiom(a, j, link[u].x & ~kAxiomLink, true, t, none);
+      } else if (link[u].x < nodes) {
+        j.slots[(uint32_t)(key[u] + link[u].y)] = (uint32_t)t;
+      }
     }
   }
-  for (unsigned long long i = tid; i < nodes; i += stride) {
-    const uint4 ext = __ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3);
-    if (ext.x == kEmptyItem || (ext.z & kAxiomLink) || ext.z >= nodes) continue;
-    const uint32_t head = atomicExch(j.slots + (uint32_t)(__ldcg(j.childKey + ext.z) + ext.w), kItemTag | (uint32_t)i);
-    j.pageNext[i] = head == kNoRecord ? kNoRecord : (head & ~kItemTag);
+  for (unsigned long long i0 = tid; i0 < nodes; i0 += stride * kUnroll) {
+    uint4 ext[kUnroll];
+    uint32_t key[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      const unsigned long long i = i0 + u * stride;
+      ext[u] = i < nodes ? __ldcg(reinterpret_cast<const uint4*>(a.nodes + i) + 3) : make_uint4(kEmptyItem, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      const bool take = ext[u].x != kEmptyItem && !(ext[u].z & kAxiomLink) && ext[u].z < nodes;
+      ext[u].x = take ? 0u : kEmptyItem;
+      key[u] = take ? __ldcg(j.childKey + ext[u].z) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      if (ext[u].x == kEmptyItem) continue;
+      const unsigned long long i = i0 + u * stride;
+      const uint32_t head = atomicExch(j.slots + (uint32_t)(key[u] + ext[u].w), kItemTag | (uint32_t)i);
+      j.pageNext[i] = head == kNoRecord ? kNoRecord : (head & ~kItemTag);
+    }
   }
   if (!grid_barrier(a, [] {})) return;
   for (int L = (int)levels; L >= 0; L--) {

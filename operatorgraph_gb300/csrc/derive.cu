@@ -288,16 +288,17 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     }
     r.nParams = (uint8_t)en.numParameters;
     r.nSucc = (uint8_t)en.numSuccessors;
-    bool pure = true;
+    bool pure = true, scalar = true;
     for (uint32_t k = 0; k < en.numParameters; k++) {
       const PgaParameter& p = en.parameters[k];
       if (p.type != PGA_PT_SCALAR && p.type != PGA_PT_BLOCK) pure = false;
+      if (p.type != PGA_PT_SCALAR) scalar = false;
       // Seeds are observable only through random ranges, expressions and the
       // seed attribute (Shape::at(15)); otherwise seed updates can be skipped.
       if (p.type == PGA_PT_RAND || p.type == PGA_PT_EXP) e->useSeeds = true;
       if (p.type == PGA_PT_SHAPE_ATTR && p.value[0] >= 15.0f && p.value[0] < 16.0f) e->useSeeds = true;
     }
-    r.flags = (uint16_t)((r.flags & kRuleMesh) | (pure ? kRulePure : 0));
+    r.flags = (uint16_t)((r.flags & kRuleMesh) | (pure ? kRulePure : 0) | (scalar ? kRuleScalar : 0));
     // A scalar terminal index is decided here once (the device truncates it
     // toward zero like __float2uint_rz; only 0..127 are valid mesh indices).
     if (r.op == PGA_OP_GENERATE && en.numParameters >= 1 && en.parameters[0].type == PGA_PT_SCALAR &&

@@ -68,6 +68,7 @@ constexpr uint16_t kRulePure = 1;
 constexpr uint16_t kRuleConstTerminal = 2;  // Generate with a scalar terminal index, kept in nChildren
 constexpr uint16_t kRuleLeaf = 4;           // Subdivide whose children all end at once (expanded in place)
 constexpr uint16_t kRuleMesh = 8;           // a triangle-mesh Generate (lowered to op GENERATE for the derivation)
+constexpr uint16_t kRuleScalar = 16;        // every parameter a scalar constant
 constexpr uint32_t kRulePhaseShift = 8;     // flags bits 8..11: the phase of the edges into the rule (multi-phase)
 constexpr uint32_t kMaxPhases = 16;
 
