@@ -110,11 +110,12 @@ __device__ __forceinline__ uint64_t term_path(const PgaTerminal* t, uint32_t i) 
 
 // The radix sort orders the keys' top bits [kSortLowBit, 64) only (the Morton
 // code and the path hash's top 10 bits), which leaves runs of equal top bits
-// in input order.  Each such run -- rare and short, since its members share a
-// Morton cell and 10 hash bits -- is ordered here by the full path hash, then
-// terminal index, and its keys are rewritten to match.  The result is the
-// order a full 64-bit sort plus tie fix gives: lexicographic in (Morton code,
-// path hash, terminal).
+// in input order.  Each such run is ordered here by insertion: by the whole
+// key (the Morton code and the path hash's top 34 bits), then, for equal keys,
+// by the full path hash, then by terminal index, keys and values moving
+// together.  The result is the order a full 64-bit sort plus tie fix gives:
+// lexicographic in (Morton code, path hash, terminal).  Runs are short; a
+// terminal record is read only for two equal 64-bit keys.
 constexpr int kSortLowBit = 24;  // 5 radix passes of 8 bits instead of 8
 
 __global__ void k_fix_ties(unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
@@ -128,20 +129,27 @@ __global__ void k_fix_ties(unsigned long long* __restrict__ keys, uint32_t* __re
   unsigned long long j = i + 1;
   while (j < n && (keys[j] >> kSortLowBit) == k) j++;
   for (unsigned long long a = i + 1; a < j; a++) {
-    uint32_t v = vals[a];
-    uint64_t pv = term_path(t, v);
+    const unsigned long long kv = keys[a];
+    const uint32_t v = vals[a];
     unsigned long long b = a;
     while (b > i) {
-      uint32_t u = vals[b - 1];
-      uint64_t pu = term_path(t, u);
-      if (pu < pv || (pu == pv && u < v)) break;
+      const unsigned long long ku = keys[b - 1];
+      const uint32_t u = vals[b - 1];
+      bool first;  // does (ku, u) stay before (kv, v)?
+      if (ku != kv) {
+        first = ku < kv;
+      } else {
+        const uint64_t pu = term_path(t, u), pv = term_path(t, v);
+        first = pu < pv || (pu == pv && u < v);
+      }
+      if (first) break;
+      keys[b] = ku;
       vals[b] = u;
       b--;
     }
+    keys[b] = kv;
     vals[b] = v;
   }
-  const unsigned long long morton = (keys[i] >> 34) << 34;
-  for (unsigned long long a = i; a < j; a++) keys[a] = morton | (term_path(t, vals[a]) >> 30);
 }
 
 __device__ __forceinline__ unsigned long long karras_code(const unsigned long long* keys, long long j) {
