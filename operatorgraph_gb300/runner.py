@@ -2,10 +2,13 @@
 test_runner app, src/test_runner/TestRunnerApp.cpp:303-345: derive a scene a
 number of times and log timings).
 
-    python -m operatorgraph_gb300.runner --scene city --runs 5 [--plain] [--lbvh]
+    python -m operatorgraph_gb300.runner --scene city --runs 5 [--plain] [--lbvh] [--step]
 
 Prints one JSON line: terminals, per-run milliseconds (CUDA events) and the
-device report of the last run.
+device report of the last run.  --step runs the differentiable step after
+each derivation (made with the tape recorded): the LBVH over the device-side
+terminal count, dL/dM = M for L = |M|^2 / 2, and the adjoint to the block
+parameters and axiom sizes, each part timed.
 """
 import argparse
 import json
@@ -24,7 +27,7 @@ def make_scene(name, n):
     if name == "facades":
         return scenes.facades(n or 1024), (-1.0, -1.0, -1.0, 70.0, 2.0, 70.0)
     if name == "mixed":
-        return scenes.mixed(n or 65536), (-50.0, -50.0, -1.0, 13000.0, 13000.0, 400.0)
+        return scenes.mixed(n or 65536), (-50.0, -50.0, -110.0, 13000.0, 13000.0, 400.0)
     raise SystemExit(f"unknown scene {name}")
 
 
@@ -39,6 +42,8 @@ def main(argv=None):
     ap.add_argument("--runs", type=int, default=3)
     ap.add_argument("--plain", action="store_true", help="plain one-grammar-per-launch form")
     ap.add_argument("--lbvh", action="store_true", help="also build the LBVH after each derivation")
+    ap.add_argument("--step", action="store_true",
+                    help="differentiable step: tape, LBVH over the device count, dL/dM = M, adjoint")
     ap.add_argument("--capacity", type=int, default=0)
     ap.add_argument("--nodes", type=int, default=1 << 22)
     ap.add_argument("--sub-item", type=int, default=0, help="children per work item (engine default 8)")
@@ -52,14 +57,21 @@ def main(argv=None):
     cap = args.capacity or 8_000_000
     eng = Engine(b["entries"], node_capacity=args.nodes, max_terminals=cap, block_stride=b["block_stride"],
                  sub_item=args.sub_item, items_per_lane=args.items_per_lane, blocks_per_sm=args.blocks_per_sm,
-                 narrow_sub_item=args.narrow_sub_item)
+                 narrow_sub_item=args.narrow_sub_item, record_tape=args.step)
     dev = torch.device("cuda", torch.cuda.current_device())
     d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).to(dev)
     d_blk = None if b["blocks"] is None else torch.from_numpy(np.asarray(b["blocks"], np.float32)).to(dev)
     out = torch.empty((cap, 64), dtype=torch.uint8, device=dev)
     count = torch.zeros(1, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
-    times, lb = [], []
+    n_ax = len(b["axioms"])
+    if args.step:
+        g_term = torch.empty((cap, 12), dtype=torch.float32, device=dev)
+        g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
+        g_blk = None if d_blk is None else torch.empty_like(d_blk)
+        n_blk = 0 if d_blk is None else d_blk.numel() // max(b["block_stride"], 1)
+        m_rows = out.view(torch.float32).view(cap, 16)
+    times, lb, steps = [], [], []
     for _ in range(args.runs):
         a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
@@ -75,6 +87,19 @@ def main(argv=None):
             z.record(stream)
             torch.cuda.synchronize()
             lb.append(a.elapsed_time(z))
+        if args.step:
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record(stream)
+            eng.lbvh(out, cap, bounds, stream=stream, count=count)
+            ev[1].record(stream)
+            g_term.copy_(m_rows[:, :12])
+            ev[2].record(stream)
+            eng.adjoint_raw(g_term.data_ptr(), None if g_blk is None else g_blk.data_ptr(), n_blk, g_sz.data_ptr(),
+                            stream=stream)
+            ev[3].record(stream)
+            torch.cuda.synchronize()
+            steps.append({"lbvh_ms": ev[0].elapsed_time(ev[1]), "loss_grad_ms": ev[1].elapsed_time(ev[2]),
+                          "adjoint_ms": ev[2].elapsed_time(ev[3])})
     rep = eng.report()
     lv = {}
     if not args.plain:
@@ -90,6 +115,8 @@ def main(argv=None):
            "ms": times, "ms_median": statistics.median(times), "report": rep, **lv}
     if lb:
         res["lbvh_ms"] = lb
+    if steps:
+        res["step"] = steps
     print(json.dumps(res))
     eng.release()
 
