@@ -417,8 +417,8 @@ def mixed_step(mx, mout, count, dev, n_expected):
     count read on the device, pga_lbvh_build_counted), dL/dM = M for the loss
     L = |M|^2 / 2 (a torch copy over the output's capacity), and the adjoint
     to the 65,536 axiom sizes (the batch's grammars take constant parameters,
-    so the sizes are its continuous inputs).  The four parts are also timed
-    one by one, eagerly."""
+    so the sizes are its continuous inputs), the axioms seeded grouped by root
+    entry.  The four parts are also timed one by one, eagerly."""
     import torch
 
     from operatorgraph_gb300.engine import Engine
@@ -426,7 +426,7 @@ def mixed_step(mx, mout, count, dev, n_expected):
     res = {}
     n_ax = len(mx["axioms"])
     mcap = mout.shape[0]
-    et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True)
+    et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True, group_axioms=True)
     d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
     g_term = torch.empty((mcap, 12), dtype=torch.float32, device=dev)
     g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
@@ -620,27 +620,32 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     del out
     # The mixed batch: 65,536 axioms (40 % Menger depth 1-3, 40 % city
     # buildings, 20 % random grammars), about 152M terminals in one launch.
+    # The axioms are interleaved by kind; the engine seeds them grouped by root
+    # entry (PGA_FLAG_GROUP_AXIOMS).  The index-order time is kept beside it.
     mx = scenes.mixed(65536)
     mcap = 160_000_000
-    em = Engine(mx["entries"], node_capacity=1 << 27, max_terminals=mcap)
     d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
     mout = torch.empty((mcap, 64), dtype=torch.uint8, device=dev)
-    ts = []
-    for it in range(6):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        em.derive_raw(d_mx.data_ptr(), 65536, None, mout.data_ptr(), mcap, count.data_ptr())
-        b.record(stream)
-        torch.cuda.synchronize()
-        if it >= 2:
-            ts.append(a.elapsed_time(b))
-    rep = em.report()
-    assert rep["status"] == 0, rep
+    for group in (False, True):
+        em = Engine(mx["entries"], node_capacity=1 << 27, max_terminals=mcap, group_axioms=group)
+        ts = []
+        for it in range(6):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            em.derive_raw(d_mx.data_ptr(), 65536, None, mout.data_ptr(), mcap, count.data_ptr())
+            b.record(stream)
+            torch.cuda.synchronize()
+            if it >= 2:
+                ts.append(a.elapsed_time(b))
+        rep = em.report()
+        assert rep["status"] == 0, rep
+        em.release()
+        if not group:
+            res["mixed65536_index_order_ms"] = statistics.median(ts)
     n_mx = int(count.item())
     res["mixed65536_terminals"] = n_mx
     res["mixed65536_ms"] = statistics.median(ts)
     res["mixed65536_terminals_per_s"] = n_mx / (res["mixed65536_ms"] * 1e-3)
-    em.release()
     res.update(mixed_step(mx, mout, count, dev, n_mx))
     del mout
     # Forest: 4096 trees (Rotate with arbitrary angles, Replicate, Translate,

@@ -141,6 +141,13 @@ typedef struct PgaTerminal {
  * at once) instead of being queued as a work item; engines with recordTape = 1
  * never do this.  PGA_FLAG_NO_INLINE turns it off. */
 #define PGA_FLAG_NO_INLINE 1u
+/* pga_derive seeds the axioms grouped by root entry (a counting sort on the
+ * device before the launch) instead of in index order, so that warps expand
+ * shapes of one grammar together, level after level.  Results are the same
+ * records (each axiom keeps its index, hence its path hashes and parameter
+ * block); only their order in the output changes.  For batches that mix
+ * grammars; pga_derive_to_host ignores it.  No reference counterpart. */
+#define PGA_FLAG_GROUP_AXIOMS 2u
 
 typedef struct PgaEngineConfig {
   uint64_t nodeCapacity;     /* non-terminal shapes held per derivation (queue storage) */

@@ -66,6 +66,7 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.axioms = axioms;
   a.numAxioms = numAxioms;
   a.axiomBase = 0;
+  a.axiomOrder = nullptr;
   a.blocks = blocks;
   a.blockStride = e->cfg.blockStride;
   a.out = out;
@@ -215,7 +216,7 @@ static void free_engine(PgaEngine* e) {
                   e->dTail, e->dTailLinks, e->dScratch,
                   e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA,
                   e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dLeafAabbSorted, e->dNodeRange, e->dNodeGrad, e->dChildKey, e->dPageNext,
-                  e->dSlots, e->dBlockSums};
+                  e->dSlots, e->dBlockSums, e->dGroupCount};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (e->dStageAxioms) cudaFree(e->dStageAxioms);
@@ -450,6 +451,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   ALLOC(e->dLevelStart, (c.maxLevels + 2) * sizeof(unsigned long long));
   ALLOC(e->dLevelClock, (c.maxLevels + 2) * sizeof(unsigned long long));
   ALLOC(e->dScratchCount, sizeof(unsigned long long));
+  ALLOC(e->dGroupCount, (e->hRules.size() + 1) * sizeof(uint32_t));
   if (c.recordTape) {
     // The reverse pass tags work-item indices with bit 31 and counts child
     // slots in 32 bits; a work item has at most max(subItem, narrowSubItem)
@@ -541,12 +543,92 @@ PgaStatus pga_engine_destroy(PgaEngine* e) {
 // One persistent launch over axioms [first, end) of dAxioms (path hashes are
 // seeded from the absolute axiom index, so a batch derived in ranges gives the
 // same terminals as one launch).
+// Axiom grouping (PGA_FLAG_GROUP_AXIOMS): a counting sort of the axiom indices
+// by root entry -- count, one-block exclusive scan, scatter -- with one atomic
+// per warp and entry (a batch may hold tens of thousands of axioms of one
+// entry).  Entries out of range share the last bucket; the seed reports them.
+__device__ __forceinline__ uint32_t group_bucket(const PgaAxiom* ax, uint32_t i, uint32_t numEntries) {
+  const uint32_t e = __ldg(&ax[i].entry);
+  return e < numEntries ? e : numEntries;
+}
+
+__global__ void k_group_count(const PgaAxiom* ax, uint32_t n, uint32_t numEntries, uint32_t* count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t e = i < n ? group_bucket(ax, i, numEntries) : 0xFFFFFFFFu;
+  const unsigned same = __match_any_sync(0xFFFFFFFFu, e);
+  if (i < n && (threadIdx.x & 31u) == (uint32_t)(__ffs(same) - 1)) atomicAdd(count + e, (uint32_t)__popc(same));
+}
+
+__global__ void k_group_scan(uint32_t* count, uint32_t buckets) {
+  __shared__ uint32_t warpSum[32];
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (uint32_t t0 = 0; t0 < buckets; t0 += blockDim.x) {
+    const uint32_t k = t0 + threadIdx.x;
+    const uint32_t v = k < buckets ? count[k] : 0u;
+    uint32_t x = v;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= (unsigned)d) x += y;
+    }
+    if (lane == 31) warpSum[warp] = x;
+    __syncthreads();
+    uint32_t before = carry, total = 0;
+    for (uint32_t w = 0; w < (blockDim.x >> 5); w++) {
+      before += w < warp ? warpSum[w] : 0u;
+      total += warpSum[w];
+    }
+    if (k < buckets) count[k] = before + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += total;
+    __syncthreads();
+  }
+}
+
+__global__ void k_group_scatter(const PgaAxiom* ax, uint32_t n, uint32_t numEntries, uint32_t* offset,
+                                uint32_t* order) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t e = i < n ? group_bucket(ax, i, numEntries) : 0xFFFFFFFFu;
+  const unsigned same = __match_any_sync(0xFFFFFFFFu, e);
+  const uint32_t leader = (uint32_t)(__ffs(same) - 1);
+  uint32_t base = 0;
+  if (i < n && (threadIdx.x & 31u) == leader) base = atomicAdd(offset + e, (uint32_t)__popc(same));
+  base = __shfl_sync(0xFFFFFFFFu, base, leader);
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  if (i < n) order[base + __popc(same & lt)] = i;
+}
+
+// The seed order of a pga_derive over n axioms: null (index order) unless the
+// engine groups axioms; the order lives in the LBVH key scratch, idle during
+// a derivation (up to 2 maxTerminals axioms; larger batches keep index order).
+static PgaStatus group_axioms(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t n, cudaStream_t s,
+                              const uint32_t** order) {
+  *order = nullptr;
+  if (!(e->cfg.flags & PGA_FLAG_GROUP_AXIOMS) || n < 2 || (uint64_t)n > 2 * e->cfg.maxTerminals) return PGA_OK;
+  const uint32_t numEntries = (uint32_t)e->hRules.size();
+  uint32_t* out = reinterpret_cast<uint32_t*>(e->dKeysA);
+  PGA_CUDA_TRY(cudaMemsetAsync(e->dGroupCount, 0, (numEntries + 1) * sizeof(uint32_t), s));
+  const unsigned blocks = (n + 255) / 256;
+  k_group_count<<<blocks, 256, 0, s>>>(dAxioms, n, numEntries, e->dGroupCount);
+  PGA_CUDA_TRY(cudaGetLastError());
+  k_group_scan<<<1, 1024, 0, s>>>(e->dGroupCount, numEntries + 1);
+  PGA_CUDA_TRY(cudaGetLastError());
+  k_group_scatter<<<blocks, 256, 0, s>>>(dAxioms, n, numEntries, e->dGroupCount, out);
+  PGA_CUDA_TRY(cudaGetLastError());
+  *order = out;
+  return PGA_OK;
+}
+
 static PgaStatus launch_persistent(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t first, uint32_t end,
                                    const float* dParamBlocks, PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount,
-                                   cudaStream_t s) {
+                                   cudaStream_t s, const uint32_t* order = nullptr) {
   PGA_CUDA_TRY(cudaMemsetAsync(e->dState, 0, sizeof(DevState), s));
   DeriveArgs a = make_args(e, dAxioms, end, dParamBlocks, dOut, capacity, (unsigned long long*)dCount);
   a.axiomBase = first;
+  a.axiomOrder = order;
   void* args[] = {&a};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)e->persistentBlocks);
@@ -688,7 +770,10 @@ PgaStatus pga_derive(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, 
     return PGA_ERR_INVALID_ARGUMENT;
   }
   if (e->phased) return derive_phases(e, dAxioms, numAxioms, dParamBlocks, dOut, capacity, dCount, (cudaStream_t)stream);
-  return launch_persistent(e, dAxioms, 0, numAxioms, dParamBlocks, dOut, capacity, dCount, (cudaStream_t)stream);
+  const uint32_t* order = nullptr;
+  const PgaStatus st = group_axioms(e, dAxioms, numAxioms, (cudaStream_t)stream, &order);
+  if (st != PGA_OK) return st;
+  return launch_persistent(e, dAxioms, 0, numAxioms, dParamBlocks, dOut, capacity, dCount, (cudaStream_t)stream, order);
 }
 
 // Grows an engine-owned device buffer (kept until the engine is destroyed).

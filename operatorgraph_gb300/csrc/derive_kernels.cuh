@@ -1199,7 +1199,8 @@ __device__ __forceinline__ void warp_items(const DeriveArgs& a, WarpOut& w, unsi
   }
 }
 
-// Seeds the axioms [first, first + count) with a warp-uniform grid-stride loop.
+// Seeds the axioms [first, first + count) with a warp-uniform grid-stride loop
+// (the i-th seeded is axiomOrder[i] when an order is given).
 template <bool PAGED, bool LEAF, int AFF>
 __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uint32_t count) {
   const unsigned lane = threadIdx.x & 31u;
@@ -1210,12 +1211,13 @@ __device__ void seed_axioms(const DeriveArgs& a, WarpOut& w, uint32_t first, uin
     const unsigned long long i = b + lane;
     int kind = kNone;
     Shape y;
-    uint32_t tidx = 0;
+    uint32_t tidx = 0, ax = (uint32_t)i;
     if (i < end) {
-      axiom_shape(a, (uint32_t)i, y);
+      if (a.axiomOrder != nullptr) ax = __ldg(a.axiomOrder + i);
+      axiom_shape(a, ax, y);
       kind = resolve<AFF>(a, y, tidx);
     }
-    emit_new<PAGED, LEAF>(a, w, kind, y, tidx, kAxiomLink | (uint32_t)i, 0u);
+    emit_new<PAGED, LEAF>(a, w, kind, y, tidx, kAxiomLink | ax, 0u);
   }
 }
 

@@ -110,6 +110,7 @@ struct DeriveArgs {
   const PgaAxiom* axioms;
   uint32_t numAxioms;
   uint32_t axiomBase;        // plain form: index of the first axiom of this launch
+  const uint32_t* axiomOrder;  // seed order: axiomOrder[i] is the i-th axiom seeded (null: index order)
   const float* blocks;
   uint32_t blockStride;
   PgaTerminal* out;

@@ -80,6 +80,10 @@ struct PgaEngine {
   unsigned long long* dBlockSums = nullptr;
   unsigned long long slotCap = 0;
 
+  // PGA_FLAG_GROUP_AXIOMS: per root entry (and one bucket for entries out of
+  // range) its axiom count, then its next free place in the seed order.
+  uint32_t* dGroupCount = nullptr;
+
   // Last pga_derive, for pga_adjoint.
   const PgaAxiom* lastAxioms = nullptr;
   uint32_t lastNumAxioms = 0;

@@ -51,13 +51,14 @@ def main(argv=None):
     ap.add_argument("--narrow-sub-item", type=int, default=0,
                     help="children per work item queued from levels narrower than the grid (default subItem)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="cap on resident blocks per SM (0: occupancy)")
+    ap.add_argument("--group", action="store_true", help="seed the axioms grouped by root entry")
     args = ap.parse_args(argv)
 
     b, bounds = make_scene(args.scene, args.n)
     cap = args.capacity or 8_000_000
     eng = Engine(b["entries"], node_capacity=args.nodes, max_terminals=cap, block_stride=b["block_stride"],
                  sub_item=args.sub_item, items_per_lane=args.items_per_lane, blocks_per_sm=args.blocks_per_sm,
-                 narrow_sub_item=args.narrow_sub_item, record_tape=args.step)
+                 narrow_sub_item=args.narrow_sub_item, record_tape=args.step, group_axioms=args.group)
     dev = torch.device("cuda", torch.cuda.current_device())
     d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).to(dev)
     d_blk = None if b["blocks"] is None else torch.from_numpy(np.asarray(b["blocks"], np.float32)).to(dev)

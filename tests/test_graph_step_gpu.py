@@ -211,3 +211,30 @@ def test_derive_lbvh_adjoint_in_one_graph():
         _close(got["gSizes"], want["gSizes"], "size gradients")
     assert step.eng.report()["status"] == 0
     step.eng.release()
+
+
+def test_adjoint_with_grouped_axioms_matches_index_order():
+    """The adjoint after a PGA_FLAG_GROUP_AXIOMS derivation (a mixed batch of
+    Menger, buildings and random grammars): the same axiom-size gradients as
+    after the index-order derivation, to FP32 accumulation order.  The loss is
+    L = |M|^2 / 2, so dL/dM = M for whatever order the records come in."""
+    from operatorgraph_gb300.engine import Engine
+
+    b = scenes.mixed(512)
+    grads = []
+    for group in (False, True):
+        eng = Engine(b["entries"], node_capacity=1 << 21, max_terminals=2_000_000, record_tape=True,
+                     group_axioms=group)
+        d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).cuda()
+        out = torch.zeros((2_000_000, 64), dtype=torch.uint8, device="cuda")
+        count = torch.zeros(1, dtype=torch.int64, device="cuda")
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None, out.data_ptr(), out.shape[0], count.data_ptr())
+        g_term = out.view(torch.float32).view(-1, 16)[:, :12].contiguous()
+        g_sz = torch.zeros((len(b["axioms"]), 3), dtype=torch.float32, device="cuda")
+        eng.adjoint_raw(g_term.data_ptr(), None, 0, g_sz.data_ptr())
+        torch.cuda.synchronize()
+        assert eng.report()["status"] == 0
+        grads.append(g_sz.cpu().numpy().astype(np.float64))
+        eng.release()
+    assert np.abs(grads[0]).max() > 0
+    _close(grads[1], grads[0], "axiom-size gradients")
