@@ -414,11 +414,12 @@ def our_arm(args):
 def mixed_step(mx, mout, count, dev, n_expected):
     """The mixed batch as one differentiable step captured in one CUDA graph:
     derivation with the tape recorded, LBVH over all its terminals (the leaf
-    count read on the device, pga_lbvh_build_counted), dL/dM = M for the loss
-    L = |M|^2 / 2 (a torch copy over the output's capacity), and the adjoint
-    to the 65,536 axiom sizes (the batch's grammars take constant parameters,
-    so the sizes are its continuous inputs), the axioms seeded grouped by root
-    entry.  The four parts are also timed one by one, eagerly."""
+    count read on the device, pga_lbvh_build_counted), and the adjoint to the
+    65,536 axiom sizes for the loss L = |M|^2 / 2, whose dL/dM = M the adjoint
+    reads in place from the terminal records (pga_adjoint_strided, stride 16
+    floats).  The batch's grammars take constant parameters, so the sizes are
+    its continuous inputs; the axioms are seeded grouped by root entry.  The
+    parts are also timed one by one, eagerly."""
     import torch
 
     from operatorgraph_gb300.engine import Engine
@@ -428,7 +429,6 @@ def mixed_step(mx, mout, count, dev, n_expected):
     mcap = mout.shape[0]
     et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True, group_axioms=True)
     d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
-    g_term = torch.empty((mcap, 12), dtype=torch.float32, device=dev)
     g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
     m_rows = mout.view(torch.float32).view(mcap, 16)
     # LBVH bounds: the box of the terminal centres of a first derivation, one
@@ -457,20 +457,18 @@ def mixed_step(mx, mout, count, dev, n_expected):
         mark(1)
         bv = et.lbvh(mout, mcap, bounds, stream=st, count=count)
         mark(2)
-        g_term.copy_(m_rows[:, :12])
+        et.adjoint_raw(mout.data_ptr(), None, 0, g_sz.data_ptr(), stream=st, grad_stride=16)
         mark(3)
-        et.adjoint_raw(g_term.data_ptr(), None, 0, g_sz.data_ptr(), stream=st)
-        mark(4)
         return bv
 
     seg = []
     with torch.cuda.stream(s):
         for it in range(5):
-            marks = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+            marks = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
             bv = step(s, marks)
             s.synchronize()
             if it >= 2:
-                seg.append([marks[k].elapsed_time(marks[k + 1]) for k in range(4)])
+                seg.append([marks[k].elapsed_time(marks[k + 1]) for k in range(3)])
     torch.cuda.current_stream().wait_stream(s)
     torch.cuda.synchronize()
     rep = et.report()
@@ -495,15 +493,14 @@ def mixed_step(mx, mout, count, dev, n_expected):
     assert rep["status"] == 0, rep
     assert int(count.item()) == n
     assert bool(torch.isfinite(g_sz).all()) and float(g_sz.abs().max()) > 0
-    names = ("derive_tape", "lbvh", "loss_grad", "adjoint")
-    med = [statistics.median(x[k] for x in seg) for k in range(4)]
+    names = ("derive_tape", "lbvh", "adjoint")
+    med = [statistics.median(x[k] for x in seg) for k in range(3)]
     # Algorithmic bytes: derivation 64 B per terminal, its 8-B tape link and
     # 48 B per axiom; LBVH 236 B per leaf (the 64-B record read, 52 B of tree
     # written, five radix passes over 12-B key/value pairs read and written);
-    # the loss gradient 48 B read and 48 B written per output slot; adjoint as
-    # for the facades (per terminal 48 + 8 B, per item 2 x 64 + 2 x 24 B, 12 B
-    # per axiom size).
-    parts = [72.0 * n + 48.0 * n_ax, 236.0 * n, 96.0 * mcap, 56.0 * n + 176.0 * n_items + 12.0 * n_ax]
+    # adjoint as for the facades (per terminal 48 + 8 B, per item 2 x 64 + 2 x
+    # 24 B, 12 B per axiom size).
+    parts = [72.0 * n + 48.0 * n_ax, 236.0 * n, 56.0 * n + 176.0 * n_items + 12.0 * n_ax]
     peak, _ = read_peaks()
     step_ms = statistics.median(ts)
     res["mixed65536_step_graph_ms"] = step_ms

@@ -336,6 +336,13 @@ PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const
 PgaStatus pga_adjoint(PgaEngine* engine, const float* dGradTerminals, float* dGradParams,
                       uint32_t numBlocks, float* dGradAxiomSizes, void* stream);
 
+/* pga_adjoint with dL/dm of terminal t at dGradTerminals[t * gradStride + 0..11]
+ * (gradStride >= 12 floats): a gradient kept inside a larger per-terminal
+ * record -- for L = |m|^2 / 2, the terminal records themselves, stride 16.
+ * pga_adjoint is this call with stride 12.  No reference counterpart. */
+PgaStatus pga_adjoint_strided(PgaEngine* engine, const float* dGradTerminals, uint32_t gradStride,
+                              float* dGradParams, uint32_t numBlocks, float* dGradAxiomSizes, void* stream);
+
 /* One vertex of a generated triangle mesh: the layout of
  * PGA::Rendering::TriangleMeshData::VertexAttributes (16-byte aligned
  * position, normal and uv; include/pga/rendering/TriangleMeshData.h:10-18). */

@@ -41,7 +41,8 @@ __device__ __forceinline__ void grad_zero(Grad& g) {
 }
 
 struct AdjArgs {
-  const float* gradTerminals;  // 12 per terminal
+  const float* gradTerminals;  // dL/dm of terminal t: gradTerminals[t * gradStride + 0..11]
+  uint32_t gradStride;         // floats, >= 12
   float* gradParams;           // numBlocks * blockStride
   uint32_t numBlocks;
   float* gradSizes;            // 3 per axiom
@@ -498,7 +499,7 @@ __device__ void chain_vjp(const DeriveArgs& a, const AdjArgs& j, const Chain& ch
 // dL/d(state) of a Generate rule's shape y from dL/dM of its terminal t:
 // M[:, k] = R[:, k] s_k and M[:, 3] = t.
 __device__ __forceinline__ Grad terminal_grad(const AdjArgs& j, unsigned long long t, const Shape& y) {
-  const float* gm = j.gradTerminals + t * 12;
+  const float* gm = j.gradTerminals + t * j.gradStride;
   Grad g;
 #pragma unroll
   for (int q = 0; q < 3; q++) {
@@ -603,7 +604,7 @@ __device__ void adj_page(const DeriveArgs& a, const AdjArgs& j, unsigned long lo
       if (sv[q] & kItemTag) {
         prefetch_l2(j.nodeGrad + (size_t)(sv[q] & ~kItemTag) * 6);
       } else {
-        const float* gm = j.gradTerminals + (size_t)sv[q] * 12;
+        const float* gm = j.gradTerminals + (size_t)sv[q] * j.gradStride;
         prefetch_l2(gm);
         prefetch_l2(gm + 11);
       }
@@ -837,11 +838,16 @@ __global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, u
 
 }  // namespace pga
 
-extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, float* dGradParams, uint32_t numBlocks,
-                                 float* dGradAxiomSizes, void* stream) {
+extern "C" PgaStatus pga_adjoint_strided(PgaEngine* e, const float* dGradTerminals, uint32_t gradStride,
+                                         float* dGradParams, uint32_t numBlocks, float* dGradAxiomSizes,
+                                         void* stream) {
   using namespace pga;
   if (!e || !dGradTerminals) {
     set_error("pga_adjoint: null engine or gradient");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  if (gradStride < 12) {
+    set_error("pga_adjoint_strided: gradStride must be at least 12 floats");
     return PGA_ERR_INVALID_ARGUMENT;
   }
   if (!e->cfg.recordTape || !e->lastWasBatched || !e->dTermLinks || !e->lastOut) {
@@ -863,6 +869,7 @@ extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, floa
   DeriveArgs a = make_args(e, e->lastAxioms, e->lastNumAxioms, e->lastBlocks, e->lastOut, e->lastCap, nullptr);
   AdjArgs j;
   j.gradTerminals = dGradTerminals;
+  j.gradStride = gradStride;
   j.gradParams = dGradParams;
   j.numBlocks = numBlocks;
   j.gradSizes = dGradAxiomSizes;
@@ -887,4 +894,9 @@ extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, floa
   cfg.numAttrs = 1;
   PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, (const void*)k_adjoint, args));
   return PGA_OK;
+}
+
+extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, float* dGradParams, uint32_t numBlocks,
+                                 float* dGradAxiomSizes, void* stream) {
+  return pga_adjoint_strided(e, dGradTerminals, 12u, dGradParams, numBlocks, dGradAxiomSizes, stream);
 }

@@ -26,7 +26,8 @@ STATUS = {
 # Every symbol include/pga_gb300.h declares.
 EXPORTS = ["pga_version", "pga_last_error", "pga_default_procs", "pga_engine_create", "pga_engine_destroy",
            "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_engine_levels", "pga_lbvh_build",
-           "pga_lbvh_build_counted", "pga_lbvh_build_static", "pga_adjoint", "pga_derive_to_host", "pga_generate_meshes"]
+           "pga_lbvh_build_counted", "pga_lbvh_build_static", "pga_adjoint", "pga_adjoint_strided",
+           "pga_derive_to_host", "pga_generate_meshes"]
 
 
 class PgaError(RuntimeError):
@@ -96,6 +97,7 @@ def load_library(path=LIB_PATH):
     L.pga_lbvh_build.argtypes = [vp, vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
     L.pga_lbvh_build_counted.argtypes = [vp, vp, vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
     L.pga_adjoint.argtypes = [vp, vp, vp, u32, vp, vp]
+    L.pga_adjoint_strided.argtypes = [vp, vp, u32, vp, u32, vp, vp]
     L.pga_engine_levels.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(u32)]
     L.pga_lbvh_build_static.argtypes = [vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
     L.pga_derive_to_host.argtypes = [vp, vp, u32, vp, vp, u64, ctypes.POINTER(u64), vp]
@@ -279,10 +281,16 @@ class Engine:
             out.append((v[:nv], i[:ni], nv, ni))
         return out
 
-    def adjoint_raw(self, d_grad_terminals, d_grad_params, num_blocks, d_grad_sizes, stream=None):
+    def adjoint_raw(self, d_grad_terminals, d_grad_params, num_blocks, d_grad_sizes, stream=None, grad_stride=12):
+        """pga_adjoint (grad_stride 12) or pga_adjoint_strided: dL/dm of terminal t at
+        d_grad_terminals + t * grad_stride floats."""
         L = load_library()
-        _check(L.pga_adjoint(self.handle, d_grad_terminals, d_grad_params, num_blocks, d_grad_sizes,
-                             _stream_handle(stream)), "pga_adjoint")
+        if grad_stride == 12:
+            _check(L.pga_adjoint(self.handle, d_grad_terminals, d_grad_params, num_blocks, d_grad_sizes,
+                                 _stream_handle(stream)), "pga_adjoint")
+        else:
+            _check(L.pga_adjoint_strided(self.handle, d_grad_terminals, grad_stride, d_grad_params, num_blocks,
+                                         d_grad_sizes, _stream_handle(stream)), "pga_adjoint_strided")
 
     def release(self):
         if getattr(self, "handle", None):

@@ -7,8 +7,9 @@ number of times and log timings).
 Prints one JSON line: terminals, per-run milliseconds (CUDA events) and the
 device report of the last run.  --step runs the differentiable step after
 each derivation (made with the tape recorded): the LBVH over the device-side
-terminal count, dL/dM = M for L = |M|^2 / 2, and the adjoint to the block
-parameters and axiom sizes, each part timed.
+terminal count, then the adjoint to the block parameters and axiom sizes for
+L = |M|^2 / 2, reading dL/dM = M in place from the terminal records
+(pga_adjoint_strided, stride 16 floats), each part timed.
 """
 import argparse
 import json
@@ -67,11 +68,9 @@ def main(argv=None):
     stream = torch.cuda.current_stream()
     n_ax = len(b["axioms"])
     if args.step:
-        g_term = torch.empty((cap, 12), dtype=torch.float32, device=dev)
         g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
         g_blk = None if d_blk is None else torch.empty_like(d_blk)
         n_blk = 0 if d_blk is None else d_blk.numel() // max(b["block_stride"], 1)
-        m_rows = out.view(torch.float32).view(cap, 16)
     times, lb, steps = [], [], []
     for _ in range(args.runs):
         a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -89,18 +88,15 @@ def main(argv=None):
             torch.cuda.synchronize()
             lb.append(a.elapsed_time(z))
         if args.step:
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
             ev[0].record(stream)
             eng.lbvh(out, cap, bounds, stream=stream, count=count)
             ev[1].record(stream)
-            g_term.copy_(m_rows[:, :12])
+            eng.adjoint_raw(out.data_ptr(), None if g_blk is None else g_blk.data_ptr(), n_blk, g_sz.data_ptr(),
+                            stream=stream, grad_stride=16)
             ev[2].record(stream)
-            eng.adjoint_raw(g_term.data_ptr(), None if g_blk is None else g_blk.data_ptr(), n_blk, g_sz.data_ptr(),
-                            stream=stream)
-            ev[3].record(stream)
             torch.cuda.synchronize()
-            steps.append({"lbvh_ms": ev[0].elapsed_time(ev[1]), "loss_grad_ms": ev[1].elapsed_time(ev[2]),
-                          "adjoint_ms": ev[2].elapsed_time(ev[3])})
+            steps.append({"lbvh_ms": ev[0].elapsed_time(ev[1]), "adjoint_ms": ev[1].elapsed_time(ev[2])})
     rep = eng.report()
     lv = {}
     if not args.plain:

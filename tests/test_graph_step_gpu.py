@@ -238,3 +238,33 @@ def test_adjoint_with_grouped_axioms_matches_index_order():
         eng.release()
     assert np.abs(grads[0]).max() > 0
     _close(grads[1], grads[0], "axiom-size gradients")
+
+
+def test_strided_gradient_read_in_place_matches_a_copy():
+    """pga_adjoint_strided reading dL/dM = M straight from the 16-float terminal
+    records gives the gradients of pga_adjoint on a 12-float copy; a stride
+    below 12 is rejected."""
+    from operatorgraph_gb300.engine import load_library
+
+    b = scenes.facades(64)
+    eng = _engine(b, record_tape=True, node_capacity=1 << 20, max_terminals=1 << 20)
+    d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).cuda()
+    d_blk = torch.from_numpy(b["blocks"]).cuda()
+    out = torch.zeros((1 << 20, 64), dtype=torch.uint8, device="cuda")
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    eng.derive_raw(d_ax.data_ptr(), 64, d_blk.data_ptr(), out.data_ptr(), out.shape[0], count.data_ptr())
+    rows = out.view(torch.float32).view(-1, 16)
+    res = []
+    for stride in (12, 16):
+        g_term = rows[:, :12].contiguous() if stride == 12 else rows
+        g_blk = torch.zeros_like(d_blk)
+        g_sz = torch.zeros((64, 3), dtype=torch.float32, device="cuda")
+        eng.adjoint_raw(g_term.data_ptr(), g_blk.data_ptr(), 64, g_sz.data_ptr(), grad_stride=stride)
+        torch.cuda.synchronize()
+        assert eng.report()["status"] == 0
+        res.append((g_blk.cpu().numpy().astype(np.float64), g_sz.cpu().numpy().astype(np.float64)))
+    assert np.abs(res[0][0]).max() > 0
+    _close(res[1][0], res[0][0], "block gradients")
+    _close(res[1][1], res[0][1], "size gradients")
+    assert load_library().pga_adjoint_strided(eng.handle, rows.data_ptr(), 11, None, 0, None, None) != 0
+    eng.release()
