@@ -574,6 +574,18 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     assert int(count.item()) == 3_200_000
     res["menger_d5_ms"] = statistics.median(ts)
     res["menger_d5_terminals_per_s"] = 3.2e6 / (res["menger_d5_ms"] * 1e-3)
+    # Its LBVH over all 3.2M terminals (30-bit Morton codes on the unit-cube bounds).
+    ts = []
+    for it in range(6):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        em.lbvh(out, 3_200_000, (-0.5, -0.5, -0.5, 0.5, 0.5, 0.5), stream=stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if it >= 2:
+            ts.append(a.elapsed_time(b))
+    res["lbvh_menger_d5_ms"] = statistics.median(ts)
+    res["menger_d5_with_lbvh_ms"] = res["menger_d5_ms"] + res["lbvh_menger_d5_ms"]
     em.release()
     # Facades (1024 axioms x 16 block parameters, 393,216 terminals): derivation
     # with the tape recorded, then the adjoint to the block parameters and sizes.

@@ -825,6 +825,7 @@ __global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, u
   if (!grid_barrier(a, [] {})) return;
   for (int L = (int)levels; L >= 0; L--) {
     const unsigned long long lv = a.levelStart[L], hv = min(a.levelStart[L + 1], nodes);
+    if (lv >= hv) continue;  // every block reads the same bounds, so all skip the barrier alike
     for (unsigned long long i = lv + tid; i < hv; i += stride) {
       if (i + stride < hv) {  // the next item's record and key, ahead of its turn
         prefetch_l2(a.nodes + i + stride);
