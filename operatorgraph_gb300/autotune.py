@@ -9,6 +9,9 @@ schedule is a handful of engine knobs, so tuning is a timed sweep at run time:
   narrowSubItem  the same for levels narrower than the grid
   itemsPerLane   work items a lane takes per warp chunk
   blocksPerSM    resident blocks per SM of the persistent launch
+  groupAxioms    rule-to-warp grouping: seed the axioms grouped by root entry
+                 (PGA_FLAG_GROUP_AXIOMS); searched only for batches whose
+                 axioms use more than one root entry
 
 Every candidate derives the batch `runs` times (CUDA events, after a warm-up);
 a candidate whose derivation reports a non-OK status (e.g. the finer splits
@@ -32,6 +35,16 @@ DEFAULT_SPACE = {
 
 # The engine's built-in defaults, as a point of the space.
 DEFAULT_CONFIG = {"sub_item": 8, "narrow_sub_item": 0, "items_per_lane": 1, "blocks_per_sm": 0}
+
+
+def space_for(batch, space=None):
+    """The search space for `batch`: `space` (default DEFAULT_SPACE), plus the
+    axiom grouping knob when the batch's axioms use more than one root entry
+    (a one-grammar batch gains nothing from it)."""
+    sp = dict(DEFAULT_SPACE if space is None else space)
+    if batch is not None and "group_axioms" not in sp and len(np.unique(np.asarray(batch["axioms"]["entry"]))) > 1:
+        sp["group_axioms"] = (False, True)
+    return sp
 
 
 def candidates(space=None):
@@ -104,7 +117,7 @@ def tune(batch, capacity, node_capacity=1 << 22, space=None, runs=5, measure_fn=
     """Times every candidate of `space` on `batch`; returns (best config, best ms, all results)."""
     measure_fn = measure_fn or (lambda cfg: measure(batch, cfg, capacity, node_capacity, runs=runs))
     results = []
-    for i, cfg in enumerate(candidates(space)):
+    for i, cfg in enumerate(candidates(space_for(batch, space))):
         ms, status = measure_fn(cfg)
         results.append({"index": i, "config": cfg, "ms": ms, "status": int(status)})
     best, ms = select(results)

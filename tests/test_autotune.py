@@ -33,6 +33,14 @@ def test_tune_picks_the_fastest_successful_candidate():
     assert len(results) == 6 and sum(r["status"] != 0 for r in results) == 2
 
 
+def test_grouping_is_searched_only_for_batches_of_several_root_entries():
+    one = A.space_for(scenes.city(16))
+    assert "group_axioms" not in one and one == A.DEFAULT_SPACE
+    mixed = A.space_for(scenes.mixed(64), {"sub_item": (4, 8)})
+    assert mixed == {"sub_item": (4, 8), "group_axioms": (False, True)}
+    assert len(A.candidates(mixed)) == 4
+
+
 def test_tune_fails_loudly_when_nothing_runs():
     with pytest.raises(RuntimeError):
         A.tune(None, 0, space={"sub_item": (8,)}, measure_fn=lambda cfg: (None, 1))
