@@ -146,7 +146,8 @@ typedef struct PgaTerminal {
  * shapes of one grammar together, level after level.  Results are the same
  * records (each axiom keeps its index, hence its path hashes and parameter
  * block); only their order in the output changes.  For batches that mix
- * grammars; pga_derive_to_host ignores it.  No reference counterpart. */
+ * grammars; pga_derive_to_host and multi-phase tables (phases, Collider,
+ * IfCollides) keep index order.  No reference counterpart. */
 #define PGA_FLAG_GROUP_AXIOMS 2u
 
 typedef struct PgaEngineConfig {
