@@ -619,7 +619,7 @@ __device__ void adj_page(const DeriveArgs& a, const AdjArgs& j, unsigned long lo
   for (uint32_t c = c0; c < c1; c++) {
     Shape y0, yEnd;
     uint32_t ord;
-    if (!expander_child(a, W, c, y0, ord)) continue;
+    if (!expander_child<1, false>(a, W, c, y0, ord)) continue;
     const uint32_t v = __ldcg(j.slots + (uint32_t)(key + ord));
     if (v == kNoRecord) continue;  // discarded
     Chain ch;

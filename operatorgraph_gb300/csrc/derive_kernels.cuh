@@ -751,7 +751,9 @@ __device__ __forceinline__ void expander_skip(const DeriveArgs& a, Expander& E, 
 
 // Produces child slot c (slots are produced in increasing order).  Returns
 // false when the slot yields no child (a zero factor of a static Subdivide).
-template <int AFF = 1>
+// PATH = false leaves y.path as the parent's (for the adjoint, which has no
+// use for path hashes).
+template <int AFF = 1, bool PATH = true>
 __device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E, uint32_t c, Shape& y,
                                                uint32_t& ordinal) {
   const Shape& x = E.base;
@@ -761,7 +763,7 @@ __device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E,
     const int32_t nxt = succ_at(a, r.succBase + c);
     y = x;
     y.entry = nxt;
-    y.path = child_path(x.path, c, nxt);
+    if (PATH) y.path = child_path(x.path, c, nxt);
     ordinal = c;
     return true;
   }
@@ -780,7 +782,7 @@ __device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E,
       translate_ref(y, x, E.axisRef, o);
       y.seed = seed_of(a, x.seed, c);
       y.entry = nxt;
-      y.path = child_path(x.path, c, nxt);
+      if (PATH) y.path = child_path(x.path, c, nxt);
       E.offset = __fadd_rn(E.offset, newSize);
       E.prevSize = newSize;
       E.prevOff = o;
@@ -813,7 +815,7 @@ __device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E,
       translate_ref(y, x, E.axisRef, o);
       y.seed = seed_of(a, x.seed, mod);
       y.entry = nxt;
-      y.path = child_path(x.path, mod, nxt);
+      if (PATH) y.path = child_path(x.path, mod, nxt);
       ordinal = mod;
       return true;
     }
@@ -865,7 +867,7 @@ __device__ __forceinline__ bool expander_child(const DeriveArgs& a, Expander& E,
       int32_t nxt = succ_at(a, r.succBase + succ);
       y.seed = seed_of(a, x.seed, mod);
       y.entry = nxt;
-      y.path = child_path(x.path, mod, nxt);
+      if (PATH) y.path = child_path(x.path, mod, nxt);
       ordinal = c;
       return true;
     }
