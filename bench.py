@@ -213,6 +213,19 @@ def cpu_baseline_single(batch):
                 "sample": f"full city-4096 ({len(t)} terminals), oracle restatement, 1 thread, {model}"}
 
 
+def max_over_ranks(ms, device):
+    """The largest of every rank's `ms` (the job is as slow as its slowest
+    replica); `ms` itself when there is one rank."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -318,13 +331,7 @@ def our_arm(args):
         barrier()
         clocks.mark(t_start, time.time())
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(step_ms) / len(step_ms), dev)
     value = world * n_term / (ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers: pga_derive_to_host
@@ -351,7 +358,7 @@ def our_arm(args):
         n_host = e2e_step()
         e2e_times.append((time.perf_counter() - h0) * 1e3)
     barrier()
-    e2e_ms = statistics.median(e2e_times)
+    e2e_ms = max_over_ranks(statistics.median(e2e_times), dev)
     assert n_host == n_term
     e2e_value = world * n_term / (e2e_ms * 1e-3)
 
