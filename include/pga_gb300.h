@@ -277,6 +277,21 @@ PgaStatus pga_derive_plain(PgaEngine* engine, const PgaAxiom* dAxioms, uint32_t 
                            const float* dParamBlocks, PgaTerminal* dOut, uint64_t capacity,
                            uint64_t* dCount, void* stream);
 
+/* SinglePhaseEvaluator::execute (GPUEvaluator.cuh:508-521) called once per
+ * grammar, as a caller without batching would: one persistent launch per
+ * axiom (the same kernel and schedule as pga_derive, each launch deriving one
+ * axiom), the launches enqueued back to back on `stream` with no host
+ * read-back, so the sequence can also be captured in a CUDA graph.  Each
+ * launch derives into an engine staging buffer and a small copy kernel
+ * appends its records at the running count, which lives on the device.  Same
+ * records as pga_derive, in axiom order; *dCount gets the total.  The staging
+ * buffer (capacity records) is allocated on first use and kept by the engine;
+ * make the first call before any capture.  The first failing axiom's status
+ * is reported by pga_engine_sync_report.  No tape for pga_adjoint. */
+PgaStatus pga_derive_per_axiom(PgaEngine* engine, const PgaAxiom* dAxioms, uint32_t numAxioms,
+                               const float* dParamBlocks, PgaTerminal* dOut, uint64_t capacity,
+                               uint64_t* dCount, void* stream);
+
 /* Synchronises `stream` and reports the device status of the last derivation:
  * PGA_ERR_OUTPUT_OVERFLOW when it produced more terminals than the capacity it
  * was given (report->terminals holds the full count; records past the
@@ -318,10 +333,15 @@ PgaStatus pga_lbvh_build_counted(PgaEngine* engine, const PgaTerminal* dTerminal
  * application): it needs no engine and calls no allocator.  Its scratch is a
  * fixed device array inside this library (6 MiB, held by every GPU that loads
  * the library until the process exits), so n is limited to
- * PGA_LBVH_STATIC_MAX_LEAVES; larger n is rejected with
- * PGA_ERR_INVALID_ARGUMENT.  The first call on a device looks the array's
- * device address up; make it before any stream capture.  Calls share the array
- * and race when they overlap on the GPU.  No counterpart in the reference. */
+ * PGA_LBVH_STATIC_MAX_LEAVES; larger n (and n = 1) is rejected with
+ * PGA_ERR_INVALID_ARGUMENT.  The first call on a device loads the library's
+ * module there (which commits the array) and looks the array's device address
+ * up: make it at start-up, before the device budget is handed out and before
+ * any stream capture -- a call with n = 0 (pointers may be null) does only
+ * that.  The address is cached for the life of the process, which assumes the
+ * device's primary context is never reset.  Calls share the array and race
+ * when they overlap on the GPU: serialise them on one stream.  No counterpart
+ * in the reference. */
 #define PGA_LBVH_STATIC_MAX_LEAVES 65536u
 PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const PgaBounds* bounds,
                                 const PgaLbvh* out, void* stream);

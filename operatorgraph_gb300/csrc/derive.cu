@@ -850,6 +850,86 @@ PgaStatus pga_derive_to_host(PgaEngine* e, const PgaAxiom* hAxioms, uint32_t num
   return status;
 }
 
+}  // extern "C"
+
+// Bookkeeping of pga_derive_per_axiom between two launches.  The launch that
+// just finished left its records at stage[0, st->termCount) and its status in
+// *st.  Append the records at out[*countIn, ...) (what fits below cap), write
+// *countOut = *countIn + termCount (the two counters alternate, so no block
+// reads the word another block writes), keep the first nonzero status in
+// book[2] (status << 32 | detail) and add the launch's queued items to book[3].
+__global__ void k_append_axiom(const DevState* st, const PgaTerminal* stage, unsigned long long stageCap,
+                               PgaTerminal* out, unsigned long long cap, const unsigned long long* countIn,
+                               unsigned long long* countOut, unsigned long long* book) {
+  const unsigned long long base = *countIn;
+  const unsigned long long n = ((const volatile DevState*)st)->termCount;
+  const unsigned long long m = min(n, stageCap);
+  const unsigned long long fit = base < cap ? min(m, cap - base) : 0ull;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < fit;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint4* from = reinterpret_cast<const uint4*>(stage + i);
+    uint4* to = reinterpret_cast<uint4*>(out + base + i);
+    uint4 r[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) r[q] = __ldcs(from + q);
+#pragma unroll
+    for (int q = 0; q < 4; q++) __stcs(to + q, r[q]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *countOut = base + n;
+    int status = ((const volatile DevState*)st)->status, detail = ((const volatile DevState*)st)->detail;
+    if (status == 0 && n > stageCap) status = PGA_ERR_OUTPUT_OVERFLOW;
+    if (status != 0 && book[2] == 0) book[2] = ((unsigned long long)(uint32_t)status << 32) | (uint32_t)detail;
+    book[3] += ((const volatile DevState*)st)->nodeNext;
+  }
+}
+
+// The end of pga_derive_per_axiom: the whole sequence's count, first status
+// and items go into the engine state (for pga_engine_sync_report) and *dCount.
+__global__ void k_finish_per_axiom(DevState* st, const unsigned long long* count, const unsigned long long* book,
+                                   unsigned long long* dCount) {
+  st->termCount = *count;
+  st->nodeNext = book[3];
+  if (book[2] != 0) {
+    st->status = (int32_t)(book[2] >> 32);
+    st->detail = (int32_t)(uint32_t)book[2];
+  }
+  if (dCount) *dCount = *count;
+}
+
+extern "C" {
+
+PgaStatus pga_derive_per_axiom(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dParamBlocks,
+                               PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount, void* stream) {
+  if (!e || (!dAxioms && numAxioms) || (!dOut && capacity)) {
+    set_error("pga_derive_per_axiom: null engine or buffers");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  if (e->phased) {
+    set_error("pga_derive_per_axiom: a multi-phase table (phases, Collider, IfCollides) needs pga_derive");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  PGA_CUDA_TRY(ensure_buffer((void**)&e->dStageOut, &e->stageOutBytes, std::max<uint64_t>(capacity, 1) * sizeof(PgaTerminal)));
+  PGA_CUDA_TRY(ensure_buffer((void**)&e->dStageCount, &e->stageCountBytes, 4 * sizeof(uint64_t)));
+  unsigned long long* book = reinterpret_cast<unsigned long long*>(e->dStageCount);
+  PGA_CUDA_TRY(cudaMemsetAsync(book, 0, 4 * sizeof(uint64_t), s));
+  const uint64_t stageCap = e->stageOutBytes / sizeof(PgaTerminal);
+  for (uint32_t ax = 0; ax < numAxioms; ax++) {
+    const PgaStatus st = launch_persistent(e, dAxioms, ax, ax + 1, dParamBlocks, e->dStageOut, stageCap, nullptr, s);
+    if (st != PGA_OK) return st;
+    k_append_axiom<<<64, 256, 0, s>>>(e->dState, e->dStageOut, stageCap, dOut, capacity, book + (ax & 1),
+                                      book + ((ax + 1) & 1), book);
+    PGA_CUDA_TRY(cudaGetLastError());
+  }
+  if (numAxioms == 0) PGA_CUDA_TRY(cudaMemsetAsync(e->dState, 0, sizeof(DevState), s));
+  k_finish_per_axiom<<<1, 1, 0, s>>>(e->dState, book + (numAxioms & 1), book, (unsigned long long*)dCount);
+  PGA_CUDA_TRY(cudaGetLastError());
+  e->lastCap = capacity;
+  e->lastWasBatched = false;  // no tape for pga_adjoint
+  return PGA_OK;
+}
+
 PgaStatus pga_derive_plain(PgaEngine* e, const PgaAxiom* dAxioms, uint32_t numAxioms, const float* dParamBlocks,
                            PgaTerminal* dOut, uint64_t capacity, uint64_t* dCount, void* stream) {
   if (!e || (!dAxioms && numAxioms) || (!dOut && capacity)) {

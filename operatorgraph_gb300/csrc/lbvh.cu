@@ -443,10 +443,17 @@ extern "C" PgaStatus pga_lbvh_build_counted(PgaEngine* e, const PgaTerminal* dTe
 // The array's name denotes a host-side stand-in in host code, not a device
 // address, so the device address is looked up once per device with
 // cudaGetSymbolAddress (with that device current) on the first call made on
-// it; make that first call before any stream capture.  All calls share the
-// array and it keeps the last call's contents: the arrival counters that must
-// start at zero are cleared on every call, and calls that overlap on the GPU
-// (on different streams, or from different threads) race on it.
+// it.  Under CUDA's lazy module loading the array itself is committed on the
+// device only when this file's module first loads there -- at that lookup at
+// the latest -- so a caller that hands out its device budget at start-up
+// makes one call on each device first: a call with n = 0 (pointers may be
+// null) does only this set-up.  Make it before any stream capture too.  The
+// address is cached per device ordinal for the life of the process: the
+// library assumes that each device's primary context lives as long as the
+// process (after cudaDeviceReset the cached address is stale).  All calls
+// share the array and it keeps the last call's contents: the arrival counters
+// that must start at zero are cleared on every call, and calls that overlap
+// on the GPU (on different streams, or from different threads) race on it.
 
 namespace pga {
 
@@ -462,12 +469,13 @@ static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const PgaBounds* bounds,
                                            const PgaLbvh* out, void* stream) {
-  if (!dTerminals || !bounds || !lbvh_out_ok(out)) {
+  if (n != 0 && (!dTerminals || !bounds || !lbvh_out_ok(out))) {
     set_error("pga_lbvh_build_static: null argument");
     return PGA_ERR_INVALID_ARGUMENT;
   }
-  if (n < 2 || n > PGA_LBVH_STATIC_MAX_LEAVES) {
-    set_error("pga_lbvh_build_static: n must be in [2, " + std::to_string(PGA_LBVH_STATIC_MAX_LEAVES) +
+  if (n == 1 || n > PGA_LBVH_STATIC_MAX_LEAVES) {
+    set_error("pga_lbvh_build_static: n must be 0 (set-up only) or in [2, " +
+              std::to_string(PGA_LBVH_STATIC_MAX_LEAVES) +
               "] (the fixed scratch holds at most that many leaves); use pga_lbvh_build for larger sets");
     return PGA_ERR_INVALID_ARGUMENT;
   }
@@ -488,6 +496,7 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
     }
     base = static_cast<unsigned char*>(g_staticAddr[dev]);
   }
+  if (n == 0) return PGA_OK;  // set-up only
   // Carve the scratch: keys, two value arrays, arrival counters, leaf boxes
   // (terminal and sorted order), node ranges, sort temp.
   size_t temp = pga_lbvh_temp_bytes(n);

@@ -27,7 +27,7 @@ STATUS = {
 EXPORTS = ["pga_version", "pga_last_error", "pga_default_procs", "pga_engine_create", "pga_engine_destroy",
            "pga_derive", "pga_derive_plain", "pga_engine_sync_report", "pga_engine_levels", "pga_lbvh_build",
            "pga_lbvh_build_counted", "pga_lbvh_build_static", "pga_adjoint", "pga_adjoint_strided",
-           "pga_derive_to_host", "pga_generate_meshes"]
+           "pga_derive_to_host", "pga_generate_meshes", "pga_derive_per_axiom"]
 
 
 class PgaError(RuntimeError):
@@ -91,7 +91,7 @@ def load_library(path=LIB_PATH):
     L.pga_default_procs.restype = ctypes.POINTER(PgaProc)
     L.pga_engine_create.argtypes = [ctypes.POINTER(PgaRuleTable), ctypes.POINTER(PgaEngineConfig), ctypes.POINTER(vp)]
     L.pga_engine_destroy.argtypes = [vp]
-    for name in ("pga_derive", "pga_derive_plain"):
+    for name in ("pga_derive", "pga_derive_plain", "pga_derive_per_axiom"):
         getattr(L, name).argtypes = [vp, vp, u32, vp, vp, u64, vp, vp]
     L.pga_engine_sync_report.argtypes = [vp, vp, ctypes.POINTER(PgaDeriveReport)]
     L.pga_lbvh_build.argtypes = [vp, vp, u64, ctypes.POINTER(PgaBounds), ctypes.POINTER(PgaLbvh), vp]
@@ -158,10 +158,12 @@ class Engine:
 
     # -- raw C-ABI calls on device pointers ------------------------------------------------
     def derive_raw(self, d_axioms, n_axioms, d_blocks, d_out, capacity, d_count, stream=None, plain=False):
+        """pga_derive; plain=True: pga_derive_plain (host-driven levels), plain="per_axiom":
+        pga_derive_per_axiom (one persistent launch per axiom, no host read-back)."""
         L = load_library()
-        fn = L.pga_derive_plain if plain else L.pga_derive
-        _check(fn(self.handle, d_axioms, n_axioms, d_blocks, d_out, capacity, d_count, _stream_handle(stream)),
-               "pga_derive_plain" if plain else "pga_derive")
+        name = {False: "pga_derive", True: "pga_derive_plain", "per_axiom": "pga_derive_per_axiom"}[plain]
+        fn = getattr(L, name)
+        _check(fn(self.handle, d_axioms, n_axioms, d_blocks, d_out, capacity, d_count, _stream_handle(stream)), name)
 
     def derive_to_host(self, h_axioms, n_axioms, h_out, capacity, d_blocks=None, stream=None, check=True):
         """pga_derive_to_host on host pointers (pinned memory is fastest); returns (count, status)."""

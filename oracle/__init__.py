@@ -13,8 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
-# Where the reference sources live in the build container (absent elsewhere).
-REFERENCE_ROOT = os.environ.get("PGA_REFERENCE_ROOT", "/root/reference")
+from .make_ref import REFERENCE_ROOT  # noqa: E402  (where the reference sources are read, if present)
 
 _lib = None
 
@@ -48,6 +47,8 @@ def lib():
         vp, u32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64
         L.oracle_derive.argtypes = [vp, u32, vp, u32, vp, u32, vp, u32, vp, u64, vp, vp]
         L.oracle_derive.restype = ctypes.c_int
+        L.oracle_derive_base.argtypes = [vp, u32, vp, u32, vp, u32, vp, u32, vp, u64, vp, vp, u64]
+        L.oracle_derive_base.restype = ctypes.c_int
         L.oracle_derive_f64.argtypes = [vp, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp, u64, vp]
         L.oracle_derive_f64.restype = ctypes.c_int
         L.oracle_lbvh.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp]
@@ -71,8 +72,10 @@ class OracleError(RuntimeError):
         self.detail = detail
 
 
-def derive(procs, entries, axioms, blocks=None, block_stride=0, capacity=None):
-    """Terminals of the batch (PgaTerminal records, derivation order)."""
+def derive(procs, entries, axioms, blocks=None, block_stride=0, capacity=None, axiom_base=0):
+    """Terminals of the batch (PgaTerminal records, derivation order).
+    axiom_base: index of the batch's first axiom in a larger batch, so a shard
+    gives the records (path hashes included) the whole batch gives for it."""
     from operatorgraph_gb300.grammar import TERMINAL_DT
 
     L = lib()
@@ -83,14 +86,14 @@ def derive(procs, entries, axioms, blocks=None, block_stride=0, capacity=None):
     cnt = np.zeros(1, np.uint64)
     det = np.zeros(1, np.int32)
     if capacity is None:
-        st = L.oracle_derive(_ptr(procs), len(procs), _ptr(entries), len(entries), _ptr(axioms), len(axioms),
-                             _ptr(blk), block_stride, None, 0, _ptr(cnt), _ptr(det))
+        st = L.oracle_derive_base(_ptr(procs), len(procs), _ptr(entries), len(entries), _ptr(axioms), len(axioms),
+                                  _ptr(blk), block_stride, None, 0, _ptr(cnt), _ptr(det), axiom_base)
         if st not in (0, 2):
             raise OracleError(st, int(det[0]))
         capacity = int(cnt[0])
     out = np.zeros(max(capacity, 1), dtype=TERMINAL_DT)
-    st = L.oracle_derive(_ptr(procs), len(procs), _ptr(entries), len(entries), _ptr(axioms), len(axioms),
-                         _ptr(blk), block_stride, _ptr(out), capacity, _ptr(cnt), _ptr(det))
+    st = L.oracle_derive_base(_ptr(procs), len(procs), _ptr(entries), len(entries), _ptr(axioms), len(axioms),
+                              _ptr(blk), block_stride, _ptr(out), capacity, _ptr(cnt), _ptr(det), axiom_base)
     if st != 0:
         raise OracleError(st, int(det[0]))
     return out[: int(cnt[0])]
@@ -177,14 +180,26 @@ def lbvh(terminals, bounds):
     return nodes, lp, aabb, lt, keys
 
 
-def run_reference(batch_file, out_file, repeats=1, timeout=600):
-    """Run the reference's own evaluator (oracle/_ref); returns its JSON summary."""
+def run_reference(batch_file, out_file, repeats=1, timeout=600, axiom_base=0, entry_mod=None, write_output=True):
+    """Run the reference's own evaluator (oracle/_ref); returns its JSON summary.
+
+    axiom_base: index of the batch's first axiom in a larger batch (root path
+    hashes); entry_mod: entries per table copy when the batch gives each axiom
+    its own copy of one table (child path hashes use the shared table's
+    indices); write_output=False times execute() without writing the terminal
+    file."""
     import json
 
     if not os.path.exists(REF_HARNESS):
         raise FileNotFoundError(REF_HARNESS)
-    r = subprocess.run([REF_HARNESS, batch_file, out_file, str(repeats)], capture_output=True, text=True,
-                       timeout=timeout)
+    cmd = [REF_HARNESS, batch_file, out_file, str(repeats)]
+    if axiom_base:
+        cmd += ["--axiom-base", str(int(axiom_base))]
+    if entry_mod:
+        cmd += ["--entry-mod", str(int(entry_mod))]
+    if not write_output:
+        cmd += ["--no-output"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError(f"ref_harness failed ({r.returncode}): {r.stderr.strip()}")
     return json.loads(r.stdout.strip().splitlines()[-1])

@@ -217,6 +217,9 @@ struct Ctx {
   // Phases (multi-phase derivation): the phase being run, the phase of the
   // edges into each entry, and the colliders of the phases before this one.
   uint32_t phase = 0;
+  // Index of the batch's first axiom in a larger batch (root path hashes, as
+  // the engine's axiomBase when it derives a batch in axiom ranges).
+  uint64_t axiomBase = 0;
   std::vector<uint32_t> entryPhase;
   std::vector<StoredCollider>* colliders = nullptr;
   size_t visibleColliders = 0;
@@ -937,7 +940,7 @@ int derive(Ctx& c, const Blocks<F>& blk, const double* axiomSizes, Out<F>& o, ui
     s.entry = (int32_t)a.entry;
     s.shape = a.shape;
     s.axiom = id;
-    s.path = root_path(id);
+    s.path = root_path((uint32_t)(c.axiomBase + id));
     dispatch(c, o, s);
     while (!o.work.empty() && c.status == PGA_OK) {
       Sym<F> cur = o.work.back();
@@ -1030,10 +1033,14 @@ void oracle_mesh_copy(uint32_t mesh, float* vertices, uint32_t* indices) {
   std::copy(g_meshes[mesh].indices.begin(), g_meshes[mesh].indices.end(), indices);
 }
 
-int oracle_derive(const PgaProc* procs, uint32_t nProcs, const PgaEntry* entries, uint32_t nEntries,
-                  const PgaAxiom* axioms, uint32_t nAxioms, const float* blocks, uint32_t blockStride,
-                  PgaTerminal* out, uint64_t cap, uint64_t* count, int32_t* detail) {
+// oracle_derive for a shard of a larger batch: axiom k of this call hashes its
+// root path as axiom axiomBase + k (the records are those the whole batch gives
+// for these axioms).
+int oracle_derive_base(const PgaProc* procs, uint32_t nProcs, const PgaEntry* entries, uint32_t nEntries,
+                       const PgaAxiom* axioms, uint32_t nAxioms, const float* blocks, uint32_t blockStride,
+                       PgaTerminal* out, uint64_t cap, uint64_t* count, int32_t* detail, uint64_t axiomBase) {
   Ctx c = {procs, nProcs, entries, nEntries, axioms, blockStride, PGA_OK, 0};
+  c.axiomBase = axiomBase;
   Blocks<float> blk = {blocks, nullptr};
   Out<float> o;
   g_meshes.clear();
@@ -1049,6 +1056,13 @@ int oracle_derive(const PgaProc* procs, uint32_t nProcs, const PgaEntry* entries
   if (detail) *detail = c.detail;
   if (c.status == PGA_OK && o.count > cap) return PGA_ERR_OUTPUT_OVERFLOW;
   return c.status;
+}
+
+int oracle_derive(const PgaProc* procs, uint32_t nProcs, const PgaEntry* entries, uint32_t nEntries,
+                  const PgaAxiom* axioms, uint32_t nAxioms, const float* blocks, uint32_t blockStride,
+                  PgaTerminal* out, uint64_t cap, uint64_t* count, int32_t* detail) {
+  return oracle_derive_base(procs, nProcs, entries, nEntries, axioms, nAxioms, blocks, blockStride, out, cap, count,
+                            detail, 0);
 }
 
 // The same derivation carried out in double precision (seeds stay float, as

@@ -9,9 +9,17 @@
 // Input  (argv[1]): a grammar batch, format written by
 //                   operatorgraph_gb300/grammar.py::write_batch_file
 // Output (argv[2]): terminal records, 64 B each (same layout as PgaTerminal in
-//                   include/pga_gb300.h, path hash left 0 because the reference
-//                   has no derivation-path hash)
+//                   include/pga_gb300.h).  The path hash is the one oracle/make_ref.py
+//                   instruments the reference's child-creation call sites with.
 // argv[3] (optional): number of timed repetitions of execute().
+// Options after the positional arguments:
+//   --axiom-base B   axiom k of the batch is axiom B + k for its root path hash
+//                    (a shard of a larger batch hashes like the whole batch)
+//   --entry-mod E    child entry indices are hashed modulo E (a batch that gives
+//                    each axiom its own copy of an E-entry table hashes like the
+//                    one shared table)
+//   --no-output      keep the terminals in memory but write no terminal file
+//                    (timing runs: only execute() is timed either way)
 //
 // ref_harness --collide <pairs.bin> <out.bin> runs the reference's collision
 // predicate PGA::ContextSensitivity::Collision::check (Collision.cuh) on shape
@@ -97,7 +105,7 @@ template <> struct GenerationFunction<HarnessFilter, 1> {
     int entry = static_cast<Symbol<ShapeT>&>(shape).entryIndex;
     t.rule = (uint32_t(entry) & 0xFFFFFFu) | ((terminalIndex & 0x7Fu) << 24) | (IsQuadShape<ShapeT>::value << 31);
     t.custom = attr1;
-    t.path = 0;
+    t.path = static_cast<Symbol<ShapeT>&>(shape).pathHash;
     g_terminals.push_back(t);
   }
   template <typename ShapeT, typename... ArgsT> static unsigned int allocateVertices(ShapeT&, unsigned int, ArgsT...) { return 0; }
@@ -212,12 +220,14 @@ static_assert(sizeof(FileEntry) == 1332, "entry size");
 static_assert(sizeof(FileAxiom) == 48, "axiom size");
 
 static std::vector<FileAxiom> g_axioms;
+static unsigned long long g_axiomBase = 0;
 
 struct HarnessAxioms {
   static unsigned int getNumAxioms() { return (unsigned int)g_axioms.size(); }
   template <typename SymbolManagerT, typename QueueT>
   static void generateAxiom(int id, QueueT* queue) {
     const FileAxiom& a = g_axioms[id];
+    PathHash::currentAxiom() = g_axiomBase + (unsigned long long)id;
     if (a.shape == 1) {
       Quad q;
       q.setSize(math::float3(a.size[0], a.size[1], a.size[2]));
@@ -270,12 +280,20 @@ static int collide_main(const char* in, const char* outPath) {
 
 int main(int argc, char** argv) {
   if (argc == 4 && strcmp(argv[1], "--collide") == 0) return collide_main(argv[2], argv[3]);
-  if (argc < 3) {
-    fprintf(stderr, "usage: ref_harness <batch.bin> <terminals.bin> [repeats]\n");
+  std::vector<const char*> pos;
+  bool writeOutput = true;
+  for (int i = 1; i < argc; i++) {
+    if (strcmp(argv[i], "--axiom-base") == 0 && i + 1 < argc) g_axiomBase = strtoull(argv[++i], nullptr, 10);
+    else if (strcmp(argv[i], "--entry-mod") == 0 && i + 1 < argc) PathHash::entryModulus() = (unsigned)atoi(argv[++i]);
+    else if (strcmp(argv[i], "--no-output") == 0) writeOutput = false;
+    else pos.push_back(argv[i]);
+  }
+  if (pos.size() < 2) {
+    fprintf(stderr, "usage: ref_harness <batch.bin> <terminals.bin> [repeats] [--axiom-base B] [--entry-mod E] [--no-output]\n");
     return 2;
   }
-  int repeats = argc > 3 ? atoi(argv[3]) : 1;
-  FILE* f = fopen(argv[1], "rb");
+  int repeats = pos.size() > 2 ? atoi(pos[2]) : 1;
+  FILE* f = fopen(pos[0], "rb");
   if (!f) { perror("open input"); return 2; }
   FileHeader h;
   if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, "PGAB", 4) != 0) { fprintf(stderr, "bad header\n"); return 2; }
@@ -329,17 +347,19 @@ int main(int argc, char** argv) {
     ev.release();
     if (rc) break;
   }
-  FILE* o = fopen(argv[2], "wb");
-  if (!o) { perror("open output"); return 2; }
   uint64_t n = g_terminals.size();
-  fwrite("PGAT", 1, 4, o);
-  uint32_t zero = 0;
-  fwrite(&zero, 4, 1, o);
-  fwrite(&n, 8, 1, o);
-  fwrite(g_terminals.data(), sizeof(HarnessTerminal), n, o);
-  fclose(o);
-  if (!g_meshes.empty()) {
-    std::string mp = std::string(argv[2]) + ".mesh";
+  if (writeOutput) {
+    FILE* o = fopen(pos[1], "wb");
+    if (!o) { perror("open output"); return 2; }
+    fwrite("PGAT", 1, 4, o);
+    uint32_t zero = 0;
+    fwrite(&zero, 4, 1, o);
+    fwrite(&n, 8, 1, o);
+    fwrite(g_terminals.data(), sizeof(HarnessTerminal), n, o);
+    fclose(o);
+  }
+  if (writeOutput && !g_meshes.empty()) {
+    std::string mp = std::string(pos[1]) + ".mesh";
     FILE* mf = fopen(mp.c_str(), "wb");
     if (!mf) { perror("open mesh output"); return 2; }
     fwrite("PGAM", 1, 4, mf);
@@ -354,9 +374,15 @@ int main(int argc, char** argv) {
     }
     fclose(mf);
   }
+  std::string all;  // in run order
+  for (size_t k = 0; k < times.size(); k++) {
+    char buf[32];
+    snprintf(buf, sizeof buf, "%s%.9g", k ? ", " : "", times[k]);
+    all += buf;
+  }
   std::sort(times.begin(), times.end());
   double med = times.empty() ? 0.0 : times[times.size() / 2];
-  printf("{\"terminals\": %llu, \"seconds\": %.9g, \"repeats\": %d, \"status\": %d}\n",
-         (unsigned long long)n, med, (int)times.size(), rc);
+  printf("{\"terminals\": %llu, \"seconds\": %.9g, \"repeats\": %d, \"status\": %d, \"all_seconds\": [%s]}\n",
+         (unsigned long long)n, med, (int)times.size(), rc, all.c_str());
   return rc;
 }

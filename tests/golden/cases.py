@@ -491,6 +491,18 @@ def canonical(terminals, num_entries=None):
     return G.sort_terminals(t)
 
 
+def canonical_paths(terminals, num_entries=None):
+    """Order-free form WITH derivation-path hashes: -0 -> +0, entry index
+    folded into the base table, sorted by path hash (the paths of one batch
+    are distinct, so the order is total)."""
+    t = terminals.copy()
+    t["m"] = t["m"] + np.float32(0)
+    if num_entries is not None:
+        e = t["rule"] & 0xFFFFFF
+        t["rule"] = (t["rule"] & 0xFF000000) | (e % num_entries)
+    return G.sort_terminals(t, by_path=True)
+
+
 def digest(canon):
     import hashlib
 

@@ -257,3 +257,78 @@ def test_adjoint_requires_tape():
         eng.adjoint_raw(g.data_ptr(), None, 0, None)
     assert e.value.status == 8
     eng.release()
+
+
+def _ref_loss32(batch, by_path, blocks32, sizes32, tmp):
+    """sum of W . M over the terminals the REFERENCE's own evaluator derives
+    (oracle/_ref, FP32 as the reference computes), matched by the path hash the
+    instrumented reference reports; (loss, path set) or (None, None) when a
+    terminal's path is unknown."""
+    import os
+
+    ax = batch["axioms"].copy()
+    ax["size"] = sizes32.reshape(-1, 3)
+    entries, ax2 = G.expand_blocks(batch["entries"], ax, blocks32, batch["block_stride"])
+    bf, tf = os.path.join(tmp, "b.bin"), os.path.join(tmp, "t.bin")
+    G.write_batch_file(bf, entries, ax2)
+    oracle.run_reference(bf, tf, entry_mod=len(batch["entries"]))
+    t = G.read_terminal_file(tf)
+    total, keys = 0.0, []
+    for m, p in zip(t["m"].astype(np.float64), t["path"].tolist()):
+        w = by_path.get(int(p))
+        if w is None:
+            return None, None
+        total += float(np.dot(w, m))
+        keys.append(int(p))
+    return total, frozenset(keys)
+
+
+def test_facade_gradients_match_reference_fp32_central_differences(tmp_path):
+    """The adjoint against a gradient taken from the reference's own evaluator:
+    central differences of L = sum(W . M) where M are the FP32 transforms the
+    reference's SinglePhaseEvaluator derives (oracle/_ref; the batch's
+    parameter blocks written into per-axiom table copies), each input moved by
+    1% of its size.  4 facades: 64 block parameters and 12 axiom sizes.
+    At that step the reference's FP32 differences agree with FP64 differences
+    of the restatement to about 6e-5 of the gradient's scale, so the bar is
+    the FP64 test's: 2e-3 of the scale."""
+    import os
+
+    if not os.path.exists(oracle.REF_HARNESS):
+        pytest.skip("oracle/_ref (the reference built from its sources) is not available")
+    batch = scenes.facades(4, seed=7)
+    by_path, gb, gs = _gpu_grad(batch)
+    b32 = batch["blocks"].astype(np.float32)
+    s32 = batch["axioms"]["size"].astype(np.float32).reshape(-1)
+    tmp = str(tmp_path)
+    base, keys0 = _ref_loss32(batch, by_path, b32, s32, tmp)
+    assert base is not None and len(keys0) == len(by_path), "the reference's terminals differ from the engine's"
+
+    def diff(vec_b, vec_s, which, k):
+        x = (vec_b if which == "b" else vec_s)
+        h = np.float32(1e-2 * max(abs(float(x[k])), 0.1))
+        out = []
+        for sgn in (1, -1):
+            bb, ss = vec_b.copy(), vec_s.copy()
+            tgt = bb if which == "b" else ss
+            tgt[k] = np.float32(tgt[k] + sgn * h)
+            step = float(tgt[k]) - float(x[k])  # the step as FP32 represents it
+            lv, kv = _ref_loss32(batch, by_path, bb, ss, tmp)
+            if lv is None or kv != keys0:
+                return None
+            out.append((lv, step))
+        (lp, hp), (lm, hm) = out
+        return (lp - lm) / (hp - hm), (lp - base) / hp, (base - lm) / -hm
+
+    tol = RTOL
+    for which, got, n in (("b", gb, len(b32)), ("s", gs.reshape(-1), len(s32))):
+        diffs = [diff(b32, s32, which, k) for k in range(n)]
+        fds = [d[0] for d in diffs if d is not None]
+        scale = max(max((abs(f) for f in fds), default=0.0), 1.0)
+        checked = 0
+        for k, d in enumerate(diffs):
+            if d is None or abs(d[1] - d[2]) > 0.5 * tol * scale:
+                continue
+            assert abs(got[k] - d[0]) <= tol * scale, f"{which}[{k}]: adjoint {got[k]:.6g} vs reference FD {d[0]:.6g}"
+            checked += 1
+        assert checked >= 0.9 * n, (which, checked, n)

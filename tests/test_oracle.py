@@ -47,7 +47,13 @@ def test_oracle_matches_reference_golden(path):
         assert np.array_equal(canon["m"].view(np.uint32), ref["m"].view(np.uint32))
         assert np.array_equal(canon["rule"], ref["rule"])
         assert np.array_equal(canon["custom"], ref["custom"])
+        assert np.array_equal(np.sort(t["path"]), z["paths"]), "path hashes differ from the reference's"
     assert digest(canon) == str(z["digest"])
+    # the records with their derivation-path hashes, as the instrumented
+    # reference derived them (each path names the same record in both)
+    import cases
+
+    assert digest(cases.canonical_paths(t, n_base)) == str(z["digest_path"]), "records by path differ"
 
 
 @pytest.mark.parametrize("path", [p for p in GOLDEN if "mesh_counts" in np.load(p)],

@@ -77,26 +77,30 @@ def _load(path):
     return b, z
 
 
-@pytest.mark.parametrize("form", ["persistent", "queued", "plain", "grouped"])
+@pytest.mark.parametrize("form", ["persistent", "queued", "plain", "grouped", "per_axiom"])
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
 def test_golden_case(path, form):
     """persistent: the batched launch (leaf children expanded in place);
     queued: the same with every branching child queued (PGA_FLAG_NO_INLINE);
     plain: one axiom and one launch per level;
     grouped: the batched launch with the axioms seeded grouped by root entry
-    (PGA_FLAG_GROUP_AXIOMS)."""
+    (PGA_FLAG_GROUP_AXIOMS);
+    per_axiom: one persistent launch per axiom, appended on the device."""
     import sys
 
     sys.path.insert(0, os.path.join(HERE, "golden"))
     import cases
 
     b, z = _load(path)
-    eng, out, got, rep = _run(b, plain=form == "plain", no_inline=form == "queued", group_axioms=form == "grouped")
+    plain = {"plain": True, "per_axiom": "per_axiom"}.get(form, False)
+    eng, out, got, rep = _run(b, plain=plain, no_inline=form == "queued", group_axioms=form == "grouped")
     assert rep["status"] == 0
     n_base = len(b["entries"]) if b["blocks"] is not None else None
     canon = cases.canonical(got, n_base)
     assert len(got) == int(z["count"])
     assert cases.digest(canon) == str(z["digest"]), "differs from the reference's own output"
+    assert cases.digest(cases.canonical_paths(got, n_base)) == str(z["digest_path"]), \
+        "records by derivation path differ from the reference's own output"
     ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"], b["blocks"], b["block_stride"])
     _assert_same(got, ref)
     if "mesh_counts" in z:
@@ -303,42 +307,72 @@ def test_grouped_axioms_give_the_same_records():
     assert (ka == kb).all()
 
 
-def test_mixed_65536_full_size_properties():
+def test_mixed_65536_full_size_bit_exact():
     """The C5 mix at full size (65,536 axioms: Menger depths 1-3, city buildings,
     random grammars; about 152M terminals) in one launch, against the oracle run
-    in axiom shards: the exact count, the exact histogram of emitting rules
-    (entry, mesh index, shape), float64 sums of every transform component, and
-    unique path hashes.  Bit-exact per-record parity is covered on the smaller
-    cases; here the shard runs renumber the axioms, so path hashes differ."""
+    in 16 axiom shards of 4,096, each hashing its root paths from its first
+    axiom's index in the whole batch.  Every oracle record is looked up by its
+    derivation-path hash among the launch's records (sorted by path on the
+    device) and compared field by field: transform bits (up to the sign of
+    zero), rule, custom attribute.  Counts add up and paths are unique, so the
+    two multisets are equal record for record."""
     import torch
 
     b = scenes.mixed(65536)
-    want_n, want_sum, want_rules = 0, np.zeros(12), {}
-    for lo in range(0, 65536, 4096):
-        t = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"][lo:lo + 4096])
-        want_n += len(t)
-        want_sum += t["m"].astype(np.float64).sum(axis=0)
-        r, c = np.unique(t["rule"], return_counts=True)
-        for k, v in zip(r.tolist(), c.tolist()):
-            want_rules[k] = want_rules.get(k, 0) + v
-        del t
-    cap = want_n + (1 << 20)
+    cap = 160_000_000
     eng = _engine(b["entries"], node_capacity=1 << 27, max_terminals=cap)
     out, n, rep = eng.execute(b["axioms"], capacity=cap)
-    assert rep["status"] == 0 and n == want_n
-    got_sum = torch.zeros(12, dtype=torch.float64, device="cuda")
-    rules, paths = [], []
-    for lo in range(0, n, 1 << 23):
-        chunk = out[lo:min(n, lo + (1 << 23))]
-        f = chunk.view(torch.float32).view(-1, 16)
-        got_sum += f[:, :12].double().sum(dim=0)
-        rules.append(chunk.view(torch.int32).view(-1, 16)[:, 12])
-        paths.append(chunk.view(torch.int64).view(-1, 8)[:, 7])
-    r, c = torch.unique(torch.cat(rules), return_counts=True)
-    got_rules = {int(k) & 0xFFFFFFFF: int(v) for k, v in zip(r.cpu().tolist(), c.cpu().tolist())}
-    assert got_rules == want_rules
-    np.testing.assert_allclose(got_sum.cpu().numpy(), want_sum, rtol=1e-9, atol=1e-3)
-    assert torch.unique(torch.cat(paths)).numel() == n
+    assert rep["status"] == 0
+    rows = out[:n].view(torch.int64).view(n, 8)
+    paths, perm = torch.sort(rows[:, 7])
+    assert bool((paths[1:] != paths[:-1]).all()), "path hashes not unique"
+    total = 0
+    for lo in range(0, 65536, 4096):
+        t = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"][lo:lo + 4096], axiom_base=lo)
+        total += len(t)
+        ref = torch.from_numpy(t.view(np.uint8).reshape(-1, 64)).cuda()
+        del t
+        rp = ref.view(torch.int64).view(-1, 8)[:, 7]
+        pos = torch.searchsorted(paths, rp).clamp_(max=n - 1)
+        assert bool((paths[pos] == rp).all()), f"shard {lo}: path hashes missing from the launch"
+        got = out[perm[pos]]
+        gm, rm = got.view(torch.float32).view(-1, 16)[:, :12], ref.view(torch.float32).view(-1, 16)[:, :12]
+        assert bool((gm == rm).all()), f"shard {lo}: transforms differ"
+        gi, ri = got.view(torch.int32).view(-1, 16)[:, 12:14], ref.view(torch.int32).view(-1, 16)[:, 12:14]
+        assert bool((gi == ri).all()), f"shard {lo}: rule or custom attribute differs"
+        del ref, rp, pos, got, gm, rm, gi, ri
+    assert total == n
+    eng.release()
+
+
+@pytest.mark.parametrize("scene", ["city_4096", "mixed_4096"])
+def test_lbvh_full_size_bit_exact(scene):
+    """The LBVH over every terminal of the full city (5.86M leaves; 30-bit
+    Morton cells of 3.2 m hold many terminals, so 85% of neighbouring sorted
+    keys share their Morton code and go through the tie fix) and of a
+    4,096-axiom mix (9.4M leaves, 93% shared) against the restatement: keys,
+    leaf order, topology, leaf parents and boxes bit for bit."""
+    if scene == "city_4096":
+        b, bounds = scenes.city(4096), (-50.0, -50.0, -1.0, 3250.0, 3250.0, 400.0)
+    else:
+        b = scenes.mixed(4096)
+        bounds = None
+    eng, out, got, rep = _run(b, node_capacity=1 << 24, max_terminals=1 << 24)
+    assert rep["status"] == 0
+    n = len(got)
+    if bounds is None:
+        c = np.stack([got["m"][:, 3], got["m"][:, 7], got["m"][:, 11]], 1)
+        bounds = tuple(float(v) for v in c.min(0) - 1.0) + tuple(float(v) for v in c.max(0) + 1.0)
+    nodes, lp, aabb, lt, keys = oracle.lbvh(got, bounds)
+    runs = int((keys[1:] >> 34 == keys[:-1] >> 34).sum())
+    assert runs > n // 4, "the scene should exercise the tie fix"
+    bv = eng.lbvh(out, n, bounds)
+    torch.cuda.synchronize()
+    assert np.array_equal(bv["keys"].cpu().numpy().view(np.uint64), keys), "Morton keys differ"
+    assert np.array_equal(bv["leafTerminal"].cpu().numpy().view(np.uint32), lt), "leaf order differs"
+    assert np.array_equal(bv["nodes"].cpu().numpy(), nodes), "topology differs"
+    assert np.array_equal(bv["leafParents"].cpu().numpy().view(np.uint32), lp)
+    assert np.array_equal(bv["aabbs"].cpu().numpy().view(np.uint32), aabb.view(np.uint32)), "boxes differ"
     eng.release()
 
 
@@ -360,6 +394,48 @@ def test_derive_to_host_matches_device_derive(scene):
         _assert_same(h_out[:n].numpy().reshape(-1).view(G.TERMINAL_DT), ref)
     out, n2, _ = eng.execute(b["axioms"], capacity=cap)
     assert n2 == n
+    eng.release()
+
+
+def test_per_axiom_form_matches_batched_in_a_graph():
+    """pga_derive_per_axiom on 256 city buildings: eagerly and captured in a
+    CUDA graph (256 launches and appends, no host read-back), the same records
+    as pga_derive in axiom order; then an output overflow is a status."""
+    b = scenes.city(256)
+    ref = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"])
+    cap = len(ref)
+    eng = _engine(b["entries"])
+    d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).cuda()
+    out = torch.zeros((cap, 64), dtype=torch.uint8, device="cuda")
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None, out.data_ptr(), cap, count.data_ptr(), stream=s,
+                       plain="per_axiom")
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    assert eng.report()["status"] == 0 and int(count.item()) == cap
+    from operatorgraph_gb300.engine import terminals_to_numpy
+
+    got = terminals_to_numpy(out, cap)
+    _assert_same(got, ref)
+    # axiom order: each axiom's records follow the previous axiom's
+    want_first = oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"][:1])
+    _assert_same(got[:len(want_first)], want_first)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None, out.data_ptr(), cap, count.data_ptr(),
+                       stream=torch.cuda.current_stream(), plain="per_axiom")
+    out.zero_()
+    count.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert eng.report()["status"] == 0 and int(count.item()) == cap
+    _assert_same(terminals_to_numpy(out, cap), ref)
+    del g
+    out2, n, rep = eng.execute(b["axioms"], capacity=cap // 2, plain="per_axiom", check=False)
+    assert rep["status"] == 2 and n == cap
     eng.release()
 
 
