@@ -312,7 +312,8 @@ PgaStatus pga_engine_levels(PgaEngine* engine, void* stream, uint64_t* starts, u
 /* Replaces ContextSensitivity::GPU::BVHConstructor::construct(min, max)
  * (include/pga/core/GPUBVHConstructor.cuh:265-331), applied to terminal boxes:
  * 30-bit Morton codes of the terminal centres in `bounds`, radix sort,
- * Karras topology and bottom-up AABB refit. `bounds` is a host pointer. */
+ * Karras topology and bottom-up AABB refit. `bounds` is a host pointer.
+ * 2 <= n <= maxTerminals and n < 2^30. */
 PgaStatus pga_lbvh_build(PgaEngine* engine, const PgaTerminal* dTerminals, uint64_t n,
                          const PgaBounds* bounds, const PgaLbvh* out, void* stream);
 
@@ -321,7 +322,7 @@ PgaStatus pga_lbvh_build(PgaEngine* engine, const PgaTerminal* dTerminals, uint6
  * dCount is a device pointer, typically the one pga_derive wrote, so a
  * derivation, its LBVH and its adjoint can be captured in one CUDA graph with
  * no host read-back between them.  `capacity` (2 <= capacity <= maxTerminals,
- * below 2^31) sizes the launches and the radix sort, which orders `capacity`
+ * below 2^30) sizes the launches and the radix sort, which orders `capacity`
  * keys: out->keys[count, capacity) holds padding (all ones) after the real
  * keys.  The tree and leaf arrays are those of pga_lbvh_build for `count`
  * leaves, bit for bit; a count below 2 builds no tree. */

@@ -10,10 +10,12 @@
 //    `(code << 32) | j` with j replaced by that deterministic position;
 //  * AABBs start from -FLT_MAX instead of FLT_MIN (AABB.cuh:20) and a fence
 //    orders each node's AABB store before its parent's arrival counter.
+// The reference sorts with thrust::sort (GPUBVHConstructor.cuh:311-312); here
+// the sort is this file's own onesweep radix sort (see k_onesweep).
 #include <cuda_runtime.h>
 
 #include <cfloat>
-#include <cub/device/device_radix_sort.cuh>
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -68,6 +70,30 @@ __device__ __forceinline__ unsigned long long leaf_count(const unsigned long lon
   return dN ? min(*dN, n) : n;
 }
 
+// The radix sort orders the keys' top bits [kSortLowBit, 64) only (the Morton
+// code and the path hash's top 10 bits): four passes of 10-bit digits.
+constexpr int kSortLowBit = 24;
+constexpr int kRadixBits = 10;
+constexpr uint32_t kBins = 1u << kRadixBits;
+constexpr int kSortPasses = (64 - kSortLowBit) / kRadixBits;
+static_assert(kSortLowBit + kSortPasses * kRadixBits == 64, "the passes cover bits [kSortLowBit, 64)");
+
+// Histogram of one digit of a warp's 32 keys into shared memory: one add for
+// the whole warp when every lane has the same digit (the Morton code's high
+// digits, for neighbouring terminals), else one add per lane.
+__device__ __forceinline__ void hist_add(uint32_t* h, uint32_t d, bool valid) {
+  const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
+  const unsigned same = __ballot_sync(0xFFFFFFFFu, valid && d == d0);
+  if (same == 0xFFFFFFFFu) {
+    if ((threadIdx.x & 31u) == 0) atomicAdd(h + d0, 32u);
+  } else if (valid) {
+    atomicAdd(h + d, 1u);
+  }
+}
+
+// generateMortonCodes (GPUBVHConstructor.cuh:66-86) on terminal centres.
+// Also writes each terminal's AABB (6 floats, terminal order) while its record
+// is in registers.
 // With a device count, the keys in [count, capacity) are padding: all ones,
 // after every real key in the stable radix sort (a real key can equal it only
 // in the sorted top bits, and it comes first there by input order).
@@ -103,21 +129,259 @@ __global__ void __launch_bounds__(kLbvhThreads) k_morton(const PgaTerminal* __re
   vals[i] = (uint32_t)i;
 }
 
+// The four digit histograms of keys [0, n) (kSortPasses x kBins, zeroed
+// before the launch): each block counts a contiguous run of keys into shared
+// memory, kHistUnroll keys per thread in flight, then adds its nonzero bins.
+constexpr int kHistThreads = 512;
+constexpr int kHistUnroll = 4;
+__global__ void __launch_bounds__(kHistThreads) k_digit_hist(const unsigned long long* __restrict__ keys,
+                                                             unsigned long long n, uint32_t* __restrict__ hist) {
+  __shared__ uint32_t sh[kSortPasses * kBins];
+  for (uint32_t k = threadIdx.x; k < kSortPasses * kBins; k += kHistThreads) sh[k] = 0u;
+  __syncthreads();
+  const unsigned long long per = (n + gridDim.x - 1) / gridDim.x;
+  const unsigned long long lo = min(n, (unsigned long long)blockIdx.x * per), hi = min(n, lo + per);
+  // every lane of a warp runs the same iterations (hist_add is warp-wide)
+  for (unsigned long long i0 = lo; i0 < hi; i0 += (unsigned long long)kHistThreads * kHistUnroll) {
+    unsigned long long key[kHistUnroll];
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; u++) {
+      const unsigned long long i = i0 + (unsigned long long)u * kHistThreads + threadIdx.x;
+      key[u] = i < hi ? __ldcs(keys + i) : 0ull;
+    }
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; u++) {
+      const bool valid = i0 + (unsigned long long)u * kHistThreads + threadIdx.x < hi;
+#pragma unroll
+      for (int q = 0; q < kSortPasses; q++)
+        hist_add(sh + q * kBins, (uint32_t)(key[u] >> (kSortLowBit + q * kRadixBits)) & (kBins - 1u), valid);
+    }
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < kSortPasses * kBins; k += kHistThreads)
+    if (sh[k] != 0u) atomicAdd(hist + k, sh[k]);
+}
+
+// Exclusive scans of the four digit histograms: gBase[q][d] = where digit d's
+// keys start in pass q's output.  One block of kBins threads.
+__global__ void __launch_bounds__(kBins) k_sort_bases(const uint32_t* __restrict__ hist, uint32_t* __restrict__ gBase) {
+  __shared__ uint32_t warpSum[kBins / 32];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (int q = 0; q < kSortPasses; q++) {
+    const uint32_t v = hist[q * kBins + threadIdx.x];
+    uint32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= (uint32_t)d) x += y;
+    }
+    if (lane == 31) warpSum[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (uint32_t w = 0; w < warp; w++) before += warpSum[w];
+    gBase[q * kBins + threadIdx.x] = before + x - v;
+    __syncthreads();
+  }
+}
+
+// One pass of the radix sort ("onesweep", Adinets & Merrill 2022), stable:
+// keys and values of [0, n) ordered by digit (key >> shift) & (kBins - 1).
+// A block takes the next tile of kSortTile keys from an atomic counter, so a
+// tile's predecessors were taken by blocks that started earlier.  Its warps
+// rank their keys by digit in input order (warp-private 16-bit histograms;
+// the lanes sharing a digit found with one ballot per digit bit), the block publishes its per-digit counts and
+// finds each digit's count over all earlier tiles by decoupled look-back:
+// walking back over their published words until one carries an inclusive
+// prefix.  Keys then go to shared memory in digit order and out in contiguous
+// runs per digit.  A look-back wait gives up after spinLimit polls, raising
+// PGA_ERR_TIMEOUT in *err (the order is then unspecified).
+constexpr int kSortThreads = 512;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortItems = 10;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;
+constexpr uint32_t kHistStride = kBins + 16;  // u16 per warp histogram; bin kBins counts keys past n
+constexpr uint32_t kFlagAggregate = 1u << 30, kFlagPrefix = 2u << 30, kCountMask = (1u << 30) - 1u;
+constexpr int kLookback = 8;  // predecessor words loaded at once by a look-back step
+constexpr size_t kOnesweepSmem =
+    (size_t)kSortTile * 8 + (size_t)kSortTile * 4 + (size_t)kSortWarps * kHistStride * 2 + (size_t)kBins * 8;
+
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(kSortThreads, 2)
+    k_onesweep(const unsigned long long* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+               unsigned long long* __restrict__ keysOut, uint32_t* __restrict__ valsOut, unsigned long long n,
+               uint32_t shift, const uint32_t* __restrict__ gBase, uint32_t* status, uint32_t* tileCounter, int* err,
+               uint32_t spinLimit) {
+  extern __shared__ __align__(16) unsigned char smem_sort[];
+  unsigned long long* sKeys = reinterpret_cast<unsigned long long*>(smem_sort);
+  uint32_t* sVals = reinterpret_cast<uint32_t*>(sKeys + kSortTile);
+  uint16_t* sHist = reinterpret_cast<uint16_t*>(sVals + kSortTile);
+  uint32_t* sStart = reinterpret_cast<uint32_t*>(sHist + kSortWarps * kHistStride);
+  int32_t* sDst = reinterpret_cast<int32_t*>(sStart + kBins);
+  __shared__ uint32_t sTile;
+  __shared__ uint32_t sWarpSum[kSortWarps];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) sTile = atomicAdd(tileCounter, 1u);
+  uint16_t* hist = sHist + warp * kHistStride;
+  for (uint32_t k = lane; k < kHistStride / 2; k += 32) reinterpret_cast<uint32_t*>(hist)[k] = 0u;
+  __syncthreads();
+  const uint32_t tile = sTile;
+  const unsigned long long tileBase = (unsigned long long)tile * kSortTile;
+  const unsigned long long warpBase = tileBase + (unsigned long long)warp * (32u * kSortItems);
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  unsigned long long key[kSortItems];
+  uint32_t rank[kSortItems];
+#pragma unroll
+  for (int k = 0; k < kSortItems; k++) {
+    const unsigned long long i = warpBase + (unsigned)k * 32u + lane;
+    key[k] = i < n ? __ldcs(keysIn + i) : 0ull;
+  }
+#pragma unroll
+  for (int k = 0; k < kSortItems; k++) {
+    const unsigned long long i = warpBase + (unsigned)k * 32u + lane;
+    const bool valid = i < n;
+    const uint32_t d = valid ? (uint32_t)(key[k] >> shift) & (kBins - 1u) : kBins;
+    // the lanes with the same digit (and validity): one ballot per digit bit
+    unsigned peers = __ballot_sync(0xFFFFFFFFu, valid);
+    if (!valid) peers = ~peers;
+#pragma unroll
+    for (int bit = 0; bit < kRadixBits; bit++) {
+      const unsigned on = __ballot_sync(0xFFFFFFFFu, (d >> bit) & 1u);
+      peers &= ((d >> bit) & 1u) ? on : ~on;
+    }
+    const int leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if ((int)lane == leader) {
+      old = hist[d];
+      hist[d] = (uint16_t)(old + __popc(peers));
+    }
+    old = __shfl_sync(0xFFFFFFFFu, old, leader);
+    rank[k] = old + __popc(peers & lt);
+    __syncwarp();
+  }
+  __syncthreads();
+  // Thread t owns bins 2t and 2t + 1: the warps' exclusive prefixes in place,
+  // the tile's count of each bin, published for the later tiles.
+  uint32_t tot[2];
+  uint32_t* st = status + (size_t)tile * kBins;
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const uint32_t d = 2u * threadIdx.x + q;
+    uint32_t run = 0;
+    for (int w = 0; w < kSortWarps; w++) {
+      uint16_t* h = sHist + w * kHistStride;
+      const uint32_t c = h[d];
+      h[d] = (uint16_t)run;
+      run += c;
+    }
+    tot[q] = run;
+    st_relaxed(st + d, (tile == 0 ? kFlagPrefix : kFlagAggregate) | run);
+  }
+  // The tile's bin starts: an exclusive scan of the bins in order.
+  {
+    const uint32_t v = tot[0] + tot[1];
+    uint32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= (uint32_t)d) x += y;
+    }
+    if (lane == 31) sWarpSum[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (uint32_t w = 0; w < warp; w++) before += sWarpSum[w];
+    sStart[2u * threadIdx.x] = before + x - v;
+    sStart[2u * threadIdx.x + 1] = before + x - v + tot[0];
+  }
+  // Decoupled look-back: each bin's count over the earlier tiles.  The words
+  // of kLookback predecessors are loaded at once (independent loads), then
+  // summed nearest first up to the first inclusive prefix; a word not yet
+  // published stops the sum there and is polled again.
+#pragma unroll 1
+  for (int q = 0; q < 2; q++) {
+    const uint32_t d = 2u * threadIdx.x + q;
+    uint32_t prefix = 0;
+    if (tile > 0) {
+      long long p = (long long)tile - 1;
+      uint32_t spins = 0;
+      while (p >= 0) {
+        uint32_t w[kLookback];
+#pragma unroll
+        for (int k = 0; k < kLookback; k++)
+          w[k] = p - k >= 0 ? ld_relaxed(status + (size_t)(p - k) * kBins + d) : kFlagPrefix;
+        int used = 0;
+        bool done = false, stalled = false;
+#pragma unroll
+        for (int k = 0; k < kLookback; k++) {
+          if (done || stalled) continue;
+          if ((w[k] >> 30) == 0u) {
+            stalled = true;
+            continue;
+          }
+          prefix += w[k] & kCountMask;
+          used++;
+          if ((w[k] & kFlagPrefix) != 0u) done = true;
+        }
+        if (done) break;
+        p -= used;
+        if (stalled) {
+          if (++spins > spinLimit) {
+            atomicCAS(err, 0, (int)PGA_ERR_TIMEOUT);
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      st_relaxed(st + d, kFlagPrefix | (prefix + (q ? tot[1] : tot[0])));
+    }
+    sDst[d] = (int32_t)(__ldg(gBase + d) + prefix);
+  }
+  __syncthreads();
+  // The tile in digit order in shared memory.
+#pragma unroll
+  for (int k = 0; k < kSortItems; k++) {
+    const unsigned long long i = warpBase + (unsigned)k * 32u + lane;
+    if (i < n) {
+      const uint32_t d = (uint32_t)(key[k] >> shift) & (kBins - 1u);
+      const uint32_t pos = sStart[d] + hist[d] + rank[k];
+      sKeys[pos] = key[k];
+      sVals[pos] = __ldcs(valsIn + i);
+    }
+  }
+  __syncthreads();
+  // Out: consecutive positions of one digit go to consecutive places.
+  const uint32_t count = (uint32_t)min((unsigned long long)kSortTile, n - tileBase);
+  for (uint32_t p = threadIdx.x; p < count; p += kSortThreads) {
+    const unsigned long long kk = sKeys[p];
+    const uint32_t d = (uint32_t)(kk >> shift) & (kBins - 1u);
+    const long long o = (long long)sDst[d] + (long long)(p - sStart[d]);
+    if (o < 0 || (unsigned long long)o >= n) continue;  // only after a look-back that gave up
+    keysOut[o] = kk;
+    valsOut[o] = sVals[p];
+  }
+}
+
 __device__ __forceinline__ uint64_t term_path(const PgaTerminal* t, uint32_t i) {
   const uint2 v = __ldg(reinterpret_cast<const uint2*>(&t[i].path));
   return ((uint64_t)v.y << 32) | v.x;
 }
 
-// The radix sort orders the keys' top bits [kSortLowBit, 64) only (the Morton
-// code and the path hash's top 10 bits), which leaves runs of equal top bits
-// in input order.  Each such run is ordered here by insertion: by the whole
+// The radix sort orders the keys' top bits [kSortLowBit, 64) only, which
+// leaves runs of equal top bits in input order.  Each such run is ordered
+// here by insertion: by the whole
 // key (the Morton code and the path hash's top 34 bits), then, for equal keys,
 // by the full path hash, then by terminal index, keys and values moving
 // together.  The result is the order a full 64-bit sort plus tie fix gives:
 // lexicographic in (Morton code, path hash, terminal).  Runs are short; a
 // terminal record is read only for two equal 64-bit keys.
-constexpr int kSortLowBit = 24;  // 5 radix passes of 8 bits instead of 8
-
 __global__ void k_fix_ties(unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
                            const PgaTerminal* __restrict__ t, unsigned long long cap,
                            const unsigned long long* __restrict__ dN) {
@@ -339,17 +603,21 @@ __global__ void __launch_bounds__(kLbvhThreads) k_refit(const float* __restrict_
 
 using namespace pga;
 
+// Sort scratch: the digit histograms, the passes' tile counters and look-back
+// words (zeroed by one memset per build), then the digit bases.
+static unsigned long long sort_tiles(unsigned long long n) { return (n + kSortTile - 1) / kSortTile; }
+
 extern "C" size_t pga_lbvh_temp_bytes(uint64_t n) {
-  size_t bytes = 0;
-  cub::DeviceRadixSort::SortPairs(nullptr, bytes, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
-                                  (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)(n ? n : 1), 0, 64);
-  return bytes ? bytes : 16;
+  const unsigned long long tiles = sort_tiles(n ? n : 1);
+  return (size_t)(kSortPasses * kBins + 64 + (unsigned long long)kSortPasses * tiles * kBins + kSortPasses * kBins) *
+         sizeof(uint32_t);
 }
 
 namespace pga {
 
 // Scratch of one build: keys, two value arrays, arrival counters, leaf boxes
-// (terminal and sorted order), node ranges and the radix sort's temp storage.
+// (terminal and sorted order), node ranges, the radix sort's scratch, and the
+// word a sort wait that gives up raises PGA_ERR_TIMEOUT in.
 struct LbvhScratch {
   unsigned long long* keysA;
   uint32_t* valsA;
@@ -360,10 +628,17 @@ struct LbvhScratch {
   int2* nodeRange;
   void* sortTemp;
   size_t sortTempBytes;
+  int* err;
 };
 
-// The five launches of a build over `cap` leaves, or over min(*dN, cap) when
-// dN is a device count (then `cap` sizes the grids and the sort).
+// Polls of a look-back wait before it gives up (each followed by a 64 ns sleep).
+constexpr uint32_t kSortSpinLimit = 1u << 22;
+
+// The launches of a build over `cap` leaves, or over min(*dN, cap) when dN is
+// a device count (then `cap` sizes the grids and the sort): Morton codes, the
+// digit histograms and bases, four sort passes (keys ping-pong
+// between out->keys and keysA, ending in out->keys), the tie fix, Karras and
+// the refit.
 static PgaStatus launch_lbvh(const PgaTerminal* t, unsigned long long cap, const unsigned long long* dN,
                              const PgaBounds* bounds, const PgaLbvh* out, const LbvhScratch& w, cudaStream_t s) {
   Bounds b;
@@ -371,17 +646,47 @@ static PgaStatus launch_lbvh(const PgaTerminal* t, unsigned long long cap, const
     b.mn[k] = bounds->min[k];
     b.sz[k] = bounds->max[k] - bounds->min[k];
   }
+  const unsigned long long tiles = sort_tiles(cap);
+  if (pga_lbvh_temp_bytes(cap) > w.sortTempBytes) {
+    set_error("LBVH: sort scratch too small for " + std::to_string(cap) + " keys");
+    return PGA_ERR_INVALID_ARGUMENT;
+  }
+  uint32_t* hist = static_cast<uint32_t*>(w.sortTemp);
+  uint32_t* counters = hist + kSortPasses * kBins;
+  uint32_t* status = counters + 64;
+  uint32_t* gBase = status + (size_t)kSortPasses * tiles * kBins;
+  PGA_CUDA_TRY(cudaMemsetAsync(hist, 0, (size_t)(gBase - hist) * sizeof(uint32_t), s));
+  int dev = 0, sms = 0;
+  PGA_CUDA_TRY(cudaGetDevice(&dev));
+  PGA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const unsigned blocks = (unsigned)((cap + kLbvhThreads - 1) / kLbvhThreads);
   unsigned long long* keys = (unsigned long long*)out->keys;
-  k_morton<<<blocks, kLbvhThreads, 0, s>>>(t, cap, dN, b, w.keysA, w.valsA, w.leafBox);
+  k_morton<<<blocks, kLbvhThreads, 0, s>>>(t, cap, dN, b, keys, w.valsA, w.leafBox);
   PGA_CUDA_TRY(cudaGetLastError());
-  size_t temp = w.sortTempBytes;
-  PGA_CUDA_TRY(cub::DeviceRadixSort::SortPairs(w.sortTemp, temp, w.keysA, keys, w.valsA, w.valsB, (int64_t)cap,
-                                               kSortLowBit, 64, s));
-  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>(keys, w.valsB, t, cap, dN);
+  const unsigned histBlocks =
+      (unsigned)std::min<unsigned long long>((cap + kHistThreads - 1) / kHistThreads, (unsigned long long)sms * 4);
+  k_digit_hist<<<histBlocks, kHistThreads, 0, s>>>(keys, cap, hist);
+  PGA_CUDA_TRY(cudaGetLastError());
+  k_sort_bases<<<1, kBins, 0, s>>>(hist, gBase);
+  PGA_CUDA_TRY(cudaGetLastError());
+  PGA_CUDA_TRY(cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOnesweepSmem));
+  unsigned long long* kIn = keys;
+  unsigned long long* kOut = w.keysA;
+  uint32_t* vIn = w.valsA;
+  uint32_t* vOut = w.valsB;
+  for (int q = 0; q < kSortPasses; q++) {
+    k_onesweep<<<(unsigned)tiles, kSortThreads, kOnesweepSmem, s>>>(
+        kIn, vIn, kOut, vOut, cap, (uint32_t)(kSortLowBit + q * kRadixBits), gBase + q * kBins,
+        status + (size_t)q * tiles * kBins, counters + q, w.err, kSortSpinLimit);
+    PGA_CUDA_TRY(cudaGetLastError());
+    std::swap(kIn, kOut);
+    std::swap(vIn, vOut);
+  }
+  static_assert(kSortPasses % 2 == 0, "an even number of passes ends in out->keys and valsA");
+  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>(keys, w.valsA, t, cap, dN);
   PGA_CUDA_TRY(cudaGetLastError());
   k_karras<<<blocks, kLbvhThreads, 0, s>>>(keys, (long long)cap, dN, out->nodes, out->leafParents, out->leafTerminal,
-                                           w.valsB, w.leafBox, w.sortedBox, w.nodeRange, w.arrival);
+                                           w.valsA, w.leafBox, w.sortedBox, w.nodeRange, w.arrival);
   PGA_CUDA_TRY(cudaGetLastError());
   k_refit<<<blocks, kLbvhThreads, 0, s>>>(w.sortedBox, (long long)cap, dN, out->nodes, w.nodeRange, out->leafParents,
                                           w.arrival, out->aabbs);
@@ -391,7 +696,7 @@ static PgaStatus launch_lbvh(const PgaTerminal* t, unsigned long long cap, const
 
 static LbvhScratch engine_scratch(PgaEngine* e) {
   return LbvhScratch{e->dKeysA,     e->dValsA,    e->dValsB,    e->dArrival,     e->dLeafAabb,
-                     e->dLeafAabbSorted, e->dNodeRange, e->dSortTemp, e->sortTempBytes};
+                     e->dLeafAabbSorted, e->dNodeRange, e->dSortTemp, e->sortTempBytes, &e->dState->status};
 }
 
 static bool lbvh_out_ok(const PgaLbvh* out) {
@@ -406,8 +711,8 @@ extern "C" PgaStatus pga_lbvh_build(PgaEngine* e, const PgaTerminal* dTerminals,
     set_error("pga_lbvh_build: null argument");
     return PGA_ERR_INVALID_ARGUMENT;
   }
-  if (n < 2 || n > e->cfg.maxTerminals || n > 0x7FFFFFFFull) {
-    set_error("pga_lbvh_build: need 2 <= n <= maxTerminals (and < 2^31)");
+  if (n < 2 || n > e->cfg.maxTerminals || n >= (1ull << 30)) {
+    set_error("pga_lbvh_build: need 2 <= n <= maxTerminals (and < 2^30)");
     return PGA_ERR_INVALID_ARGUMENT;
   }
   return launch_lbvh(dTerminals, n, nullptr, bounds, out, engine_scratch(e), (cudaStream_t)stream);
@@ -420,8 +725,8 @@ extern "C" PgaStatus pga_lbvh_build_counted(PgaEngine* e, const PgaTerminal* dTe
     set_error("pga_lbvh_build_counted: null argument");
     return PGA_ERR_INVALID_ARGUMENT;
   }
-  if (capacity < 2 || capacity > e->cfg.maxTerminals || capacity > 0x7FFFFFFFull) {
-    set_error("pga_lbvh_build_counted: need 2 <= capacity <= maxTerminals (and < 2^31)");
+  if (capacity < 2 || capacity > e->cfg.maxTerminals || capacity >= (1ull << 30)) {
+    set_error("pga_lbvh_build_counted: need 2 <= capacity <= maxTerminals (and < 2^30)");
     return PGA_ERR_INVALID_ARGUMENT;
   }
   return launch_lbvh(dTerminals, capacity, (const unsigned long long*)dCount, bounds, out, engine_scratch(e),
@@ -517,10 +822,12 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
   off += align256(n * sizeof(int2));
   void* sortTemp = base + off;
   off += align256(temp);
+  int* err = reinterpret_cast<int*>(base + off);  // a sort wait that gives up marks it (unreported)
+  off += 256;
   if (off > kStaticScratchBytes) {
     set_error("pga_lbvh_build_static: fixed scratch too small for the radix sort of " + std::to_string(n) + " keys");
     return PGA_ERR_INVALID_ARGUMENT;
   }
-  const LbvhScratch w{keysA, valsA, valsB, arrival, leafBox, sortedBox, nodeRange, sortTemp, temp};
+  const LbvhScratch w{keysA, valsA, valsB, arrival, leafBox, sortedBox, nodeRange, sortTemp, temp, err};
   return launch_lbvh(dTerminals, n, nullptr, bounds, out, w, (cudaStream_t)stream);
 }
