@@ -419,29 +419,34 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
-def mixed_step(mx, mout, count, dev, n_expected):
+def mixed_step(n_ax, mout, count, dev, n_expected):
     """The mixed batch as one differentiable step captured in one CUDA graph:
     derivation with the tape recorded, LBVH over all its terminals (the leaf
-    count read on the device, pga_lbvh_build_counted), and the adjoint to the
-    65,536 axiom sizes for the loss L = |M|^2 / 2, whose dL/dM = M the adjoint
-    reads in place from the terminal records (pga_adjoint_strided, stride 16
-    floats).  The batch's grammars take constant parameters, so the sizes are
-    its continuous inputs; the axioms are seeded grouped by root entry.  The
-    parts are also timed one by one, eagerly."""
+    count read on the device, pga_lbvh_build_counted), and the adjoint for the
+    loss L = |M|^2 / 2, whose dL/dM = M the adjoint reads in place from the
+    terminal records (pga_adjoint_strided, stride 16 floats), to every DynParam
+    and axiom size: the batch with parameter blocks (scenes.mixed(blocks=True):
+    each building's floor height, tile width and window wall widths, each
+    sponge's split factors; the same terminals as the scalar batch).  The
+    axioms are seeded grouped by root entry.  The parts are also timed one by
+    one, eagerly."""
     import torch
 
     from operatorgraph_gb300.engine import Engine
 
     res = {}
-    n_ax = len(mx["axioms"])
+    mx = scenes.mixed(n_ax, blocks=True)
     mcap = mout.shape[0]
-    et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True, group_axioms=True)
+    et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True, group_axioms=True,
+                block_stride=mx["block_stride"])
     d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
+    d_blk = torch.from_numpy(mx["blocks"]).to(dev)
+    g_blk = torch.empty_like(d_blk)
     g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
     m_rows = mout.view(torch.float32).view(mcap, 16)
     # LBVH bounds: the box of the terminal centres of a first derivation, one
     # metre wider on every side.
-    et.derive_raw(d_mx.data_ptr(), n_ax, None, mout.data_ptr(), mcap, count.data_ptr())
+    et.derive_raw(d_mx.data_ptr(), n_ax, d_blk.data_ptr(), mout.data_ptr(), mcap, count.data_ptr())
     torch.cuda.synchronize()
     rep = et.report()
     assert rep["status"] == 0, rep
@@ -461,11 +466,11 @@ def mixed_step(mx, mout, count, dev, n_expected):
                 marks[k].record(st)
 
         mark(0)
-        et.derive_raw(d_mx.data_ptr(), n_ax, None, mout.data_ptr(), mcap, count.data_ptr(), stream=st)
+        et.derive_raw(d_mx.data_ptr(), n_ax, d_blk.data_ptr(), mout.data_ptr(), mcap, count.data_ptr(), stream=st)
         mark(1)
         bv = et.lbvh(mout, mcap, bounds, stream=st, count=count)
         mark(2)
-        et.adjoint_raw(mout.data_ptr(), None, 0, g_sz.data_ptr(), stream=st, grad_stride=16)
+        et.adjoint_raw(mout.data_ptr(), g_blk.data_ptr(), n_ax, g_sz.data_ptr(), stream=st, grad_stride=16)
         mark(3)
         return bv
 
@@ -501,27 +506,88 @@ def mixed_step(mx, mout, count, dev, n_expected):
     assert rep["status"] == 0, rep
     assert int(count.item()) == n
     assert bool(torch.isfinite(g_sz).all()) and float(g_sz.abs().max()) > 0
+    assert bool(torch.isfinite(g_blk).all()) and float(g_blk.abs().max()) > 0
     names = ("derive_tape", "lbvh", "adjoint")
     med = [statistics.median(x[k] for x in seg) for k in range(3)]
-    # Algorithmic bytes: derivation 64 B per terminal, its 8-B tape link and
-    # 48 B per axiom; LBVH 236 B per leaf (the 64-B record read, 52 B of tree
-    # written, five radix passes over 12-B key/value pairs read and written);
-    # adjoint as for the facades (per terminal 48 + 8 B, per item 2 x 64 + 2 x
-    # 24 B, 12 B per axiom size).
-    parts = [72.0 * n + 48.0 * n_ax, 236.0 * n, 56.0 * n + 176.0 * n_items + 12.0 * n_ax]
+    n_par = int(d_blk.numel())
+    # Algorithmic bytes, counted two ways.  This bench's count: derivation 64 B
+    # per terminal, its 8-B tape link and 48 B per axiom; LBVH 204 B per leaf
+    # (the 64-B record read, 52 B of tree written, four radix passes over 12-B
+    # key/value pairs read and written); adjoint per terminal 48 + 8 B, per
+    # item 2 x 64 + 2 x 24 B, 4 B per parameter and axiom size.  The
+    # reference-path formulas: B_fwd = 64 T + 32 A, B_lbvh = 108 T,
+    # B_adj = 112 T + 140 N + 4 P.
+    parts = [72.0 * n + 48.0 * n_ax, 204.0 * n, 56.0 * n + 176.0 * n_items + 4.0 * (n_par + 3 * n_ax)]
+    parts_8d = [64.0 * n + 32.0 * n_ax, 108.0 * n, 112.0 * n + 140.0 * n_items + 4.0 * (n_par + 3 * n_ax)]
     peak, _ = read_peaks()
     step_ms = statistics.median(ts)
     res["mixed65536_step_graph_ms"] = step_ms
     res["mixed65536_step_items"] = n_items
+    res["mixed65536_step_params"] = n_par
     res["mixed65536_step_segments_ms"] = {k: v for k, v in zip(names, med)}
     res["mixed65536_step_segments_gbs"] = {k: b / (v * 1e-3) / 1e9 for k, b, v in zip(names, parts, med)}
     res["mixed65536_step_bytes"] = sum(parts)
     res["mixed65536_step_gbs"] = sum(parts) / (step_ms * 1e-3) / 1e9
     res["mixed65536_step_roofline_frac"] = res["mixed65536_step_gbs"] / peak
+    res["mixed65536_step_bytes_formula"] = sum(parts_8d)
+    res["mixed65536_step_roofline_frac_formula"] = sum(parts_8d) / (step_ms * 1e-3) / 1e9 / peak
+    # the forward + adjoint step alone (no LBVH), by the formulas
+    fa_ms = med[0] + med[2]
+    res["mixed65536_fwd_adjoint_ms"] = fa_ms
+    res["mixed65536_fwd_adjoint_roofline_frac_formula"] = (parts_8d[0] + parts_8d[2]) / (fa_ms * 1e-3) / 1e9 / peak
     res["mixed65536_step_lbvh_bounds"] = [round(v, 3) for v in bounds]
     del g, bv
     et.release()
     return res
+
+
+def c4_step(f, dev):
+    """Differentiable facade fitting (1024 facades, 16 parameters each): the
+    target is the same trees with every parameter moved by N(0, 0.02) and
+    clamped so no branch flips; one step is the forward derivation through
+    torch.autograd, the SSE of terminal centres and extents matched by path,
+    and the backward pass (the adjoint), then an Adam update.  Timed with CUDA
+    events around whole steps."""
+    import torch
+
+    from operatorgraph_gb300.autograd import PathTarget, axioms_tensor, derive_transforms
+    from operatorgraph_gb300.engine import Engine
+
+    n_f = len(f["axioms"]) * 384
+    ef = Engine(f["entries"], node_capacity=1 << 20, max_terminals=1 << 20, block_stride=f["block_stride"],
+                record_tape=True)
+    d_ax = axioms_tensor(f["axioms"], dev)
+    sizes = torch.tensor(f["axioms"]["size"], dtype=torch.float32, device=dev)
+    tb = torch.tensor(scenes.facade_target_params(f["blocks"]), dtype=torch.float32, device=dev)
+    Mt, pt = derive_transforms(ef, d_ax, tb, sizes, n_f)
+    target = PathTarget(Mt, pt)
+    blocks = torch.tensor(f["blocks"], dtype=torch.float32, device=dev, requires_grad=True)
+    opt = torch.optim.Adam([blocks], lr=2e-3)
+
+    def step():
+        opt.zero_grad()
+        M, paths = derive_transforms(ef, d_ax, blocks, sizes, n_f)
+        loss = target.sse(M, paths, check=False)
+        loss.backward()
+        opt.step()
+        return loss.detach()
+
+    losses = [float(step()) for _ in range(3)]
+    ts = []
+    for _ in range(10):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        loss = step()
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+        losses.append(float(loss))
+    M, paths = derive_transforms(ef, d_ax, blocks.detach(), sizes, n_f)
+    target.sse(M, paths, check=True)  # still the target's trees
+    ef.release()
+    return {"facades1024_c4_step_ms": statistics.median(ts), "facades1024_c4_loss_first": losses[0],
+            "facades1024_c4_loss_last": losses[-1], "facades1024_c4_steps": len(losses)}
 
 
 def extras(eng, batch, out, n_term, dev, stream, flush):
@@ -678,6 +744,7 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["facades1024_adjoint_roofline_frac"] = res["facades1024_adjoint_gbs"] / peak
     res["facades1024_fwd_adjoint_step_ms"] = res["facades1024_forward_tape_ms"] + res["facades1024_adjoint_ms"]
     ef.release()
+    res.update(c4_step(f, dev))
     del out
     # The mixed batch: 65,536 axioms (40 % Menger depth 1-3, 40 % city
     # buildings, 20 % random grammars), about 152M terminals in one launch.
@@ -707,7 +774,7 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["mixed65536_terminals"] = n_mx
     res["mixed65536_ms"] = statistics.median(ts)
     res["mixed65536_terminals_per_s"] = n_mx / (res["mixed65536_ms"] * 1e-3)
-    res.update(mixed_step(mx, mout, count, dev, n_mx))
+    res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx))
     del mout
     # Forest: 4096 trees (Rotate with arbitrary angles, Replicate, Translate,
     # Scale: the general-frame kernels), about 13.4M terminals in one launch.

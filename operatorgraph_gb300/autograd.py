@@ -10,6 +10,12 @@ repetition counts, discards) is the one of this forward pass.
 
 The engine must be created with record_tape=True, and backward must run before
 the engine derives again (the tape holds one derivation).
+
+`PathTarget` holds a target derivation's terminal centres and extents keyed
+by derivation path, and `PathTarget.sse(M, paths)` is the fitting loss of
+differentiable facade fitting: the sum of squared errors of the centres
+(M[:, 3, 7, 11]) and the extents (the lengths of M's first three columns,
+the terminal's size along its own axes) over terminals matched by path.
 """
 import numpy as np
 import torch
@@ -56,3 +62,30 @@ def axioms_tensor(axioms, device="cuda"):
 def derive_transforms(engine, axioms, blocks, sizes, capacity):
     """Differentiable derivation: (M [n, 12], paths [n]) from blocks and axiom sizes."""
     return _Derive.apply(blocks, sizes, engine, axioms, capacity)
+
+
+def centres_extents(M):
+    """Terminal centres (n x 3) and extents (n x 3, the column lengths of the
+    3 x 3 part of model * scale(size)) of transforms M (n x 12)."""
+    c = M[:, [3, 7, 11]]
+    R = M.reshape(-1, 3, 4)[:, :, :3]
+    return c, torch.sqrt((R * R).sum(dim=1))
+
+
+class PathTarget:
+    """Centres and extents of a target derivation, keyed by derivation path."""
+
+    def __init__(self, M, paths):
+        order = torch.argsort(paths)
+        self.paths = paths[order]
+        self.c, self.e = centres_extents(M.detach()[order])
+
+    def sse(self, M, paths, check=True):
+        """Sum of squared errors of centres and extents against the target;
+        check=True verifies that the derivation has exactly the target's
+        paths (no branch, repetition count or discard changed)."""
+        order = torch.argsort(paths)
+        if check and not torch.equal(paths[order], self.paths):
+            raise ValueError("the derivation's paths differ from the target's")
+        c, e = centres_extents(M[order])
+        return ((c - self.c) ** 2).sum() + ((e - self.e) ** 2).sum()

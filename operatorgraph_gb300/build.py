@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 # access checked; a failed check raises PGA_ERR_INTERNAL instead of accessing).
 CHECKED = os.environ.get("PGA_CHECKS") == "1"
 LIB = os.path.join(HERE, "libpga_gb300_checked.so" if CHECKED else "libpga_gb300.so")
-SOURCES = ["derive.cu", "derive_gen.cu", "lbvh.cu", "mesh.cu"]
+SOURCES = ["derive.cu", "derive_gen.cu", "derive_blk.cu", "lbvh.cu", "mesh.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: no FMA contraction anywhere in the derivation path (the kernels
 # also use explicit round-to-nearest intrinsics); -ffp-contract=off for the

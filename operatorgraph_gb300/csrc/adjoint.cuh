@@ -30,6 +30,7 @@
 //  Generate   M[:, j] = R[:, j] s_j, M[:, 3] = t.
 
 namespace pga {
+inline namespace PGA_FRAMES_NS {
 
 struct Grad {
   float t[3], s[3];
@@ -696,7 +697,14 @@ __device__ __forceinline__ unsigned long long block_sum(unsigned long long v) {
 // or overflowed forward pass leaves the gradients zero (the engine report
 // keeps the forward's status; a tape too short for the terminals or a slot
 // map larger than its buffer raises PGA_ERR_NO_TAPE).
-__global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, unsigned long long numParamFloats,
+// The block build pins 2 blocks per SM (up to 128 registers): left free,
+// its register choice there came out at 80 with spills.
+#if PGA_INLINE_BLOCKS
+#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads, 2)
+#else
+#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads)
+#endif
+__global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned long long numParamFloats,
                                                       uint32_t numAxioms) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
@@ -837,8 +845,13 @@ __global__ void __launch_bounds__(kThreads) k_adjoint(DeriveArgs a, AdjArgs j, u
   }
 }
 
+// This build's adjoint kernel, for the host code.
+inline const void* adjoint_kernel() { return (const void*)k_adjoint; }
+
+}  // inline namespace PGA_FRAMES_NS
 }  // namespace pga
 
+#ifndef PGA_ADJOINT_DEVICE_ONLY
 extern "C" PgaStatus pga_adjoint_strided(PgaEngine* e, const float* dGradTerminals, uint32_t gradStride,
                                          float* dGradParams, uint32_t numBlocks, float* dGradAxiomSizes,
                                          void* stream) {
@@ -851,16 +864,16 @@ extern "C" PgaStatus pga_adjoint_strided(PgaEngine* e, const float* dGradTermina
     set_error("pga_adjoint_strided: gradStride must be at least 12 floats");
     return PGA_ERR_INVALID_ARGUMENT;
   }
-  if (!e->cfg.recordTape || !e->lastWasBatched || !e->dTermLinks || !e->lastOut) {
+  if (!e->cfg.recordTape || !e->lastWasBatched || !e->dTermLinks || !e->lastOut || !e->kernels.adjoint) {
     set_error("pga_adjoint: the last derivation was not a pga_derive on an engine created with recordTape = 1");
     return PGA_ERR_NO_TAPE;
   }
   if (e->adjointBlocks == 0) {
     // One cooperative launch: as many blocks as can be resident with the
     // engine's dynamic shared memory.
-    PGA_CUDA_TRY(cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes));
+    PGA_CUDA_TRY(cudaFuncSetAttribute(e->kernels.adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smemBytes));
     int perSM = 0;
-    PGA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_adjoint, kThreads, e->smemBytes));
+    PGA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, e->kernels.adjoint, kThreads, e->smemBytes));
     if (perSM < 1) {
       set_error("pga_adjoint: the adjoint kernel does not fit on an SM");
       return PGA_ERR_CUDA;
@@ -893,7 +906,7 @@ extern "C" PgaStatus pga_adjoint_strided(PgaEngine* e, const float* dGradTermina
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, (const void*)k_adjoint, args));
+  PGA_CUDA_TRY(cudaLaunchKernelExC(&cfg, e->kernels.adjoint, args));
   return PGA_OK;
 }
 
@@ -901,3 +914,4 @@ extern "C" PgaStatus pga_adjoint(PgaEngine* e, const float* dGradTerminals, floa
                                  float* dGradAxiomSizes, void* stream) {
   return pga_adjoint_strided(e, dGradTerminals, 12u, dGradParams, numBlocks, dGradAxiomSizes, stream);
 }
+#endif  // PGA_ADJOINT_DEVICE_ONLY

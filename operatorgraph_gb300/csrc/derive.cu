@@ -118,6 +118,10 @@ using namespace pga;
 
 namespace pga {
 FrameKernels general_frame_kernels();  // derive_gen.cu
+FrameKernels block_frame_kernels();    // derive_blk.cu
+inline namespace PGA_FRAMES_NS {
+inline const void* adjoint_kernel();   // this build's k_adjoint (adjoint.cuh, included below)
+}
 }
 
 // The instantiation of the persistent kernel for an engine: its frame build,
@@ -409,7 +413,18 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     delete e;
     return PGA_ERR_BAD_PARAM;
   }
-  e->kernels = e->generalFrames ? general_frame_kernels() : frame_kernels();
+  // Tables with block parameters (and no Rotate) run the build that reads
+  // them inline; the others keep this file's kernels.
+  bool blockParams = false;
+  for (const DevParam& p : e->hParams) blockParams = blockParams || p.type == PGA_PT_BLOCK;
+  if (e->generalFrames) {
+    e->kernels = general_frame_kernels();
+  } else if (blockParams) {
+    e->kernels = block_frame_kernels();
+  } else {
+    e->kernels = frame_kernels();
+    e->kernels.adjoint = adjoint_kernel();
+  }
   if (e->hParams.empty()) e->hParams.push_back(DevParam{0, 0.f, 0.f, 0});
   if (e->hSucc.empty()) e->hSucc.push_back(-1);
   if (e->hExpPool.empty()) e->hExpPool.push_back(0.f);

@@ -1,7 +1,9 @@
 // Derivation kernels (device code of derive.cu), compiled once per frame
 // representation: derive.cu includes it with signed-permutation frame codes,
-// derive_gen.cu with PGA_GENERAL_FRAMES (general rotations, for Rotate).
-// Everything here is in the build's inline namespace (pga::perm / pga::gen).
+// derive_gen.cu with PGA_GENERAL_FRAMES (general rotations, for Rotate) and
+// derive_blk.cu with PGA_INLINE_BLOCKS (frame codes, block parameters read
+// inline).  Everything here is in the build's inline namespace
+// (pga::perm / pga::gen / pga::permb).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -86,8 +88,22 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t& total) 
 
 // ------------------------------------------------------------- parameters
 
-// Non-scalar parameters (random ranges, shape attributes, expressions, block
-// values) take this out-of-line path so the common scalar case stays small.
+// A block value (PGA_PT_BLOCK): slot p.v0 of the parameter block of the
+// shape's axiom.  The block build (PGA_INLINE_BLOCKS) reads it inline in
+// param(), since it needs only the axiom index: two loads.
+__device__ __forceinline__ float block_param(const DeriveArgs& a, const DevParam& p, const Shape& x) {
+  const uint32_t slot = f2u(p.v0);
+  if (a.blocks == nullptr || slot >= a.blockStride) {
+    raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
+    return 0.0f;
+  }
+  const uint32_t b = __ldg(&a.axioms[x.axiom].block);
+  return __ldg(&a.blocks[(size_t)b * a.blockStride + slot]);
+}
+
+// Non-scalar parameters (random ranges, shape attributes, expressions, and
+// block values outside the block build) take this out-of-line path so the
+// common scalar case stays small.
 __device__ __noinline__ float eval_param_slow(const DeriveArgs& a, DevParam p, Shape x) {
   switch (p.type) {
     case PGA_PT_SCALAR:
@@ -102,15 +118,8 @@ __device__ __noinline__ float eval_param_slow(const DeriveArgs& a, DevParam p, S
     }
     case PGA_PT_EXP:
       return eval_exp(a.tab.expPool + p.aux, x, __ldg(&a.axioms[x.axiom].custom), a.st);
-    case PGA_PT_BLOCK: {
-      uint32_t slot = f2u(p.v0);
-      if (a.blocks == nullptr || slot >= a.blockStride) {
-        raise_error(a.st, PGA_ERR_BAD_PARAM, x.entry);
-        return 0.0f;
-      }
-      uint32_t b = __ldg(&a.axioms[x.axiom].block);
-      return __ldg(&a.blocks[(size_t)b * a.blockStride + slot]);
-    }
+    case PGA_PT_BLOCK:
+      return block_param(a, p, x);
     default:
       return 0.0f;  // unknown types evaluate to 0 (Parameters.cuh:697-709 without invariant checks)
   }
@@ -119,6 +128,9 @@ __device__ __noinline__ float eval_param_slow(const DeriveArgs& a, DevParam p, S
 __device__ __forceinline__ float param(const DeriveArgs& a, const DevRule& r, uint32_t k, const Shape& x) {
   const DevParam p = param_at(a, r.paramBase + k);
   if (p.type == PGA_PT_SCALAR) return p.v0;
+#if PGA_INLINE_BLOCKS
+  if (p.type == PGA_PT_BLOCK) return block_param(a, p, x);
+#endif
   return eval_param_slow(a, p, x);
 }
 
@@ -1607,6 +1619,7 @@ inline FrameKernels frame_kernels() {
   k.phased = (const void*)k_derive_persistent<false, 2>;
   k.seed = (const void*)k_seed;
   k.expand = (const void*)k_expand_level;
+  k.adjoint = nullptr;  // set by the builds that include adjoint.cuh
   return k;
 }
 

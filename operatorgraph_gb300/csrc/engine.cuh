@@ -35,8 +35,17 @@
 #ifndef PGA_GENERAL_FRAMES
 #define PGA_GENERAL_FRAMES 0
 #endif
+// PGA_INLINE_BLOCKS (derive_blk.cu): the frame-code build again, with block
+// parameters (PGA_PT_BLOCK) read inline instead of on the out-of-line path;
+// engines whose table has block parameters launch it.  A separate build so
+// that the kernels of tables without them keep their register allocation.
+#ifndef PGA_INLINE_BLOCKS
+#define PGA_INLINE_BLOCKS 0
+#endif
 #if PGA_GENERAL_FRAMES
 #define PGA_FRAMES_NS gen
+#elif PGA_INLINE_BLOCKS
+#define PGA_FRAMES_NS permb
 #else
 #define PGA_FRAMES_NS perm
 #endif
@@ -162,6 +171,7 @@ struct FrameKernels {
   const void* phased;         // k_derive_persistent<false, 2>: multi-phase tables
   const void* seed;           // k_seed (plain form)
   const void* expand;         // k_expand_level (plain form)
+  const void* adjoint;        // k_adjoint (frame-code builds only; null in the general-frame build)
 };
 
 __device__ __forceinline__ void raise_error(DevState* st, int code, int detail) {

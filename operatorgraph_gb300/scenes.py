@@ -20,7 +20,9 @@ returns a dict with ``entries`` (ENTRY_DT array), ``axioms`` (AXIOM_DT array),
   into 4 sides (IfSizeLess guard) and a top halved along X: 384 terminals.
 * random_grammars(): 64-rule random grammars (branching U{2..6}, IfSizeLess
   thresholds U[0.01, 0.2], Discard probability 0.15, depth cap 12).
-* mixed(n): 40 % Menger (depth 1-3), 40 % city buildings, 20 % random grammars.
+* mixed(n): 40 % Menger (depth 1-3), 40 % city buildings, 20 % random grammars
+  (16 generated grammars shared by the random axioms); with blocks=True the
+  buildings' and sponges' continuous parameters come from per-axiom blocks.
 * collisions(...): a two-phase scene for Collider / IfCollides: in phase 0
   buildings (boxes, tag 1) and billboards (quads, tag 2) store themselves and
   emit terminals; trees (boxes, optionally turned) wait for phase 1, where a
@@ -45,10 +47,12 @@ def _batch(entries, axioms, blocks=None, block_stride=0, name=""):
     return {"entries": entries, "axioms": axioms, "blocks": blocks, "block_stride": block_stride, "name": name}
 
 
-def menger_table(threshold):
-    """The Menger sponge dispatch table (MengerSponge.cuh:35-45) on generic codes."""
+def menger_table(threshold, blocks=False):
+    """The Menger sponge dispatch table (MengerSponge.cuh:35-45) on generic codes.
+    blocks=True reads the three relative factors of every split from the
+    axiom's parameter block, slots 0..2 (value -1 each gives the sponge)."""
     S3, DIS, IFL, GEN = G.BOX_SUBDIVIDE3, G.BOX_DISCARD, G.BOX_IF_SIZE_LESS, G.BOX_GENERATE
-    rel = [scalar(-1), scalar(-1), scalar(-1)]
+    rel = [block(0), block(1), block(2)] if blocks else [scalar(-1), scalar(-1), scalar(-1)]
     return DispatchTable([
         Entry(IFL, [scalar(0), scalar(threshold)], [(1, 0), (2, 0)]),   # 0 A
         Entry(GEN, [scalar(0)], []),                                     # 1 B (terminal)
@@ -76,18 +80,22 @@ def menger(threshold=0.05, n=1, seed=0.5):
     return _batch(menger_table(threshold), ax, name=f"menger(threshold={threshold})")
 
 
-def building_table(mode=G.ANCHOR_TO_START, meshes=False):
+def building_table(mode=G.ANCHOR_TO_START, meshes=False, blocks=False):
     """One city building: Extrude -> ComponentSplit -> Repeat Y -> Repeat X -> IfSizeLess -> Subdivide.
     meshes=True makes the walls, windows and roofs triangle-mesh terminals
-    (meshes 0, 1, 2) instead of instanced ones."""
+    (meshes 0, 1, 2) instead of instanced ones.  blocks=True reads the floor
+    height, the tile width and the window's two wall widths from the axiom's
+    parameter block, slots 0..3 (3.0, 2.5, 0.2, 0.2 give the city)."""
     gen = G.QUAD_GENERATE_MESH if meshes else G.QUAD_GENERATE
+    floor, tile = (block(0), block(1)) if blocks else (scalar(3.0), scalar(2.5))
+    wl, wr = (block(2), block(3)) if blocks else (scalar(0.2), scalar(0.2))
     return DispatchTable([
         Entry(G.QUAD_EXTRUDE, [scalar(1), shape_attr(16)], [(1, 0)]),                      # 0 extrude to height
         Entry(G.BOX_COMPONENT_SPLIT, [], [(9, 0), (7, 0), (2, 0)]),                       # 1 top, bottom, sides
-        Entry(G.QUAD_REPEAT, [scalar(1), scalar(3.0), scalar(mode)], [(3, 0)]),           # 2 floors
-        Entry(G.QUAD_REPEAT, [scalar(0), scalar(2.5), scalar(mode)], [(4, 0)]),           # 3 tiles
+        Entry(G.QUAD_REPEAT, [scalar(1), floor, scalar(mode)], [(3, 0)]),                 # 2 floors
+        Entry(G.QUAD_REPEAT, [scalar(0), tile, scalar(mode)], [(4, 0)]),                  # 3 tiles
         Entry(G.QUAD_IF_SIZE_LESS, [scalar(0), scalar(1.2)], [(7, 0), (5, 0)]),           # 4 narrow tile?
-        Entry(G.QUAD_SUBDIVIDE, [scalar(0), scalar(0.2), scalar(-1), scalar(0.2)],
+        Entry(G.QUAD_SUBDIVIDE, [scalar(0), wl, scalar(-1), wr],
               [(8, 0), (6, 0), (8, 0)]),                                                  # 5 window
         Entry(gen, [scalar(1)], []),                                                      # 6 window terminal
         Entry(G.QUAD_DISCARD, [], []),                                                    # 7
@@ -219,13 +227,24 @@ def random_grammars(num_grammars=16, seed=99):
     return tables
 
 
-def mixed(n=65536, seed=99, menger_depths=(1, 2, 3), num_random_grammars=16):
-    """Heterogeneous batch: 40 % Menger, 40 % buildings, 20 % random grammars."""
+MIXED_STRIDE = 4
+
+
+def mixed(n=65536, seed=99, menger_depths=(1, 2, 3), num_random_grammars=16, blocks=False):
+    """Heterogeneous batch: 40 % Menger, 40 % buildings, 20 % random grammars.
+
+    The random axioms share `num_random_grammars` generated grammars (16 by
+    default; one grammar per random axiom would be 13,107 x 130 dispatch-table
+    entries).  blocks=True gives every axiom a parameter block of
+    MIXED_STRIDE floats: a building reads its floor height, tile width and
+    window wall widths from it, a Menger sponge its split factors (the values
+    are the scalar grammars' own, so the terminals are the same); random
+    grammars read none.  The adjoint then reaches those DynParams."""
     rng = np.random.default_rng(seed)
     thresholds = {1: 0.5, 2: 0.15, 3: 0.05, 4: 0.015, 5: 0.005}
-    menger_tables = [menger_table(thresholds[d]) for d in menger_depths]
+    menger_tables = [menger_table(thresholds[d], blocks=blocks) for d in menger_depths]
     rand_tables = random_grammars(num_random_grammars, seed)
-    tables = menger_tables + [building_table()] + rand_tables
+    tables = menger_tables + [building_table(blocks=blocks)] + rand_tables
     entries, offs = G.concat_tables(tables)
     kind = rng.choice(3, size=n, p=[0.4, 0.4, 0.2])
     ax = G.make_axioms(n)
@@ -252,7 +271,13 @@ def mixed(n=65536, seed=99, menger_depths=(1, 2, 3), num_random_grammars=16):
             ax[j]["shape"] = G.SHAPE_BOX
             ax[j]["entry"] = offs[len(menger_tables) + 1 + rand_pick[j]]
             ax[j]["size"] = (1.0, 1.0, 1.0)
-    return _batch(entries, ax, name=f"mixed({n})")
+    if not blocks:
+        return _batch(entries, ax, name=f"mixed({n})")
+    blk = np.zeros((n, MIXED_STRIDE), np.float32)
+    blk[kind == 0] = (-1.0, -1.0, -1.0, 0.0)
+    blk[kind == 1] = (3.0, 2.5, 0.2, 0.2)
+    ax["block"] = np.arange(n)
+    return _batch(entries, ax, blk.reshape(-1), MIXED_STRIDE, name=f"mixed({n}, blocks)")
 
 
 def forest_table(angles=(0.0, 22.5, 45.0, 67.5)):

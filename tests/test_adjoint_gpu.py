@@ -320,15 +320,149 @@ def test_facade_gradients_match_reference_fp32_central_differences(tmp_path):
         (lp, hp), (lm, hm) = out
         return (lp - lm) / (hp - hm), (lp - base) / hp, (base - lm) / -hm
 
+    # Facades have no kinks (relative shares only, no Repeat; the side guard
+    # sits far from every size), and one-sided FP32 differences carry ~5e-3 of
+    # rounding noise, so no kink filter: every central difference is compared.
     tol = RTOL
     for which, got, n in (("b", gb, len(b32)), ("s", gs.reshape(-1), len(s32))):
         diffs = [diff(b32, s32, which, k) for k in range(n)]
-        fds = [d[0] for d in diffs if d is not None]
-        scale = max(max((abs(f) for f in fds), default=0.0), 1.0)
-        checked = 0
+        assert all(d is not None for d in diffs), which  # a 1 % step flips no branch here
+        scale = max(max(abs(d[0]) for d in diffs), 1.0)
         for k, d in enumerate(diffs):
-            if d is None or abs(d[1] - d[2]) > 0.5 * tol * scale:
-                continue
             assert abs(got[k] - d[0]) <= tol * scale, f"{which}[{k}]: adjoint {got[k]:.6g} vs reference FD {d[0]:.6g}"
-            checked += 1
-        assert checked >= 0.9 * n, (which, checked, n)
+
+
+def _loss64_vec(batch, paths_sorted, w_sorted, blocks64, sizes64, loss_fn=None):
+    """Vectorised FP64 loss over the oracle's double-precision derivation:
+    sum(W . M) with W matched by path (paths_sorted / w_sorted sorted by path),
+    or loss_fn(M matched to paths_sorted order); (loss, True) or (None, None)
+    when the set of paths differs."""
+    M, P = oracle.derive_f64(G.DEFAULT_PROCS, batch["entries"], batch["axioms"], blocks64, batch["block_stride"],
+                             sizes64)
+    if len(P) != len(paths_sorted):
+        return None, None
+    order = np.argsort(P)
+    if not np.array_equal(P[order], paths_sorted):
+        return None, None
+    Ms = M[order]
+    if loss_fn is not None:
+        return loss_fn(Ms), True
+    return float((Ms * w_sorted).sum()), True
+
+
+def test_mixed_block_gradients_match_fp64_central_differences():
+    """The mixed batch with parameter blocks (scenes.mixed(blocks=True)): the
+    buildings' floor heights, tile widths and window wall widths and the
+    sponges' split factors, read from per-axiom blocks, get the adjoint's
+    gradient; checked with FP64 central differences for every block slot and
+    axiom size of 10 axioms (3 sponges, 4 buildings, 3 random grammars)."""
+    full = scenes.mixed(64, blocks=True)
+    kind = np.where(full["axioms"]["shape"] == G.SHAPE_QUAD, 1, 0)
+    quad = np.nonzero(kind == 1)[0][:4]
+    box = np.nonzero(kind == 0)[0]
+    blk_all = full["blocks"].reshape(-1, scenes.MIXED_STRIDE)
+    sponge = [i for i in box if blk_all[i, 0] < 0][:3]
+    rand = [i for i in box if blk_all[i, 0] == 0][:3]
+    pick = np.array(sorted(list(quad) + sponge + rand))
+    ax = full["axioms"][pick].copy()
+    ax["block"] = np.arange(len(pick))
+    batch = {"entries": full["entries"], "axioms": ax, "blocks": blk_all[pick].reshape(-1).copy(),
+             "block_stride": scenes.MIXED_STRIDE}
+    by_path, gb, gs = _gpu_grad(batch)
+    paths = np.array(sorted(by_path), dtype=np.uint64)
+    w = np.array([by_path[int(p)] for p in paths])
+    b64 = batch["blocks"].astype(np.float64)
+    s64 = batch["axioms"]["size"].astype(np.float64)
+    base, _ = _loss64_vec(batch, paths, w, b64, s64)
+    assert base is not None
+
+    def fd(vec_b, vec_s, which, k):
+        vals = []
+        for sgn in (1, -1):
+            b, sz = vec_b.copy(), vec_s.copy()
+            (b if which == "b" else sz.reshape(-1))[k] += sgn * H
+            lv, _ = _loss64_vec(batch, paths, w, b, sz)
+            if lv is None:
+                return None
+            vals.append(lv)
+        return (vals[0] - vals[1]) / (2 * H), (vals[0] - base) / H, (base - vals[1]) / H
+
+    diffs = [fd(b64, s64, "b", k) for k in range(len(b64))]
+    assert _compare("block", gb, diffs) >= 0.9 * len(b64)
+    # every used slot carries gradient: 4 per building, 3 per sponge
+    for j, i in enumerate(pick):
+        used = 4 if kind[i] == 1 else (3 if blk_all[i, 0] < 0 else 0)
+        assert np.count_nonzero(gb[j * 4:j * 4 + used]) == used, (i, gb[j * 4:j * 4 + 4])
+    diffs = [fd(b64, s64, "s", k) for k in range(s64.size)]
+    assert _compare("size", gs.reshape(-1), diffs) >= 0.8 * s64.size
+
+
+def test_c4_facade_fitting_through_autograd():
+    """Differentiable facade fitting as BASELINE's config 4 states it, on 8
+    facades: the target is the terminals of the same trees with every
+    parameter moved by N(0, 0.02) (clamped so no branch flips,
+    scenes.facade_target_params); the loss is the SSE of terminal centres and
+    extents matched by derivation path (autograd.PathTarget); forward and
+    adjoint run through torch.autograd.Function.  The gradient matches FP64
+    central differences (h = 1e-4) of the same loss on the restatement, and
+    40 Adam steps on the parameters cut the loss by more than 10x."""
+    from operatorgraph_gb300.autograd import PathTarget, axioms_tensor, derive_transforms
+    from operatorgraph_gb300.engine import Engine
+
+    batch = scenes.facades(8, seed=7)
+    target_blocks = scenes.facade_target_params(batch["blocks"])
+    n_ref = 8 * 384
+    eng = Engine(batch["entries"], block_stride=batch["block_stride"], record_tape=True, node_capacity=1 << 18,
+                 max_terminals=1 << 16)
+    d_ax = axioms_tensor(batch["axioms"])
+    sizes = torch.tensor(batch["axioms"]["size"], dtype=torch.float32, device="cuda", requires_grad=True)
+    tb = torch.tensor(target_blocks, dtype=torch.float32, device="cuda")
+    Mt, pt = derive_transforms(eng, d_ax, tb, sizes.detach(), n_ref)
+    target = PathTarget(Mt, pt)
+    blocks = torch.tensor(batch["blocks"], dtype=torch.float32, device="cuda", requires_grad=True)
+    M, paths = derive_transforms(eng, d_ax, blocks, sizes, n_ref)
+    loss = target.sse(M, paths)
+    loss.backward()
+    g = blocks.grad.detach().cpu().numpy().astype(np.float64)
+    # FP64 central differences of the same loss (target values as the GPU derived them)
+    tp = target.paths.cpu().numpy().view(np.uint64)  # sorted as signed int64 on the device
+    order = np.argsort(tp)
+    tp = tp[order]
+    tc, te = target.c.cpu().numpy().astype(np.float64)[order], target.e.cpu().numpy().astype(np.float64)[order]
+
+    def sse64(Ms):
+        c = Ms[:, [3, 7, 11]]
+        R = Ms.reshape(-1, 3, 4)[:, :, :3]
+        e = np.sqrt((R * R).sum(axis=1))
+        return float(((c - tc) ** 2).sum() + ((e - te) ** 2).sum())
+
+    b64 = batch["blocks"].astype(np.float64)
+    s64 = batch["axioms"]["size"].astype(np.float64)
+    base, _ = _loss64_vec(batch, tp, None, b64, s64, sse64)
+    assert base is not None and abs(base - float(loss.detach())) <= 1e-3 * max(base, 1e-6) + 1e-7
+    diffs = []
+    for k in range(len(b64)):
+        vals = []
+        for sgn in (1, -1):
+            b = b64.copy()
+            b[k] += sgn * H
+            lv, _ = _loss64_vec(batch, tp, None, b, s64, sse64)
+            vals.append(lv)
+        assert None not in vals, k  # the target's perturbation keeps every branch
+        diffs.append((vals[0] - vals[1]) / (2 * H))
+    # the loss is quadratic, so one-sided differences differ by h f'' and are
+    # no kink test here: every central difference is compared
+    scale = max(max(abs(d) for d in diffs), 1.0)
+    for k, d in enumerate(diffs):
+        _check(f"c4[{k}]", g[k], d, scale)
+    # fit: Adam on the parameters toward the target
+    opt = torch.optim.Adam([blocks], lr=2e-3)
+    first = float(loss.detach())
+    for _ in range(40):
+        opt.zero_grad()
+        M, paths = derive_transforms(eng, d_ax, blocks, sizes, n_ref)
+        loss = target.sse(M, paths)
+        loss.backward()
+        opt.step()
+    assert float(loss.detach()) < 0.1 * first, (first, float(loss.detach()))
+    eng.release()
