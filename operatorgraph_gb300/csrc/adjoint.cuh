@@ -110,6 +110,22 @@ __device__ __noinline__ void exp_grad(const float* b, const Shape& x, float cust
   }
 }
 
+// atomicAdd(addr, v) with the lanes of the warp that add to the same address
+// summed first (shuffles over the group), so that a group makes one atomic:
+// the items of one axiom, expanded side by side, add to the same few block
+// gradients.
+__device__ __forceinline__ void atomic_add_grouped(float* addr, float v) {
+  const unsigned active = __activemask();
+  const unsigned peers = __match_any_sync(active, (unsigned long long)addr);
+  if ((peers & (peers - 1u)) == 0u) {
+    atomicAdd(addr, v);
+    return;
+  }
+  float sum = 0.0f;
+  for (unsigned m = peers; m != 0u; m &= m - 1u) sum += __shfl_sync(peers, v, __ffs(m) - 1);
+  if ((int)(threadIdx.x & 31u) == __ffs(peers) - 1) atomicAdd(addr, sum);
+}
+
 // Gradient g of a parameter evaluated on shape x: a block value feeds the
 // parameter gradient; a translation or size attribute (Shape::at 3/7/11,
 // 12..14) and an expression reading them feed gx, the gradient of x (null
@@ -122,8 +138,13 @@ __device__ __forceinline__ void param_grad(const DeriveArgs& a, const AdjArgs& j
   if (p.type == PGA_PT_BLOCK) {
     const uint32_t slot = f2u(p.v0);
     const uint32_t b = __ldg(&a.axioms[x.axiom].block);
-    if (j.gradParams != nullptr && slot < a.blockStride && b < j.numBlocks)
+    if (j.gradParams != nullptr && slot < a.blockStride && b < j.numBlocks) {
+#if PGA_INLINE_BLOCKS
+      atomic_add_grouped(&j.gradParams[(size_t)b * a.blockStride + slot], g);
+#else
       atomicAdd(&j.gradParams[(size_t)b * a.blockStride + slot], g);
+#endif
+    }
   } else if (p.type == PGA_PT_SHAPE_ATTR && gx != nullptr) {
     const uint32_t i = f2u(p.v0);
     if (i >= 12 && i < 15) gx->s[i - 12] += g;
@@ -156,6 +177,22 @@ struct SubTerm {
   float gN, goI;
 };
 
+// Per-page sums for the factor and extent gradients of operators whose
+// parameters do not read the shape, issued once per page (one add per factor)
+// instead of once per child (the block build, PGA_INLINE_BLOCKS: the other
+// builds serve tables without block parameters, whose per-child path needs
+// fewer registers).  A Subdivide with at most kPureMax factors:
+// W[k] = sum over the page's children of the coefficient of dN_k in dL
+// (gN for the child's own slot, go / 2 there and go for every slot below it),
+// Q = sum of W[k] f_k over the negative (relative) f_k.  A Repeat: the extent
+// parameter's gradient.
+constexpr uint32_t kPureMax = 4;
+struct PageAcc {
+  float W[kPureMax];
+  float Q;
+  float ext;
+};
+
 __device__ __forceinline__ void sub_add(SubAcc& acc, int idx, float gN, float goI) {
   if (idx < 0 || idx >= (int)kMaxN) return;
   while (acc.last < idx) {
@@ -171,8 +208,8 @@ __device__ __forceinline__ void sub_add(SubAcc& acc, int idx, float gN, float go
 // i.e. right after expander_init).  gc is the gradient of the child's state;
 // the parent's gradient is accumulated into gp, except a Subdivide's terms
 // through its recurrence, which are returned in st for subdivide_sweep.
-__device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander& E0, uint32_t c, const Grad& gc,
-                          Grad& gp, SubTerm& st) {
+__device__ __forceinline__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander& E0, uint32_t c,
+                                          const Grad& gc, Grad& gp, SubTerm& st, PageAcc& pa) {
   const Shape& x = E0.base;
   const DevRule& r = E0.r;
 #pragma unroll
@@ -187,16 +224,19 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
         if (k != ax) gp.s[k] += gc.s[k];
       const uint32_t i = min(c, n - 1u);
       const float gN = pick3(gc.s, ax), go = axis_dot(x, ax, gc.t);
-      if (r.flags & kRuleScalar) {
-        // Constant factors: N_k = f_k (f_k > 0) or scale * -f_k (f_k < 0) with
-        // scale = (S - sum of the positive f) / relSum, relSum = sum of -f over
-        // the negative f, and o_c = -S/2 + sum_{k<c} N_k + N_c/2.  So
-        // dN_k/dS = -f_k / relSum (f_k < 0, else 0) and
-        // do_c/dS = -1/2 + sum_{k<c} dN_k/dS + dN_c/dS / 2: child c's whole
-        // share of dL/dS, with nothing left for subdivide_sweep.
+      const bool scalar = (r.flags & kRuleScalar) != 0;
+      if (scalar || (PGA_INLINE_BLOCKS && (r.flags & kRulePure) && n <= kPureMax)) {
+        // Factors that do not read the shape: N_k = f_k (f_k > 0) or
+        // scale * -f_k (f_k < 0) with scale = (S - sum of the positive f) /
+        // relSum, relSum = sum of -f over the negative f, and
+        // o_c = -S/2 + sum_{k<c} N_k + N_c/2.  So dN_k/dS = -f_k / relSum
+        // (f_k < 0, else 0) and do_c/dS = -1/2 + sum_{k<c} dN_k/dS + dN_c/dS / 2:
+        // child c's whole share of dL/dS, with nothing left for
+        // subdivide_sweep.  Block factors also get their gradient, gathered
+        // in pa and issued once per page (pure_factor_grads).
         float relSum = 0.0f, below = 0.0f, fc = 0.0f;
         for (uint32_t k = 0; k < n; k++) {
-          const float f = param_at(a, r.paramBase + k + 1).v0;
+          const float f = scalar ? param_at(a, r.paramBase + k + 1).v0 : param(a, r, k + 1, x);
           if (f < 0.0f) {
             relSum += -f;
             if (k < i) below += -f;
@@ -211,6 +251,12 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
         gp.s[0] += (ax == 0) ? gS : 0.0f;
         gp.s[1] += (ax == 1) ? gS : 0.0f;
         gp.s[2] += (ax == 2) ? gS : 0.0f;
+        if (PGA_INLINE_BLOCKS && !scalar) {
+          const float own = gN + 0.5f * go;
+#pragma unroll
+          for (uint32_t k = 0; k < kPureMax; k++) pa.W[k] += (k == i) ? own : ((k < i) ? go : 0.0f);
+          pa.Q += go * -below + own * (fc < 0.0f ? fc : 0.0f);
+        }
         return;
       }
       st.idx = (int)i;
@@ -249,12 +295,21 @@ __device__ void child_vjp(const DeriveArgs& a, const AdjArgs& j, const Expander&
           gE += -truncf(S / E) * ge1;
         }
       }
+#if PGA_INLINE_BLOCKS
+      if (ext < 0.0f) {
+        gS += gE * fabsf(ext);
+        pa.ext += gE * (-S);
+      } else {
+        pa.ext += gE;
+      }
+#else
       if (ext < 0.0f) {
         gS += gE * fabsf(ext);
         param_grad(a, j, r, 1, x, gE * (-S), &gp);
       } else {
         param_grad(a, j, r, 1, x, gE, &gp);
       }
+#endif
       gp.s[0] += (ax == 0) ? gS : 0.0f;
       gp.s[1] += (ax == 1) ? gS : 0.0f;
       gp.s[2] += (ax == 2) ? gS : 0.0f;
@@ -570,6 +625,39 @@ __device__ __forceinline__ Grad pages_grad(const AdjArgs& j, uint32_t v, unsigne
   return g;
 }
 
+// The page's gathered parameter gradients (PageAcc): a Repeat's extent, and
+// the factors of a Subdivide whose factors do not read the shape (at most
+// kPureMax): dL/df_j = W_j + Q / relSum for f_j > 0 and
+// -(W_j + Q / relSum) * scale for f_j < 0 (the size terms through N_j and,
+// via scale, through every relative N_k).
+__device__ __forceinline__ void page_param_grads(const DeriveArgs& a, const AdjArgs& j, const Expander& E,
+                                                 const PageAcc& pa, Grad& gp) {
+  const DevRule& r = E.r;
+  const Shape& x = E.base;
+  if (r.op == PGA_OP_REPEAT) {
+    param_grad(a, j, r, 1, x, pa.ext, &gp);
+    return;
+  }
+  if ((r.op != PGA_OP_SUBDIVIDE && r.op != PGA_OP_SUBDIVIDE_STATIC) || (r.flags & kRuleScalar) ||
+      !(r.flags & kRulePure))
+    return;
+  const uint32_t n = r.op == PGA_OP_SUBDIVIDE ? r.nParams - 1u : r.nChildren;
+  if (n > kPureMax) return;
+  float f[kPureMax], relSum = 0.0f;
+#pragma unroll
+  for (uint32_t k = 0; k < kPureMax; k++) {
+    f[k] = k < n ? param(a, r, k + 1, x) : 0.0f;
+    relSum += f[k] < 0.0f ? -f[k] : 0.0f;
+  }
+  const float q = relSum != 0.0f ? pa.Q / relSum : 0.0f;
+#pragma unroll
+  for (uint32_t k = 0; k < kPureMax; k++) {
+    if (k >= n) break;
+    const float g = f[k] > 0.0f ? pa.W[k] + q : (f[k] < 0.0f ? -(pa.W[k] + q) * E.scale : 0.0f);
+    param_grad(a, j, r, k + 1, x, g, &gp);
+  }
+}
+
 // Reverse step of work item i: its children in order -- each one's gradient
 // read through the slot map (a terminal's dL/dM, or the sum over the pages it
 // was queued as) and pushed back through its chain and the operator that
@@ -615,6 +703,11 @@ __device__ void adj_page(const DeriveArgs& a, const AdjArgs& j, unsigned long lo
   grad_zero(gp);
   SubAcc acc;
   acc.last = -1;
+  PageAcc pa;
+#pragma unroll
+  for (uint32_t k = 0; k < kPureMax; k++) pa.W[k] = 0.0f;
+  pa.Q = 0.0f;
+  pa.ext = 0.0f;
   Expander W = E;
   if (c0 < c1) expander_skip(a, W, c0);
   for (uint32_t c = c0; c < c1; c++) {
@@ -637,9 +730,12 @@ __device__ void adj_page(const DeriveArgs& a, const AdjArgs& j, unsigned long lo
     chain_vjp(a, j, ch, g);
     SubTerm st;
     st.idx = -1;
-    child_vjp(a, j, E, c, g, gp, st);
+    child_vjp(a, j, E, c, g, gp, st, pa);
     sub_add(acc, st.idx, st.gN, st.goI);
   }
+#if PGA_INLINE_BLOCKS
+  page_param_grads(a, j, E, pa, gp);
+#endif
   subdivide_sweep(a, j, E, acc, gp);
   if (ext.z & kAxiomLink) {
     push_to_axiom(a, j, ext.z & ~kAxiomLink, false, 0, gp);
