@@ -419,34 +419,39 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
-def mixed_step(n_ax, mout, count, dev, n_expected):
+def mixed_step(n_ax, mout, count, dev, n_expected, blocks=True):
     """The mixed batch as one differentiable step captured in one CUDA graph:
     derivation with the tape recorded, LBVH over all its terminals (the leaf
     count read on the device, pga_lbvh_build_counted), and the adjoint for the
     loss L = |M|^2 / 2, whose dL/dM = M the adjoint reads in place from the
-    terminal records (pga_adjoint_strided, stride 16 floats), to every DynParam
-    and axiom size: the batch with parameter blocks (scenes.mixed(blocks=True):
-    each building's floor height, tile width and window wall widths, each
-    sponge's split factors; the same terminals as the scalar batch).  The
+    terminal records (pga_adjoint_strided, stride 16 floats).  blocks=True:
+    to every DynParam and axiom size, on the batch with parameter blocks
+    (scenes.mixed(blocks=True): each building's floor height, tile width and
+    window wall widths, each sponge's split factors; the same terminals as the
+    scalar batch); blocks=False: to the axiom sizes of the scalar batch.  The
     axioms are seeded grouped by root entry.  The parts are also timed one by
-    one, eagerly."""
+    one, eagerly.  Keys are prefixed mixed65536_step_ (blocks) or
+    mixed65536_sizes_step_."""
     import torch
 
     from operatorgraph_gb300.engine import Engine
 
     res = {}
-    mx = scenes.mixed(n_ax, blocks=True)
+    mx = scenes.mixed(n_ax, blocks=blocks)
     mcap = mout.shape[0]
     et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True, group_axioms=True,
                 block_stride=mx["block_stride"])
     d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
-    d_blk = torch.from_numpy(mx["blocks"]).to(dev)
+    d_blk = torch.from_numpy(mx["blocks"]).to(dev) if blocks else torch.zeros(1, dtype=torch.float32, device=dev)
     g_blk = torch.empty_like(d_blk)
+    blk_ptr = d_blk.data_ptr() if blocks else None
+    gblk_ptr = g_blk.data_ptr() if blocks else None
+    n_blocks = n_ax if blocks else 0
     g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
     m_rows = mout.view(torch.float32).view(mcap, 16)
     # LBVH bounds: the box of the terminal centres of a first derivation, one
     # metre wider on every side.
-    et.derive_raw(d_mx.data_ptr(), n_ax, d_blk.data_ptr(), mout.data_ptr(), mcap, count.data_ptr())
+    et.derive_raw(d_mx.data_ptr(), n_ax, blk_ptr, mout.data_ptr(), mcap, count.data_ptr())
     torch.cuda.synchronize()
     rep = et.report()
     assert rep["status"] == 0, rep
@@ -466,11 +471,11 @@ def mixed_step(n_ax, mout, count, dev, n_expected):
                 marks[k].record(st)
 
         mark(0)
-        et.derive_raw(d_mx.data_ptr(), n_ax, d_blk.data_ptr(), mout.data_ptr(), mcap, count.data_ptr(), stream=st)
+        et.derive_raw(d_mx.data_ptr(), n_ax, blk_ptr, mout.data_ptr(), mcap, count.data_ptr(), stream=st)
         mark(1)
         bv = et.lbvh(mout, mcap, bounds, stream=st, count=count)
         mark(2)
-        et.adjoint_raw(mout.data_ptr(), g_blk.data_ptr(), n_ax, g_sz.data_ptr(), stream=st, grad_stride=16)
+        et.adjoint_raw(mout.data_ptr(), gblk_ptr, n_blocks, g_sz.data_ptr(), stream=st, grad_stride=16)
         mark(3)
         return bv
 
@@ -506,10 +511,11 @@ def mixed_step(n_ax, mout, count, dev, n_expected):
     assert rep["status"] == 0, rep
     assert int(count.item()) == n
     assert bool(torch.isfinite(g_sz).all()) and float(g_sz.abs().max()) > 0
-    assert bool(torch.isfinite(g_blk).all()) and float(g_blk.abs().max()) > 0
+    if blocks:
+        assert bool(torch.isfinite(g_blk).all()) and float(g_blk.abs().max()) > 0
     names = ("derive_tape", "lbvh", "adjoint")
     med = [statistics.median(x[k] for x in seg) for k in range(3)]
-    n_par = int(d_blk.numel())
+    n_par = int(d_blk.numel()) if blocks else 0
     # Algorithmic bytes, counted two ways.  This bench's count: derivation 64 B
     # per terminal, its 8-B tape link and 48 B per axiom; LBVH 204 B per leaf
     # (the 64-B record read, 52 B of tree written, four radix passes over 12-B
@@ -519,23 +525,24 @@ def mixed_step(n_ax, mout, count, dev, n_expected):
     # B_adj = 112 T + 140 N + 4 P.
     parts = [72.0 * n + 48.0 * n_ax, 204.0 * n, 56.0 * n + 176.0 * n_items + 4.0 * (n_par + 3 * n_ax)]
     parts_8d = [64.0 * n + 32.0 * n_ax, 108.0 * n, 112.0 * n + 140.0 * n_items + 4.0 * (n_par + 3 * n_ax)]
+    pre = "mixed65536_step_" if blocks else "mixed65536_sizes_step_"
     peak, _ = read_peaks()
     step_ms = statistics.median(ts)
-    res["mixed65536_step_graph_ms"] = step_ms
-    res["mixed65536_step_items"] = n_items
-    res["mixed65536_step_params"] = n_par
-    res["mixed65536_step_segments_ms"] = {k: v for k, v in zip(names, med)}
-    res["mixed65536_step_segments_gbs"] = {k: b / (v * 1e-3) / 1e9 for k, b, v in zip(names, parts, med)}
-    res["mixed65536_step_bytes"] = sum(parts)
-    res["mixed65536_step_gbs"] = sum(parts) / (step_ms * 1e-3) / 1e9
-    res["mixed65536_step_roofline_frac"] = res["mixed65536_step_gbs"] / peak
-    res["mixed65536_step_bytes_formula"] = sum(parts_8d)
-    res["mixed65536_step_roofline_frac_formula"] = sum(parts_8d) / (step_ms * 1e-3) / 1e9 / peak
+    res[pre + "graph_ms"] = step_ms
+    res[pre + "items"] = n_items
+    res[pre + "params"] = n_par
+    res[pre + "segments_ms"] = {k: v for k, v in zip(names, med)}
+    res[pre + "segments_gbs"] = {k: b / (v * 1e-3) / 1e9 for k, b, v in zip(names, parts, med)}
+    res[pre + "bytes"] = sum(parts)
+    res[pre + "gbs"] = sum(parts) / (step_ms * 1e-3) / 1e9
+    res[pre + "roofline_frac"] = res[pre + "gbs"] / peak
+    res[pre + "bytes_formula"] = sum(parts_8d)
+    res[pre + "roofline_frac_formula"] = sum(parts_8d) / (step_ms * 1e-3) / 1e9 / peak
     # the forward + adjoint step alone (no LBVH), by the formulas
     fa_ms = med[0] + med[2]
-    res["mixed65536_fwd_adjoint_ms"] = fa_ms
-    res["mixed65536_fwd_adjoint_roofline_frac_formula"] = (parts_8d[0] + parts_8d[2]) / (fa_ms * 1e-3) / 1e9 / peak
-    res["mixed65536_step_lbvh_bounds"] = [round(v, 3) for v in bounds]
+    res[pre + "fwd_adjoint_ms"] = fa_ms
+    res[pre + "fwd_adjoint_roofline_frac_formula"] = (parts_8d[0] + parts_8d[2]) / (fa_ms * 1e-3) / 1e9 / peak
+    res[pre + "lbvh_bounds"] = [round(v, 3) for v in bounds]
     del g, bv
     et.release()
     return res
@@ -774,7 +781,8 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["mixed65536_terminals"] = n_mx
     res["mixed65536_ms"] = statistics.median(ts)
     res["mixed65536_terminals_per_s"] = n_mx / (res["mixed65536_ms"] * 1e-3)
-    res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx))
+    res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx, blocks=True))
+    res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx, blocks=False))
     del mout
     # Forest: 4096 trees (Rotate with arbitrary angles, Replicate, Translate,
     # Scale: the general-frame kernels), about 13.4M terminals in one launch.

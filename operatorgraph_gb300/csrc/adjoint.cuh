@@ -4,7 +4,8 @@
 // discard and the rule of every shape as recorded by the forward pass -- a
 // terminal's transform is a smooth function of the continuous inputs: the
 // per-axiom parameter blocks (PGA_PT_BLOCK parameters) and the axiom sizes.
-// Rotations are signed permutations that no continuous input changes, so the
+// Rotations -- signed permutations, or in the general-frame build the products
+// of Rotate's scalar angles -- are changed by no continuous input, so the
 // state that carries gradient is a shape's translation t and size s.
 //
 // Tape: every queued work item stores (parent item or kAxiomLink | axiom,
@@ -154,11 +155,16 @@ __device__ __forceinline__ void param_grad(const DeriveArgs& a, const AdjArgs& j
   }
 }
 
-// d(offset along the split axis) seen through the translation: R[:,a] has one
-// nonzero entry, +-1 in row perm_a.
+// d(offset along the split axis) seen through the translation: R[:,a] . g_t,
+// which for a signed-permutation frame is +-g_t in row perm_a.
 __device__ __forceinline__ float axis_dot(const Shape& x, uint32_t ax, const float gt[3]) {
+#if PGA_GENERAL_FRAMES
+  // general frames: t' = t + R[:,ax] * o, so dL/do = R[:,ax] . g_t
+  return frame_at(x, 0, ax) * gt[0] + frame_at(x, 1, ax) * gt[1] + frame_at(x, 2, ax) * gt[2];
+#else
   const float v = pick3(gt, frame_row(x.frame, ax));
   return frame_neg(x.frame, ax) ? -v : v;
+#endif
 }
 
 // Per-child terms of a Subdivide's VJP, gathered over the children of one
@@ -476,6 +482,16 @@ __device__ int replay_chain(const DeriveArgs& a, Shape x, Chain& ch, Shape& yEnd
       x.entry = succ_at(a, r.succBase + branch);
       continue;
     }
+#if PGA_GENERAL_FRAMES
+    if (r.op == PGA_OP_ROTATE) {
+      // model * rotateXYZ of scalar angles (built at engine creation): the
+      // frame turns, translation and size pass through, and no continuous
+      // input reaches the rotation, so the gradient passes through unchanged
+      frame_rotate(x, a.tab.expPool + param_at(a, r.paramBase).aux);
+      x.entry = succ_at(a, r.succBase);
+      continue;
+    }
+#endif
     if (r.op == PGA_OP_TRANSLATE || r.op == PGA_OP_SCALE || r.op == PGA_OP_SWAP_SIZE) {
       if (ch.n >= kChainSteps) return kEndFail;
       ch.entry[ch.n] = x.entry;
@@ -496,8 +512,7 @@ __device__ int replay_chain(const DeriveArgs& a, Shape x, Chain& ch, Shape& yEnd
       ch.before[ch.n] = x;
       ch.n++;
       const float extent = param(a, r, 1, x);
-      const uint32_t f = x.frame;
-      x.frame = frame_set(frame_set(f, 1, f, 2, 0), 2, f, 1, 1);
+      frame_set2(x, x, 1, 2, 0, 2, 1, 1);  // model * [x, z, -y] columns, as the forward
       x.s[2] = x.s[1];
       x.s[1] = extent;
       x.seed = seed_of(a, x.seed, 0u);
@@ -560,9 +575,15 @@ __device__ __forceinline__ Grad terminal_grad(const AdjArgs& j, unsigned long lo
 #pragma unroll
   for (int q = 0; q < 3; q++) {
     g.t[q] = __ldg(gm + q * 4 + 3);
+#if PGA_GENERAL_FRAMES
+    // M[i][q] = R[i][q] s_q: dL/ds_q = sum_i dL/dM[i][q] R[i][q]
+    g.s[q] = __ldg(gm + q) * frame_at(y, 0, q) + __ldg(gm + 4 + q) * frame_at(y, 1, q) +
+             __ldg(gm + 8 + q) * frame_at(y, 2, q);
+#else
     const uint32_t row = frame_row(y.frame, q);
     const float v = __ldg(gm + row * 4 + q);
     g.s[q] = frame_neg(y.frame, q) ? -v : v;
+#endif
   }
   return g;
 }

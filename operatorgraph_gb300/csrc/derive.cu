@@ -408,8 +408,8 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
     e->leafKernel = false;
     for (DevRule& r : e->hRules) r.flags = (uint16_t)(r.flags & ~kRuleLeaf);
   }
-  if ((e->generalFrames || e->phased) && c.recordTape) {
-    set_error("pga_engine_create: the adjoint (recordTape) covers neither Rotate nor phases and colliders");
+  if (e->phased && c.recordTape) {
+    set_error("pga_engine_create: the adjoint (recordTape) does not cover phases and colliders");
     delete e;
     return PGA_ERR_BAD_PARAM;
   }

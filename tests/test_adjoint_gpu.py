@@ -145,11 +145,11 @@ def _size_cases():
     sys.path.insert(0, str(Path(__file__).parent / "golden"))
     import cases as C
 
-    # the adjoint does not cover Rotate (engine creation with a tape rejects it)
-    rot = {G.BOX_ROTATE, G.QUAD_ROTATE}
-    out = [c for c in C.cases() if not rot & set(int(k) for k in c[1]["entries"]["operatorCode"])]
+    # every golden case, Rotate ones included (the general-frame build's adjoint)
+    out = list(C.cases())
     for mode in (G.ANCHOR_TO_START, G.ANCHOR_TO_END, G.ADJUST_TO_FILL):
         out.append((f"building_off_grid_m{mode}", scenes.building(w=25.3, d=19.7, h=31.0, mode=mode)))
+    out.append(("forest_2", scenes.forest(2)))
     return out
 
 
@@ -160,7 +160,9 @@ _SIZE_CASES = _size_cases()
 def test_axiom_size_gradients_match_fp64_central_differences(name, batch):
     """Every operator's VJP through the axiom sizes: Subdivide (static, dynamic,
     absolute / relative / zero factors), Repeat (three modes, relative and
-    absolute extents), ComponentSplit, Extrude, IfSizeLess chains."""
+    absolute extents), ComponentSplit, Extrude, IfSizeLess chains, and with
+    Rotate at arbitrary angles (the general-frame kernels: the turned frame
+    carries the translation and size gradients), Replicate, Translate, Scale."""
     by_path, _, gs = _gpu_grad(batch)
     b64 = None if batch["blocks"] is None else batch["blocks"].astype(np.float64)
     s64 = batch["axioms"]["size"].astype(np.float64)
