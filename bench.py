@@ -761,25 +761,25 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     mcap = 160_000_000
     d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
     mout = torch.empty((mcap, 64), dtype=torch.uint8, device=dev)
-    for group in (False, True):
-        em = Engine(mx["entries"], node_capacity=1 << 27, max_terminals=mcap, group_axioms=group)
-        ts = []
-        for it in range(6):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            em.derive_raw(d_mx.data_ptr(), 65536, None, mout.data_ptr(), mcap, count.data_ptr())
-            b.record(stream)
-            torch.cuda.synchronize()
-            if it >= 2:
-                ts.append(a.elapsed_time(b))
-        rep = em.report()
-        assert rep["status"] == 0, rep
-        em.release()
-        if not group:
-            res["mixed65536_index_order_ms"] = statistics.median(ts)
+    # Schedule: a sweep of the split knobs and of the rule-to-warp grouping
+    # (axioms grouped by root entry), against the engine's defaults.
+    from operatorgraph_gb300 import autotune
+
+    mspace = {"sub_item": (4, 8), "narrow_sub_item": (0, 2), "items_per_lane": (1,), "blocks_per_sm": (0,)}
+    mbest, mms, mres = autotune.tune(mx, mcap, node_capacity=1 << 27, space=mspace, runs=3)
+    dflt = dict(autotune.DEFAULT_CONFIG, group_axioms=False)
+    res["mixed65536_schedule"] = mbest
+    res["mixed65536_default_ms"] = next((r["ms"] for r in mres if r["config"] == dflt), None)
+    res["mixed65536_index_order_ms"] = min(r["ms"] for r in mres
+                                           if r["ms"] is not None and not r["config"]["group_axioms"])
+    em = Engine(mx["entries"], node_capacity=1 << 27, max_terminals=mcap, **mbest)
+    em.derive_raw(d_mx.data_ptr(), 65536, None, mout.data_ptr(), mcap, count.data_ptr())
+    rep = em.report()
+    assert rep["status"] == 0, rep
+    em.release()
     n_mx = int(count.item())
     res["mixed65536_terminals"] = n_mx
-    res["mixed65536_ms"] = statistics.median(ts)
+    res["mixed65536_ms"] = mms
     res["mixed65536_terminals_per_s"] = n_mx / (res["mixed65536_ms"] * 1e-3)
     res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx, blocks=True))
     res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx, blocks=False))
@@ -792,10 +792,12 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     # a short autotune over the split knobs (the city's sweep, reduced).
     from operatorgraph_gb300 import autotune
 
-    fbest, _, _ = autotune.tune(fo, fcap, node_capacity=1 << 23, runs=3,
-                                space={"sub_item": (1, 2, 4, 8), "narrow_sub_item": (0, 1), "items_per_lane": (1,),
-                                       "blocks_per_sm": (0,)})
+    fbest, fms, fres = autotune.tune(fo, fcap, node_capacity=1 << 23, runs=3,
+                                     space={"sub_item": (1, 2, 4, 8), "narrow_sub_item": (0, 1), "items_per_lane": (1,),
+                                            "blocks_per_sm": (0,)})
     res["forest4096_schedule"] = fbest
+    res["forest4096_tuned_ms"] = fms
+    res["forest4096_default_ms"] = next((r["ms"] for r in fres if r["config"] == autotune.DEFAULT_CONFIG), None)
     eo = Engine(fo["entries"], node_capacity=1 << 23, max_terminals=fcap, **fbest)
     d_fo = torch.from_numpy(fo["axioms"].view(np.uint8).copy()).to(dev)
     fout = torch.empty((fcap, 64), dtype=torch.uint8, device=dev)

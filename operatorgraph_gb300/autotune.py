@@ -17,10 +17,22 @@ Every candidate derives the batch `runs` times (CUDA events, after a warm-up);
 a candidate whose derivation reports a non-OK status (e.g. the finer splits
 overflow the item arena) is discarded.  The result is the fastest candidate's
 configuration, ready for Engine(**config).
+
+Threads per block is not a knob: every kernel is compiled for 256 (its block
+scans and the output compaction's shared-memory tables are sized for it), and
+the persistent kernel's 128 registers fix the warps per SM at 16 whatever the
+block size; the grid's shape is searched through blocksPerSM.
+
+`size_capacities` sizes the item arena and the terminal capacity from one
+counting derivation (statuses report the full counts, so an undersized first
+guess is grown and retried), and `tune_cached` keeps the best schedule on disk
+per (rule table, batch signature, GPU name, library version).
 """
 import argparse
+import hashlib
 import itertools
 import json
+import os
 import statistics
 
 import numpy as np
@@ -122,6 +134,89 @@ def tune(batch, capacity, node_capacity=1 << 22, space=None, runs=5, measure_fn=
         results.append({"index": i, "config": cfg, "ms": ms, "status": int(status)})
     best, ms = select(results)
     return best, ms, results
+
+
+def size_capacities(batch, node_capacity=1 << 20, max_terminals=1 << 20, margin=0.05, limit=1 << 31, config=None):
+    """Item-arena and terminal capacities for `batch`: derives it once with
+    the given capacities, doubling whichever the device status says was too
+    small (the counts keep counting past it), then returns the counts plus
+    `margin`: {"node_capacity": ..., "max_terminals": ...}."""
+    import torch
+
+    from .engine import Engine
+
+    config = dict(config or {})
+    d_ax = torch.from_numpy(np.ascontiguousarray(batch["axioms"]).view(np.uint8).copy()).cuda()
+    d_blk = None
+    if batch.get("blocks") is not None:
+        d_blk = torch.from_numpy(np.asarray(batch["blocks"], np.float32)).cuda()
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    while True:
+        eng = Engine(batch["entries"], node_capacity=node_capacity, max_terminals=max_terminals,
+                     block_stride=batch.get("block_stride", 0), **config)
+        out = torch.empty((max_terminals, 64), dtype=torch.uint8, device="cuda")
+        try:
+            eng.derive_raw(d_ax.data_ptr(), len(batch["axioms"]), None if d_blk is None else d_blk.data_ptr(),
+                           out.data_ptr(), max_terminals, count.data_ptr())
+            rep = eng.report()
+        finally:
+            eng.release()
+        del out
+        if rep["status"] == 1 and node_capacity < limit:  # queue overflow
+            node_capacity *= 2
+            continue
+        if rep["status"] == 2 and max_terminals < limit:  # output overflow: the report holds the full count
+            max_terminals = max(2 * max_terminals, int(rep["terminals"]))
+            continue
+        if rep["status"] != 0:
+            raise RuntimeError(f"size_capacities: device status {rep['status']}")
+        grow = lambda x: int(min(limit, max(1024, x * (1.0 + margin))))
+        return {"node_capacity": grow(rep["nodes"]), "max_terminals": grow(rep["terminals"])}
+
+
+def schedule_key(batch, gpu_name, library_version=""):
+    """Cache key of a batch's schedule: the rule table's bytes, the batch's
+    signature (axiom count and the histogram of root entries), the GPU name and
+    the library version."""
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(batch["entries"]).view(np.uint8).tobytes())
+    ax = np.asarray(batch["axioms"])
+    roots, counts = np.unique(np.asarray(ax["entry"]), return_counts=True)
+    h.update(np.asarray([len(ax)], np.int64).tobytes() + roots.astype(np.int64).tobytes() +
+             counts.astype(np.int64).tobytes())
+    h.update(gpu_name.encode() + b"|" + library_version.encode())
+    return h.hexdigest()[:32]
+
+
+def default_cache_dir():
+    return os.environ.get("PGA_SCHEDULE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "pga_gb300")
+
+
+def tune_cached(batch, capacity, node_capacity=1 << 22, space=None, runs=5, cache_dir=None, gpu_name=None,
+                library_version=None, measure_fn=None):
+    """tune() with the best schedule kept on disk per schedule_key: a hit
+    returns (config, ms, [] , True) without timing anything; a miss tunes,
+    stores and returns (config, ms, results, False)."""
+    if gpu_name is None or library_version is None:
+        import torch
+
+        from .engine import load_library
+
+        gpu_name = gpu_name or torch.cuda.get_device_name()
+        library_version = library_version or load_library().pga_version().decode()
+    cache_dir = cache_dir or default_cache_dir()
+    path = os.path.join(cache_dir, schedule_key(batch, gpu_name, library_version) + ".json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d["config"], d["ms"], [], True
+    best, ms, results = tune(batch, capacity, node_capacity, space=space, runs=runs, measure_fn=measure_fn)
+    os.makedirs(cache_dir, exist_ok=True)
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump({"config": best, "ms": ms, "gpu": gpu_name, "version": library_version}, f)
+    os.replace(tmp, path)
+    return best, ms, results, False
 
 
 def main(argv=None):

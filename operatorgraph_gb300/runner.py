@@ -2,10 +2,14 @@
 test_runner app, src/test_runner/TestRunnerApp.cpp:303-345: derive a scene a
 number of times and log timings).
 
-    python -m operatorgraph_gb300.runner --scene city --runs 5 [--plain] [--lbvh] [--step]
+    python -m operatorgraph_gb300.runner --scene city --runs 5 [--plain | --per-axiom] [--lbvh] [--step]
+                                         [--meshes] [--blocks]
 
 Prints one JSON line: terminals, per-run milliseconds (CUDA events) and the
-device report of the last run.  --step runs the differentiable step after
+device report of the last run.  --meshes (city) makes walls, windows and roofs
+triangle-mesh terminals and runs pga_generate_meshes after each derivation;
+--blocks (mixed) gives the axioms parameter blocks (scenes.mixed(blocks=True));
+--per-axiom derives with one persistent launch per axiom.  --step runs the differentiable step after
 each derivation (made with the tape recorded): the LBVH over the device-side
 terminal count, then the adjoint to the block parameters and axiom sizes for
 L = |M|^2 / 2, reading dL/dM = M in place from the terminal records
@@ -20,15 +24,15 @@ import numpy as np
 from . import scenes
 
 
-def make_scene(name, n):
+def make_scene(name, n, meshes=False, blocks=False):
     if name == "city":
-        return scenes.city(n or 4096), (-50.0, -50.0, -1.0, 3250.0, 3250.0, 400.0)
+        return scenes.city(n or 4096, meshes=meshes), (-50.0, -50.0, -1.0, 3250.0, 3250.0, 400.0)
     if name == "menger":
         return scenes.menger({1: 0.5, 2: 0.15, 3: 0.05, 4: 0.015, 5: 0.005}[n or 5]), (-0.5, -0.5, -0.5, 0.5, 0.5, 0.5)
     if name == "facades":
         return scenes.facades(n or 1024), (-1.0, -1.0, -1.0, 70.0, 2.0, 70.0)
     if name == "mixed":
-        return scenes.mixed(n or 65536), (-50.0, -50.0, -110.0, 13000.0, 13000.0, 400.0)
+        return scenes.mixed(n or 65536, blocks=blocks), (-50.0, -50.0, -110.0, 13000.0, 13000.0, 400.0)
     raise SystemExit(f"unknown scene {name}")
 
 
@@ -53,9 +57,12 @@ def main(argv=None):
                     help="children per work item queued from levels narrower than the grid (default subItem)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="cap on resident blocks per SM (0: occupancy)")
     ap.add_argument("--group", action="store_true", help="seed the axioms grouped by root entry")
+    ap.add_argument("--per-axiom", action="store_true", help="one persistent launch per axiom (pga_derive_per_axiom)")
+    ap.add_argument("--meshes", action="store_true", help="city: triangle-mesh terminals, then pga_generate_meshes")
+    ap.add_argument("--blocks", action="store_true", help="mixed: per-axiom parameter blocks")
     args = ap.parse_args(argv)
 
-    b, bounds = make_scene(args.scene, args.n)
+    b, bounds = make_scene(args.scene, args.n, meshes=args.meshes, blocks=args.blocks)
     cap = args.capacity or 8_000_000
     eng = Engine(b["entries"], node_capacity=args.nodes, max_terminals=cap, block_stride=b["block_stride"],
                  sub_item=args.sub_item, items_per_lane=args.items_per_lane, blocks_per_sm=args.blocks_per_sm,
@@ -71,12 +78,13 @@ def main(argv=None):
         g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
         g_blk = None if d_blk is None else torch.empty_like(d_blk)
         n_blk = 0 if d_blk is None else d_blk.numel() // max(b["block_stride"], 1)
-    times, lb, steps = [], [], []
+    times, lb, steps, mesh_ms = [], [], [], []
+    form = "per_axiom" if args.per_axiom else args.plain
     for _ in range(args.runs):
         a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None if d_blk is None else d_blk.data_ptr(),
-                       out.data_ptr(), cap, count.data_ptr(), plain=args.plain)
+                       out.data_ptr(), cap, count.data_ptr(), plain=form)
         z.record(stream)
         torch.cuda.synchronize()
         times.append(a.elapsed_time(z))
@@ -87,6 +95,13 @@ def main(argv=None):
             z.record(stream)
             torch.cuda.synchronize()
             lb.append(a.elapsed_time(z))
+        if args.meshes:
+            n = int(count.item())
+            a.record(stream)
+            eng.generate_meshes(out, n, [(4 * n, 6 * n)] * 3)
+            z.record(stream)
+            torch.cuda.synchronize()
+            mesh_ms.append(a.elapsed_time(z))
         if args.step:
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
             ev[0].record(stream)
@@ -99,7 +114,7 @@ def main(argv=None):
             steps.append({"lbvh_ms": ev[0].elapsed_time(ev[1]), "adjoint_ms": ev[1].elapsed_time(ev[2])})
     rep = eng.report()
     lv = {}
-    if not args.plain:
+    if not args.plain and not args.per_axiom:
         starts, nanos = eng.levels()
         nanos = nanos.astype(np.int64)
         d = np.diff(nanos) / 1e3
@@ -112,6 +127,8 @@ def main(argv=None):
            "ms": times, "ms_median": statistics.median(times), "report": rep, **lv}
     if lb:
         res["lbvh_ms"] = lb
+    if mesh_ms:
+        res["meshes_ms"] = mesh_ms
     if steps:
         res["step"] = steps
     print(json.dumps(res))

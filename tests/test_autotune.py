@@ -41,6 +41,30 @@ def test_grouping_is_searched_only_for_batches_of_several_root_entries():
     assert len(A.candidates(mixed)) == 4
 
 
+def test_schedule_cache_round_trip(tmp_path):
+    """tune_cached tunes on a miss, stores the winner under the key of (rule
+    table, batch signature, GPU, version), and returns it untimed on a hit; a
+    different GPU name or batch is a different key."""
+    b = scenes.city(16)
+    calls = []
+
+    def measure(cfg):
+        calls.append(cfg)
+        return 0.3 + 0.01 * cfg["sub_item"], 0
+
+    kw = dict(space={"sub_item": (4, 8)}, cache_dir=str(tmp_path), gpu_name="GB300", library_version="x",
+              measure_fn=measure)
+    best, ms, res, hit = A.tune_cached(b, 0, **kw)
+    assert not hit and best == {"sub_item": 4} and len(calls) == 2
+    best2, ms2, res2, hit2 = A.tune_cached(b, 0, **kw)
+    assert hit2 and best2 == best and ms2 == ms and len(calls) == 2
+    assert A.schedule_key(b, "GB300", "x") != A.schedule_key(b, "B200", "x")
+    assert A.schedule_key(b, "GB300", "x") != A.schedule_key(scenes.city(32), "GB300", "x")
+    kw["gpu_name"] = "B200"
+    A.tune_cached(b, 0, **kw)
+    assert len(calls) == 4
+
+
 def test_tune_fails_loudly_when_nothing_runs():
     with pytest.raises(RuntimeError):
         A.tune(None, 0, space={"sub_item": (8,)}, measure_fn=lambda cfg: (None, 1))
@@ -67,3 +91,24 @@ def test_tuned_schedule_derives_the_same_terminals():
     kb = np.sort(want.view(np.uint8).reshape(len(want), 64).view(np.dtype((np.void, 64))).ravel())
     assert n == len(want) and (ka == kb).all()
     assert torch.cuda.is_available()
+
+
+@pytest.mark.gpu
+def test_capacities_are_sized_from_a_counting_derivation():
+    """size_capacities grows undersized capacities from the statuses' counts;
+    the result derives the batch with no overflow and little slack."""
+    pytest.importorskip("torch")
+    from operatorgraph_gb300 import build as B
+
+    B.build()
+    b = scenes.city(256)
+    want = len(oracle.derive(G.DEFAULT_PROCS, b["entries"], b["axioms"]))
+    caps = A.size_capacities(b, node_capacity=1 << 10, max_terminals=1 << 10)
+    assert want <= caps["max_terminals"] <= 1.06 * want + 1024
+    assert caps["node_capacity"] >= 1024
+    from operatorgraph_gb300.engine import Engine
+
+    eng = Engine(b["entries"], **caps)
+    out, n, rep = eng.execute(b["axioms"], capacity=caps["max_terminals"])
+    assert rep["status"] == 0 and n == want
+    eng.release()
