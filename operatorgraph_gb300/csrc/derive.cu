@@ -219,7 +219,7 @@ static void free_engine(PgaEngine* e) {
   void* ptrs[] = {e->dRules, e->dParams, e->dSucc, e->dExpPool, e->dState, e->dNodes, e->dNodeRot, e->dLevelClock,
                   e->dTail, e->dTailLinks, e->dScratch,
                   e->dTermLinks, e->dLevelStart, e->dScratchCount, e->dSortTemp, e->dKeysA,
-                  e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dLeafAabbSorted, e->dNodeRange, e->dNodeGrad, e->dChildKey, e->dPageNext,
+                  e->dValsA, e->dValsB, e->dArrival, e->dLeafAabb, e->dLeafAabbSorted, e->dNodeOther, e->dNodeGrad, e->dChildKey, e->dPageNext,
                   e->dSlots, e->dBlockSums, e->dGroupCount};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -489,7 +489,7 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   ALLOC(e->dKeysA, c.maxTerminals * sizeof(unsigned long long));
   ALLOC(e->dLeafAabb, c.maxTerminals * 6 * sizeof(float));
   ALLOC(e->dLeafAabbSorted, c.maxTerminals * 6 * sizeof(float));
-  ALLOC(e->dNodeRange, c.maxTerminals * sizeof(int2));
+  ALLOC(e->dNodeOther, c.maxTerminals * sizeof(int32_t));
   ALLOC(e->dValsA, c.maxTerminals * sizeof(uint32_t));
   ALLOC(e->dValsB, c.maxTerminals * sizeof(uint32_t));
   ALLOC(e->dArrival, c.maxTerminals * sizeof(uint32_t));

@@ -68,7 +68,7 @@ struct PgaEngine {
   uint32_t* dArrival = nullptr;
   float* dLeafAabb = nullptr;        // LBVH leaf boxes in terminal order
   float* dLeafAabbSorted = nullptr;  // the same in sorted (leaf) order
-  int2* dNodeRange = nullptr;        // LBVH internal node leaf ranges [lo, hi]
+  int32_t* dNodeOther = nullptr;     // LBVH internal node i: the other end of its leaf range (one end is i)
 
   // Adjoint scratch: per work item the gradient of (translation, size), its
   // child key and the next page of the same child; the child slots (slotCap

@@ -60,9 +60,6 @@ __device__ __forceinline__ void leaf_aabb(const float4 r[3], bool quad, float mn
       }
 }
 
-// generateMortonCodes (GPUBVHConstructor.cuh:66-86) on terminal centres.
-// Also writes each terminal's AABB (6 floats, terminal order) while its record
-// is in registers.
 // Leaf count of a build: the host value `n`, or, when the count lives on the
 // device (dN != nullptr), min(*dN, n) with `n` the capacity the launches and
 // the sort were sized for.
@@ -93,19 +90,19 @@ __device__ __forceinline__ void hist_add(uint32_t* h, uint32_t d, bool valid) {
 
 // generateMortonCodes (GPUBVHConstructor.cuh:66-86) on terminal centres.
 // Also writes each terminal's AABB (6 floats, terminal order) while its record
-// is in registers.
+// is in registers.  The sort's values start as the terminal index, which its
+// first pass generates, so none are written here.
 // With a device count, the keys in [count, capacity) are padding: all ones,
 // after every real key in the stable radix sort (a real key can equal it only
 // in the sorted top bits, and it comes first there by input order).
 __global__ void __launch_bounds__(kLbvhThreads) k_morton(const PgaTerminal* __restrict__ t, unsigned long long cap,
                                                          const unsigned long long* __restrict__ dN, Bounds b,
                                                          unsigned long long* __restrict__ keys,
-                                                         uint32_t* __restrict__ vals, float* __restrict__ leafBox) {
+                                                         float* __restrict__ leafBox) {
   unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cap) return;
   if (i >= leaf_count(dN, cap)) {
     keys[i] = ~0ull;
-    vals[i] = (uint32_t)i;
     return;
   }
   const float4* p = reinterpret_cast<const float4*>(t + i);
@@ -126,7 +123,6 @@ __global__ void __launch_bounds__(kLbvhThreads) k_morton(const PgaTerminal* __re
   }
   uint64_t path = ((uint64_t)meta.w << 32) | meta.z;
   keys[i] = ((unsigned long long)code << 34) | (path >> 30);
-  vals[i] = (uint32_t)i;
 }
 
 // The four digit histograms of keys [0, n) (kSortPasses x kBins, zeroed
@@ -189,11 +185,13 @@ __global__ void __launch_bounds__(kBins) k_sort_bases(const uint32_t* __restrict
 // A block takes the next tile of kSortTile keys from an atomic counter, so a
 // tile's predecessors were taken by blocks that started earlier.  Its warps
 // rank their keys by digit in input order (warp-private 16-bit histograms;
-// the lanes sharing a digit found with one ballot per digit bit), the block publishes its per-digit counts and
-// finds each digit's count over all earlier tiles by decoupled look-back:
-// walking back over their published words until one carries an inclusive
-// prefix.  Keys then go to shared memory in digit order and out in contiguous
-// runs per digit.  A look-back wait gives up after spinLimit polls, raising
+// the lanes sharing a digit found with one ballot per digit bit) and the tile
+// goes to shared memory in digit order.  Thread t owns bins 2t and 2t + 1 and
+// publishes their counts as one 64-bit word (each half carries the flag), so
+// one walk serves both bins: decoupled look-back over the earlier tiles'
+// words until one carries an inclusive prefix.  Keys then go out in
+// contiguous runs per digit.  valsIn == nullptr means the identity (value =
+// index).  A look-back wait gives up after spinLimit polls, raising
 // PGA_ERR_TIMEOUT in *err (the order is then unspecified).
 constexpr int kSortThreads = 512;
 constexpr int kSortWarps = kSortThreads / 32;
@@ -201,24 +199,28 @@ constexpr int kSortItems = 10;
 constexpr uint32_t kSortTile = kSortThreads * kSortItems;
 constexpr uint32_t kHistStride = kBins + 16;  // u16 per warp histogram; bin kBins counts keys past n
 constexpr uint32_t kFlagAggregate = 1u << 30, kFlagPrefix = 2u << 30, kCountMask = (1u << 30) - 1u;
-constexpr int kLookback = 8;  // predecessor words loaded at once by a look-back step
+constexpr int kLookback = 16;  // predecessor words loaded at once by a look-back step
+static_assert(kBins == 2 * kSortThreads, "each thread owns two bins");
 constexpr size_t kOnesweepSmem =
     (size_t)kSortTile * 8 + (size_t)kSortTile * 4 + (size_t)kSortWarps * kHistStride * 2 + (size_t)kBins * 8;
 
-__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
-  uint32_t v;
-  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
+}
+__device__ __forceinline__ unsigned long long pair_word(uint32_t flag, uint32_t c0, uint32_t c1) {
+  return ((unsigned long long)(flag | c1) << 32) | (flag | c0);
 }
 
 __global__ void __launch_bounds__(kSortThreads, 2)
     k_onesweep(const unsigned long long* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
                unsigned long long* __restrict__ keysOut, uint32_t* __restrict__ valsOut, unsigned long long n,
-               uint32_t shift, const uint32_t* __restrict__ gBase, uint32_t* status, uint32_t* tileCounter, int* err,
-               uint32_t spinLimit) {
+               uint32_t shift, const uint32_t* __restrict__ gBase, unsigned long long* status,
+               uint32_t* tileCounter, int* err, uint32_t spinLimit) {
   extern __shared__ __align__(16) unsigned char smem_sort[];
   unsigned long long* sKeys = reinterpret_cast<unsigned long long*>(smem_sort);
   uint32_t* sVals = reinterpret_cast<uint32_t*>(sKeys + kSortTile);
@@ -238,11 +240,13 @@ __global__ void __launch_bounds__(kSortThreads, 2)
   unsigned lt;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
   unsigned long long key[kSortItems];
+  uint32_t val[kSortItems];
   uint32_t rank[kSortItems];
 #pragma unroll
   for (int k = 0; k < kSortItems; k++) {
     const unsigned long long i = warpBase + (unsigned)k * 32u + lane;
     key[k] = i < n ? __ldcs(keysIn + i) : 0ull;
+    val[k] = valsIn == nullptr ? (uint32_t)i : (i < n ? __ldcs(valsIn + i) : 0u);
   }
 #pragma unroll
   for (int k = 0; k < kSortItems; k++) {
@@ -271,7 +275,6 @@ __global__ void __launch_bounds__(kSortThreads, 2)
   // Thread t owns bins 2t and 2t + 1: the warps' exclusive prefixes in place,
   // the tile's count of each bin, published for the later tiles.
   uint32_t tot[2];
-  uint32_t* st = status + (size_t)tile * kBins;
 #pragma unroll
   for (int q = 0; q < 2; q++) {
     const uint32_t d = 2u * threadIdx.x + q;
@@ -283,8 +286,9 @@ __global__ void __launch_bounds__(kSortThreads, 2)
       run += c;
     }
     tot[q] = run;
-    st_relaxed(st + d, (tile == 0 ? kFlagPrefix : kFlagAggregate) | run);
   }
+  unsigned long long* st = status + (size_t)tile * (kBins / 2) + threadIdx.x;
+  st_relaxed64(st, pair_word(tile == 0 ? kFlagPrefix : kFlagAggregate, tot[0], tot[1]));
   // The tile's bin starts: an exclusive scan of the bins in order.
   {
     const uint32_t v = tot[0] + tot[1];
@@ -301,51 +305,9 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     sStart[2u * threadIdx.x] = before + x - v;
     sStart[2u * threadIdx.x + 1] = before + x - v + tot[0];
   }
-  // Decoupled look-back: each bin's count over the earlier tiles.  The words
-  // of kLookback predecessors are loaded at once (independent loads), then
-  // summed nearest first up to the first inclusive prefix; a word not yet
-  // published stops the sum there and is polled again.
-#pragma unroll 1
-  for (int q = 0; q < 2; q++) {
-    const uint32_t d = 2u * threadIdx.x + q;
-    uint32_t prefix = 0;
-    if (tile > 0) {
-      long long p = (long long)tile - 1;
-      uint32_t spins = 0;
-      while (p >= 0) {
-        uint32_t w[kLookback];
-#pragma unroll
-        for (int k = 0; k < kLookback; k++)
-          w[k] = p - k >= 0 ? ld_relaxed(status + (size_t)(p - k) * kBins + d) : kFlagPrefix;
-        int used = 0;
-        bool done = false, stalled = false;
-#pragma unroll
-        for (int k = 0; k < kLookback; k++) {
-          if (done || stalled) continue;
-          if ((w[k] >> 30) == 0u) {
-            stalled = true;
-            continue;
-          }
-          prefix += w[k] & kCountMask;
-          used++;
-          if ((w[k] & kFlagPrefix) != 0u) done = true;
-        }
-        if (done) break;
-        p -= used;
-        if (stalled) {
-          if (++spins > spinLimit) {
-            atomicCAS(err, 0, (int)PGA_ERR_TIMEOUT);
-            break;
-          }
-          __nanosleep(32);
-        }
-      }
-      st_relaxed(st + d, kFlagPrefix | (prefix + (q ? tot[1] : tot[0])));
-    }
-    sDst[d] = (int32_t)(__ldg(gBase + d) + prefix);
-  }
   __syncthreads();
-  // The tile in digit order in shared memory.
+  // The tile in digit order in shared memory (before the look-back: it needs
+  // only the tile's own counts).
 #pragma unroll
   for (int k = 0; k < kSortItems; k++) {
     const unsigned long long i = warpBase + (unsigned)k * 32u + lane;
@@ -353,9 +315,52 @@ __global__ void __launch_bounds__(kSortThreads, 2)
       const uint32_t d = (uint32_t)(key[k] >> shift) & (kBins - 1u);
       const uint32_t pos = sStart[d] + hist[d] + rank[k];
       sKeys[pos] = key[k];
-      sVals[pos] = __ldcs(valsIn + i);
+      sVals[pos] = val[k];
     }
   }
+  // Decoupled look-back: both bins' counts over the earlier tiles.  The words
+  // of kLookback predecessors are loaded at once (independent loads), then
+  // summed nearest first up to the first inclusive prefix; a word not yet
+  // published stops the sum there and is polled again.
+  uint32_t prefix0 = 0, prefix1 = 0;
+  if (tile > 0) {
+    long long p = (long long)tile - 1;
+    uint32_t spins = 0;
+    while (p >= 0) {
+      unsigned long long w[kLookback];
+#pragma unroll
+      for (int k = 0; k < kLookback; k++)
+        w[k] = p - k >= 0 ? ld_relaxed64(status + (size_t)(p - k) * (kBins / 2) + threadIdx.x)
+                          : pair_word(kFlagPrefix, 0u, 0u);
+      int used = 0;
+      bool done = false, stalled = false;
+#pragma unroll
+      for (int k = 0; k < kLookback; k++) {
+        if (done || stalled) continue;
+        const uint32_t lo = (uint32_t)w[k], hi = (uint32_t)(w[k] >> 32);
+        if ((lo >> 30) == 0u) {
+          stalled = true;
+          continue;
+        }
+        prefix0 += lo & kCountMask;
+        prefix1 += hi & kCountMask;
+        used++;
+        if ((lo & kFlagPrefix) != 0u) done = true;
+      }
+      if (done) break;
+      p -= used;
+      if (stalled) {
+        if (++spins > spinLimit) {
+          atomicCAS(err, 0, (int)PGA_ERR_TIMEOUT);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    st_relaxed64(st, pair_word(kFlagPrefix, prefix0 + tot[0], prefix1 + tot[1]));
+  }
+  sDst[2u * threadIdx.x] = (int32_t)(__ldg(gBase + 2u * threadIdx.x) + prefix0);
+  sDst[2u * threadIdx.x + 1] = (int32_t)(__ldg(gBase + 2u * threadIdx.x + 1) + prefix1);
   __syncthreads();
   // Out: consecutive positions of one digit go to consecutive places.
   const uint32_t count = (uint32_t)min((unsigned long long)kSortTile, n - tileBase);
@@ -375,45 +380,125 @@ __device__ __forceinline__ uint64_t term_path(const PgaTerminal* t, uint32_t i) 
 }
 
 // The radix sort orders the keys' top bits [kSortLowBit, 64) only, which
-// leaves runs of equal top bits in input order.  Each such run is ordered
-// here by insertion: by the whole
-// key (the Morton code and the path hash's top 34 bits), then, for equal keys,
-// by the full path hash, then by terminal index, keys and values moving
-// together.  The result is the order a full 64-bit sort plus tie fix gives:
-// lexicographic in (Morton code, path hash, terminal).  Runs are short; a
-// terminal record is read only for two equal 64-bit keys.
-__global__ void k_fix_ties(unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
-                           const PgaTerminal* __restrict__ t, unsigned long long cap,
-                           const unsigned long long* __restrict__ dN) {
-  const unsigned long long n = leaf_count(dN, cap);
-  unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i + 1 >= n) return;
-  const unsigned long long k = keys[i] >> kSortLowBit;
-  if ((keys[i + 1] >> kSortLowBit) != k || (i > 0 && (keys[i - 1] >> kSortLowBit) == k)) return;
-  unsigned long long j = i + 1;
-  while (j < n && (keys[j] >> kSortLowBit) == k) j++;
-  for (unsigned long long a = i + 1; a < j; a++) {
-    const unsigned long long kv = keys[a];
-    const uint32_t v = vals[a];
-    unsigned long long b = a;
-    while (b > i) {
-      const unsigned long long ku = keys[b - 1];
-      const uint32_t u = vals[b - 1];
-      bool first;  // does (ku, u) stay before (kv, v)?
-      if (ku != kv) {
-        first = ku < kv;
-      } else {
-        const uint64_t pu = term_path(t, u), pv = term_path(t, v);
-        first = pu < pv || (pu == pv && u < v);
+// leaves runs of equal top bits in input order (terminals in one Morton cell
+// whose path hashes share their top 10 bits: short runs, but about half of
+// the keys of a crowded scene lie in one).  The final order inside a run is
+// by the whole key (the Morton code and the path hash's top 34 bits), then,
+// for equal keys, by the full path hash, then by terminal index:
+// lexicographic in (Morton code, path hash, terminal), the order a full
+// 64-bit sort plus tie fix gives.  Each member of a run counts the members
+// that come before it and writes its key and value at run start + that count
+// into tieKeys / tieVals; one bit per position in tieMask marks the members.
+// The Karras pass takes a marked position's value from tieVals and the refit
+// writes its key from tieKeys, so the keys' top bits, all the Karras codes
+// read, do not change while a later kernel reads them.
+//
+// A warp ranks its 32 keys inside a window of kTieReach keys either side
+// (lane l holds window positions l and 32 + l): run boundaries from two
+// ballots of "equal to the left neighbour", and each member compares the low
+// 32 bits of its key (the rest is equal inside a run) with those of its run's
+// members, staged in shared memory.  A run that reaches the window's edge, or
+// that holds equal keys (then the paths decide), is ranked by the member
+// alone in global memory, reading a terminal record only for equal keys.
+constexpr int kTieReach = 16;
+__device__ __noinline__ void tie_rank_global(const unsigned long long* __restrict__ keys,
+                                             const uint32_t* __restrict__ vals, const PgaTerminal* __restrict__ t,
+                                             unsigned long long n, unsigned long long i,
+                                             unsigned long long* __restrict__ tieKeys,
+                                             uint32_t* __restrict__ tieVals) {
+  const unsigned long long ki = keys[i], k = ki >> kSortLowBit;
+  unsigned long long s = i, e = i + 1;
+  while (s > 0 && (keys[s - 1] >> kSortLowBit) == k) s--;
+  while (e < n && (keys[e] >> kSortLowBit) == k) e++;
+  const uint32_t vi = vals[i];
+  bool havePath = false;
+  uint64_t pi = 0;
+  unsigned long long before = 0;
+  for (unsigned long long b = s; b < e; b++) {
+    const unsigned long long kb = keys[b];
+    if (kb != ki) {
+      before += kb < ki;
+    } else if (b != i) {
+      if (!havePath) {
+        pi = term_path(t, vi);
+        havePath = true;
       }
-      if (first) break;
-      keys[b] = ku;
-      vals[b] = u;
-      b--;
+      const uint32_t vb = vals[b];
+      const uint64_t pb = term_path(t, vb);
+      before += pb < pi || (pb == pi && vb < vi);
     }
-    keys[b] = kv;
-    vals[b] = v;
   }
+  tieKeys[s + before] = ki;
+  tieVals[s + before] = vi;
+}
+
+__global__ void __launch_bounds__(kLbvhThreads) k_tie_rank(const unsigned long long* __restrict__ keys,
+                                                           const uint32_t* __restrict__ vals,
+                                                           const PgaTerminal* __restrict__ t, unsigned long long cap,
+                                                           const unsigned long long* __restrict__ dN,
+                                                           unsigned long long* __restrict__ tieKeys,
+                                                           uint32_t* __restrict__ tieVals,
+                                                           uint32_t* __restrict__ tieMask) {
+  constexpr unsigned kAll = 0xFFFFFFFFu;
+  __shared__ uint32_t sWin[kLbvhThreads / 32 * 64];
+  const long long n = (long long)leaf_count(dN, cap);
+  const int lane = (int)(threadIdx.x & 31u);
+  const long long w0 = ((long long)blockIdx.x * kLbvhThreads + threadIdx.x) & ~31ll;
+  if (w0 >= n) return;  // the whole warp
+  // window position q <-> key w0 - kTieReach + q; lane holds q = lane (a) and q = 32 + lane (b)
+  const long long ga = w0 - kTieReach + lane, gb = ga + 32;
+  const bool va = ga >= 0 && ga < n, vb = gb < n;
+  const unsigned long long ka = va ? keys[ga] : 0ull, kb = vb ? keys[gb] : 0ull;
+  const unsigned long long ta = ka >> kSortLowBit, tb = kb >> kSortLowBit;
+  // left neighbours: a's is lane - 1's a; b's is lane - 1's b, lane 0's is lane 31's a
+  const unsigned long long la = __shfl_up_sync(kAll, ta, 1);
+  const int lva = __shfl_up_sync(kAll, (int)va, 1);
+  const int src = (lane + 31) & 31;
+  const unsigned long long lb = __shfl_sync(kAll, lane == 31 ? ta : tb, src);
+  const int lvb = __shfl_sync(kAll, lane == 31 ? (int)va : (int)vb, src);
+  const bool eqa = lane > 0 && va && lva && la == ta;
+  const bool eqb = vb && lvb && lb == tb;
+  const unsigned long long eq = (unsigned long long)__ballot_sync(kAll, eqa) |
+                                ((unsigned long long)__ballot_sync(kAll, eqb) << 32);
+  // this lane's key sits at window position p (eq bit q: q and q - 1 in one run)
+  const int p = kTieReach + lane;
+  const long long i = w0 + lane;
+  const bool inRun = i < n && (((eq >> p) & 1ull) || ((eq >> (p + 1)) & 1ull));
+  const unsigned members = __ballot_sync(kAll, inRun);
+  if (lane == 0) tieMask[w0 >> 5] = members;
+  if (members == 0u) return;  // the whole warp
+  const unsigned long long upto = (2ull << p) - 1ull;  // positions [0, p]
+  const int s = 63 - __clzll(~eq & upto);              // eq bit 0 is clear: the run's first position
+  const unsigned long long past = ~eq & ~upto;
+  const int e = past ? __ffsll((long long)past) - 2 : 63;  // the run's last position
+  const bool inWindow = inRun && s > 0 && e < 63;
+  // the window's low key halves in this warp's slice of shared memory
+  uint32_t* win = sWin + (threadIdx.x >> 5) * 64;
+  win[lane] = (uint32_t)ka;
+  win[32 + lane] = (uint32_t)kb;
+  __syncwarp();
+  uint32_t before = 0;
+  bool equal = false;
+  if (inWindow) {
+    const uint32_t li = win[p];
+    for (int q = s; q <= e; q++) {
+      const uint32_t v = win[q];
+      before += v < li;
+      equal |= v == li && q != p;
+    }
+  }
+  if (!inRun) return;
+  if (inWindow && !equal) {
+    const long long dst = w0 - kTieReach + s + (long long)before;
+    tieKeys[dst] = keys[i];
+    tieVals[dst] = vals[i];
+  } else {
+    tie_rank_global(keys, vals, t, (unsigned long long)n, (unsigned long long)i, tieKeys, tieVals);
+  }
+}
+
+__device__ __forceinline__ bool tie_member(const uint32_t* tieMask, unsigned long long i) {
+  return (__ldg(tieMask + (i >> 5)) >> (i & 31u)) & 1u;
 }
 
 __device__ __forceinline__ unsigned long long karras_code(const unsigned long long* keys, long long j) {
@@ -422,21 +507,25 @@ __device__ __forceinline__ unsigned long long karras_code(const unsigned long lo
 
 // buildRadixTree (GPUBVHConstructor.cuh:88-213), one thread per internal node,
 // with bounds checks on every probe.
-// Also gathers the leaf boxes into sorted order (one independent load per
-// leaf here instead of a dependent one inside the refit's climb) and clears
+// Also gathers the leaves' terminal indices (a tie-run member's from
+// tieVals) and boxes into sorted order (one independent load per leaf here
+// instead of a dependent one ahead of the refit's climb), writes the other
+// end of each node's leaf range (one end is the node's own index) and clears
 // the refit's arrival counters.  Fewer than two leaves make no tree.
 __global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long long* __restrict__ keys, long long cap,
                                                          const unsigned long long* __restrict__ dN,
                                                          int32_t* __restrict__ nodes, uint32_t* __restrict__ leafParents,
                                                          uint32_t* __restrict__ sortedVals, const uint32_t* __restrict__ vals,
+                                                         const uint32_t* __restrict__ tieMask,
+                                                         const uint32_t* __restrict__ tieVals,
                                                          const float* __restrict__ leafBox,
-                                                         float* __restrict__ sortedBox, int2* __restrict__ nodeRange,
-                                                         uint32_t* __restrict__ arrival) {
+                                                         float* __restrict__ sortedBox,
+                                                         int32_t* __restrict__ nodeOther, uint32_t* __restrict__ arrival) {
   const long long n = (long long)leaf_count(dN, (unsigned long long)cap);
   if (n < 2) return;
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
-    const uint32_t v = vals[i];
+    const uint32_t v = tie_member(tieMask, (unsigned long long)i) ? tieVals[i] : vals[i];
     sortedVals[i] = v;
     const float2* src = reinterpret_cast<const float2*>(leafBox + (size_t)v * 6);
     float2* dst = reinterpret_cast<float2*>(sortedBox + (size_t)i * 6);
@@ -486,7 +575,7 @@ __global__ void __launch_bounds__(kLbvhThreads) k_karras(const unsigned long lon
   if (right < 0) nodes[(-right) * 3 + 0] = (int32_t)i;
   else leafParents[right] = (uint32_t)i;
   if (i == 0) nodes[0] = -1;
-  nodeRange[i] = make_int2((int)min(i, j), (int)max(i, j));
+  nodeOther[i] = (int32_t)j;
 }
 
 // Arrival counter bump at GPU scope with only the ordering the step needs.
@@ -530,72 +619,150 @@ __device__ __forceinline__ void load_box(const float* p, float mn[3], float mx[3
 // climber keeps the box of the child it comes from in registers and reads
 // only the sibling's; the union is min/max(left, right) in that order.
 //
-// Thread j handles sorted leaf j, so a block holds leaves [B, B + 256).  A node
-// whose leaf range lies inside that span is reached only by threads of the
-// block: its arrival counter and box sit in shared memory (index node - B;
-// a Karras node's index is one end of its range) with block-scope ordering.
-// Only nodes whose range crosses a block boundary -- a few percent -- use
-// global counters at GPU scope (`arrive`).  Every node's box is also stored
-// to aabbs, the output.  A node's links, its range and a leaf sibling's box
-// are fixed before this kernel, so they are read ahead of the arrival.
-__global__ void __launch_bounds__(kLbvhThreads) k_refit(const float* __restrict__ sortedBox, long long cap,
-                                                        const unsigned long long* __restrict__ dN,
-                                                        const int32_t* __restrict__ nodes,
-                                                        const int2* __restrict__ nodeRange,
-                                                        const uint32_t* __restrict__ leafParents,
-                                                        uint32_t* __restrict__ arrival, float* __restrict__ aabbs) {
+// Two kernels.  In k_refit_local thread j handles sorted leaf j, so a block
+// holds leaves [B, B + 256).  Its threads first stage their leaves' boxes and
+// the records of internal nodes [B, B + 256) (links and the other end of the
+// leaf range) in shared memory: one round of independent, coalesced loads.
+// A node whose leaf range lies inside [B, B + 256) is reached only by threads
+// of the block: its arrival counter and box sit in shared memory (index
+// node - B; a Karras node's index is one end of its range) with block-scope
+// ordering.  A climber that reaches a node whose range crosses the block's
+// boundary (a few percent of the nodes; all their ancestors cross too) stops
+// there and queues the child it comes from.  k_refit_global then carries the
+// queued climbers up through those nodes with arrival counters at GPU scope,
+// so no block of the first kernel waits on a long climb to the root.  Every
+// node's box is also stored to aabbs, the output.  Each leaf's thread also
+// writes the final key of a tie-run member.
+__device__ __forceinline__ void load_box_ldg(const float* __restrict__ p, float mn[3], float mx[3]) {
+  const float2* q = reinterpret_cast<const float2*>(p);
+  const float2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+  mn[0] = a.x; mn[1] = a.y; mn[2] = b.x; mx[0] = b.y; mx[1] = c.x; mx[2] = c.y;
+}
+
+__device__ __forceinline__ void store_box(float* p, const float mn[3], const float mx[3]) {
+  float2* o = reinterpret_cast<float2*>(p);
+  __stcg(o + 0, make_float2(mn[0], mn[1]));
+  __stcg(o + 1, make_float2(mn[2], mx[0]));
+  __stcg(o + 2, make_float2(mx[1], mx[2]));
+}
+
+// The union in (left, right) order of the climber's box (mn, mx; from the
+// left child when fromLeft) and its sibling's.
+__device__ __forceinline__ void merge_box(bool fromLeft, float mn[3], float mx[3], const float smn[3],
+                                          const float smx[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float lmn = fromLeft ? mn[k] : smn[k], rmn = fromLeft ? smn[k] : mn[k];
+    const float lmx = fromLeft ? mx[k] : smx[k], rmx = fromLeft ? smx[k] : mx[k];
+    mn[k] = fminf(lmn, rmn);
+    mx[k] = fmaxf(lmx, rmx);
+  }
+}
+
+__global__ void __launch_bounds__(kLbvhThreads) k_refit_local(const float* __restrict__ sortedBox, long long cap,
+                                                              const unsigned long long* __restrict__ dN,
+                                                              const int32_t* __restrict__ nodes,
+                                                              const int32_t* __restrict__ nodeOther,
+                                                              const uint32_t* __restrict__ leafParents,
+                                                              float* __restrict__ aabbs,
+                                                              int32_t* __restrict__ queue, uint32_t* __restrict__ queued,
+                                                              const uint32_t* __restrict__ tieMask,
+                                                              const unsigned long long* __restrict__ tieKeys,
+                                                              unsigned long long* __restrict__ keys) {
   __shared__ uint32_t blockArrive[kLbvhThreads];
-  __shared__ float blockBox[kLbvhThreads * 6];
+  __shared__ float blockBox[kLbvhThreads * 6];  // internal nodes [B, E)
+  __shared__ float sLeafBox[kLbvhThreads * 6];  // leaves [B, E)
+  __shared__ int4 sNode[kLbvhThreads];          // internal nodes [B, E): parent, left, right, other end
   const long long n = (long long)leaf_count(dN, (unsigned long long)cap);
   if (n < 2) return;
-  blockArrive[threadIdx.x] = 0u;
-  __syncthreads();
   const long long B = (long long)blockIdx.x * kLbvhThreads;
+  if (B >= n) return;  // the whole block
   const long long E = min(B + kLbvhThreads, n);
-  long long leaf = B + threadIdx.x;
-  if (leaf >= n) return;
+  const long long leaf = B + threadIdx.x;
+  blockArrive[threadIdx.x] = 0u;
   float mn[3], mx[3];
-  load_box(sortedBox + (size_t)leaf * 6, mn, mx);
-  long long cur = leafParents[leaf];
+  long long cur = -1;
+  if (leaf < n) {
+    if (tie_member(tieMask, (unsigned long long)leaf)) keys[leaf] = tieKeys[leaf];
+    load_box_ldg(sortedBox + (size_t)leaf * 6, mn, mx);
+    float* q = &sLeafBox[threadIdx.x * 6];
+    q[0] = mn[0]; q[1] = mn[1]; q[2] = mn[2]; q[3] = mx[0]; q[4] = mx[1]; q[5] = mx[2];
+    cur = __ldg(leafParents + leaf);
+  }
+  if (leaf < n - 1)
+    sNode[threadIdx.x] = make_int4(__ldg(nodes + leaf * 3 + 0), __ldg(nodes + leaf * 3 + 1),
+                                   __ldg(nodes + leaf * 3 + 2), __ldg(nodeOther + leaf));
+  __syncthreads();
+  if (leaf >= n) return;
   int32_t from = (int32_t)leaf;  // child id as the node table stores it: leaf j -> j, internal k -> -k
-  for (long long guard = 0; guard < n; guard++) {
-    const int32_t l = __ldg(&nodes[cur * 3 + 1]), r = __ldg(&nodes[cur * 3 + 2]);
-    const int32_t parent = __ldg(&nodes[cur * 3 + 0]);
-    const int2 range = __ldg(&nodeRange[cur]);
-    const bool local = range.x >= B && range.y < E;  // then B <= cur < E
-    const bool fromLeft = l == from;
-    const int32_t sib = fromLeft ? r : l;
-    float smn[3], smx[3];
-    if (sib >= 0) load_box(sortedBox + (size_t)sib * 6, smn, smx);
+  for (int level = 0; level < kLbvhThreads; level++) {
+    bool local = cur >= B && cur < E;
+    int4 rec = make_int4(0, 0, 0, 0);
     if (local) {
-      if (arrive_block(&blockArrive[cur - B]) == 0) return;
-      if (sib < 0) {  // an internal sibling of a local node is local too
-        const float* q = &blockBox[(-(long long)sib - B) * 6];
-        smn[0] = q[0]; smn[1] = q[1]; smn[2] = q[2]; smx[0] = q[3]; smx[1] = q[4]; smx[2] = q[5];
-      }
-    } else {
-      if (arrive(&arrival[cur], from < 0, sib < 0) == 0) return;
-      if (sib < 0) load_box(aabbs + (size_t)(-(long long)sib) * 6, smn, smx);
+      rec = sNode[cur - B];
+      local = min(cur, (long long)rec.w) >= B && max(cur, (long long)rec.w) < E;
     }
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const float lmn = fromLeft ? mn[k] : smn[k], rmn = fromLeft ? smn[k] : mn[k];
-      const float lmx = fromLeft ? mx[k] : smx[k], rmx = fromLeft ? smx[k] : mx[k];
-      mn[k] = fminf(lmn, rmn);
-      mx[k] = fmaxf(lmx, rmx);
+    if (!local) {  // the node's range crosses the block's boundary: k_refit_global goes on from here
+      queue[atomicAdd(queued, 1u)] = from;
+      return;
     }
-    float2* o = reinterpret_cast<float2*>(aabbs + (size_t)cur * 6);
-    __stcg(o + 0, make_float2(mn[0], mn[1]));
-    __stcg(o + 1, make_float2(mn[2], mx[0]));
-    __stcg(o + 2, make_float2(mx[1], mx[2]));
-    if (local) {
-      float* q = &blockBox[(cur - B) * 6];
-      q[0] = mn[0]; q[1] = mn[1]; q[2] = mn[2]; q[3] = mx[0]; q[4] = mx[1]; q[5] = mx[2];
-    }
+    if (arrive_block(&blockArrive[cur - B]) == 0) return;
+    const bool fromLeft = rec.y == from;
+    const int32_t sib = fromLeft ? rec.z : rec.y;  // inside [B, E): the node is local
+    const float* q = sib >= 0 ? &sLeafBox[(sib - B) * 6] : &blockBox[(-(long long)sib - B) * 6];
+    const float smn[3] = {q[0], q[1], q[2]}, smx[3] = {q[3], q[4], q[5]};
+    merge_box(fromLeft, mn, mx, smn, smx);
+    store_box(aabbs + (size_t)cur * 6, mn, mx);
+    float* o = &blockBox[(cur - B) * 6];
+    o[0] = mn[0]; o[1] = mn[1]; o[2] = mn[2]; o[3] = mx[0]; o[4] = mx[1]; o[5] = mx[2];
     if (cur == 0) return;
     from = -(int32_t)cur;
-    cur = parent;
-    if (cur < 0) return;
+    cur = rec.x;
+  }
+}
+
+// The queued climbers (*queued of them, each the child it comes from) up
+// through the nodes that cross block boundaries: arrival counters at GPU
+// scope, the boxes of the children the first kernel finished read from
+// aabbs / sortedBox (written before this launch), those of this kernel with
+// release / acquire on the counter.  Grid-stride over the queue.
+__global__ void __launch_bounds__(kLbvhThreads) k_refit_global(const float* __restrict__ sortedBox, long long cap,
+                                                               const unsigned long long* __restrict__ dN,
+                                                               const int32_t* __restrict__ nodes,
+                                                               const uint32_t* __restrict__ leafParents,
+                                                               uint32_t* __restrict__ arrival, float* aabbs,
+                                                               const int32_t* __restrict__ queue,
+                                                               const uint32_t* __restrict__ queued) {
+  const long long n = (long long)leaf_count(dN, (unsigned long long)cap);
+  if (n < 2) return;
+  const uint32_t count = *queued;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    int32_t from = queue[k];
+    float mn[3], mx[3];
+    long long cur;
+    if (from >= 0) {
+      load_box_ldg(sortedBox + (size_t)from * 6, mn, mx);
+      cur = leafParents[from];
+    } else {
+      load_box(aabbs + (size_t)(-(long long)from) * 6, mn, mx);
+      cur = nodes[(size_t)(-(long long)from) * 3 + 0];
+    }
+    bool published = false;  // the climber's box was stored by this kernel
+    for (long long guard = 0; guard < n && cur >= 0; guard++) {
+      const int32_t parent = __ldg(nodes + cur * 3 + 0), l = __ldg(nodes + cur * 3 + 1), r = __ldg(nodes + cur * 3 + 2);
+      const bool fromLeft = l == from;
+      const int32_t sib = fromLeft ? r : l;
+      float smn[3], smx[3];
+      if (sib >= 0) load_box_ldg(sortedBox + (size_t)sib * 6, smn, smx);
+      if (arrive(&arrival[cur], published, sib < 0) == 0) break;
+      if (sib < 0) load_box(aabbs + (size_t)(-(long long)sib) * 6, smn, smx);
+      merge_box(fromLeft, mn, mx, smn, smx);
+      store_box(aabbs + (size_t)cur * 6, mn, mx);
+      published = true;
+      if (cur == 0) break;
+      from = -(int32_t)cur;
+      cur = parent;
+    }
   }
 }
 
@@ -616,8 +783,8 @@ extern "C" size_t pga_lbvh_temp_bytes(uint64_t n) {
 namespace pga {
 
 // Scratch of one build: keys, two value arrays, arrival counters, leaf boxes
-// (terminal and sorted order), node ranges, the radix sort's scratch, and the
-// word a sort wait that gives up raises PGA_ERR_TIMEOUT in.
+// (terminal and sorted order), the other ends of the node ranges, the radix sort's
+// scratch, and the word a sort wait that gives up raises PGA_ERR_TIMEOUT in.
 struct LbvhScratch {
   unsigned long long* keysA;
   uint32_t* valsA;
@@ -625,20 +792,20 @@ struct LbvhScratch {
   uint32_t* arrival;
   float* leafBox;
   float* sortedBox;
-  int2* nodeRange;
+  int32_t* nodeOther;
   void* sortTemp;
   size_t sortTempBytes;
   int* err;
 };
 
-// Polls of a look-back wait before it gives up (each followed by a 64 ns sleep).
+// Polls of a look-back wait before it gives up (each followed by a 32 ns sleep).
 constexpr uint32_t kSortSpinLimit = 1u << 22;
 
 // The launches of a build over `cap` leaves, or over min(*dN, cap) when dN is
 // a device count (then `cap` sizes the grids and the sort): Morton codes, the
 // digit histograms and bases, four sort passes (keys ping-pong
-// between out->keys and keysA, ending in out->keys), the tie fix, Karras and
-// the refit.
+// between out->keys and keysA, ending in out->keys), the tie-run ranks,
+// Karras and the two refit kernels.
 static PgaStatus launch_lbvh(const PgaTerminal* t, unsigned long long cap, const unsigned long long* dN,
                              const PgaBounds* bounds, const PgaLbvh* out, const LbvhScratch& w, cudaStream_t s) {
   Bounds b;
@@ -661,7 +828,7 @@ static PgaStatus launch_lbvh(const PgaTerminal* t, unsigned long long cap, const
   PGA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const unsigned blocks = (unsigned)((cap + kLbvhThreads - 1) / kLbvhThreads);
   unsigned long long* keys = (unsigned long long*)out->keys;
-  k_morton<<<blocks, kLbvhThreads, 0, s>>>(t, cap, dN, b, keys, w.valsA, w.leafBox);
+  k_morton<<<blocks, kLbvhThreads, 0, s>>>(t, cap, dN, b, keys, w.leafBox);
   PGA_CUDA_TRY(cudaGetLastError());
   const unsigned histBlocks =
       (unsigned)std::min<unsigned long long>((cap + kHistThreads - 1) / kHistThreads, (unsigned long long)sms * 4);
@@ -670,33 +837,50 @@ static PgaStatus launch_lbvh(const PgaTerminal* t, unsigned long long cap, const
   k_sort_bases<<<1, kBins, 0, s>>>(hist, gBase);
   PGA_CUDA_TRY(cudaGetLastError());
   PGA_CUDA_TRY(cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOnesweepSmem));
+  // The first pass reads the identity values (terminal index); the values
+  // then ping-pong valsB -> valsA -> valsB -> valsA.
   unsigned long long* kIn = keys;
   unsigned long long* kOut = w.keysA;
-  uint32_t* vIn = w.valsA;
+  uint32_t* vIn = nullptr;
   uint32_t* vOut = w.valsB;
+  unsigned long long* words = reinterpret_cast<unsigned long long*>(status);
   for (int q = 0; q < kSortPasses; q++) {
     k_onesweep<<<(unsigned)tiles, kSortThreads, kOnesweepSmem, s>>>(
         kIn, vIn, kOut, vOut, cap, (uint32_t)(kSortLowBit + q * kRadixBits), gBase + q * kBins,
-        status + (size_t)q * tiles * kBins, counters + q, w.err, kSortSpinLimit);
+        words + (size_t)q * tiles * (kBins / 2), counters + q, w.err, kSortSpinLimit);
     PGA_CUDA_TRY(cudaGetLastError());
     std::swap(kIn, kOut);
-    std::swap(vIn, vOut);
+    vIn = vOut;
+    vOut = vOut == w.valsB ? w.valsA : w.valsB;
   }
   static_assert(kSortPasses % 2 == 0, "an even number of passes ends in out->keys and valsA");
-  k_fix_ties<<<blocks, kLbvhThreads, 0, s>>>(keys, w.valsA, t, cap, dN);
+  // The tie runs' order goes to keysA / valsB (free after the sort), the
+  // member bits over the look-back words (free too; tiles * kBins * passes
+  // words >= cap / 32).
+  uint32_t* tieMask = status;
+  k_tie_rank<<<blocks, kLbvhThreads, 0, s>>>(keys, w.valsA, t, cap, dN, w.keysA, w.valsB, tieMask);
   PGA_CUDA_TRY(cudaGetLastError());
   k_karras<<<blocks, kLbvhThreads, 0, s>>>(keys, (long long)cap, dN, out->nodes, out->leafParents, out->leafTerminal,
-                                           w.valsA, w.leafBox, w.sortedBox, w.nodeRange, w.arrival);
+                                           w.valsA, tieMask, w.valsB, w.leafBox, w.sortedBox, w.nodeOther, w.arrival);
   PGA_CUDA_TRY(cudaGetLastError());
-  k_refit<<<blocks, kLbvhThreads, 0, s>>>(w.sortedBox, (long long)cap, dN, out->nodes, w.nodeRange, out->leafParents,
-                                          w.arrival, out->aabbs);
+  // The refit's queue of climbers that leave their block goes to valsB (free
+  // after Karras), its length to the sort scratch's counter word kSortPasses.
+  uint32_t* queued = counters + kSortPasses;
+  k_refit_local<<<blocks, kLbvhThreads, 0, s>>>(w.sortedBox, (long long)cap, dN, out->nodes, w.nodeOther,
+                                                out->leafParents, out->aabbs, reinterpret_cast<int32_t*>(w.valsB),
+                                                queued, tieMask, w.keysA, keys);
+  PGA_CUDA_TRY(cudaGetLastError());
+  const unsigned globalBlocks = std::min<unsigned>(blocks, (unsigned)sms * (2048 / kLbvhThreads));
+  k_refit_global<<<globalBlocks, kLbvhThreads, 0, s>>>(w.sortedBox, (long long)cap, dN, out->nodes,
+                                                       out->leafParents, w.arrival, out->aabbs,
+                                                       reinterpret_cast<const int32_t*>(w.valsB), queued);
   PGA_CUDA_TRY(cudaGetLastError());
   return PGA_OK;
 }
 
 static LbvhScratch engine_scratch(PgaEngine* e) {
-  return LbvhScratch{e->dKeysA,     e->dValsA,    e->dValsB,    e->dArrival,     e->dLeafAabb,
-                     e->dLeafAabbSorted, e->dNodeRange, e->dSortTemp, e->sortTempBytes, &e->dState->status};
+  return LbvhScratch{e->dKeysA,     e->dValsA,     e->dValsB,    e->dArrival,      e->dLeafAabb,
+                     e->dLeafAabbSorted, e->dNodeOther, e->dSortTemp, e->sortTempBytes, &e->dState->status};
 }
 
 static bool lbvh_out_ok(const PgaLbvh* out) {
@@ -803,7 +987,7 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
   }
   if (n == 0) return PGA_OK;  // set-up only
   // Carve the scratch: keys, two value arrays, arrival counters, leaf boxes
-  // (terminal and sorted order), node ranges, sort temp.
+  // (terminal and sorted order), the other ends of the node ranges, sort temp.
   size_t temp = pga_lbvh_temp_bytes(n);
   size_t off = 0;
   unsigned long long* keysA = reinterpret_cast<unsigned long long*>(base + off);
@@ -818,8 +1002,8 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
   off += align256(n * 6 * sizeof(float));
   float* sortedBox = reinterpret_cast<float*>(base + off);
   off += align256(n * 6 * sizeof(float));
-  int2* nodeRange = reinterpret_cast<int2*>(base + off);
-  off += align256(n * sizeof(int2));
+  int32_t* nodeOther = reinterpret_cast<int32_t*>(base + off);
+  off += align256(n * sizeof(int32_t));
   void* sortTemp = base + off;
   off += align256(temp);
   int* err = reinterpret_cast<int*>(base + off);  // a sort wait that gives up marks it (unreported)
@@ -828,6 +1012,6 @@ extern "C" PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64
     set_error("pga_lbvh_build_static: fixed scratch too small for the radix sort of " + std::to_string(n) + " keys");
     return PGA_ERR_INVALID_ARGUMENT;
   }
-  const LbvhScratch w{keysA, valsA, valsB, arrival, leafBox, sortedBox, nodeRange, sortTemp, temp, err};
+  const LbvhScratch w{keysA, valsA, valsB, arrival, leafBox, sortedBox, nodeOther, sortTemp, temp, err};
   return launch_lbvh(dTerminals, n, nullptr, bounds, out, w, (cudaStream_t)stream);
 }

@@ -349,9 +349,10 @@ def test_mixed_65536_full_size_bit_exact():
 def test_lbvh_full_size_bit_exact(scene):
     """The LBVH over every terminal of the full city (5.86M leaves; 30-bit
     Morton cells of 3.2 m hold many terminals, so 85% of neighbouring sorted
-    keys share their Morton code and go through the tie fix) and of a
-    4,096-axiom mix (9.4M leaves, 93% shared) against the restatement: keys,
-    leaf order, topology, leaf parents and boxes bit for bit."""
+    keys share their Morton code and are ordered by sub-cell code and path)
+    and of a 4,096-axiom mix (9.4M leaves, 93% shared) against the
+    restatement: keys, leaf order, topology, leaf parents and boxes bit for
+    bit."""
     if scene == "city_4096":
         b, bounds = scenes.city(4096), (-50.0, -50.0, -1.0, 3250.0, 3250.0, 400.0)
     else:
@@ -365,7 +366,7 @@ def test_lbvh_full_size_bit_exact(scene):
         bounds = tuple(float(v) for v in c.min(0) - 1.0) + tuple(float(v) for v in c.max(0) + 1.0)
     nodes, lp, aabb, lt, keys = oracle.lbvh(got, bounds)
     runs = int((keys[1:] >> 34 == keys[:-1] >> 34).sum())
-    assert runs > n // 4, "the scene should exercise the tie fix"
+    assert runs > n // 4, "the scene should share Morton codes"
     bv = eng.lbvh(out, n, bounds)
     torch.cuda.synchronize()
     assert np.array_equal(bv["keys"].cpu().numpy().view(np.uint64), keys), "Morton keys differ"
@@ -373,6 +374,65 @@ def test_lbvh_full_size_bit_exact(scene):
     assert np.array_equal(bv["nodes"].cpu().numpy(), nodes), "topology differs"
     assert np.array_equal(bv["leafParents"].cpu().numpy().view(np.uint32), lp)
     assert np.array_equal(bv["aabbs"].cpu().numpy().view(np.uint32), aabb.view(np.uint32)), "boxes differ"
+    eng.release()
+
+
+@pytest.mark.parametrize("counted", [False, True])
+def test_lbvh_tie_runs_bit_exact(counted):
+    """Terminals that share a Morton cell and their path hash's top 10 bits
+    share the sorted part of the key, so their order comes from the tie ranks:
+    200,000 synthetic records, half of them at 250 shared centres; groups of 2
+    to 48 records (and one of 3,000) at one centre whose path hashes share
+    their top 10 bits (runs inside and across the 64-key windows of the
+    ranking warps, and one far longer); a tenth with a path hash and centre
+    copied from another record (equal keys, then equal paths: ordered by
+    terminal index); a third of them quads.  Keys, leaf order, topology,
+    parents and boxes against the restatement bit for bit, built over the host
+    count and over a device count with padding."""
+    from operatorgraph_gb300.engine import Engine
+
+    n, cap = 200_000, 200_000 + (4096 if counted else 0)
+    rng = np.random.default_rng(5)
+    rec = np.zeros(n, G.TERMINAL_DT)
+    m = rng.uniform(-0.5, 0.5, (n, 12)).astype(np.float32)
+    centres = rng.uniform(-9.0, 9.0, (250, 3)).astype(np.float32)
+    m[:, [3, 7, 11]] = rng.uniform(-9.0, 9.0, (n, 3)).astype(np.float32)
+    shared = rng.choice(n, n // 2, replace=False)
+    m[np.ix_(shared, [3, 7, 11])] = centres[rng.integers(0, 250, len(shared))]
+    paths = rng.integers(0, 2**64, size=n, dtype=np.uint64)
+    grouped = rng.permutation(n)
+    at = 0
+    for size in [3000] + [int(x) for x in rng.integers(2, 49, 400)]:
+        g = grouped[at:at + size]
+        at += size
+        m[np.ix_(g, [3, 7, 11])] = rng.uniform(-9.0, 9.0, 3).astype(np.float32)
+        top = np.uint64(int(rng.integers(0, 1024)) << 54)
+        paths[g] = top | (paths[g] & np.uint64((1 << 54) - 1))
+    dst, src = rng.choice(n, n // 10, replace=False), rng.choice(n, n // 10, replace=False)
+    paths[dst] = paths[src]
+    m[np.ix_(dst, [3, 7, 11])] = m[np.ix_(src, [3, 7, 11])]  # same centre and path: equal keys
+    rec["m"] = m
+    rec["rule"] = np.where(rng.random(n) < 1 / 3, np.uint32(1 << 31), np.uint32(0)) | rng.integers(0, 64, n).astype(np.uint32)
+    rec["path"] = paths
+    bounds = (-10.0, -10.0, -10.0, 10.0, 10.0, 10.0)
+    nodes, lp, aabb, lt, keys = oracle.lbvh(rec, bounds)
+    _, runs = np.unique(keys >> np.uint64(24), return_counts=True)
+    assert runs.max() >= 2500 and int(runs[runs > 1].sum()) > 20_000, "the records should make tie runs"
+    assert int((keys[1:] == keys[:-1]).sum()) > 100, "some keys should be equal"
+    out = torch.zeros((cap, 64), dtype=torch.uint8, device="cuda")
+    out[:n] = torch.from_numpy(rec.view(np.uint8).reshape(n, 64).copy()).cuda()
+    eng = Engine(scenes.building()["entries"], node_capacity=1 << 16, max_terminals=cap)
+    if counted:
+        bv = eng.lbvh(out, cap, bounds, count=torch.tensor([n], dtype=torch.int64, device="cuda"))
+    else:
+        bv = eng.lbvh(out, n, bounds)
+    torch.cuda.synchronize()
+    k = bv["keys"].cpu().numpy().view(np.uint64)
+    assert np.array_equal(k[:n], keys), "Morton keys differ"
+    assert np.array_equal(bv["leafTerminal"][:n].cpu().numpy().view(np.uint32), lt), "leaf order differs"
+    assert np.array_equal(bv["nodes"][: n - 1].cpu().numpy(), nodes), "topology differs"
+    assert np.array_equal(bv["leafParents"][:n].cpu().numpy().view(np.uint32), lp)
+    assert np.array_equal(bv["aabbs"][: n - 1].cpu().numpy().view(np.uint32), aabb.view(np.uint32)), "boxes differ"
     eng.release()
 
 
