@@ -8,7 +8,7 @@ instanced terminals (375 MB of 64-byte records, larger than the 129 MB L2;
 L2 is also flushed with a 256 MB write before every timed step).
 
 schedule: before timing, the engine knobs are autotuned on this workload
-         (operatorgraph_gb300/autotune.py, 32 candidates); the fastest drives
+         (operatorgraph_gb300/autotune.py, 64 candidates); the fastest drives
          the timed engine ("batched + autotuned").
 value  : terminals/s with axioms and grammar resident in HBM (CUDA events on
          the launching stream around pga_derive).
@@ -292,7 +292,7 @@ def our_arm(args):
         tuned_ms, tuning, default_ms = None, [], None
     else:
         best, tuned_ms, tuning = autotune.tune(batch, cap, node_capacity=1 << 22, runs=5)
-        default_ms = next((r["ms"] for r in tuning if r["config"] == autotune.DEFAULT_CONFIG), None)
+        default_ms = next((r["ms"] for r in tuning if autotune.is_default(r["config"])), None)
     eng = Engine(batch["entries"], node_capacity=1 << 22, max_terminals=cap, **best)
     d_ax = torch.from_numpy(batch["axioms"].view(np.uint8).copy()).to(dev)
     out = torch.empty((cap, 64), dtype=torch.uint8, device=dev)
@@ -765,11 +765,11 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     # (axioms grouped by root entry), against the engine's defaults.
     from operatorgraph_gb300 import autotune
 
-    mspace = {"sub_item": (4, 8), "narrow_sub_item": (0, 2), "items_per_lane": (1,), "blocks_per_sm": (0,)}
+    mspace = {"sub_item": (4, 8), "narrow_sub_item": (0, 2), "items_per_lane": (1,), "blocks_per_sm": (0,),
+              "dynamic_chunks": (False, True)}
     mbest, mms, mres = autotune.tune(mx, mcap, node_capacity=1 << 27, space=mspace, runs=3)
-    dflt = dict(autotune.DEFAULT_CONFIG, group_axioms=False)
     res["mixed65536_schedule"] = mbest
-    res["mixed65536_default_ms"] = next((r["ms"] for r in mres if r["config"] == dflt), None)
+    res["mixed65536_default_ms"] = next((r["ms"] for r in mres if autotune.is_default(r["config"])), None)
     res["mixed65536_index_order_ms"] = min(r["ms"] for r in mres
                                            if r["ms"] is not None and not r["config"]["group_axioms"])
     em = Engine(mx["entries"], node_capacity=1 << 27, max_terminals=mcap, **mbest)
@@ -794,10 +794,10 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
 
     fbest, fms, fres = autotune.tune(fo, fcap, node_capacity=1 << 23, runs=3,
                                      space={"sub_item": (1, 2, 4, 8), "narrow_sub_item": (0, 1), "items_per_lane": (1,),
-                                            "blocks_per_sm": (0,)})
+                                            "blocks_per_sm": (0,), "dynamic_chunks": (False, True)})
     res["forest4096_schedule"] = fbest
     res["forest4096_tuned_ms"] = fms
-    res["forest4096_default_ms"] = next((r["ms"] for r in fres if r["config"] == autotune.DEFAULT_CONFIG), None)
+    res["forest4096_default_ms"] = next((r["ms"] for r in fres if autotune.is_default(r["config"])), None)
     eo = Engine(fo["entries"], node_capacity=1 << 23, max_terminals=fcap, **fbest)
     d_fo = torch.from_numpy(fo["axioms"].view(np.uint8).copy()).to(dev)
     fout = torch.empty((fcap, 64), dtype=torch.uint8, device=dev)

@@ -12,6 +12,9 @@ schedule is a handful of engine knobs, so tuning is a timed sweep at run time:
   groupAxioms    rule-to-warp grouping: seed the axioms grouped by root entry
                  (PGA_FLAG_GROUP_AXIOMS); searched only for batches whose
                  axioms use more than one root entry
+  dynamicChunks  the last quarter of each wide level's items from a shared
+                 counter instead of the static grid-stride order
+                 (PGA_FLAG_DYNAMIC_CHUNKS): pays where items differ in cost
 
 Every candidate derives the batch `runs` times (CUDA events, after a warm-up);
 a candidate whose derivation reports a non-OK status (e.g. the finer splits
@@ -42,11 +45,20 @@ DEFAULT_SPACE = {
     "narrow_sub_item": (0, 2, 4),  # 0: same as sub_item
     "items_per_lane": (1, 2),
     "blocks_per_sm": (0, 1),      # 0: occupancy maximum
+    "dynamic_chunks": (False, True),
 }
 
 
 # The engine's built-in defaults, as a point of the space.
-DEFAULT_CONFIG = {"sub_item": 8, "narrow_sub_item": 0, "items_per_lane": 1, "blocks_per_sm": 0}
+DEFAULT_CONFIG = {"sub_item": 8, "narrow_sub_item": 0, "items_per_lane": 1, "blocks_per_sm": 0, "dynamic_chunks": False}
+
+
+def is_default(config):
+    """Whether `config` is the engine's default schedule: every knob of
+    DEFAULT_CONFIG at its default (a knob the config leaves out counts as
+    default) and no axiom grouping."""
+    return (all(config.get(k, v) == v for k, v in DEFAULT_CONFIG.items())
+            and not config.get("group_axioms", False))
 
 
 def space_for(batch, space=None):

@@ -1273,14 +1273,32 @@ __device__ void seed_deferred(const DeriveArgs& a, WarpOut& w) {
 }
 
 // All items of one level [lo, hi): warp chunks of 32 K items in a static
-// grid-stride order (no shared work counter).
+// grid-stride order (no shared work counter).  With dynamicChunks (persistent
+// engine only), on a level of at least four rounds of chunks, the static order
+// covers whole rounds up to the last quarter of the level (at least two rounds
+// of chunks are left); warps then take the rest one chunk at a time from the
+// level's cursor, which the level snapshot set to lo.
 template <bool PAGED, bool LEAF, int AFF>
 __device__ __forceinline__ void expand_level(const DeriveArgs& a, WarpOut& w, unsigned long long lo,
                                              unsigned long long hi, uint32_t K) {
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
   const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
-  for (unsigned long long b = lo + warpId * 32ull * K; b < hi; b += numWarps * 32ull * K)
-    warp_items<PAGED, LEAF, AFF>(a, w, b, hi, K);
+  const unsigned long long chunk = 32ull * K, stride = numWarps * chunk;
+  unsigned long long dynLo = hi;  // items from dynLo on come from the cursor
+  if (PAGED && a.dynamicChunks && hi - lo >= 4 * stride) {
+    const unsigned long long n = hi - lo, rest = max(n / 4, 2 * stride);
+    dynLo = lo + ((n - rest) / stride) * stride;
+  }
+  for (unsigned long long b = lo + warpId * chunk; b < dynLo; b += stride) warp_items<PAGED, LEAF, AFF>(a, w, b, hi, K);
+  if (dynLo < hi) {
+    for (;;) {
+      unsigned long long b = 0;
+      if ((threadIdx.x & 31u) == 0) b = atomicAdd(&a.st->cursor, chunk);
+      b = dynLo + (__shfl_sync(kFull, b, 0) - lo);
+      if (b >= hi) break;
+      warp_items<PAGED, LEAF, AFF>(a, w, b, hi, K);
+    }
+  }
 }
 
 // Copies the rule table into shared memory when it fits (decided at engine

@@ -104,7 +104,7 @@ struct DevState {
   unsigned long long nodeNext;    // queued item slots handed out (plain form)
   unsigned long long termPages;   // terminal pages handed out (paged engine)
   unsigned long long nodePages;   // item pages handed out (paged engine)
-  unsigned long long cursor;
+  unsigned long long cursor;      // next dynamic chunk of the level being expanded (PGA_FLAG_DYNAMIC_CHUNKS)
   unsigned long long levelLo, levelHi;
   unsigned long long maxLevelNodes;
   int32_t status, detail;
@@ -138,7 +138,8 @@ struct DeriveArgs {
   uint32_t useSeeds;    // 0: no parameter of the grammar reads a seed, skip seed updates
   uint32_t itemsPerLane;
   uint32_t narrowSubItem;
-  uint32_t inlineLeaves;      // expand kRuleLeaf children in the lane that creates them  // work items per lane in one warp chunk
+  uint32_t inlineLeaves;  // expand kRuleLeaf children in the lane that creates them
+  uint32_t dynamicChunks; // the last quarter of a level's chunks from DevState::cursor (PGA_FLAG_DYNAMIC_CHUNKS)
   PgaTerminal* tail;      // terminal slots at or beyond `cap` (pages straddling the end of the output)
   uint2* tailLinks;
   unsigned long long tailCap;

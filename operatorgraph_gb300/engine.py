@@ -74,6 +74,7 @@ _lib = None
 
 PGA_FLAG_NO_INLINE = 1  # PgaEngineConfig.flags: queue leaf children instead of expanding them in place
 PGA_FLAG_GROUP_AXIOMS = 2  # seed the axioms grouped by root entry (same records, another output order)
+PGA_FLAG_DYNAMIC_CHUNKS = 4  # the last quarter of each level's items from a shared counter (another output order)
 
 
 def load_library(path=LIB_PATH):
@@ -140,7 +141,7 @@ class Engine:
 
     def __init__(self, entries, procs=None, node_capacity=1 << 22, max_terminals=1 << 22, block_stride=0,
                  record_tape=False, blocks_per_sm=0, spin_limit=0, max_levels=0, sub_item=0, items_per_lane=0,
-                 narrow_sub_item=0, no_inline=False, group_axioms=False):
+                 narrow_sub_item=0, no_inline=False, group_axioms=False, dynamic_chunks=False):
         L = load_library()
         self.entries = np.ascontiguousarray(entries, dtype=G.ENTRY_DT)
         self.procs = np.ascontiguousarray(G.DEFAULT_PROCS if procs is None else procs, dtype=G.PROC_DT)
@@ -148,7 +149,8 @@ class Engine:
         self.config = PgaEngineConfig(node_capacity, max_terminals, block_stride, 256, blocks_per_sm,
                                       1 if record_tape else 0, spin_limit, max_levels,
                                       (PGA_FLAG_NO_INLINE if no_inline else 0)
-                                      | (PGA_FLAG_GROUP_AXIOMS if group_axioms else 0), sub_item,
+                                      | (PGA_FLAG_GROUP_AXIOMS if group_axioms else 0)
+                                      | (PGA_FLAG_DYNAMIC_CHUNKS if dynamic_chunks else 0), sub_item,
                                       items_per_lane, narrow_sub_item)
         h = ctypes.c_void_p()
         _check(L.pga_engine_create(ctypes.byref(table), ctypes.byref(self.config), ctypes.byref(h)),

@@ -57,6 +57,8 @@ def main(argv=None):
                     help="children per work item queued from levels narrower than the grid (default subItem)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="cap on resident blocks per SM (0: occupancy)")
     ap.add_argument("--group", action="store_true", help="seed the axioms grouped by root entry")
+    ap.add_argument("--dynamic", action="store_true",
+                    help="the last quarter of each level's items from a shared counter (PGA_FLAG_DYNAMIC_CHUNKS)")
     ap.add_argument("--per-axiom", action="store_true", help="one persistent launch per axiom (pga_derive_per_axiom)")
     ap.add_argument("--meshes", action="store_true", help="city: triangle-mesh terminals, then pga_generate_meshes")
     ap.add_argument("--blocks", action="store_true", help="mixed: per-axiom parameter blocks")
@@ -66,7 +68,8 @@ def main(argv=None):
     cap = args.capacity or 8_000_000
     eng = Engine(b["entries"], node_capacity=args.nodes, max_terminals=cap, block_stride=b["block_stride"],
                  sub_item=args.sub_item, items_per_lane=args.items_per_lane, blocks_per_sm=args.blocks_per_sm,
-                 narrow_sub_item=args.narrow_sub_item, record_tape=args.step, group_axioms=args.group)
+                 narrow_sub_item=args.narrow_sub_item, record_tape=args.step, group_axioms=args.group,
+                 dynamic_chunks=args.dynamic)
     dev = torch.device("cuda", torch.cuda.current_device())
     d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).to(dev)
     d_blk = None if b["blocks"] is None else torch.from_numpy(np.asarray(b["blocks"], np.float32)).to(dev)

@@ -41,6 +41,15 @@ def test_grouping_is_searched_only_for_batches_of_several_root_entries():
     assert len(A.candidates(mixed)) == 4
 
 
+def test_default_schedule_is_recognised_with_or_without_optional_knobs():
+    assert A.is_default(dict(A.DEFAULT_CONFIG))
+    assert A.is_default({"sub_item": 8, "narrow_sub_item": 0, "items_per_lane": 1, "blocks_per_sm": 0})
+    assert A.is_default(dict(A.DEFAULT_CONFIG, group_axioms=False))
+    assert not A.is_default(dict(A.DEFAULT_CONFIG, group_axioms=True))
+    assert not A.is_default(dict(A.DEFAULT_CONFIG, dynamic_chunks=True))
+    assert not A.is_default(dict(A.DEFAULT_CONFIG, sub_item=4))
+
+
 def test_schedule_cache_round_trip(tmp_path):
     """tune_cached tunes on a miss, stores the winner under the key of (rule
     table, batch signature, GPU, version), and returns it untimed on a hit; a

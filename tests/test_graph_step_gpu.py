@@ -240,6 +240,42 @@ def test_adjoint_with_grouped_axioms_matches_index_order():
     _close(grads[1], grads[0], "axiom-size gradients")
 
 
+def test_dynamic_chunks_give_the_same_records_and_gradients():
+    """PGA_FLAG_DYNAMIC_CHUNKS on a batch whose widest levels take the dynamic
+    path (a 4,096-axiom mix: levels of up to ~2M work items, above the four
+    rounds of 77,824-item chunks the flag needs): the same terminal records as
+    the static order (as a multiset, bit for bit) and, after the tape-recording
+    derivation, the same axiom-size gradients to FP32 accumulation order."""
+    from operatorgraph_gb300.engine import Engine
+
+    b = scenes.mixed(4096)
+    cap = 10_000_000
+    d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).cuda()
+    out = torch.zeros((cap, 64), dtype=torch.uint8, device="cuda")
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    records, grads = [], []
+    for dynamic in (False, True):
+        eng = Engine(b["entries"], node_capacity=1 << 23, max_terminals=cap, dynamic_chunks=dynamic)
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None, out.data_ptr(), cap, count.data_ptr())
+        torch.cuda.synchronize()
+        rep = eng.report()
+        assert rep["status"] == 0 and rep["max_level_nodes"] >= 4 * 77_824
+        n = int(count.item())
+        records.append(np.sort(out[:n].cpu().numpy().view(np.dtype((np.void, 64))).ravel()))
+        eng.release()
+        eng = Engine(b["entries"], node_capacity=1 << 23, max_terminals=cap, record_tape=True, dynamic_chunks=dynamic)
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None, out.data_ptr(), cap, count.data_ptr())
+        g_sz = torch.zeros((len(b["axioms"]), 3), dtype=torch.float32, device="cuda")
+        eng.adjoint_raw(out.data_ptr(), None, 0, g_sz.data_ptr(), grad_stride=16)
+        torch.cuda.synchronize()
+        assert eng.report()["status"] == 0
+        grads.append(g_sz.cpu().numpy().astype(np.float64))
+        eng.release()
+    assert len(records[0]) == len(records[1]) and (records[0] == records[1]).all()
+    assert np.abs(grads[0]).max() > 0
+    _close(grads[1], grads[0], "axiom-size gradients")
+
+
 def test_strided_gradient_read_in_place_matches_a_copy():
     """pga_adjoint_strided reading dL/dM = M straight from the 16-float terminal
     records gives the gradients of pga_adjoint on a 12-float copy; a stride

@@ -113,10 +113,16 @@ def test_golden_case(path, form):
     eng.release()
 
 
-@pytest.mark.parametrize("name", ["menger_d5", "city_4096", "facades_1024", "random_16", "city_4096_queued"])
+@pytest.mark.parametrize("name", ["menger_d5", "city_4096", "facades_1024", "random_16", "city_4096_queued",
+                                  "city_4096_dynamic"])
 def test_full_size_bit_exact(name):
+    """_queued: leaf children queued as work items; _dynamic: the last quarter
+    of each wide level's items from the shared counter (the city's deepest
+    level has ~0.4M items, above the four rounds of chunks the flag needs)."""
     kw = {"no_inline": True} if name.endswith("_queued") else {}
-    name = name.replace("_queued", "")
+    if name.endswith("_dynamic"):
+        kw = {"dynamic_chunks": True}
+    name = name.replace("_queued", "").replace("_dynamic", "")
     if name == "menger_d5":
         b = scenes.menger(0.005)
     elif name == "city_4096":
