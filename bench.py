@@ -419,7 +419,43 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
-def mixed_step(n_ax, mout, count, dev, n_expected, blocks=True):
+def step_order(n_ax, mout, count, dev, schedule, runs=3):
+    """The level order for the differentiable mixed step: times the
+    tape-recording derivation plus the adjoint of the scalar batch (eagerly,
+    CUDA events) with dynamic chunks off and on, keeps the faster.  The
+    forward-only autotune cannot see this choice: dynamic chunks pay mostly in
+    the adjoint, whose items differ more in cost.  Returns (dynamic_chunks,
+    {False: ms, True: ms})."""
+    import torch
+
+    from operatorgraph_gb300.engine import Engine
+
+    mx = scenes.mixed(n_ax)
+    mcap = mout.shape[0]
+    d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
+    g_sz = torch.empty((n_ax, 3), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    times = {}
+    for dyn in (False, True):
+        knobs = dict(schedule or {}, group_axioms=True, dynamic_chunks=dyn)
+        eng = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True, **knobs)
+        ts = []
+        for k in range(runs + 1):
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.derive_raw(d_mx.data_ptr(), n_ax, None, mout.data_ptr(), mcap, count.data_ptr())
+            eng.adjoint_raw(mout.data_ptr(), None, 0, g_sz.data_ptr(), stream=stream, grad_stride=16)
+            z.record(stream)
+            torch.cuda.synchronize()
+            if k:
+                ts.append(a.elapsed_time(z))
+        assert eng.report()["status"] == 0
+        eng.release()
+        times[dyn] = statistics.median(ts)
+    return times[True] < times[False], times
+
+
+def mixed_step(n_ax, mout, count, dev, n_expected, blocks=True, schedule=None):
     """The mixed batch as one differentiable step captured in one CUDA graph:
     derivation with the tape recorded, LBVH over all its terminals (the leaf
     count read on the device, pga_lbvh_build_counted), and the adjoint for the
@@ -429,9 +465,10 @@ def mixed_step(n_ax, mout, count, dev, n_expected, blocks=True):
     (scenes.mixed(blocks=True): each building's floor height, tile width and
     window wall widths, each sponge's split factors; the same terminals as the
     scalar batch); blocks=False: to the axiom sizes of the scalar batch.  The
-    axioms are seeded grouped by root entry.  The parts are also timed one by
-    one, eagerly.  Keys are prefixed mixed65536_step_ (blocks) or
-    mixed65536_sizes_step_."""
+    axioms are seeded grouped by root entry.  `schedule`: engine knobs (the
+    mixed batch's autotuned schedule, dynamic chunks included), else the
+    defaults.  The parts are also timed one by one, eagerly.  Keys are prefixed
+    mixed65536_step_ (blocks) or mixed65536_sizes_step_."""
     import torch
 
     from operatorgraph_gb300.engine import Engine
@@ -439,8 +476,10 @@ def mixed_step(n_ax, mout, count, dev, n_expected, blocks=True):
     res = {}
     mx = scenes.mixed(n_ax, blocks=blocks)
     mcap = mout.shape[0]
-    et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True, group_axioms=True,
-                block_stride=mx["block_stride"])
+    knobs = dict(schedule or {})
+    knobs["group_axioms"] = True
+    et = Engine(mx["entries"], node_capacity=1 << 28, max_terminals=mcap, record_tape=True,
+                block_stride=mx["block_stride"], **knobs)
     d_mx = torch.from_numpy(mx["axioms"].view(np.uint8).copy()).to(dev)
     d_blk = torch.from_numpy(mx["blocks"]).to(dev) if blocks else torch.zeros(1, dtype=torch.float32, device=dev)
     g_blk = torch.empty_like(d_blk)
@@ -543,6 +582,7 @@ def mixed_step(n_ax, mout, count, dev, n_expected, blocks=True):
     res[pre + "fwd_adjoint_ms"] = fa_ms
     res[pre + "fwd_adjoint_roofline_frac_formula"] = (parts_8d[0] + parts_8d[2]) / (fa_ms * 1e-3) / 1e9 / peak
     res[pre + "lbvh_bounds"] = [round(v, 3) for v in bounds]
+    res[pre + "schedule"] = knobs
     del g, bv
     et.release()
     return res
@@ -781,8 +821,11 @@ def extras(eng, batch, out, n_term, dev, stream, flush):
     res["mixed65536_terminals"] = n_mx
     res["mixed65536_ms"] = mms
     res["mixed65536_terminals_per_s"] = n_mx / (res["mixed65536_ms"] * 1e-3)
-    res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx, blocks=True))
-    res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx, blocks=False))
+    dyn, order_ms = step_order(len(mx["axioms"]), mout, count, dev, mbest)
+    res["mixed65536_step_order_ms"] = {"static": order_ms[False], "dynamic": order_ms[True]}
+    sched = dict(mbest, dynamic_chunks=dyn)
+    res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx, blocks=True, schedule=sched))
+    res.update(mixed_step(len(mx["axioms"]), mout, count, dev, n_mx, blocks=False, schedule=sched))
     del mout
     # Forest: 4096 trees (Rotate with arbitrary angles, Replicate, Translate,
     # Scale: the general-frame kernels), about 13.4M terminals in one launch.

@@ -947,18 +947,35 @@ __global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned l
       j.pageNext[i] = head == kNoRecord ? kNoRecord : (head & ~kItemTag);
     }
   }
-  if (!grid_barrier(a, [] {})) return;
+  // The levels, last first.  With dynamicChunks a level of at least four
+  // rounds of the grid leaves its last quarter (at least two rounds) to warps
+  // that take 32 items at a time from DevState::cursor, reset at each barrier.
+  if (!grid_barrier(a, [&] { a.st->cursor = 0ull; })) return;
   for (int L = (int)levels; L >= 0; L--) {
     const unsigned long long lv = a.levelStart[L], hv = min(a.levelStart[L + 1], nodes);
     if (lv >= hv) continue;  // every block reads the same bounds, so all skip the barrier alike
-    for (unsigned long long i = lv + tid; i < hv; i += stride) {
-      if (i + stride < hv) {  // the next item's record and key, ahead of its turn
+    unsigned long long dynLo = hv;
+    if (a.dynamicChunks && hv - lv >= 4 * stride) {
+      const unsigned long long n = hv - lv;
+      dynLo = lv + ((n - max(n / 4, 2 * stride)) / stride) * stride;
+    }
+    // one call site of adj_page for both orders
+    for (unsigned long long i = lv + tid;; i += stride) {
+      if (i >= dynLo) {
+        if (dynLo >= hv) break;
+        unsigned long long c = 0;
+        if ((threadIdx.x & 31u) == 0) c = atomicAdd(&a.st->cursor, 32ull);
+        c = dynLo + __shfl_sync(kFull, c, 0);
+        if (c >= hv) break;
+        i = c + (threadIdx.x & 31u);  // the loop step never lands below dynLo again
+        if (i >= hv) continue;        // this lane has no item in the last chunk
+      } else if (i + stride < dynLo) {  // the next item's record and key, ahead of its turn
         prefetch_l2(a.nodes + i + stride);
         prefetch_l2(j.childKey + i + stride);
       }
       adj_page(a, j, i, nodes);
     }
-    if (!grid_barrier(a, [] {})) return;
+    if (!grid_barrier(a, [&] { a.st->cursor = 0ull; })) return;
   }
 }
 

@@ -129,17 +129,24 @@ inline const void* adjoint_kernel();   // this build's k_adjoint (adjoint.cuh, i
 // leaf children in place or not, with or without the 1 -> 1 affine steps.
 static const void* persistent_kernel(const PgaEngine* e) {
   if (e->phased) return e->kernels.phased;
+  if (!e->leafKernel && (e->cfg.flags & PGA_FLAG_DYNAMIC_CHUNKS)) return e->kernels.persistentDyn[e->affineKernel ? 1 : 0];
   return e->kernels.persistent[(e->leafKernel ? 1 : 0) + (e->affineKernel ? 2 : 0)];
 }
+
+// The persistent instantiations of a build: the four static ones, the phased
+// one and the two with dynamic chunks.
+static const void* persistent_at(const FrameKernels& k, int i) {
+  return i < 4 ? k.persistent[i] : (i == 4 ? k.phased : k.persistentDyn[i - 5]);
+}
+constexpr int kPersistentKernels = 7;
 
 // All kernels of the engine's build get the same dynamic shared memory limit;
 // the launch uses the smallest of the persistent instantiations' occupancies,
 // so any of them can run co-resident.
 static cudaError_t set_kernel_smem(const FrameKernels& k, size_t bytes) {
   cudaError_t err = cudaSuccess;
-  for (int i = 0; i < 5 && err == cudaSuccess; i++)
-    err = cudaFuncSetAttribute(i < 4 ? k.persistent[i] : k.phased, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)bytes);
+  for (int i = 0; i < kPersistentKernels && err == cudaSuccess; i++)
+    err = cudaFuncSetAttribute(persistent_at(k, i), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (err == cudaSuccess) err = cudaFuncSetAttribute(k.seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (err == cudaSuccess) err = cudaFuncSetAttribute(k.expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   return err;
@@ -147,9 +154,9 @@ static cudaError_t set_kernel_smem(const FrameKernels& k, size_t bytes) {
 static cudaError_t persistent_occupancy(const FrameKernels& k, int* perSM, int threads, size_t smem) {
   int best = 1 << 30;
   cudaError_t err = cudaSuccess;
-  for (int i = 0; i < 5 && err == cudaSuccess; i++) {
+  for (int i = 0; i < kPersistentKernels && err == cudaSuccess; i++) {
     int n = 0;
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, i < 4 ? k.persistent[i] : k.phased, threads, smem);
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, persistent_at(k, i), threads, smem);
     best = std::min(best, n);
   }
   *perSM = best;

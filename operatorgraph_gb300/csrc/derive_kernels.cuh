@@ -1273,29 +1273,37 @@ __device__ void seed_deferred(const DeriveArgs& a, WarpOut& w) {
 }
 
 // All items of one level [lo, hi): warp chunks of 32 K items in a static
-// grid-stride order (no shared work counter).  With dynamicChunks (persistent
-// engine only), on a level of at least four rounds of chunks, the static order
-// covers whole rounds up to the last quarter of the level (at least two rounds
-// of chunks are left); warps then take the rest one chunk at a time from the
-// level's cursor, which the level snapshot set to lo.
-template <bool PAGED, bool LEAF, int AFF>
+// grid-stride order (no shared work counter).  DYN (PGA_FLAG_DYNAMIC_CHUNKS; a
+// separate instantiation, so that the static one keeps its register
+// allocation): on a level of at least four rounds of chunks the static order
+// covers whole rounds up to the last quarter of the level (at least two
+// rounds of chunks are left); warps then take the rest one chunk at a time
+// from the level's cursor, which the level snapshot set to lo.
+template <bool PAGED, bool LEAF, int AFF, bool DYN = false>
 __device__ __forceinline__ void expand_level(const DeriveArgs& a, WarpOut& w, unsigned long long lo,
                                              unsigned long long hi, uint32_t K) {
   const unsigned long long warpId = ((unsigned long long)blockIdx.x * kThreads + threadIdx.x) >> 5;
   const unsigned long long numWarps = ((unsigned long long)gridDim.x * kThreads) >> 5;
-  const unsigned long long chunk = 32ull * K, stride = numWarps * chunk;
-  unsigned long long dynLo = hi;  // items from dynLo on come from the cursor
-  if (PAGED && a.dynamicChunks && hi - lo >= 4 * stride) {
-    const unsigned long long n = hi - lo, rest = max(n / 4, 2 * stride);
-    dynLo = lo + ((n - rest) / stride) * stride;
-  }
-  for (unsigned long long b = lo + warpId * chunk; b < dynLo; b += stride) warp_items<PAGED, LEAF, AFF>(a, w, b, hi, K);
-  if (dynLo < hi) {
-    for (;;) {
-      unsigned long long b = 0;
-      if ((threadIdx.x & 31u) == 0) b = atomicAdd(&a.st->cursor, chunk);
-      b = dynLo + (__shfl_sync(kFull, b, 0) - lo);
-      if (b >= hi) break;
+  if constexpr (!DYN) {
+    for (unsigned long long b = lo + warpId * 32ull * K; b < hi; b += numWarps * 32ull * K)
+      warp_items<PAGED, LEAF, AFF>(a, w, b, hi, K);
+  } else {
+    const unsigned long long chunk = 32ull * K, stride = numWarps * chunk;
+    unsigned long long dynLo = hi;  // items from dynLo on come from the cursor
+    if (hi - lo >= 4 * stride) {
+      const unsigned long long n = hi - lo, rest = max(n / 4, 2 * stride);
+      dynLo = lo + ((n - rest) / stride) * stride;
+    }
+    // one call site of warp_items for both orders (a second inlined copy costs
+    // the kernel its register allocation)
+    for (unsigned long long b = lo + warpId * chunk;; b += stride) {
+      if (b >= dynLo) {
+        if (dynLo >= hi) break;
+        unsigned long long c = 0;
+        if ((threadIdx.x & 31u) == 0) c = atomicAdd(&a.st->cursor, chunk);
+        b = dynLo + (__shfl_sync(kFull, c, 0) - lo);  // the loop step never lands below dynLo again
+        if (b >= hi) break;
+      }
       warp_items<PAGED, LEAF, AFF>(a, w, b, hi, K);
     }
   }
@@ -1563,7 +1571,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 #define PGA_PERSISTENT_MIN_BLOCKS 2
 #endif
 
-template <bool LEAF, int AFF>
+template <bool LEAF, int AFF, bool DYN = false>
 __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_persistent(DeriveArgs a) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   if (blockIdx.x == 0 && threadIdx.x == 0) a.st->clockStart = global_ns();
@@ -1590,7 +1598,7 @@ __global__ void __launch_bounds__(kThreads, PGA_PERSISTENT_MIN_BLOCKS) k_derive_
     if (vs->stop) break;
     const unsigned long long lo = vs->levelLo, hi = vs->levelHi;
     warpout_level(a, w, hi - lo);
-    expand_level<true, LEAF, AFF>(a, w, lo, hi, a.itemsPerLane);
+    expand_level<true, LEAF, AFF, DYN>(a, w, lo, hi, a.itemsPerLane);
     close_node_page(a, w);
     if (!grid_barrier(a, [&] { level_snapshot(a, level + 1); })) return;
   }
@@ -1628,11 +1636,14 @@ inline FrameKernels frame_kernels() {
 #if PGA_GENERAL_FRAMES
   k.persistent[0] = k.persistent[2] = (const void*)k_derive_persistent<false, 1>;
   k.persistent[1] = k.persistent[3] = (const void*)k_derive_persistent<true, 1>;
+  k.persistentDyn[0] = k.persistentDyn[1] = (const void*)k_derive_persistent<false, 1, true>;
 #else
   k.persistent[0] = (const void*)k_derive_persistent<false, 0>;
   k.persistent[1] = (const void*)k_derive_persistent<true, 0>;
   k.persistent[2] = (const void*)k_derive_persistent<false, 1>;
   k.persistent[3] = (const void*)k_derive_persistent<true, 1>;
+  k.persistentDyn[0] = (const void*)k_derive_persistent<false, 0, true>;
+  k.persistentDyn[1] = (const void*)k_derive_persistent<false, 1, true>;
 #endif
   k.phased = (const void*)k_derive_persistent<false, 2>;
   k.seed = (const void*)k_seed;

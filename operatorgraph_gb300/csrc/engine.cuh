@@ -139,7 +139,6 @@ struct DeriveArgs {
   uint32_t itemsPerLane;
   uint32_t narrowSubItem;
   uint32_t inlineLeaves;  // expand kRuleLeaf children in the lane that creates them
-  uint32_t dynamicChunks; // the last quarter of a level's chunks from DevState::cursor (PGA_FLAG_DYNAMIC_CHUNKS)
   PgaTerminal* tail;      // terminal slots at or beyond `cap` (pages straddling the end of the output)
   uint2* tailLinks;
   unsigned long long tailCap;
@@ -164,11 +163,13 @@ struct DeriveArgs {
   const float* colAabbs;
   const uint32_t* colLeaf;
   uint32_t numColliders;
+  uint32_t dynamicChunks;  // adjoint: the last quarter of a wide level's items from DevState::cursor (PGA_FLAG_DYNAMIC_CHUNKS)
 };
 
 // Entry points of one build of the kernels (host stubs), for the host code.
 struct FrameKernels {
   const void* persistent[4];  // k_derive_persistent<LEAF, AFF = 0 / 1>, index LEAF + 2 AFF
+  const void* persistentDyn[2];  // k_derive_persistent<false, AFF = 0 / 1, DYN = true> (PGA_FLAG_DYNAMIC_CHUNKS)
   const void* phased;         // k_derive_persistent<false, 2>: multi-phase tables
   const void* seed;           // k_seed (plain form)
   const void* expand;         // k_expand_level (plain form)
