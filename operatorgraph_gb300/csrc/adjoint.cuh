@@ -445,6 +445,13 @@ __device__ void subdivide_sweep(const DeriveArgs& a, const AdjArgs& j, const Exp
 // (Extrude, Translate, Scale, SwapSize) are recorded so that the reverse pass
 // can undo them.  A chain with more than kChainSteps of them has no adjoint
 // (PGA_ERR_NO_TAPE).
+// The share of a wide level that the adjoint hands out dynamically: 1 / this
+// (1: all of it; measured on the 65,536-axiom step, sizes / all parameters:
+// a quarter 22 / 57-66 ms, half 20.3 / 40-46 ms, all 19.3 / 35 ms).
+#ifndef PGA_ADJOINT_DYNAMIC_SHARE
+#define PGA_ADJOINT_DYNAMIC_SHARE 1
+#endif
+
 constexpr int kChainSteps = 8;
 struct Chain {
   uint32_t n;                   // smooth steps
@@ -948,8 +955,9 @@ __global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned l
     }
   }
   // The levels, last first.  With dynamicChunks a level of at least four
-  // rounds of the grid leaves its last quarter (at least two rounds) to warps
-  // that take 32 items at a time from DevState::cursor, reset at each barrier.
+  // rounds of the grid leaves its last 1 / PGA_ADJOINT_DYNAMIC_SHARE (at least
+  // two rounds) to warps that take 32 items at a time from DevState::cursor,
+  // reset at each barrier.
   if (!grid_barrier(a, [&] { a.st->cursor = 0ull; })) return;
   for (int L = (int)levels; L >= 0; L--) {
     const unsigned long long lv = a.levelStart[L], hv = min(a.levelStart[L + 1], nodes);
@@ -957,7 +965,7 @@ __global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned l
     unsigned long long dynLo = hv;
     if (a.dynamicChunks && hv - lv >= 4 * stride) {
       const unsigned long long n = hv - lv;
-      dynLo = lv + ((n - max(n / 4, 2 * stride)) / stride) * stride;
+      dynLo = lv + ((n - max(n / PGA_ADJOINT_DYNAMIC_SHARE, 2 * stride)) / stride) * stride;
     }
     // one call site of adj_page for both orders
     for (unsigned long long i = lv + tid;; i += stride) {

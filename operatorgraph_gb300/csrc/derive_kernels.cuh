@@ -1272,6 +1272,12 @@ __device__ void seed_deferred(const DeriveArgs& a, WarpOut& w) {
   }
 }
 
+// The share of a wide level the dynamic instantiation hands out from the
+// level's counter: 1 / this.
+#ifndef PGA_DERIVE_DYNAMIC_SHARE
+#define PGA_DERIVE_DYNAMIC_SHARE 4
+#endif
+
 // All items of one level [lo, hi): warp chunks of 32 K items in a static
 // grid-stride order (no shared work counter).  DYN (PGA_FLAG_DYNAMIC_CHUNKS; a
 // separate instantiation, so that the static one keeps its register
@@ -1291,7 +1297,7 @@ __device__ __forceinline__ void expand_level(const DeriveArgs& a, WarpOut& w, un
     const unsigned long long chunk = 32ull * K, stride = numWarps * chunk;
     unsigned long long dynLo = hi;  // items from dynLo on come from the cursor
     if (hi - lo >= 4 * stride) {
-      const unsigned long long n = hi - lo, rest = max(n / 4, 2 * stride);
+      const unsigned long long n = hi - lo, rest = max(n / PGA_DERIVE_DYNAMIC_SHARE, 2 * stride);
       dynLo = lo + ((n - rest) / stride) * stride;
     }
     // one call site of warp_items for both orders (a second inlined copy costs
