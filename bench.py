@@ -422,10 +422,10 @@ def our_arm(args):
 def step_order(n_ax, mout, count, dev, schedule, runs=3):
     """The level order for the differentiable mixed step: times the
     tape-recording derivation plus the adjoint of the scalar batch (eagerly,
-    CUDA events) with dynamic chunks off and on, keeps the faster.  The
-    forward-only autotune cannot see this choice: dynamic chunks pay mostly in
-    the adjoint, whose items differ more in cost.  Returns (dynamic_chunks,
-    {False: ms, True: ms})."""
+    CUDA events) with the derivation's dynamic chunks off and on (the adjoint
+    hands out its wide levels dynamically either way), keeps the faster.  The
+    forward-only autotune times derivations without the tape.  Returns
+    (dynamic_chunks, {False: ms, True: ms})."""
     import torch
 
     from operatorgraph_gb300.engine import Engine

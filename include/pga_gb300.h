@@ -149,15 +149,16 @@ typedef struct PgaTerminal {
  * grammars; pga_derive_to_host and multi-phase tables (phases, Collider,
  * IfCollides) keep index order.  No reference counterpart. */
 #define PGA_FLAG_GROUP_AXIOMS 2u
-/* pga_derive (and pga_adjoint after it) hands out the last quarter of each
- * wide level's work items (a level of at least four rounds of warp chunks; at
- * least two rounds are left) from a shared per-level counter, one chunk per
- * warp at a time, instead of in the fixed grid-stride order, so that warps
- * whose items had more children do not hold the level's end.  A derivation
- * that expands leaf children in place (the default without recordTape, for
- * tables with leaf rules) keeps the fixed order.  The records are the same;
- * their order in the output changes from run to run.  No reference
- * counterpart (the reference's queues are dynamic throughout). */
+/* pga_derive hands out the last quarter of each wide level's work items (a
+ * level of at least four rounds of warp chunks; at least two rounds are left)
+ * from a shared per-level counter, one chunk per warp at a time, instead of in
+ * the fixed grid-stride order, so that warps whose items had more children do
+ * not hold the level's end.  A derivation that expands leaf children in place
+ * (the default without recordTape, for tables with leaf rules) keeps the
+ * fixed order.  The records are the same; their order in the output changes
+ * from run to run.  (pga_adjoint hands out its wide levels this way with or
+ * without the flag.)  No reference counterpart (the reference's queues are
+ * dynamic throughout). */
 #define PGA_FLAG_DYNAMIC_CHUNKS 4u
 
 typedef struct PgaEngineConfig {

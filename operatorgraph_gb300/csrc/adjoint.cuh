@@ -954,16 +954,18 @@ __global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned l
       j.pageNext[i] = head == kNoRecord ? kNoRecord : (head & ~kItemTag);
     }
   }
-  // The levels, last first.  With dynamicChunks a level of at least four
-  // rounds of the grid leaves its last 1 / PGA_ADJOINT_DYNAMIC_SHARE (at least
-  // two rounds) to warps that take 32 items at a time from DevState::cursor,
-  // reset at each barrier.
+  // The levels, last first.  A level of at least four rounds of the grid
+  // leaves its last 1 / PGA_ADJOINT_DYNAMIC_SHARE (at least two rounds) to
+  // warps that take 32 items at a time from DevState::cursor, reset at each
+  // barrier: pages differ widely in cost, and the gradients are sums of
+  // atomics whose order was never fixed, so the order of the pages changes
+  // nothing a caller sees.
   if (!grid_barrier(a, [&] { a.st->cursor = 0ull; })) return;
   for (int L = (int)levels; L >= 0; L--) {
     const unsigned long long lv = a.levelStart[L], hv = min(a.levelStart[L + 1], nodes);
     if (lv >= hv) continue;  // every block reads the same bounds, so all skip the barrier alike
     unsigned long long dynLo = hv;
-    if (a.dynamicChunks && hv - lv >= 4 * stride) {
+    if (hv - lv >= 4 * stride) {
       const unsigned long long n = hv - lv;
       dynLo = lv + ((n - max(n / PGA_ADJOINT_DYNAMIC_SHARE, 2 * stride)) / stride) * stride;
     }

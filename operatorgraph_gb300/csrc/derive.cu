@@ -85,7 +85,6 @@ DeriveArgs make_args(PgaEngine* e, const PgaAxiom* axioms, uint32_t numAxioms, c
   a.useSeeds = e->useSeeds ? 1u : 0u;
   a.itemsPerLane = e->cfg.itemsPerLane;
   a.narrowSubItem = e->cfg.narrowSubItem;
-  a.dynamicChunks = (e->cfg.flags & PGA_FLAG_DYNAMIC_CHUNKS) ? 1u : 0u;
   a.tail = e->dTail;
   a.tailLinks = e->dTailLinks;
   a.tailCap = e->tailCap;

@@ -163,7 +163,6 @@ struct DeriveArgs {
   const float* colAabbs;
   const uint32_t* colLeaf;
   uint32_t numColliders;
-  uint32_t dynamicChunks;  // adjoint: the last quarter of a wide level's items from DevState::cursor (PGA_FLAG_DYNAMIC_CHUNKS)
 };
 
 // Entry points of one build of the kernels (host stubs), for the host code.
