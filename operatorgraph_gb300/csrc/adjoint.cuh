@@ -821,12 +821,18 @@ __device__ __forceinline__ unsigned long long block_sum(unsigned long long v) {
 // or overflowed forward pass leaves the gradients zero (the engine report
 // keeps the forward's status; a tape too short for the terminals or a slot
 // map larger than its buffer raises PGA_ERR_NO_TAPE).
-// The block build pins 2 blocks per SM (up to 128 registers): left free,
-// its register choice there came out at 80 with spills.
-#if PGA_INLINE_BLOCKS
-#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads, 2)
-#else
+// The frame-code builds run 3 blocks of 256 per SM (80 registers, ~300 B of
+// spills): with the level's pages handed out on demand the extra warps hide
+// more of the scattered reads (65,536-axiom step: sizes 19.2 -> 18.2 ms, all
+// parameters 35 -> 32 ms against 2 blocks per SM).  The general-frame build,
+// which spills at 2 blocks already, keeps the compiler's choice.
+// PGA_ADJOINT_MIN_BLOCKS overrides both.
+#if defined(PGA_ADJOINT_MIN_BLOCKS)
+#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads, PGA_ADJOINT_MIN_BLOCKS)
+#elif PGA_GENERAL_FRAMES
 #define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads)
+#else
+#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads, 3)
 #endif
 __global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned long long numParamFloats,
                                                       uint32_t numAxioms) {
