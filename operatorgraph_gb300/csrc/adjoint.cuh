@@ -821,21 +821,25 @@ __device__ __forceinline__ unsigned long long block_sum(unsigned long long v) {
 // or overflowed forward pass leaves the gradients zero (the engine report
 // keeps the forward's status; a tape too short for the terminals or a slot
 // map larger than its buffer raises PGA_ERR_NO_TAPE).
-// The frame-code builds run 3 blocks of 256 per SM (80 registers, ~300 B of
-// spills): with the level's pages handed out on demand the extra warps hide
-// more of the scattered reads (65,536-axiom step: sizes 19.2 -> 18.2 ms, all
-// parameters 35 -> 32 ms against 2 blocks per SM).  The general-frame build,
-// which spills at 2 blocks already, keeps the compiler's choice.
-// PGA_ADJOINT_MIN_BLOCKS overrides both.
+// Two launch shapes of the same pass.  k_adjoint keeps the compiler's
+// register choice (2 blocks of 256 per SM; the block build pins 2 blocks: left
+// free, its choice there came out at 80 registers with spills).
+// k_adjoint_wide (frame-code builds) runs 3 blocks per SM (80 registers, ~300
+// B of spills): with the level's pages handed out on demand the extra warps
+// hide more of the scattered reads on large tapes (65,536-axiom step: sizes
+// 19.2 -> 18.2 ms, all parameters 35 -> 32 ms), while on small ones the
+// spills and the larger grid's barriers cost more (1,024 facades: forward +
+// adjoint 0.264 -> 0.302 ms).  Engines choose by terminal capacity
+// (kWideAdjointTerminals).  PGA_ADJOINT_MIN_BLOCKS overrides k_adjoint's shape.
 #if defined(PGA_ADJOINT_MIN_BLOCKS)
 #define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads, PGA_ADJOINT_MIN_BLOCKS)
-#elif PGA_GENERAL_FRAMES
-#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads)
+#elif PGA_INLINE_BLOCKS
+#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads, 2)
 #else
-#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads, 3)
+#define PGA_ADJOINT_BOUNDS __launch_bounds__(kThreads)
 #endif
-__global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned long long numParamFloats,
-                                                      uint32_t numAxioms) {
+__device__ __forceinline__ void adjoint_pass(const DeriveArgs& a, const AdjArgs& j, unsigned long long numParamFloats,
+                                             uint32_t numAxioms) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   setup_block(a, sm);
   volatile DevState* vs = a.st;
@@ -995,8 +999,26 @@ __global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned l
   }
 }
 
-// This build's adjoint kernel, for the host code.
+__global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned long long numParamFloats,
+                                             uint32_t numAxioms) {
+  adjoint_pass(a, j, numParamFloats, numAxioms);
+}
+
+#if !PGA_GENERAL_FRAMES
+__global__ void __launch_bounds__(kThreads, 3) k_adjoint_wide(DeriveArgs a, AdjArgs j,
+                                                              unsigned long long numParamFloats, uint32_t numAxioms) {
+  adjoint_pass(a, j, numParamFloats, numAxioms);
+}
+#endif
+
+// This build's adjoint kernels, for the host code (the general-frame build
+// has one shape).
 inline const void* adjoint_kernel() { return (const void*)k_adjoint; }
+#if PGA_GENERAL_FRAMES
+inline const void* adjoint_kernel_wide() { return (const void*)k_adjoint; }
+#else
+inline const void* adjoint_kernel_wide() { return (const void*)k_adjoint_wide; }
+#endif
 
 }  // inline namespace PGA_FRAMES_NS
 }  // namespace pga

@@ -120,7 +120,8 @@ namespace pga {
 FrameKernels general_frame_kernels();  // derive_gen.cu
 FrameKernels block_frame_kernels();    // derive_blk.cu
 inline namespace PGA_FRAMES_NS {
-inline const void* adjoint_kernel();   // this build's k_adjoint (adjoint.cuh, included below)
+inline const void* adjoint_kernel();       // this build's k_adjoint (adjoint.cuh, included below)
+inline const void* adjoint_kernel_wide();  // and k_adjoint_wide
 }
 }
 
@@ -431,7 +432,10 @@ PgaStatus pga_engine_create(const PgaRuleTable* table, const PgaEngineConfig* co
   } else {
     e->kernels = frame_kernels();
     e->kernels.adjoint = adjoint_kernel();
+    e->kernels.adjointWide = adjoint_kernel_wide();
   }
+  // Large tapes take the 3-blocks-per-SM adjoint (see k_adjoint_wide).
+  if (c.maxTerminals >= kWideAdjointTerminals && e->kernels.adjointWide) e->kernels.adjoint = e->kernels.adjointWide;
   if (e->hParams.empty()) e->hParams.push_back(DevParam{0, 0.f, 0.f, 0});
   if (e->hSucc.empty()) e->hSucc.push_back(-1);
   if (e->hExpPool.empty()) e->hExpPool.push_back(0.f);

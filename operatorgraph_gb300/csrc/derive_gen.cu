@@ -10,6 +10,7 @@ namespace pga {
 FrameKernels general_frame_kernels() {
   FrameKernels k = frame_kernels();
   k.adjoint = adjoint_kernel();
+  k.adjointWide = adjoint_kernel_wide();
   return k;
 }
 }  // namespace pga

@@ -18,6 +18,8 @@ constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr uint32_t kMaxAdjointBlocks = 8192;  // blocks of the reverse launch (slot-map scan)
+// Engines with at least this terminal capacity launch the 3-blocks-per-SM adjoint (k_adjoint_wide).
+constexpr unsigned long long kWideAdjointTerminals = 1ull << 23;
 enum Kind { kNone = 0, kTerm = 1, kNode = 2 };
 
 struct __align__(16) Smem {
@@ -1655,6 +1657,7 @@ inline FrameKernels frame_kernels() {
   k.seed = (const void*)k_seed;
   k.expand = (const void*)k_expand_level;
   k.adjoint = nullptr;  // set by the builds that include adjoint.cuh
+  k.adjointWide = nullptr;
   return k;
 }
 

@@ -172,7 +172,8 @@ struct FrameKernels {
   const void* phased;         // k_derive_persistent<false, 2>: multi-phase tables
   const void* seed;           // k_seed (plain form)
   const void* expand;         // k_expand_level (plain form)
-  const void* adjoint;        // k_adjoint (frame-code builds only; null in the general-frame build)
+  const void* adjoint;        // k_adjoint: the one the engine launches
+  const void* adjointWide;    // k_adjoint_wide (3 blocks per SM; the general-frame build: k_adjoint)
 };
 
 __device__ __forceinline__ void raise_error(DevState* st, int code, int detail) {
