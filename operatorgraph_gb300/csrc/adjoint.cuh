@@ -825,7 +825,7 @@ __device__ __forceinline__ unsigned long long block_sum(unsigned long long v) {
 // register choice (2 blocks of 256 per SM; the block build pins 2 blocks: left
 // free, its choice there came out at 80 registers with spills).
 // k_adjoint_wide (frame-code builds) runs 3 blocks per SM (80 registers, ~300
-// B of spills): with the level's pages handed out on demand the extra warps
+// B of spills; the block build 4 blocks, 64 registers): with the level's pages handed out on demand the extra warps
 // hide more of the scattered reads on large tapes (65,536-axiom step: sizes
 // 19.2 -> 18.2 ms, all parameters 35 -> 32 ms), while on small ones the
 // spills and the larger grid's barriers cost more (1,024 facades: forward +
@@ -1005,7 +1005,14 @@ __global__ void PGA_ADJOINT_BOUNDS k_adjoint(DeriveArgs a, AdjArgs j, unsigned l
 }
 
 #if !PGA_GENERAL_FRAMES
-__global__ void __launch_bounds__(kThreads, 3) k_adjoint_wide(DeriveArgs a, AdjArgs j,
+#ifndef PGA_ADJOINT_WIDE_BLOCKS
+#if PGA_INLINE_BLOCKS
+#define PGA_ADJOINT_WIDE_BLOCKS 4  // 64 registers: all parameters 33 -> 31 ms on the 65,536-axiom step
+#else
+#define PGA_ADJOINT_WIDE_BLOCKS 3  // at 4 the sizes step's adjoint lost 3%
+#endif
+#endif
+__global__ void __launch_bounds__(kThreads, PGA_ADJOINT_WIDE_BLOCKS) k_adjoint_wide(DeriveArgs a, AdjArgs j,
                                                               unsigned long long numParamFloats, uint32_t numAxioms) {
   adjoint_pass(a, j, numParamFloats, numAxioms);
 }

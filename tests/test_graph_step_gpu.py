@@ -276,6 +276,45 @@ def test_dynamic_chunks_give_the_same_records_and_gradients():
     _close(grads[1], grads[0], "axiom-size gradients")
 
 
+@pytest.mark.parametrize("blocks", [False, True])
+def test_wide_adjoint_matches_the_standard_one(blocks):
+    """Engines of at least 8M terminals of capacity launch the adjoint with 3
+    (block build: 4) blocks per SM, smaller ones the standard kernel: on a
+    2,048-axiom mix (~4.7M terminals) an engine of 9M capacity and one of 6M
+    derive the same terminals and must give the same block and size gradients
+    to FP32 accumulation order."""
+    from operatorgraph_gb300.engine import Engine
+
+    b = scenes.mixed(2048, blocks=blocks)
+    d_ax = torch.from_numpy(b["axioms"].view(np.uint8).copy()).cuda()
+    d_blk = torch.from_numpy(b["blocks"]).cuda() if blocks else None
+    grads, counts = [], []
+    for cap in (9_000_000, 6_000_000):
+        eng = Engine(b["entries"], node_capacity=1 << 23, max_terminals=cap, record_tape=True,
+                     block_stride=b["block_stride"])
+        out = torch.zeros((cap, 64), dtype=torch.uint8, device="cuda")
+        count = torch.zeros(1, dtype=torch.int64, device="cuda")
+        eng.derive_raw(d_ax.data_ptr(), len(b["axioms"]), None if d_blk is None else d_blk.data_ptr(), out.data_ptr(),
+                       cap, count.data_ptr())
+        g_sz = torch.zeros((len(b["axioms"]), 3), dtype=torch.float32, device="cuda")
+        g_blk = torch.zeros_like(d_blk) if blocks else None
+        eng.adjoint_raw(out.data_ptr(), None if g_blk is None else g_blk.data_ptr(),
+                        len(b["axioms"]) if blocks else 0, g_sz.data_ptr(), grad_stride=16)
+        torch.cuda.synchronize()
+        assert eng.report()["status"] == 0
+        counts.append(int(count.item()))
+        grads.append((g_sz.cpu().numpy().astype(np.float64),
+                      None if g_blk is None else g_blk.cpu().numpy().astype(np.float64)))
+        eng.release()
+        del out
+    assert counts[0] == counts[1] and 6_000_000 > counts[0] > 3_000_000
+    assert np.abs(grads[0][0]).max() > 0
+    _close(grads[0][0], grads[1][0], "axiom-size gradients")
+    if blocks:
+        assert np.abs(grads[0][1]).max() > 0
+        _close(grads[0][1], grads[1][1], "block gradients")
+
+
 def test_strided_gradient_read_in_place_matches_a_copy():
     """pga_adjoint_strided reading dL/dM = M straight from the 16-float terminal
     records gives the gradients of pga_adjoint on a 12-float copy; a stride
