@@ -182,6 +182,54 @@ def test_oracle_lbvh_invariants(scene):
                 assert np.all(aabb[-ch, :3] >= aabb[i, :3]) and np.all(aabb[-ch, 3:] <= aabb[i, 3:])
 
 
+def _spread10(v):
+    v = v.astype(np.uint32)
+    v = (v | (v << np.uint32(16))) & np.uint32(0x030000FF)
+    v = (v | (v << np.uint32(8))) & np.uint32(0x0300F00F)
+    v = (v | (v << np.uint32(4))) & np.uint32(0x030C30C3)
+    v = (v | (v << np.uint32(2))) & np.uint32(0x09249249)
+    return v
+
+
+def test_oracle_lbvh_leaf_order_is_morton_then_path_then_index():
+    """The LBVH's leaf order, pinned independently of the restatement's C++:
+    30-bit Morton codes of the terminal centres (FP32 (c - min) / size * 1023,
+    truncated, clamped at 0), then the full derivation-path hash, then the
+    terminal index; keys morton << 34 | path >> 30.  Synthetic records with
+    many shared centres, shared top path bits and repeated paths, so every
+    tie-break level decides somewhere."""
+    n = 20_000
+    rng = np.random.default_rng(3)
+    rec = np.zeros(n, G.TERMINAL_DT)
+    m = rng.uniform(-0.5, 0.5, (n, 12)).astype(np.float32)
+    m[:, [3, 7, 11]] = rng.uniform(-9.0, 9.0, (n, 3)).astype(np.float32)
+    shared = rng.choice(n, n // 2, replace=False)
+    m[np.ix_(shared, [3, 7, 11])] = rng.uniform(-9.0, 9.0, (40, 3)).astype(np.float32)[rng.integers(0, 40, n // 2)]
+    paths = rng.integers(0, 2**64, size=n, dtype=np.uint64)
+    top = rng.choice(n, n // 4, replace=False)
+    paths[top] = (paths[top] & np.uint64((1 << 54) - 1)) | np.uint64(0x155 << 54)  # shared top 10 bits
+    dst, src = rng.choice(n, n // 20, replace=False), rng.choice(n, n // 20, replace=False)
+    paths[dst] = paths[src]
+    m[np.ix_(dst, [3, 7, 11])] = m[np.ix_(src, [3, 7, 11])]  # equal keys and equal paths
+    rec["m"] = m
+    rec["path"] = paths
+    bounds = np.array([-10.0, -10.0, -10.0, 10.0, 10.0, 10.0], np.float32)
+    _, _, _, lt, keys = oracle.lbvh(rec, tuple(float(v) for v in bounds))
+    size = bounds[3:] - bounds[:3]
+    code = np.zeros(n, np.uint32)
+    for k, col in enumerate((3, 7, 11)):
+        nc = (m[:, col] - bounds[k]) / size[k]
+        q = nc * np.float32(1023.0)
+        v = np.where(q > 0, np.minimum(q, np.float32(4294967040.0)), 0).astype(np.uint32)
+        code |= _spread10(v) << np.uint32(k)
+    want_keys = (code.astype(np.uint64) << np.uint64(34)) | (paths >> np.uint64(30))
+    order = np.lexsort((np.arange(n), paths, code))  # last key is the primary one
+    assert np.array_equal(lt.astype(np.int64), order), "leaf order differs"
+    assert np.array_equal(keys, want_keys[order]), "keys differ"
+    assert int((code[order][1:] == code[order][:-1]).sum()) > n // 4
+    assert int((paths[order][1:] == paths[order][:-1]).sum()) > 100
+
+
 def test_phases_defer_and_collide():
     """Multi-phase semantics of the restatement: a shape reaching a rule of a
     later phase waits for it; IfCollides in phase 1 sees the colliders stored
