@@ -364,8 +364,10 @@ PgaStatus pga_lbvh_build_static(const PgaTerminal* dTerminals, uint64_t n, const
  * and dL/d(axiom size) into dGradAxiomSizes (3 per axiom; may be NULL).
  * Both outputs are overwritten, not added to.  One cooperative launch on
  * `stream`, asynchronous; if the last derivation failed or overflowed, the
- * gradients are zero and pga_engine_sync_report gives the status.  No
- * reference counterpart. */
+ * gradients are zero and pga_engine_sync_report gives the status.  Engines
+ * created with maxTerminals >= 2^23 launch a variant with more resident
+ * blocks per SM (faster on large tapes, slower on small ones); the gradients
+ * agree to FP32 accumulation order.  No reference counterpart. */
 PgaStatus pga_adjoint(PgaEngine* engine, const float* dGradTerminals, float* dGradParams,
                       uint32_t numBlocks, float* dGradAxiomSizes, void* stream);
 
